@@ -1,0 +1,177 @@
+// common.cuh — shared device helpers, state layout and launch checking for
+// the sm_103a rasteriser.  Everything here is internal to libdmgs_gb300.so;
+// the public surface is include/dmgs.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/dmgs.h"
+
+namespace dmgs {
+
+constexpr int TILE = DMGS_TILE;               // 16 x 16 pixel tiles
+constexpr int TILE_PIX = TILE * TILE;         // 256 pixels, one thread each
+constexpr int NUM_SMS_HINT = 152;             // GB300: 2 dies x 76 SMs
+
+// Status word bits written by kernels (never a trap or assert).
+constexpr uint32_t ST_PREFILTER = 1u;   // prefiltered point failed the z test
+constexpr uint32_t ST_OVERFLOW = 2u;    // instance slots exhausted
+constexpr uint32_t ST_BOUNDS = 4u;      // an index left its buffer
+
+__host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// ---------------------------------------------------------------------------
+// IEEE single-precision ops with explicit rounding: the integer-determining
+// part of preprocess must not be contracted into FMAs so that the CPU oracle
+// (numpy float32) reproduces radii, rectangles and depth keys bit for bit.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float dvd(float a, float b) { return __fdiv_rn(a, b); }
+
+// Per-view constants after host-side preparation.
+struct ViewParams {
+  int W, H;
+  int gx, gy;            // tile grid
+  float fx, fy;          // focal lengths (host float32, see focal())
+  float tanfovx, tanfovy;
+  float scale_modifier;
+  int D;                 // active SH degree
+  int prefiltered;
+};
+
+// ---------------------------------------------------------------------------
+// Geometry state (per Gaussian, 48-byte record = 3 x float4):
+//   f0 = (x, y, conic_a, conic_b)    pixel-space mean, conic (a b; b c)
+//   f1 = (conic_c, opacity, r, g)
+//   f2 = (b, depth, rect_lo, rect_hi) rect packed as 2 x (u16 | u16 << 16)
+// A culled Gaussian has rect_lo == rect_hi == 0 and radius 0.
+// ---------------------------------------------------------------------------
+struct GeomLayout {
+  size_t feat, clamped, diff, tile_start, counters, total;
+  int P, gx, gy;
+  __host__ __device__ int T() const { return gx * gy; }
+};
+
+__host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
+  GeomLayout L;
+  L.P = P;
+  L.gx = (W + TILE - 1) / TILE;
+  L.gy = (H + TILE - 1) / TILE;
+  size_t o = 0;
+  L.feat = o;        o = align_up(o + (size_t)P * 48, 256);
+  L.clamped = o;     o = align_up(o + (size_t)P, 256);
+  L.diff = o;        o = align_up(o + (size_t)(L.gx + 1) * (L.gy + 1) * 4, 256);
+  L.tile_start = o;  o = align_up(o + (size_t)(L.gx * L.gy + 1) * 4, 256);
+  L.counters = o;    o = align_up(o + 64, 256);
+  L.total = o;
+  return L;
+}
+
+// counters[0] = status bits, counters[1] = num_rendered (low 32),
+// counters[2] = num_rendered (high 32), counters[3] = longest tile list
+struct BinLayout {
+  size_t keys, keys_alt, point_list, cursor, ranges, total;
+};
+
+__host__ __device__ inline BinLayout bin_layout(int64_t K, int W, int H) {
+  BinLayout L;
+  int gx = (W + TILE - 1) / TILE, gy = (H + TILE - 1) / TILE;
+  size_t T = (size_t)gx * gy;
+  size_t o = 0;
+  L.keys = o;       o = align_up(o + (size_t)K * 8, 256);
+  L.keys_alt = o;   o = align_up(o + (size_t)K * 8, 256);
+  L.point_list = o; o = align_up(o + (size_t)K * 4, 256);
+  L.cursor = o;     o = align_up(o + T * 4, 256);
+  L.ranges = o;     o = align_up(o + T * 8, 256);
+  L.total = o;
+  return L;
+}
+
+struct ImgLayout {
+  size_t final_T, n_contrib, total;
+};
+
+__host__ __device__ inline ImgLayout img_layout(int W, int H) {
+  ImgLayout L;
+  size_t n = (size_t)W * H;
+  size_t o = 0;
+  L.final_T = o;   o = align_up(o + n * 4, 256);
+  L.n_contrib = o; o = align_up(o + n * 4, 256);
+  L.total = o;
+  return L;
+}
+
+// Backward scratch: per-Gaussian 2D gradient accumulators, 48 B record:
+//   g0 = (dL/dndc_x, dL/dndc_y, dL/dconic_a, dL/dconic_b)
+//   g1 = (dL/dconic_c, dL/dopacity, dL/dr, dL/dg)
+//   g2 = (dL/db, 0, 0, 0)
+inline size_t bwd_scratch_bytes(int P) { return align_up((size_t)P * 48, 256); }
+
+__device__ __forceinline__ uint32_t pack_u16x2(int lo, int hi) {
+  return (uint32_t)lo | ((uint32_t)hi << 16);
+}
+
+__device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};"
+               :: "l"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// SH constants of the real spherical-harmonics basis up to degree 3
+// (the same polynomial as utils/sh_utils.py:41-99).
+__constant__ static const float kSH_C0 = 0.28209479177387814f;
+__constant__ static const float kSH_C1 = 0.4886025119029199f;
+__constant__ static const float kSH_C2[5] = {1.0925484305920792f, -1.0925484305920792f,
+                                             0.31539156525252005f, -1.0925484305920792f,
+                                             0.5462742152960396f};
+__constant__ static const float kSH_C3[7] = {-0.5900435899266435f, 2.890611442640554f,
+                                             -0.4570457994644658f, 0.3731763325901154f,
+                                             -0.4570457994644658f, 1.445305721320277f,
+                                             -0.5900435899266435f};
+
+}  // namespace dmgs
+
+// Host-side error plumbing shared by the C-ABI translation units.
+namespace dmgs_host {
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+// Kernel timing registry (timing.cu).  Kernel ids index kKernelNames.
+enum KernelId {
+  K_PREPROCESS = 0, K_TILE_OFFSETS, K_INIT_CURSOR, K_SCATTER, K_SEGMENT_SORT, K_BLEND_FWD,
+  K_BLEND_BWD, K_PREPROCESS_BWD, K_MARK_VISIBLE, K_BIND_FWD, K_BIND_BWD, K_BIND3_FWD,
+  K_BIND3_BWD, K_DEBUG, K_BATCH_PREPROCESS, K_BATCH_BINNING, K_BATCH_BLEND_FWD,
+  K_BATCH_BLEND_BWD, K_BATCH_PREPROCESS_BWD, K_COUNT
+};
+void timing_begin(int kid, cudaStream_t s);
+void timing_end(int kid, cudaStream_t s);
+}  // namespace dmgs_host
+
+// Bracket one kernel launch with the timing registry (no-op when disabled).
+#define DMGS_TIMED(kid, stream, ...)               \
+  do {                                             \
+    dmgs_host::timing_begin(dmgs_host::kid, stream); \
+    __VA_ARGS__;                                   \
+    dmgs_host::timing_end(dmgs_host::kid, stream);   \
+  } while (0)
+
+#define DMGS_CUDA(call)                                                  \
+  do {                                                                   \
+    cudaError_t e_ = (call);                                             \
+    if (e_ != cudaSuccess) return dmgs_host::cuda_fail(e_, #call);       \
+  } while (0)
+
+#define DMGS_LAUNCH_CHECK(name)                                          \
+  do {                                                                   \
+    cudaError_t e_ = cudaGetLastError();                                 \
+    if (e_ != cudaSuccess) return dmgs_host::cuda_fail(e_, name);        \
+  } while (0)

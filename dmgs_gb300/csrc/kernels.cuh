@@ -1,0 +1,57 @@
+// kernels.cuh — internal launch wrappers (one per kernel family).  Each
+// returns DMGS_OK or a DMGS_ERR_* code; they enqueue work on `stream` only.
+#pragma once
+#include "common.cuh"
+
+namespace dmgs {
+
+struct GaussianPtrs {
+  int P, M;
+  const float *means3D, *opacities, *shs, *colors, *scales, *rotations, *cov3D;
+};
+
+// preprocess.cu
+int launch_preprocess(const ViewParams &vp, const float *viewm, const float *projm,
+                      const float *campos, const GaussianPtrs &g, int32_t *radii,
+                      const GeomLayout &L, char *geom, cudaStream_t s);
+int launch_tile_offsets(const GeomLayout &L, char *geom, cudaStream_t s);
+int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t *present,
+                        cudaStream_t s);
+
+// binning.cu
+int launch_scatter(const GeomLayout &L, const char *geom, const BinLayout &B, char *bin,
+                   int64_t K, cudaStream_t s);
+int launch_segment_sort(const GeomLayout &L, const char *geom, const BinLayout &B, char *bin,
+                        int64_t K, cudaStream_t s);
+int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
+                      uint64_t *keys, uint32_t *values, cudaStream_t s);
+int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,
+                          uint32_t *tiles_touched, float *depth, float *xy, float *conic_opacity,
+                          float *rgb, cudaStream_t s);
+
+// blend.cu
+int launch_blend_fwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
+                     const BinLayout &B, const char *bin, const ImgLayout &I, char *img,
+                     const float *bg, float *out_color, cudaStream_t s);
+int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
+                     const BinLayout &B, const char *bin, const ImgLayout &I, const char *img,
+                     const float *bg, const float *dL_dout, float *gacc, cudaStream_t s);
+
+// preprocess_bwd.cu
+int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float *projm,
+                          const float *campos, const GaussianPtrs &g, const GeomLayout &L,
+                          const char *geom, const float *gacc, const DmgsGrads &out,
+                          cudaStream_t s);
+
+// binding.cu
+int launch_bind_fwd(const DmgsFaceBinding &b, float *xyz, float *cov, float *rot, float *covL,
+                    cudaStream_t s);
+int launch_bind_bwd(const DmgsFaceBinding &b, const float *dxyz, const float *dcov,
+                    float *dverts, float *dsf, cudaStream_t s);
+int launch_bind3_fwd(const DmgsFaceBinding3 &b, float *xyz, float *scales, float *rots,
+                     cudaStream_t s);
+int launch_bind3_bwd(const DmgsFaceBinding3 &b, const float *dxyz, const float *dscales,
+                     const float *drots, float *dverts, float *dscaling, float *drot2d,
+                     cudaStream_t s);
+
+}  // namespace dmgs

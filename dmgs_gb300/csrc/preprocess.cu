@@ -1,0 +1,396 @@
+// preprocess.cu — per-Gaussian forward geometry (EWA projection, conic,
+// radius, tile rectangle, SH colour) and the per-tile instance counts.
+//
+// Semantics follow the 3DGS preprocess the reference calls through
+// GaussianRasterizer (gaussian_renderer/__init__.py:86-94); the rotation and
+// covariance packing conventions are those of utils/general_utils.py:64-110
+// and the SH polynomial that of utils/sh_utils.py:75-99.
+//
+// Design: one thread per Gaussian.  The integer-determining chain (view z,
+// NDC position, 2D covariance, radius, rectangle) uses explicitly rounded
+// IEEE ops so that it is reproducible on the CPU.  Tile counting does not
+// touch every covered tile: each visible Gaussian adds +1/-1 at the four
+// corners of its rectangle in a (gy+1) x (gx+1) difference grid (4 atomics
+// per Gaussian instead of one per tile); a 2D prefix sum then yields the
+// per-tile counts.
+#include "kernels.cuh"
+
+namespace dmgs {
+
+namespace {
+
+struct Mat4 { float m[16]; };
+
+__device__ __forceinline__ void load_mat(const float *__restrict__ p, float *m) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) m[i] = __ldg(p + i);
+}
+
+// Sigma = R diag(s)^2 R^T in the fixed op order of the CPU oracle.
+__device__ __forceinline__ void cov3d_scale_rot(float sx, float sy, float sz, float4 q,
+                                                float *cov) {
+  const float r = q.x, x = q.y, y = q.z, z = q.w;
+  float R[9];
+  R[0] = sub(1.f, mul(2.f, add(mul(y, y), mul(z, z))));
+  R[1] = mul(2.f, sub(mul(x, y), mul(r, z)));
+  R[2] = mul(2.f, add(mul(x, z), mul(r, y)));
+  R[3] = mul(2.f, add(mul(x, y), mul(r, z)));
+  R[4] = sub(1.f, mul(2.f, add(mul(x, x), mul(z, z))));
+  R[5] = mul(2.f, sub(mul(y, z), mul(r, x)));
+  R[6] = mul(2.f, sub(mul(x, z), mul(r, y)));
+  R[7] = mul(2.f, add(mul(y, z), mul(r, x)));
+  R[8] = sub(1.f, mul(2.f, add(mul(x, x), mul(y, y))));
+  float Mm[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Mm[i * 3 + 0] = mul(R[i * 3 + 0], sx);
+    Mm[i * 3 + 1] = mul(R[i * 3 + 1], sy);
+    Mm[i * 3 + 2] = mul(R[i * 3 + 2], sz);
+  }
+  auto sig = [&](int i, int k) {
+    return add(add(mul(Mm[i * 3], Mm[k * 3]), mul(Mm[i * 3 + 1], Mm[k * 3 + 1])),
+               mul(Mm[i * 3 + 2], Mm[k * 3 + 2]));
+  };
+  cov[0] = sig(0, 0); cov[1] = sig(0, 1); cov[2] = sig(0, 2);
+  cov[3] = sig(1, 1); cov[4] = sig(1, 2); cov[5] = sig(2, 2);
+}
+
+__device__ __forceinline__ int trunc_sat(float v) { return __float2int_rz(v); }
+
+__global__ void __launch_bounds__(256)
+preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
+                  const float *__restrict__ projm_g, const float *__restrict__ campos_g,
+                  int P, int M, const float *__restrict__ means,
+                  const float *__restrict__ opac, const float *__restrict__ shs,
+                  const float *__restrict__ colors, const float *__restrict__ scales,
+                  const float *__restrict__ rots, const float *__restrict__ cov3D,
+                  int32_t *__restrict__ radii, float4 *__restrict__ feat,
+                  uint8_t *__restrict__ clamped, uint32_t *__restrict__ diff,
+                  uint32_t *__restrict__ counters) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= P) return;
+
+  float V[16], Pm[16];
+  load_mat(viewm_g, V);
+  load_mat(projm_g, Pm);
+
+  const float x = __ldg(means + 3 * idx), y = __ldg(means + 3 * idx + 1),
+              z = __ldg(means + 3 * idx + 2);
+  const float vx = add(add(add(mul(V[0], x), mul(V[4], y)), mul(V[8], z)), V[12]);
+  const float vy = add(add(add(mul(V[1], x), mul(V[5], y)), mul(V[9], z)), V[13]);
+  const float vz = add(add(add(mul(V[2], x), mul(V[6], y)), mul(V[10], z)), V[14]);
+
+  auto cull = [&]() {
+    radii[idx] = 0;
+    feat[3 * idx + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  if (!(vz > 0.2f)) {
+    if (vp.prefiltered) atomicOr(counters, ST_PREFILTER);
+    cull();
+    return;
+  }
+  const float hx = add(add(add(mul(Pm[0], x), mul(Pm[4], y)), mul(Pm[8], z)), Pm[12]);
+  const float hy = add(add(add(mul(Pm[1], x), mul(Pm[5], y)), mul(Pm[9], z)), Pm[13]);
+  const float hw = add(add(add(mul(Pm[3], x), mul(Pm[7], y)), mul(Pm[11], z)), Pm[15]);
+  const float pw = dvd(1.f, add(hw, 1e-7f));
+  const float ndcx = mul(hx, pw), ndcy = mul(hy, pw);
+  const float Wf = (float)vp.W, Hf = (float)vp.H;
+  const float px = mul(sub(mul(add(ndcx, 1.f), Wf), 1.f), 0.5f);
+  const float py = mul(sub(mul(add(ndcy, 1.f), Hf), 1.f), 0.5f);
+
+  float S[6];
+  if (cov3D != nullptr) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) S[i] = __ldg(cov3D + 6 * idx + i);
+  } else {
+    const float mod = vp.scale_modifier;
+    const float sx = mul(__ldg(scales + 3 * idx), mod);
+    const float sy = mul(__ldg(scales + 3 * idx + 1), mod);
+    const float sz = mul(__ldg(scales + 3 * idx + 2), mod);
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(rots) + idx);
+    cov3d_scale_rot(sx, sy, sz, q, S);
+  }
+
+  // EWA: cov2D = (J W) Sigma (J W)^T with the Jacobian evaluated at the
+  // position clamped to 1.3x the field of view.
+  const float limx = mul(1.3f, vp.tanfovx), limy = mul(1.3f, vp.tanfovy);
+  const float txtz = dvd(vx, vz), tytz = dvd(vy, vz);
+  const float tx = mul(fminf(limx, fmaxf(-limx, txtz)), vz);
+  const float ty = mul(fminf(limy, fmaxf(-limy, tytz)), vz);
+  const float vz2 = mul(vz, vz);
+  const float J00 = dvd(vp.fx, vz);
+  const float J02 = dvd(-mul(vp.fx, tx), vz2);
+  const float J11 = dvd(vp.fy, vz);
+  const float J12 = dvd(-mul(vp.fy, ty), vz2);
+  float T0[3], T1[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    T0[j] = add(mul(J00, V[4 * j + 0]), mul(J02, V[4 * j + 2]));
+    T1[j] = add(mul(J11, V[4 * j + 1]), mul(J12, V[4 * j + 2]));
+  }
+  const float Sg[9] = {S[0], S[1], S[2], S[1], S[3], S[4], S[2], S[4], S[5]};
+  float U0[3], U1[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    U0[j] = add(add(mul(T0[0], Sg[j]), mul(T0[1], Sg[3 + j])), mul(T0[2], Sg[6 + j]));
+    U1[j] = add(add(mul(T1[0], Sg[j]), mul(T1[1], Sg[3 + j])), mul(T1[2], Sg[6 + j]));
+  }
+  float c00 = add(add(mul(U0[0], T0[0]), mul(U0[1], T0[1])), mul(U0[2], T0[2]));
+  const float c01 = add(add(mul(U0[0], T1[0]), mul(U0[1], T1[1])), mul(U0[2], T1[2]));
+  float c11 = add(add(mul(U1[0], T1[0]), mul(U1[1], T1[1])), mul(U1[2], T1[2]));
+  c00 = add(c00, 0.3f);
+  c11 = add(c11, 0.3f);
+  const float det = sub(mul(c00, c11), mul(c01, c01));
+  if (det == 0.f) { cull(); return; }
+  const float det_inv = dvd(1.f, det);
+  const float ca = mul(c11, det_inv), cb = mul(-c01, det_inv), cc = mul(c00, det_inv);
+  const float mid = mul(0.5f, add(c00, c11));
+  const float disc = fmaxf(0.1f, sub(mul(mid, mid), det));
+  const float sq = __fsqrt_rn(disc);
+  const float l1 = add(mid, sq), l2 = sub(mid, sq);
+  const int rad = trunc_sat(ceilf(mul(3.f, __fsqrt_rn(fmaxf(l1, l2)))));
+  if (rad <= 0) { cull(); return; }
+  const float r = (float)rad;
+  const int x0 = min(vp.gx, max(0, trunc_sat(dvd(sub(px, r), (float)TILE))));
+  const int y0 = min(vp.gy, max(0, trunc_sat(dvd(sub(py, r), (float)TILE))));
+  const int x1 = min(vp.gx, max(0, trunc_sat(dvd(add(add(px, r), (float)(TILE - 1)), (float)TILE))));
+  const int y1 = min(vp.gy, max(0, trunc_sat(dvd(add(add(py, r), (float)(TILE - 1)), (float)TILE))));
+  if ((x1 - x0) * (y1 - y0) == 0) { cull(); return; }
+
+  // Colour: precomputed, or SH (degree <= 3) at the view direction, +0.5,
+  // clamped at 0 with the clamp recorded for the adjoint.
+  float cr, cg, cbl;
+  uint8_t clampbits = 0;
+  if (colors != nullptr) {
+    cr = __ldg(colors + 3 * idx); cg = __ldg(colors + 3 * idx + 1); cbl = __ldg(colors + 3 * idx + 2);
+  } else {
+    const float *sh = shs + (size_t)idx * M * 3;
+    float dx = x - __ldg(campos_g), dy = y - __ldg(campos_g + 1), dz = z - __ldg(campos_g + 2);
+    const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
+    dx *= inv; dy *= inv; dz *= inv;
+    float b[16];
+    b[0] = kSH_C0;
+    int nb = 1;
+    if (vp.D > 0) {
+      b[1] = -kSH_C1 * dy; b[2] = kSH_C1 * dz; b[3] = -kSH_C1 * dx;
+      nb = 4;
+      if (vp.D > 1) {
+        const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
+        b[4] = kSH_C2[0] * dx * dy;
+        b[5] = kSH_C2[1] * dy * dz;
+        b[6] = kSH_C2[2] * (2.f * zz - xx - yy);
+        b[7] = kSH_C2[3] * dx * dz;
+        b[8] = kSH_C2[4] * (xx - yy);
+        nb = 9;
+        if (vp.D > 2) {
+          b[9] = kSH_C3[0] * dy * (3.f * xx - yy);
+          b[10] = kSH_C3[1] * dx * dy * dz;
+          b[11] = kSH_C3[2] * dy * (4.f * zz - xx - yy);
+          b[12] = kSH_C3[3] * dz * (2.f * zz - 3.f * xx - 3.f * yy);
+          b[13] = kSH_C3[4] * dx * (4.f * zz - xx - yy);
+          b[14] = kSH_C3[5] * dz * (xx - yy);
+          b[15] = kSH_C3[6] * dx * (xx - 3.f * yy);
+          nb = 16;
+        }
+      }
+    }
+    float rr = 0.f, gg = 0.f, bb = 0.f;
+    for (int k = 0; k < nb; ++k) {
+      rr += b[k] * __ldg(sh + 3 * k);
+      gg += b[k] * __ldg(sh + 3 * k + 1);
+      bb += b[k] * __ldg(sh + 3 * k + 2);
+    }
+    rr += 0.5f; gg += 0.5f; bb += 0.5f;
+    clampbits = (rr < 0.f ? 1 : 0) | (gg < 0.f ? 2 : 0) | (bb < 0.f ? 4 : 0);
+    cr = fmaxf(rr, 0.f); cg = fmaxf(gg, 0.f); cbl = fmaxf(bb, 0.f);
+    clamped[idx] = clampbits;
+  }
+
+  const float o = __ldg(opac + idx);
+  radii[idx] = rad;
+  feat[3 * idx + 0] = make_float4(px, py, ca, cb);
+  feat[3 * idx + 1] = make_float4(cc, o, cr, cg);
+  feat[3 * idx + 2] = make_float4(cbl, vz, __uint_as_float(pack_u16x2(x0, y0)),
+                                  __uint_as_float(pack_u16x2(x1, y1)));
+
+  // +1 at (x0,y0), -1 at (x1,y0) and (x0,y1), +1 at (x1,y1).
+  const int stride = vp.gx + 1;
+  atomicAdd(diff + y0 * stride + x0, 1u);
+  atomicAdd(diff + y0 * stride + x1, 0xffffffffu);
+  atomicAdd(diff + y1 * stride + x0, 0xffffffffu);
+  atomicAdd(diff + y1 * stride + x1, 1u);
+}
+
+// One block: 2D prefix sum of the difference grid (in shared memory) ->
+// per-tile counts -> exclusive scan in tile order -> tile_start[T+1].
+// counters[1..2] = total instances (64-bit), counters[3] = longest list.
+__global__ void __launch_bounds__(1024)
+tile_offsets_kernel(int gx, int gy, const uint32_t *__restrict__ diff,
+                    uint32_t *__restrict__ tile_start, uint32_t *__restrict__ counters) {
+  extern __shared__ uint32_t sm[];
+  const int stride = gx + 1;
+  const int n = stride * (gy + 1);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) sm[i] = diff[i];
+  __syncthreads();
+  for (int yrow = threadIdx.x; yrow < gy; yrow += blockDim.x) {
+    uint32_t run = 0;
+    for (int xx = 0; xx < gx; ++xx) { run += sm[yrow * stride + xx]; sm[yrow * stride + xx] = run; }
+  }
+  __syncthreads();
+  for (int xc = threadIdx.x; xc < gx; xc += blockDim.x) {
+    uint32_t run = 0;
+    for (int yy = 0; yy < gy; ++yy) { run += sm[yy * stride + xc]; sm[yy * stride + xc] = run; }
+  }
+  __syncthreads();
+  // Exclusive scan over T counts, each thread a contiguous chunk.
+  const int T = gx * gy;
+  const int per = (T + blockDim.x - 1) / blockDim.x;
+  const int beg = min(T, (int)threadIdx.x * per), end = min(T, beg + per);
+  unsigned long long local = 0;
+  uint32_t lmax = 0;
+  for (int t = beg; t < end; ++t) {
+    const uint32_t c = sm[(t / gx) * stride + (t % gx)];
+    local += c;
+    lmax = max(lmax, c);
+  }
+  __shared__ unsigned long long warp_tot[32];
+  __shared__ uint32_t warp_max[32];
+  // inclusive warp scan of `local`
+  unsigned long long inc = local;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned long long v = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += v;
+  }
+  uint32_t wm = lmax;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+  if (lane == 31) warp_tot[wid] = inc;
+  if (lane == 0) warp_max[wid] = wm;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    unsigned long long v = lane < nw ? warp_tot[lane] : 0ull;
+    uint32_t m = lane < nw ? warp_max[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane < nw) warp_tot[lane] = v;  // inclusive per-warp totals
+    if (lane == 0) warp_max[0] = m;
+  }
+  __syncthreads();
+  unsigned long long base = (wid > 0 ? warp_tot[wid - 1] : 0ull) + inc - local;
+  for (int t = beg; t < end; ++t) {
+    tile_start[t] = (uint32_t)base;
+    base += sm[(t / gx) * stride + (t % gx)];
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    const unsigned long long total = warp_tot[(blockDim.x >> 5) - 1];
+    tile_start[T] = (uint32_t)total;
+    counters[1] = (uint32_t)(total & 0xffffffffull);
+    counters[2] = (uint32_t)(total >> 32);
+    counters[3] = warp_max[0];
+  }
+}
+
+__global__ void mark_visible_kernel(int P, const float *__restrict__ means,
+                                    const float *__restrict__ viewm_g,
+                                    uint8_t *__restrict__ present) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= P) return;
+  const float x = means[3 * idx], y = means[3 * idx + 1], z = means[3 * idx + 2];
+  const float vz = add(add(add(mul(__ldg(viewm_g + 2), x), mul(__ldg(viewm_g + 6), y)),
+                           mul(__ldg(viewm_g + 10), z)), __ldg(viewm_g + 14));
+  present[idx] = vz > 0.2f ? 1 : 0;
+}
+
+}  // namespace
+
+int launch_preprocess(const ViewParams &vp, const float *viewm, const float *projm,
+                      const float *campos, const GaussianPtrs &g, int32_t *radii,
+                      const GeomLayout &L, char *geom, cudaStream_t s) {
+  float4 *feat = reinterpret_cast<float4 *>(geom + L.feat);
+  uint8_t *clamped = reinterpret_cast<uint8_t *>(geom + L.clamped);
+  uint32_t *diff = reinterpret_cast<uint32_t *>(geom + L.diff);
+  uint32_t *counters = reinterpret_cast<uint32_t *>(geom + L.counters);
+  DMGS_CUDA(cudaMemsetAsync(diff, 0, (size_t)(L.gx + 1) * (L.gy + 1) * 4, s));
+  DMGS_CUDA(cudaMemsetAsync(counters, 0, 64, s));
+  if (g.P > 0) {
+    const int threads = 256;
+    const int blocks = (g.P + threads - 1) / threads;
+    DMGS_TIMED(K_PREPROCESS, s, preprocess_kernel<<<blocks, threads, 0, s>>>(vp, viewm, projm, campos, g.P, g.M, g.means3D,
+                                                 g.opacities, g.shs, g.colors, g.scales,
+                                                 g.rotations, g.cov3D, radii, feat, clamped, diff,
+                                                 counters));
+    DMGS_LAUNCH_CHECK("preprocess_kernel");
+  }
+  return DMGS_OK;
+}
+
+int launch_tile_offsets(const GeomLayout &L, char *geom, cudaStream_t s) {
+  const size_t smem = (size_t)(L.gx + 1) * (L.gy + 1) * 4;
+  if (smem > 200 * 1024) {
+    dmgs_host::set_error("image too large: %d x %d tiles exceeds the tile-offset kernel", L.gx, L.gy);
+    return DMGS_ERR_ARG;
+  }
+  if (smem > 48 * 1024)
+    DMGS_CUDA(cudaFuncSetAttribute(tile_offsets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  DMGS_TIMED(K_TILE_OFFSETS, s, tile_offsets_kernel<<<1, 1024, smem, s>>>(
+      L.gx, L.gy, reinterpret_cast<const uint32_t *>(geom + L.diff),
+      reinterpret_cast<uint32_t *>(geom + L.tile_start),
+      reinterpret_cast<uint32_t *>(geom + L.counters)));
+  DMGS_LAUNCH_CHECK("tile_offsets_kernel");
+  return DMGS_OK;
+}
+
+int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t *present,
+                        cudaStream_t s) {
+  if (P <= 0) return DMGS_OK;
+  DMGS_TIMED(K_MARK_VISIBLE, s, mark_visible_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, means3D, viewm, present));
+  DMGS_LAUNCH_CHECK("mark_visible_kernel");
+  return DMGS_OK;
+}
+
+}  // namespace dmgs
+
+namespace dmgs {
+namespace {
+__global__ void debug_geometry_kernel(int P, int gx, const float4 *__restrict__ feat,
+                                      int32_t *rect, uint32_t *tiles_touched, float *depth,
+                                      float *xy, float *conic_opacity, float *rgb) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= P) return;
+  const float4 f0 = feat[3 * idx], f1 = feat[3 * idx + 1], f2 = feat[3 * idx + 2];
+  const uint32_t lo = __float_as_uint(f2.z), hi = __float_as_uint(f2.w);
+  const int x0 = lo & 0xffff, y0 = lo >> 16, x1 = hi & 0xffff, y1 = hi >> 16;
+  const bool vis = (lo | hi) != 0u;
+  if (rect) { rect[4 * idx] = x0; rect[4 * idx + 1] = y0; rect[4 * idx + 2] = x1; rect[4 * idx + 3] = y1; }
+  if (tiles_touched) tiles_touched[idx] = vis ? (uint32_t)((x1 - x0) * (y1 - y0)) : 0u;
+  if (depth) depth[idx] = vis ? f2.y : 0.f;
+  if (xy) { xy[2 * idx] = vis ? f0.x : 0.f; xy[2 * idx + 1] = vis ? f0.y : 0.f; }
+  if (conic_opacity) {
+    conic_opacity[4 * idx] = vis ? f0.z : 0.f; conic_opacity[4 * idx + 1] = vis ? f0.w : 0.f;
+    conic_opacity[4 * idx + 2] = vis ? f1.x : 0.f; conic_opacity[4 * idx + 3] = vis ? f1.y : 0.f;
+  }
+  if (rgb) { rgb[3 * idx] = vis ? f1.z : 0.f; rgb[3 * idx + 1] = vis ? f1.w : 0.f; rgb[3 * idx + 2] = vis ? f2.x : 0.f; }
+  (void)gx;
+}
+}  // namespace
+
+int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,
+                          uint32_t *tiles_touched, float *depth, float *xy, float *conic_opacity,
+                          float *rgb, cudaStream_t s) {
+  if (L.P <= 0) return DMGS_OK;
+  DMGS_TIMED(K_DEBUG, s, debug_geometry_kernel<<<(L.P + 255) / 256, 256, 0, s>>>(
+      L.P, L.gx, reinterpret_cast<const float4 *>(geom + L.feat), rect, tiles_touched, depth, xy,
+      conic_opacity, rgb));
+  DMGS_LAUNCH_CHECK("debug_geometry_kernel");
+  return DMGS_OK;
+}
+}  // namespace dmgs

@@ -1,0 +1,315 @@
+// preprocess_bwd.cu — per-Gaussian adjoint of the forward geometry.
+//
+// Input: the per-Gaussian 2D gradients the blend adjoint accumulated
+// (dL/d NDC mean, dL/d conic (a, b, c) with b the off-diagonal scalar,
+// dL/d opacity, dL/d rgb).  Output: gradients w.r.t. every forward input.
+//
+// Chain (derived here, conventions of the reference adjoint):
+//   conic = inverse(cov2D)           -> dL/dA, dL/dB, dL/dC (cov2D = [[A,B],[B,C]])
+//   cov2D = T Sigma T^T, T = J W     -> dL/dSigma = T^T Gs T, dL/dT = 2 Gs T Sigma
+//   J(t), t = W m + t0               -> dL/dt with the 1.3 tan(fov) clamp: zero
+//                                        gradient through a clamped coordinate,
+//                                        the clamped value held constant
+//   ndc = hom.xy / (hom.w + 1e-7)    -> dL/dm
+//   rgb = max(0, SH(dir) + 0.5)      -> dL/dsh, dL/dm through dir = unit(m - campos)
+//   Sigma = (R S)(R S)^T             -> dL/dscale, dL/dquaternion (unnormalised)
+// Culled Gaussians (radius 0, empty rectangle in the geometry state) get
+// zeros in every output.
+#include "kernels.cuh"
+
+namespace dmgs {
+
+namespace {
+
+__global__ void __launch_bounds__(256)
+preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
+                      const float *__restrict__ projm_g, const float *__restrict__ campos_g,
+                      int P, int M, const float *__restrict__ means,
+                      const float *__restrict__ shs, const float *__restrict__ scales,
+                      const float *__restrict__ rots, const float *__restrict__ cov3D,
+                      const float4 *__restrict__ feat, const uint8_t *__restrict__ clamped,
+                      const float *__restrict__ gacc, DmgsGrads out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= P) return;
+  // visible <=> the forward stored a non-empty tile rectangle (radius > 0)
+  const float4 f2 = feat[3 * idx + 2];
+  const bool vis = (__float_as_uint(f2.z) | __float_as_uint(f2.w)) != 0u;
+  const int nsh = (vp.D + 1) * (vp.D + 1);
+
+  if (!vis) {
+    if (out.dL_dmeans2D) { out.dL_dmeans2D[3 * idx] = 0.f; out.dL_dmeans2D[3 * idx + 1] = 0.f; out.dL_dmeans2D[3 * idx + 2] = 0.f; }
+    if (out.dL_dcolors) { out.dL_dcolors[3 * idx] = 0.f; out.dL_dcolors[3 * idx + 1] = 0.f; out.dL_dcolors[3 * idx + 2] = 0.f; }
+    if (out.dL_dopacity) out.dL_dopacity[idx] = 0.f;
+    if (out.dL_dmeans3D) { out.dL_dmeans3D[3 * idx] = 0.f; out.dL_dmeans3D[3 * idx + 1] = 0.f; out.dL_dmeans3D[3 * idx + 2] = 0.f; }
+    if (out.dL_dcov3D) for (int i = 0; i < 6; ++i) out.dL_dcov3D[6 * idx + i] = 0.f;
+    if (out.dL_dsh) for (int i = 0; i < 3 * M; ++i) out.dL_dsh[(size_t)idx * 3 * M + i] = 0.f;
+    if (out.dL_dscales) { out.dL_dscales[3 * idx] = 0.f; out.dL_dscales[3 * idx + 1] = 0.f; out.dL_dscales[3 * idx + 2] = 0.f; }
+    if (out.dL_drotations) reinterpret_cast<float4 *>(out.dL_drotations)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+
+  const float4 ga = reinterpret_cast<const float4 *>(gacc)[3 * idx];
+  const float4 gb = reinterpret_cast<const float4 *>(gacc)[3 * idx + 1];
+  const float gblue = gacc[12 * idx + 8];
+  const float dndc_x = ga.x, dndc_y = ga.y;
+  const float dca = ga.z, dcb = ga.w, dcc = gb.x;
+  const float dop = gb.y;
+  float drgb[3] = {gb.z, gb.w, gblue};
+
+  if (out.dL_dmeans2D) { out.dL_dmeans2D[3 * idx] = dndc_x; out.dL_dmeans2D[3 * idx + 1] = dndc_y; out.dL_dmeans2D[3 * idx + 2] = 0.f; }
+  if (out.dL_dopacity) out.dL_dopacity[idx] = dop;
+  if (out.dL_dcolors) { out.dL_dcolors[3 * idx] = drgb[0]; out.dL_dcolors[3 * idx + 1] = drgb[1]; out.dL_dcolors[3 * idx + 2] = drgb[2]; }
+
+  float V[16], Pm[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) { V[i] = __ldg(viewm_g + i); Pm[i] = __ldg(projm_g + i); }
+  const float mx = means[3 * idx], my = means[3 * idx + 1], mz = means[3 * idx + 2];
+
+  // --- recompute the forward quantities ---------------------------------
+  const float tx0 = V[0] * mx + V[4] * my + V[8] * mz + V[12];
+  const float ty0 = V[1] * mx + V[5] * my + V[9] * mz + V[13];
+  const float tz = V[2] * mx + V[6] * my + V[10] * mz + V[14];
+
+  float S[6];
+  float R[9], sc[3];
+  const bool from_sr = (cov3D == nullptr);
+  float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!from_sr) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) S[i] = cov3D[6 * idx + i];
+  } else {
+    q = reinterpret_cast<const float4 *>(rots)[idx];
+    const float r = q.x, x = q.y, y = q.z, z = q.w;
+    R[0] = 1.f - 2.f * (y * y + z * z); R[1] = 2.f * (x * y - r * z); R[2] = 2.f * (x * z + r * y);
+    R[3] = 2.f * (x * y + r * z); R[4] = 1.f - 2.f * (x * x + z * z); R[5] = 2.f * (y * z - r * x);
+    R[6] = 2.f * (x * z - r * y); R[7] = 2.f * (y * z + r * x); R[8] = 1.f - 2.f * (x * x + y * y);
+    sc[0] = vp.scale_modifier * scales[3 * idx];
+    sc[1] = vp.scale_modifier * scales[3 * idx + 1];
+    sc[2] = vp.scale_modifier * scales[3 * idx + 2];
+    float Mm[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Mm[i * 3 + j] = R[i * 3 + j] * sc[j];
+    auto sig = [&](int i, int k) {
+      return Mm[i * 3] * Mm[k * 3] + Mm[i * 3 + 1] * Mm[k * 3 + 1] + Mm[i * 3 + 2] * Mm[k * 3 + 2];
+    };
+    S[0] = sig(0, 0); S[1] = sig(0, 1); S[2] = sig(0, 2); S[3] = sig(1, 1); S[4] = sig(1, 2); S[5] = sig(2, 2);
+  }
+  const float Sg[9] = {S[0], S[1], S[2], S[1], S[3], S[4], S[2], S[4], S[5]};
+
+  const float limx = 1.3f * vp.tanfovx, limy = 1.3f * vp.tanfovy;
+  const float txtz = tx0 / tz, tytz = ty0 / tz;
+  const float tx = fminf(limx, fmaxf(-limx, txtz)) * tz;
+  const float ty = fminf(limy, fmaxf(-limy, tytz)) * tz;
+  const float xmul = (txtz < -limx || txtz > limx) ? 0.f : 1.f;
+  const float ymul = (tytz < -limy || tytz > limy) ? 0.f : 1.f;
+  const float inv = 1.f / tz, inv2 = inv * inv, inv3 = inv2 * inv;
+  const float J00 = vp.fx * inv, J02 = -vp.fx * tx * inv2;
+  const float J11 = vp.fy * inv, J12 = -vp.fy * ty * inv2;
+  // W_ij = V[i + 4j]
+  float T[2][3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    T[0][j] = J00 * V[4 * j + 0] + J02 * V[4 * j + 2];
+    T[1][j] = J11 * V[4 * j + 1] + J12 * V[4 * j + 2];
+  }
+  float TS[2][3];  // T Sigma
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      TS[a][j] = T[a][0] * Sg[j] + T[a][1] * Sg[3 + j] + T[a][2] * Sg[6 + j];
+  const float A = TS[0][0] * T[0][0] + TS[0][1] * T[0][1] + TS[0][2] * T[0][2] + 0.3f;
+  const float Bc = TS[0][0] * T[1][0] + TS[0][1] * T[1][1] + TS[0][2] * T[1][2];
+  const float C = TS[1][0] * T[1][0] + TS[1][1] * T[1][1] + TS[1][2] * T[1][2] + 0.3f;
+
+  // --- conic -> cov2D ----------------------------------------------------
+  const float det = A * C - Bc * Bc;
+  const float det2 = det * det;
+  float dA = 0.f, dB = 0.f, dC = 0.f;
+  if (det2 != 0.f) {
+    const float id2 = 1.f / det2;
+    dA = id2 * (-C * C * dca + Bc * C * dcb - Bc * Bc * dcc);
+    dB = id2 * (2.f * Bc * C * dca - (A * C + Bc * Bc) * dcb + 2.f * A * Bc * dcc);
+    dC = id2 * (-Bc * Bc * dca + A * Bc * dcb - A * A * dcc);
+  }
+  // Gs = [[dA, dB/2], [dB/2, dC]]
+  const float Gs00 = dA, Gs01 = 0.5f * dB, Gs11 = dC;
+
+  // dL/dSigma_sym = T^T Gs T
+  float GT[2][3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    GT[0][j] = Gs00 * T[0][j] + Gs01 * T[1][j];
+    GT[1][j] = Gs01 * T[0][j] + Gs11 * T[1][j];
+  }
+  float dS[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dS[i * 3 + j] = T[0][i] * GT[0][j] + T[1][i] * GT[1][j];
+  if (out.dL_dcov3D) {
+    float *o = out.dL_dcov3D + 6 * idx;
+    o[0] = dS[0]; o[1] = 2.f * dS[1]; o[2] = 2.f * dS[2];
+    o[3] = dS[4]; o[4] = 2.f * dS[5]; o[5] = dS[8];
+  }
+
+  // dL/dT = 2 Gs T Sigma
+  float dT[2][3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dT[0][j] = 2.f * (Gs00 * TS[0][j] + Gs01 * TS[1][j]);
+    dT[1][j] = 2.f * (Gs01 * TS[0][j] + Gs11 * TS[1][j]);
+  }
+  // dL/dJ = dL/dT W^T  (W_bk = V[b + 4k])
+  float dJ00 = 0.f, dJ02 = 0.f, dJ11 = 0.f, dJ12 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dJ00 += dT[0][k] * V[4 * k + 0];
+    dJ02 += dT[0][k] * V[4 * k + 2];
+    dJ11 += dT[1][k] * V[4 * k + 1];
+    dJ12 += dT[1][k] * V[4 * k + 2];
+  }
+  const float dtx = xmul * (-vp.fx * inv2) * dJ02;
+  const float dty = ymul * (-vp.fy * inv2) * dJ12;
+  const float dtz = -vp.fx * inv2 * dJ00 - vp.fy * inv2 * dJ11 +
+                    2.f * vp.fx * tx * inv3 * dJ02 + 2.f * vp.fy * ty * inv3 * dJ12;
+  float dm[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) dm[k] = V[4 * k] * dtx + V[4 * k + 1] * dty + V[4 * k + 2] * dtz;
+
+  // --- projected mean ----------------------------------------------------
+  {
+    const float hx = Pm[0] * mx + Pm[4] * my + Pm[8] * mz + Pm[12];
+    const float hy = Pm[1] * mx + Pm[5] * my + Pm[9] * mz + Pm[13];
+    const float hw = Pm[3] * mx + Pm[7] * my + Pm[11] * mz + Pm[15];
+    const float mw = 1.f / (hw + 1e-7f);
+    const float mw2 = mw * mw;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float jx = Pm[4 * k] * mw - hx * mw2 * Pm[4 * k + 3];
+      const float jy = Pm[4 * k + 1] * mw - hy * mw2 * Pm[4 * k + 3];
+      dm[k] += dndc_x * jx + dndc_y * jy;
+    }
+  }
+
+  // --- SH colour ---------------------------------------------------------
+  if (shs != nullptr) {
+    const uint8_t cl = clamped[idx];
+    if (cl & 1) drgb[0] = 0.f;
+    if (cl & 2) drgb[1] = 0.f;
+    if (cl & 4) drgb[2] = 0.f;
+    const float vx_ = mx - campos_g[0], vy_ = my - campos_g[1], vz_ = mz - campos_g[2];
+    const float len = sqrtf(vx_ * vx_ + vy_ * vy_ + vz_ * vz_);
+    const float il = 1.f / len;
+    const float x = vx_ * il, y = vy_ * il, z = vz_ * il;
+    const float *sh = shs + (size_t)idx * M * 3;
+    float *dsh = out.dL_dsh ? out.dL_dsh + (size_t)idx * M * 3 : nullptr;
+    // basis value b_k and its partial derivatives (bx, by, bz) w.r.t. the
+    // unnormalised-direction components x, y, z
+    float gdx = 0.f, gdy = 0.f, gdz = 0.f;
+    auto term = [&](int k, float b, float bx, float by, float bz) {
+      const float s0 = sh[3 * k], s1 = sh[3 * k + 1], s2 = sh[3 * k + 2];
+      if (dsh) { dsh[3 * k] = b * drgb[0]; dsh[3 * k + 1] = b * drgb[1]; dsh[3 * k + 2] = b * drgb[2]; }
+      const float dot = s0 * drgb[0] + s1 * drgb[1] + s2 * drgb[2];
+      gdx += bx * dot; gdy += by * dot; gdz += bz * dot;
+    };
+    term(0, kSH_C0, 0.f, 0.f, 0.f);
+    if (vp.D > 0) {
+      term(1, -kSH_C1 * y, 0.f, -kSH_C1, 0.f);
+      term(2, kSH_C1 * z, 0.f, 0.f, kSH_C1);
+      term(3, -kSH_C1 * x, -kSH_C1, 0.f, 0.f);
+      if (vp.D > 1) {
+        const float xx = x * x, yy = y * y, zz = z * z;
+        term(4, kSH_C2[0] * x * y, kSH_C2[0] * y, kSH_C2[0] * x, 0.f);
+        term(5, kSH_C2[1] * y * z, 0.f, kSH_C2[1] * z, kSH_C2[1] * y);
+        term(6, kSH_C2[2] * (2.f * zz - xx - yy), -2.f * kSH_C2[2] * x, -2.f * kSH_C2[2] * y, 4.f * kSH_C2[2] * z);
+        term(7, kSH_C2[3] * x * z, kSH_C2[3] * z, 0.f, kSH_C2[3] * x);
+        term(8, kSH_C2[4] * (xx - yy), 2.f * kSH_C2[4] * x, -2.f * kSH_C2[4] * y, 0.f);
+        if (vp.D > 2) {
+          term(9, kSH_C3[0] * y * (3.f * xx - yy), 6.f * kSH_C3[0] * x * y, kSH_C3[0] * (3.f * xx - 3.f * yy), 0.f);
+          term(10, kSH_C3[1] * x * y * z, kSH_C3[1] * y * z, kSH_C3[1] * x * z, kSH_C3[1] * x * y);
+          term(11, kSH_C3[2] * y * (4.f * zz - xx - yy), -2.f * kSH_C3[2] * x * y,
+               kSH_C3[2] * (4.f * zz - xx - 3.f * yy), 8.f * kSH_C3[2] * y * z);
+          term(12, kSH_C3[3] * z * (2.f * zz - 3.f * xx - 3.f * yy), -6.f * kSH_C3[3] * x * z,
+               -6.f * kSH_C3[3] * y * z, kSH_C3[3] * (6.f * zz - 3.f * xx - 3.f * yy));
+          term(13, kSH_C3[4] * x * (4.f * zz - xx - yy), kSH_C3[4] * (4.f * zz - 3.f * xx - yy),
+               -2.f * kSH_C3[4] * x * y, 8.f * kSH_C3[4] * x * z);
+          term(14, kSH_C3[5] * z * (xx - yy), 2.f * kSH_C3[5] * x * z, -2.f * kSH_C3[5] * y * z,
+               kSH_C3[5] * (xx - yy));
+          term(15, kSH_C3[6] * x * (xx - 3.f * yy), kSH_C3[6] * (3.f * xx - 3.f * yy),
+               -6.f * kSH_C3[6] * x * y, 0.f);
+        }
+      }
+    }
+    if (dsh)
+      for (int i = 3 * nsh; i < 3 * M; ++i) dsh[i] = 0.f;
+    // d unit(v)/dv . g = (g - u (u . g)) / |v|
+    const float ug = x * gdx + y * gdy + z * gdz;
+    dm[0] += (gdx - x * ug) * il;
+    dm[1] += (gdy - y * ug) * il;
+    dm[2] += (gdz - z * ug) * il;
+  }
+
+  if (out.dL_dmeans3D) {
+    out.dL_dmeans3D[3 * idx] = dm[0];
+    out.dL_dmeans3D[3 * idx + 1] = dm[1];
+    out.dL_dmeans3D[3 * idx + 2] = dm[2];
+  }
+
+  // --- scale / rotation --------------------------------------------------
+  if (from_sr && (out.dL_dscales || out.dL_drotations)) {
+    // dL/dM = 2 dS M,  M = R diag(sc)
+    float Mm[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Mm[i * 3 + j] = R[i * 3 + j] * sc[j];
+    float dM[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        dM[i * 3 + j] = 2.f * (dS[i * 3] * Mm[j] + dS[i * 3 + 1] * Mm[3 + j] + dS[i * 3 + 2] * Mm[6 + j]);
+    if (out.dL_dscales) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        out.dL_dscales[3 * idx + j] =
+            vp.scale_modifier * (dM[j] * R[j] + dM[3 + j] * R[3 + j] + dM[6 + j] * R[6 + j]);
+    }
+    if (out.dL_drotations) {
+      float G[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) G[i * 3 + j] = dM[i * 3 + j] * sc[j];
+      const float r = q.x, x = q.y, y = q.z, z = q.w;
+      const float dr = 2.f * (-z * G[1] + y * G[2] + z * G[3] - x * G[5] - y * G[6] + x * G[7]);
+      const float dx = 2.f * (y * G[1] + z * G[2] + y * G[3] - 2.f * x * G[4] - r * G[5] + z * G[6] +
+                              r * G[7] - 2.f * x * G[8]);
+      const float dy = 2.f * (-2.f * y * G[0] + x * G[1] + r * G[2] + x * G[3] + z * G[5] - r * G[6] +
+                              z * G[7] - 2.f * y * G[8]);
+      const float dz = 2.f * (-2.f * z * G[0] - r * G[1] + x * G[2] + r * G[3] - 2.f * z * G[4] +
+                              y * G[5] + x * G[6] + y * G[7]);
+      reinterpret_cast<float4 *>(out.dL_drotations)[idx] = make_float4(dr, dx, dy, dz);
+    }
+  }
+}
+
+}  // namespace
+
+int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float *projm,
+                          const float *campos, const GaussianPtrs &g, const GeomLayout &L,
+                          const char *geom, const float *gacc, const DmgsGrads &out,
+                          cudaStream_t s) {
+  if (g.P <= 0) return DMGS_OK;
+  DMGS_TIMED(K_PREPROCESS_BWD, s, preprocess_bwd_kernel<<<(g.P + 255) / 256, 256, 0, s>>>(
+      vp, viewm, projm, campos, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D,
+      reinterpret_cast<const float4 *>(geom + L.feat),
+      reinterpret_cast<const uint8_t *>(geom + L.clamped), gacc, out));
+  DMGS_LAUNCH_CHECK("preprocess_bwd_kernel");
+  return DMGS_OK;
+}
+
+}  // namespace dmgs

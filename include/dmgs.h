@@ -1,0 +1,249 @@
+/*
+ * dmgs.h — C ABI of the GB300 (sm_103a) Gaussian-splatting rasteriser and
+ * mesh->Gaussian face binding.
+ *
+ * Plain pointers and sizes only.  Every pointer argument documented as
+ * "device" is a CUDA device address; every call is asynchronous on the given
+ * stream unless documented otherwise.  Functions return DMGS_OK (0) or a
+ * negative DMGS_ERR_* code; dmgs_last_error() then holds a message for the
+ * calling thread.  No exception crosses this boundary.
+ *
+ * The reference calls its rasteriser through the pybind module
+ * `diff_gaussian_rasterization._C` of the un-vendored submodule
+ * submodules/diff-gaussian-rasterization (.gitmodules:4-6): entry points
+ * `rasterize_gaussians`, `rasterize_gaussians_backward` and `mark_visible`,
+ * reached from `GaussianRasterizer.forward` / `markVisible`, which the
+ * reference tree calls at gaussian_renderer/__init__.py:51,86-94 and
+ * :144,178-186.  The binding entry points replace the torch-op chains of
+ * scene/gaussian_geo_model_mlp_flex.py:267-316,370-385 and
+ * scene/gaussian_geo_model_finetune.py:414-421,446-483.
+ */
+#ifndef DMGS_H
+#define DMGS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *dmgs_stream_t; /* identical to cudaStream_t */
+
+enum {
+  DMGS_OK = 0,
+  DMGS_ERR_ARG = -1,       /* invalid argument: size, null pointer, input mode */
+  DMGS_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+  DMGS_ERR_STATE = -3,     /* a state buffer is smaller than required */
+  DMGS_ERR_PREFILTER = -4, /* prefiltered=1 but a point failed the frustum test */
+  DMGS_ERR_OVERFLOW = -5,  /* a capacity-bounded buffer ran out of instance slots */
+  DMGS_ERR_DEVICE = -6     /* a kernel reported a bounds or wait-limit failure */
+};
+
+#define DMGS_TILE 16 /* tile edge in pixels (16 x 16 tiles) */
+
+/* Per-view constants: the fields of GaussianRasterizationSettings
+ * (built at gaussian_renderer/__init__.py:36-49). */
+typedef struct DmgsView {
+  int32_t width, height;   /* image size in pixels */
+  float tanfovx, tanfovy;  /* tan(FoV/2) */
+  float scale_modifier;    /* multiplies `scales` (scale/rotation mode) */
+  int32_t sh_degree;       /* active SH degree D, 0..3 */
+  int32_t prefiltered;     /* 1: caller guarantees every point is in front of z=0.2 */
+  int32_t debug;           /* 1: synchronise and check after every kernel */
+  const float *bg;         /* [3] device, background colour */
+  const float *viewmatrix; /* [16] device, world->view, column-major
+                              (scene/cameras.py:54 storage) */
+  const float *projmatrix; /* [16] device, world->clip (scene/cameras.py:56) */
+  const float *campos;     /* [3] device, camera centre (scene/cameras.py:57) */
+} DmgsView;
+
+/* Gaussian inputs.  Exactly one of {shs, colors_precomp} and exactly one of
+ * {scales+rotations, cov3D_precomp} must be non-NULL (the reference raises
+ * otherwise).  All arrays are device, fp32, contiguous. */
+typedef struct DmgsGaussians {
+  int32_t P;                   /* number of Gaussians */
+  int32_t M;                   /* SH coefficients per Gaussian in `shs` */
+  const float *means3D;        /* [P,3] */
+  const float *opacities;      /* [P] (activated) */
+  const float *shs;            /* [P,M,3] coefficient-major, or NULL */
+  const float *colors_precomp; /* [P,3] or NULL */
+  const float *scales;         /* [P,3] or NULL */
+  const float *rotations;      /* [P,4] quaternion (r,x,y,z), used as given */
+  const float *cov3D_precomp;  /* [P,6] (xx,xy,xz,yy,yz,zz) or NULL */
+} DmgsGaussians;
+
+/* Gradient outputs of the backward pass (all device, fp32).  Every array
+ * given is fully written (zeros for culled Gaussians); NULL entries are
+ * skipped.  dL_dmeans2D is w.r.t. NDC (x, y); its third column is zero. */
+typedef struct DmgsGrads {
+  float *dL_dmeans2D;   /* [P,3] */
+  float *dL_dcolors;    /* [P,3] */
+  float *dL_dopacity;   /* [P]   */
+  float *dL_dmeans3D;   /* [P,3] */
+  float *dL_dcov3D;     /* [P,6] */
+  float *dL_dsh;        /* [P,M,3] */
+  float *dL_dscales;    /* [P,3] */
+  float *dL_drotations; /* [P,4] */
+} DmgsGrads;
+
+/* ---------------------------------------------------------------------- *
+ * State buffers.  The forward pass keeps three caller-owned device buffers
+ * (the reference's geomBuffer / binningBuffer / imgBuffer) that the
+ * backward pass reads again.  Sizes in bytes; every buffer 256-B aligned.
+ * ---------------------------------------------------------------------- */
+size_t dmgs_geom_state_bytes(int32_t P, int32_t width, int32_t height);
+size_t dmgs_binning_state_bytes(int64_t num_rendered, int32_t width, int32_t height);
+size_t dmgs_image_state_bytes(int32_t width, int32_t height);
+size_t dmgs_bwd_scratch_bytes(int32_t P);
+
+/* Forward, phase 1 (replaces the preprocess + tile-count half of
+ * `rasterize_gaussians`): per-Gaussian projection, covariance, conic, radius,
+ * SH colour and tile rectangle; per-tile instance counts and offsets.
+ * Writes radii [P] (device, int32).  Synchronises the stream once and
+ * returns the number of (tile, Gaussian) instances in *num_rendered (host). */
+int dmgs_raster_fwd_geometry(const DmgsView *view, const DmgsGaussians *g,
+                             void *geom_state, size_t geom_bytes, int32_t *radii,
+                             int64_t *num_rendered, dmgs_stream_t stream);
+
+/* Forward, phase 2 (replaces the binning + blend half of
+ * `rasterize_gaussians`): emits the instances, sorts every tile's list by
+ * (depth, index), writes tile ranges and blends out_color [3,H,W] (device). */
+int dmgs_raster_fwd_render(const DmgsView *view, const DmgsGaussians *g,
+                           void *geom_state, size_t geom_bytes,
+                           void *binning_state, size_t binning_bytes,
+                           int64_t num_rendered, void *image_state,
+                           size_t image_bytes, float *out_color,
+                           dmgs_stream_t stream);
+
+/* One-call forward with caller allocation callbacks (the reference's
+ * resize-functor design): alloc(ctx, which, bytes) returns a device buffer
+ * of at least `bytes` for which = 0 (geometry), 1 (binning), 2 (image), or
+ * NULL on failure.  Returns num_rendered in *num_rendered. */
+typedef void *(*dmgs_alloc_fn)(void *ctx, int32_t which, size_t bytes);
+int dmgs_raster_fwd(const DmgsView *view, const DmgsGaussians *g,
+                    dmgs_alloc_fn alloc, void *alloc_ctx, int32_t *radii,
+                    float *out_color, int64_t *num_rendered,
+                    dmgs_stream_t stream);
+
+/* Backward (replaces `rasterize_gaussians_backward`): blend adjoint then
+ * preprocess adjoint.  dL_dout_color [3,H,W] device.  `bwd_scratch` holds
+ * dmgs_bwd_scratch_bytes(P) bytes. */
+int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g,
+                    const float *dL_dout_color, const void *geom_state,
+                    size_t geom_bytes, const void *binning_state,
+                    size_t binning_bytes, int64_t num_rendered,
+                    const void *image_state, size_t image_bytes,
+                    void *bwd_scratch, size_t bwd_scratch_bytes,
+                    const DmgsGrads *grads, dmgs_stream_t stream);
+
+/* Frustum test (replaces `mark_visible`): present[i] = 1 iff point i lies in
+ * front of view-space z = 0.2.  present: [P] uint8 device. */
+int dmgs_mark_visible(int32_t P, const float *means3D, const float *viewmatrix,
+                      const float *projmatrix, uint8_t *present,
+                      dmgs_stream_t stream);
+
+/* ---------------------------------------------------------------------- *
+ * Debug views of the forward state (tests): copy the integer binning
+ * outputs to device arrays.  rect: [P,4] int32 (xmin,ymin,xmax,ymax) tile
+ * rectangle (zeros when culled); tiles_touched [P] uint32; depth [P] f32;
+ * keys [K] uint64 ((tile<<32)|depth_bits), values [K] uint32, ranges [T,2]
+ * uint32.  Any output may be NULL.
+ * ---------------------------------------------------------------------- */
+int dmgs_debug_geometry(int32_t P, int32_t width, int32_t height,
+                        const void *geom_state, size_t geom_bytes,
+                        int32_t *rect, uint32_t *tiles_touched, float *depth,
+                        float *xy, float *conic_opacity, float *rgb,
+                        dmgs_stream_t stream);
+int dmgs_debug_binning(int32_t P, int32_t width, int32_t height,
+                       int64_t num_rendered, const void *geom_state,
+                       size_t geom_bytes, const void *binning_state,
+                       size_t binning_bytes, uint64_t *keys, uint32_t *values,
+                       uint32_t *ranges, dmgs_stream_t stream);
+int dmgs_debug_image(int32_t width, int32_t height, const void *image_state,
+                     size_t image_bytes, float *final_T, uint32_t *n_contrib,
+                     dmgs_stream_t stream);
+
+/* ---------------------------------------------------------------------- *
+ * Mesh -> Gaussian face binding, stage-2 form
+ * (scene/gaussian_geo_model_mlp_flex.py:258-335 renew_gaussian,
+ *  :370-385 get_covariance_dyn; geo/mesh_utils.py:16-57).
+ * Per face f with vertices v0,v1,v2: frame R = [x, y, n] (x = unit(v1-v0),
+ * n = unit((v1-v0) x (v2-v0)), y = unit(n x x)); Gaussian g of the face sits
+ * at bc[g] . (v0,v1,v2); the face covariance is (R L k)(R L k)^T packed to 6
+ * floats with L = [[s, m01 s, 0], [0, m11 s, 0], [0, 0, z_scale]],
+ * s = |v1-v0| rad_base, (m01, m11) the affine map of the equilateral
+ * triangle onto the face (identity when adaptive_cov = 0), and
+ * k = tanh(scale_factor) * max_scale.  Gradients flow to the vertices through
+ * the means and through R only (L is a constant, as in the reference).
+ * ---------------------------------------------------------------------- */
+typedef struct DmgsFaceBinding {
+  int32_t F;             /* faces */
+  int32_t V;             /* vertices */
+  int32_t G;             /* Gaussians per face */
+  int32_t bc_per_gaussian; /* 1: bc is [F*G,3]; 0: bc is a shared [G,3] table */
+  int32_t adaptive_cov;  /* 1: affine covariance (reference default) */
+  float rad_base;        /* generate_barycentric_v2 radius for G */
+  float z_scale;         /* spatial_lr_scale * 1e-6 */
+  float max_scale;       /* 2.0 in the reference */
+  const float *verts;    /* [V,3] device */
+  const int64_t *faces;  /* [F,3] device */
+  const float *bc;       /* barycentric weights, device */
+  const float *scale_factor; /* [1] device (pre-tanh) */
+} DmgsFaceBinding;
+
+/* Forward: xyz [F*G,3], cov [F*G,6] (device); rot_t2w [F,9] (row-major 3x3,
+ * may be NULL) and cov3D_L [F,9] (may be NULL). */
+int dmgs_bind_fwd(const DmgsFaceBinding *b, float *xyz, float *cov,
+                  float *rot_t2w, float *cov3D_L, dmgs_stream_t stream);
+
+/* Adjoint: from dL_dxyz [F*G,3] and dL_dcov [F*G,6] (either may be NULL)
+ * accumulate dL_dverts [V,3] (zeroed here) and dL_dscale_factor [1]
+ * (zeroed here, may be NULL). */
+int dmgs_bind_bwd(const DmgsFaceBinding *b, const float *dL_dxyz,
+                  const float *dL_dcov, float *dL_dverts,
+                  float *dL_dscale_factor, dmgs_stream_t stream);
+
+/* Stage-3 form (scene/gaussian_geo_model_finetune.py:396-421 renew_gaussian,
+ * :446-483 get_scaling / get_rotation / get_rot_matrix): per Gaussian
+ * xyz = bc . tri, scales = (exp(s0), exp(s1), thin_z), rotation = the unit
+ * quaternion of R_t2w * [[a,-b,0],[b,a,0],[0,0,1]] with (a,b) = unit(rot2d).
+ * The quaternion's sign is fixed so that its real part is >= 0. */
+typedef struct DmgsFaceBinding3 {
+  int32_t F, V, G;
+  float thin_z;             /* thin_z_scale */
+  const float *verts;       /* [V,3] */
+  const int64_t *faces;     /* [F,3] */
+  const float *bc;          /* [G,3] shared table */
+  const float *scaling2d;   /* [F*G,2] pre-activation */
+  const float *rotation2d;  /* [F*G,2] */
+} DmgsFaceBinding3;
+
+int dmgs_bind3_fwd(const DmgsFaceBinding3 *b, float *xyz, float *scales,
+                   float *rotations, dmgs_stream_t stream);
+/* Adjoint: dL_dverts [V,3], dL_dscaling2d [F*G,2], dL_drotation2d [F*G,2]
+ * (all zeroed/written here; any may be NULL except dL_dverts). */
+int dmgs_bind3_bwd(const DmgsFaceBinding3 *b, const float *dL_dxyz,
+                   const float *dL_dscales, const float *dL_drotations,
+                   float *dL_dverts, float *dL_dscaling2d,
+                   float *dL_drotation2d, dmgs_stream_t stream);
+
+/* ---------------------------------------------------------------------- *
+ * Kernel timing (a profiling aid with no counterpart in the reference).
+ * While enabled, every kernel this library launches is bracketed by CUDA
+ * events on its own stream.  dmgs_timing_collect synchronises on the
+ * recorded events, returns per-kernel totals (at most *n entries; *n is set
+ * to the number written) and resets them.  Names stay valid until unload.
+ * ---------------------------------------------------------------------- */
+int dmgs_timing_enable(int32_t on);
+int dmgs_timing_collect(int32_t *n, const char **names, double *total_ms,
+                        int64_t *launches);
+
+/* Library information. */
+const char *dmgs_last_error(void);
+int32_t dmgs_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMGS_H */

@@ -1,0 +1,95 @@
+"""The C ABI library: it loads, exports every symbol include/dmgs.h
+declares, and rejects invalid arguments on the host (no GPU needed: these
+paths return before any CUDA call)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from dmgs_gb300 import _lib
+from dmgs_gb300.build import build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build()
+    return _lib.load()
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "dmgs.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"\b(dmgs_[a-z0-9_]+)\s*\(", src)
+    return sorted(set(n for n in names if n != "dmgs_alloc_fn"))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) >= 18
+    for n in names:
+        assert hasattr(lib, n), n
+    bound = {s[0] for s in _lib.SIGNATURES}
+    assert set(names) == bound
+
+
+def test_sizes_are_consistent(lib):
+    assert lib.dmgs_abi_version() == 1
+    g1 = lib.dmgs_geom_state_bytes(1000, 256, 256)
+    g2 = lib.dmgs_geom_state_bytes(2000, 256, 256)
+    assert g2 > g1 and g1 % 256 == 0
+    assert lib.dmgs_binning_state_bytes(0, 256, 256) < lib.dmgs_binning_state_bytes(10**6, 256, 256)
+    # 20 bytes per instance (keys, merge scratch, sorted index)
+    d = lib.dmgs_binning_state_bytes(2 * 10**6, 64, 64) - lib.dmgs_binning_state_bytes(10**6, 64, 64)
+    assert 19 * 10**6 <= d <= 21 * 10**6
+    assert lib.dmgs_image_state_bytes(1237, 822) >= 1237 * 822 * 8
+    assert lib.dmgs_bwd_scratch_bytes(10) >= 480
+
+
+def _view(**kw):
+    v = dict(width=64, height=64, tanfovx=0.5, tanfovy=0.5, scale_modifier=1.0, sh_degree=3,
+             prefiltered=0, debug=0, bg=8, viewmatrix=8, projmatrix=8, campos=8)
+    v.update(kw)
+    return _lib.DmgsView(**v)
+
+
+def _gauss(**kw):
+    g = dict(P=10, M=16, means3D=16, opacities=16, shs=16, colors_precomp=None, scales=16,
+             rotations=16, cov3D_precomp=None)
+    g.update(kw)
+    return _lib.DmgsGaussians(**g)
+
+
+def _fwd(lib, view, g):
+    K = C.c_int64(0)
+    return lib.dmgs_raster_fwd_geometry(view, g, 16, 1 << 30, 16, C.byref(K), None)
+
+
+def test_input_mode_rules(lib):
+    assert _fwd(lib, _view(), _gauss(shs=None)) == -1
+    assert b"exactly one of either SHs" in lib.dmgs_last_error()
+    assert _fwd(lib, _view(), _gauss(colors_precomp=16)) == -1
+    assert _fwd(lib, _view(), _gauss(cov3D_precomp=16)) == -1
+    assert b"scale/rotation" in lib.dmgs_last_error()
+    assert _fwd(lib, _view(), _gauss(scales=None)) == -1
+    assert _fwd(lib, _view(), _gauss(M=4)) == -1          # degree 3 needs 16 coefficients
+    assert _fwd(lib, _view(), _gauss(rotations=20)) == -1  # misaligned quaternions
+
+
+def test_view_validation(lib):
+    assert _fwd(lib, _view(width=0), _gauss()) == -1
+    assert _fwd(lib, _view(sh_degree=4), _gauss()) == -1
+    assert _fwd(lib, _view(bg=None), _gauss()) == -1
+    assert _fwd(lib, _view(tanfovx=0.0), _gauss()) == -1
+
+
+def test_state_size_checks(lib):
+    K = C.c_int64(0)
+    need = lib.dmgs_geom_state_bytes(10, 64, 64)
+    assert lib.dmgs_raster_fwd_geometry(_view(), _gauss(), 16, need - 1, 16, C.byref(K), None) == -3
+    assert lib.dmgs_raster_fwd_render(_view(), _gauss(), 16, need, 16, 0, 5, 16, 1 << 20, 16, None) == -3
+    assert lib.dmgs_raster_fwd_render(_view(), _gauss(), 16, need, 16, 1 << 30, 5, 16, 0, 16, None) == -3
+    assert lib.dmgs_bind_fwd(None, None, None, None, None, None) == -1
+    assert lib.dmgs_mark_visible(-1, None, None, None, None, None) == -1

@@ -1,0 +1,206 @@
+"""GPU parity of the rasteriser (C ABI) against the CPU oracle.
+
+Bars: integer outputs (radii, tile rectangles, tiles_touched, depth keys,
+sorted keys/values, tile ranges, n_contrib) bit-exact; images within
+2e-4 max-abs on pixels whose value FP32 can decide (the oracle flags the
+rest); gradients within 1e-3 relative L2 per input.
+"""
+import numpy as np
+import pytest
+import torch
+
+from dmgs_gb300.scenes import small_scene
+from helpers import GRAD_NAMES, MODES, AbiRun, mode_inputs, oracle_camera, rel_l2
+from oracle import raster as R
+
+pytestmark = pytest.mark.gpu
+
+IMG_TOL = 2e-4
+GRAD_TOL = 1e-3
+
+
+def _check_integer_outputs(run, ref, cam):
+    dv = run.debug_views()
+    g = ref.geom
+    vis = g["visible"]
+    np.testing.assert_array_equal(run.radii.cpu().numpy()[:run.P], ref.radii)
+    rect_ref = np.where(vis[:, None], g["rect"], 0)
+    np.testing.assert_array_equal(dv["rect"], rect_ref)
+    np.testing.assert_array_equal(dv["tiles_touched"], g["tiles_touched"])
+    np.testing.assert_array_equal(dv["depth"][vis].view(np.uint32), g["depth"][vis].view(np.uint32))
+    assert run.K == ref.num_rendered
+    np.testing.assert_array_equal(dv["keys"], ref.keys)
+    np.testing.assert_array_equal(dv["values"], ref.values)
+    np.testing.assert_array_equal(dv["ranges"], ref.ranges)
+    return dv
+
+
+@pytest.mark.parametrize("mode", MODES, ids=["-".join(m) for m in MODES])
+def test_cfg1_forward_backward(mode):
+    """10k Gaussians, 256x256: the plain-rasteriser workload, all four input modes."""
+    sc = small_scene()
+    view = sc.views[0]
+    inp = mode_inputs(sc, mode)
+    cam = oracle_camera(view)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], colors=inp["colors"],
+                   scales=inp["scales"], rotations=inp["rotations"], cov3D=inp["cov3D"])
+    run = AbiRun(view, inp).forward()
+    dv = _check_integer_outputs(run, ref, cam)
+    img = run.color.cpu().numpy()
+    ok = ~ref.ambiguous
+    err = np.abs(img - ref.image)[:, ok].max()
+    assert err <= IMG_TOL, err
+    np.testing.assert_array_equal(dv["n_contrib"][ok], ref.n_contrib[ok])
+    assert np.abs(dv["final_T"] - ref.final_T)[ok].max() <= IMG_TOL
+
+    dimg = np.random.default_rng(0).standard_normal(img.shape).astype(np.float32)
+    gk = run.backward(dimg)
+    go = ref.backward(dimg)
+    for name, gref in go.items():
+        mine = gk[GRAD_NAMES[name]]
+        assert np.isfinite(mine).all(), name
+        e = rel_l2(mine, gref)
+        assert e <= GRAD_TOL, (name, e)
+
+
+def test_background_and_scale_modifier():
+    sc = small_scene(P=3000, width=200, height=120, seed=3)
+    view = sc.views[0]
+    inp = mode_inputs(sc, ("shs", "sr"))
+    bg = (0.2, 0.5, 1.0)
+    cam = oracle_camera(view, bg=bg, scale_modifier=1.7)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], scales=inp["scales"],
+                   rotations=inp["rotations"])
+    run = AbiRun(view, inp, bg=bg, scale_modifier=1.7).forward()
+    _check_integer_outputs(run, ref, cam)
+    ok = ~ref.ambiguous
+    assert np.abs(run.color.cpu().numpy() - ref.image)[:, ok].max() <= IMG_TOL
+    dimg = np.random.default_rng(1).standard_normal((3, 120, 200)).astype(np.float32)
+    gk, go = run.backward(dimg), ref.backward(dimg)
+    for name, gref in go.items():
+        assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
+
+
+@pytest.mark.parametrize("deg", [0, 1, 2])
+def test_lower_sh_degrees(deg):
+    sc = small_scene(P=2000, width=96, height=80, seed=4)
+    view = sc.views[0]
+    inp = mode_inputs(sc, ("shs", "sr"))
+    cam = oracle_camera(view, sh_degree=deg)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], scales=inp["scales"],
+                   rotations=inp["rotations"])
+    run = AbiRun(view, inp, sh_degree=deg).forward()
+    ok = ~ref.ambiguous
+    assert np.abs(run.color.cpu().numpy() - ref.image)[:, ok].max() <= IMG_TOL
+    dimg = np.random.default_rng(2).standard_normal((3, 80, 96)).astype(np.float32)
+    gk, go = run.backward(dimg), ref.backward(dimg)
+    for name, gref in go.items():
+        assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
+    # coefficients above the active degree get zero gradient
+    assert np.all(gk["shs"][:, (deg + 1) ** 2:, :] == 0)
+
+
+def test_empty_and_all_culled():
+    sc = small_scene(P=500, width=64, height=64, seed=5)
+    view = sc.views[0]
+    # everything behind the camera: move the means far behind
+    inp = mode_inputs(sc, ("colors", "sr"))
+    eye = view.campos.astype(np.float64)
+    inp["means3D"] = (eye + 3.0 * (eye / np.linalg.norm(eye))
+                      + 0.1 * inp["means3D"]).astype(np.float32)
+    run = AbiRun(view, inp, bg=(0.3, 0.2, 0.1)).forward()
+    assert run.K == 0
+    assert (run.radii.cpu().numpy()[:run.P] == 0).all()
+    img = run.color.cpu().numpy()
+    np.testing.assert_allclose(img, np.broadcast_to(np.array([0.3, 0.2, 0.1], np.float32)[:, None, None], img.shape))
+    gk = run.backward(np.ones((3, 64, 64), np.float32))
+    for k, v in gk.items():
+        if v is not None:
+            assert (v == 0).all(), k
+    # P == 0
+    empty = {k: (None if v is None else v[:0]) for k, v in mode_inputs(sc, ("colors", "sr")).items()}
+    run0 = AbiRun(view, empty, bg=(1.0, 1.0, 1.0)).forward()
+    assert run0.K == 0
+    assert np.all(run0.color.cpu().numpy() == 1.0)
+
+
+def test_ragged_image_and_long_tile_lists():
+    """Image size not a multiple of 16, and > 4096 Gaussians in single tiles
+    (the segment sort's chunk-and-merge path)."""
+    rng = np.random.default_rng(11)
+    P = 12000
+    sc = small_scene(P=P, width=37, height=21, seed=6)
+    # concentrate everything in a small volume in front of the camera
+    view = sc.views[0]
+    eye = view.campos.astype(np.float64)
+    fwd = -eye / np.linalg.norm(eye)
+    sc.means3D[:] = (eye + 2.0 * fwd + rng.normal(0, 0.02, (P, 3))).astype(np.float32)
+    sc.scales[:] = np.exp(rng.uniform(-5, -3.5, (P, 3))).astype(np.float32)
+    sc.opacities[:] = 0.05
+    inp = mode_inputs(sc, ("shs", "sr"))
+    cam = oracle_camera(view)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], scales=inp["scales"],
+                   rotations=inp["rotations"])
+    assert (ref.ranges[:, 1] - ref.ranges[:, 0]).max() > 4096
+    run = AbiRun(view, inp).forward()
+    _check_integer_outputs(run, ref, cam)
+    ok = ~ref.ambiguous
+    assert np.abs(run.color.cpu().numpy() - ref.image)[:, ok].max() <= IMG_TOL
+    dimg = rng.standard_normal((3, 21, 37)).astype(np.float32)
+    gk, go = run.backward(dimg), ref.backward(dimg)
+    for name, gref in go.items():
+        assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
+
+
+def test_large_footprints_and_clamped_jacobian():
+    """Gaussians close to the camera (hundreds of tiles each) and beyond the
+    1.3x field-of-view clamp."""
+    rng = np.random.default_rng(12)
+    sc = small_scene(P=300, width=160, height=96, seed=7)
+    view = sc.views[0]
+    eye = view.campos.astype(np.float64)
+    fwd = -eye / np.linalg.norm(eye)
+    side = np.cross(fwd, [0, 1, 0]); side /= np.linalg.norm(side)
+    d = rng.uniform(0.5, 1.5, (300, 1))
+    lat = rng.uniform(-1.2, 1.2, (300, 1)) * d
+    sc.means3D[:] = (eye + d * fwd + lat * side + rng.normal(0, 0.05, (300, 3))).astype(np.float32)
+    sc.scales[:] = np.exp(rng.uniform(-3, -1.5, (300, 3))).astype(np.float32)
+    inp = mode_inputs(sc, ("shs", "sr"))
+    cam = oracle_camera(view)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], scales=inp["scales"],
+                   rotations=inp["rotations"])
+    run = AbiRun(view, inp).forward()
+    _check_integer_outputs(run, ref, cam)
+    ok = ~ref.ambiguous
+    assert np.abs(run.color.cpu().numpy() - ref.image)[:, ok].max() <= IMG_TOL
+    dimg = rng.standard_normal((3, 96, 160)).astype(np.float32)
+    gk, go = run.backward(dimg), ref.backward(dimg)
+    for name, gref in go.items():
+        assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
+
+
+def test_prefiltered_violation_is_an_error():
+    sc = small_scene(P=100, width=32, height=32, seed=8)
+    view = sc.views[0]
+    inp = mode_inputs(sc, ("colors", "sr"))
+    eye = view.campos.astype(np.float64)
+    inp["means3D"][0] = (eye * 2.0).astype(np.float32)  # behind the camera
+    from dmgs_gb300._lib import DmgsError
+    with pytest.raises(DmgsError) as ei:
+        AbiRun(view, inp, prefiltered=True).forward()
+    assert ei.value.code == -4
+
+
+def test_mark_visible_matches_oracle():
+    from dmgs_gb300 import GaussianRasterizationSettings, GaussianRasterizer
+    sc = small_scene(P=5000, seed=9)
+    view = sc.views[0]
+    d = "cuda"
+    rs = GaussianRasterizationSettings(view.height, view.width, view.tanfovx, view.tanfovy,
+                                       torch.zeros(3, device=d), 1.0,
+                                       torch.tensor(view.viewmatrix, device=d),
+                                       torch.tensor(view.projmatrix, device=d), 3,
+                                       torch.tensor(view.campos, device=d), False, False)
+    pts = np.random.default_rng(0).uniform(-8, 8, (5000, 3)).astype(np.float32)
+    vis = GaussianRasterizer(rs).markVisible(torch.tensor(pts, device=d)).cpu().numpy()
+    np.testing.assert_array_equal(vis, R.mark_visible(pts, view.viewmatrix))

@@ -1,0 +1,97 @@
+"""The oracle's conventions pinned against vectors produced by the
+reference's own Python (tests/golden/make_golden.py)."""
+import os
+
+import numpy as np
+import torch
+
+from dmgs_gb300 import camera as cammod
+from oracle import binding as OB
+from oracle import raster as R
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_sh_polynomial_matches_reference():
+    z = np.load(os.path.join(GOLD, "sh_golden.npz"))
+    sh = torch.tensor(z["sh"], dtype=torch.float64).transpose(1, 2)  # -> [n,16,3]
+    dirs = torch.tensor(z["dirs"], dtype=torch.float64)
+    for d in range(4):
+        mine = (R.eval_sh_rgb(d, sh, dirs) - 0.5).numpy()
+        np.testing.assert_allclose(mine, z[f"deg{d}"], rtol=1e-5, atol=1e-6)
+
+
+def test_rotation_and_covariance_packing_match_reference():
+    z = np.load(os.path.join(GOLD, "rot_golden.npz"))
+    q = torch.tensor(z["q"], dtype=torch.float64)
+    qn = q / q.norm(dim=1, keepdim=True)
+    np.testing.assert_allclose(R._quat_to_rot(qn).numpy(), z["R"], atol=1e-6)
+    qn32 = (z["q"] / np.linalg.norm(z["q"], axis=1, keepdims=True)).astype(np.float32)
+    cov = R.cov3d_from_scale_rot_f32(z["s"], qn32, 1.0)
+    np.testing.assert_allclose(cov, z["cov"], rtol=1e-4, atol=1e-7)
+
+
+def test_camera_matrices_match_reference():
+    z = np.load(os.path.join(GOLD, "camera_golden.npz"))
+    for i in range(3):
+        Rm, T = z[f"R{i}"], z[f"T{i}"]
+        eye = -Rm @ T  # camera centre: T = -R^T eye
+        W2V = cammod.world_to_view(Rm, eye)
+        np.testing.assert_allclose(W2V.T, z[f"view{i}"], atol=1e-5)
+        Pm = cammod.projection(0.01, 100.0, float(z[f"fovx{i}"]), float(z[f"fovy{i}"]))
+        np.testing.assert_allclose(Pm.T, z[f"proj{i}"], rtol=1e-6, atol=1e-6)
+        np.testing.assert_allclose((Pm @ W2V).T, z[f"full{i}"], rtol=1e-5, atol=1e-5)
+        np.testing.assert_allclose(eye, z[f"center{i}"], atol=1e-5)
+
+
+def test_look_at_convention():
+    v = cammod.make_view((0.0, 0.0, -4.0), (0, 0, 0), 64, 48, fovx_deg=50)
+    V = v.viewmatrix.reshape(16)
+    # the target maps to the optical axis, in front of the camera
+    p = np.array([0, 0, 0, 1], np.float32) @ v.viewmatrix
+    assert abs(p[0]) < 1e-6 and abs(p[1]) < 1e-6 and p[2] > 3.99
+    # world +y (up) projects to smaller image y (image y points down)
+    q = np.array([0, 0.5, 0, 1], np.float32) @ v.viewmatrix
+    assert q[1] < 0
+    assert V.shape == (16,)
+
+
+def test_barycentric_table_matches_reference():
+    z = np.load(os.path.join(GOLD, "binding_golden.npz"))
+    for G in (1, 3, 6):
+        bc, rad = OB.barycentric_table(G)
+        np.testing.assert_allclose(bc.numpy(), z[f"G{G}_a_bc"], atol=1e-7)
+        assert abs(rad - float(z[f"G{G}_a_rad"])) < 1e-9
+
+
+def test_stage2_binding_oracle_matches_reference():
+    z = np.load(os.path.join(GOLD, "binding_golden.npz"))
+    for G in (1, 3, 6):
+        for adaptive in (True, False):
+            tag = f"G{G}_{'a' if adaptive else 'n'}"
+            v = torch.tensor(z["verts"], dtype=torch.float64, requires_grad=True)
+            sf = torch.tensor([0.37], dtype=torch.float64, requires_grad=True)
+            bc, rad = OB.barycentric_table(G)
+            xyz, cov, Rm, L = OB.bind_stage2(v, torch.tensor(z["faces"]), bc, rad, 4e-6, sf, 2.0, adaptive)
+            np.testing.assert_allclose(xyz.detach().numpy(), z[f"{tag}_xyz"], rtol=1e-5, atol=1e-6)
+            np.testing.assert_allclose(cov.detach().numpy(), z[f"{tag}_cov"], rtol=1e-4, atol=1e-9)
+            np.testing.assert_allclose(L.numpy(), z[f"{tag}_covL"], rtol=1e-5, atol=1e-8)
+            ((xyz * torch.tensor(z[f"{tag}_gxyz"], dtype=torch.float64)).sum()
+             + (cov * torch.tensor(z[f"{tag}_gcov"], dtype=torch.float64)).sum()).backward()
+            g = v.grad.numpy()
+            assert np.linalg.norm(g - z[f"{tag}_dverts"]) / np.linalg.norm(z[f"{tag}_dverts"]) < 1e-4
+            assert abs(sf.grad.item() - z[f"{tag}_dsf"][0]) <= 1e-4 * abs(z[f"{tag}_dsf"][0])
+
+
+def test_stage3_binding_oracle_matches_reference():
+    z = np.load(os.path.join(GOLD, "binding3_golden.npz"))
+    v = torch.tensor(z["verts"], dtype=torch.float64)
+    xyz, scales, Rm, q = OB.bind_stage3(v, torch.tensor(z["faces"]), torch.tensor(z["bc"], dtype=torch.float64),
+                                        torch.tensor(z["scaling2d"], dtype=torch.float64),
+                                        torch.tensor(z["rotation2d"], dtype=torch.float64), float(z["thin_z"]))
+    np.testing.assert_allclose(xyz.numpy(), z["xyz"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(scales.numpy(), z["scales"], rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(Rm.numpy(), z["R"], atol=1e-5)
+    # the quaternion reproduces the rotation
+    np.testing.assert_allclose(R._quat_to_rot(q).numpy(), z["R"], atol=1e-5)
+    assert (q[:, 0] >= 0).all()
