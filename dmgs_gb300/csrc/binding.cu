@@ -31,6 +31,12 @@ __device__ __forceinline__ float norm(f3 a) { return sqrtf(dot(a, a)); }
 
 constexpr float NRM_EPS = 1e-12f;  // torch.nn.functional.normalize default eps
 
+// Faces whose vertex indices leave [0, V) are skipped (their outputs are
+// left as written by the caller; no gradient is scattered).
+__device__ __forceinline__ bool face_ok(int64_t i0, int64_t i1, int64_t i2, int V) {
+  return i0 >= 0 && i1 >= 0 && i2 >= 0 && i0 < V && i1 < V && i2 < V;
+}
+
 __device__ __forceinline__ f3 load_v(const float *verts, int64_t i) {
   return mk(verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]);
 }
@@ -105,6 +111,7 @@ __global__ void bind_fwd_kernel(DmgsFaceBinding b, float *__restrict__ xyz,
   if (f >= b.F) return;
   const int64_t i0 = b.faces[3 * (size_t)f], i1 = b.faces[3 * (size_t)f + 1],
                 i2 = b.faces[3 * (size_t)f + 2];
+  if (!face_ok(i0, i1, i2, b.V)) return;
   const f3 v0 = load_v(b.verts, i0), v1 = load_v(b.verts, i1), v2 = load_v(b.verts, i2);
   const Frame F = face_frame(v0, v1, v2);
   float L[9];
@@ -146,6 +153,7 @@ __global__ void bind_bwd_kernel(DmgsFaceBinding b, const float *__restrict__ dxy
   if (f < b.F) {
     const int64_t i0 = b.faces[3 * (size_t)f], i1 = b.faces[3 * (size_t)f + 1],
                   i2 = b.faces[3 * (size_t)f + 2];
+    if (face_ok(i0, i1, i2, b.V)) {
     const f3 v0 = load_v(b.verts, i0), v1 = load_v(b.verts, i1), v2 = load_v(b.verts, i2);
     f3 g0 = mk(0.f, 0.f, 0.f), g1 = g0, g2 = g0;
     float gc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -204,6 +212,7 @@ __global__ void bind_bwd_kernel(DmgsFaceBinding b, const float *__restrict__ dxy
     atomicAdd(dverts + 3 * i0, g0.x); atomicAdd(dverts + 3 * i0 + 1, g0.y); atomicAdd(dverts + 3 * i0 + 2, g0.z);
     atomicAdd(dverts + 3 * i1, g1.x); atomicAdd(dverts + 3 * i1 + 1, g1.y); atomicAdd(dverts + 3 * i1 + 2, g1.z);
     atomicAdd(dverts + 3 * i2, g2.x); atomicAdd(dverts + 3 * i2 + 1, g2.y); atomicAdd(dverts + 3 * i2 + 2, g2.z);
+    }
   }
   if (dsf) {
     const float s = warp_sum(dk_local);
@@ -306,6 +315,7 @@ __global__ void bind3_fwd_kernel(DmgsFaceBinding3 b, float *__restrict__ xyz,
   if (f >= b.F) return;
   const int64_t i0 = b.faces[3 * (size_t)f], i1 = b.faces[3 * (size_t)f + 1],
                 i2 = b.faces[3 * (size_t)f + 2];
+  if (!face_ok(i0, i1, i2, b.V)) return;
   const f3 v0 = load_v(b.verts, i0), v1 = load_v(b.verts, i1), v2 = load_v(b.verts, i2);
   const Frame F = face_frame(v0, v1, v2);
   const float Rw[9] = {F.x.x, F.y.x, F.n.x, F.x.y, F.y.y, F.n.y, F.x.z, F.y.z, F.n.z};
@@ -347,6 +357,7 @@ __global__ void bind3_bwd_kernel(DmgsFaceBinding3 b, const float *__restrict__ d
   if (f >= b.F) return;
   const int64_t i0 = b.faces[3 * (size_t)f], i1 = b.faces[3 * (size_t)f + 1],
                 i2 = b.faces[3 * (size_t)f + 2];
+  if (!face_ok(i0, i1, i2, b.V)) return;
   const f3 v0 = load_v(b.verts, i0), v1 = load_v(b.verts, i1), v2 = load_v(b.verts, i2);
   const Frame F = face_frame(v0, v1, v2);
   const float Rw[9] = {F.x.x, F.y.x, F.n.x, F.x.y, F.y.y, F.n.y, F.x.z, F.y.z, F.n.z};
