@@ -69,6 +69,9 @@ SIGNATURES = [
     ("dmgs_raster_bwd", C.c_int, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians), vp, vp,
                                   C.c_size_t, vp, C.c_size_t, C.c_int64, vp, C.c_size_t, vp,
                                   C.c_size_t, C.POINTER(DmgsGrads), vp]),
+    ("dmgs_raster_bwd_noalloc", C.c_int, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians), vp,
+                                          vp, C.c_size_t, vp, C.c_size_t, C.c_int64, vp,
+                                          C.c_size_t, C.POINTER(DmgsGrads), vp]),
     ("dmgs_mark_visible", C.c_int, [C.c_int32, vp, vp, vp, vp, vp]),
     ("dmgs_debug_geometry", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, C.c_size_t, vp, vp,
                                       vp, vp, vp, vp, vp]),

@@ -137,6 +137,26 @@ int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g,
                     void *bwd_scratch, size_t bwd_scratch_bytes,
                     const DmgsGrads *grads, dmgs_stream_t stream);
 
+/* Backward for callers that cannot allocate device memory (this entry point
+ * has no counterpart in the reference).  A plugin inside a host application
+ * that owns the device's memory pool, or a real-time loop that must not call
+ * cudaMalloc/cudaFree between frames, cannot hand dmgs_raster_bwd its
+ * scratch buffer; this variant keeps that scratch in a static device array
+ * of the library instead (DMGS_NOALLOC_MAX_GAUSSIANS x 48 bytes = 12 MiB,
+ * held by every GPU that loads the library until exit) and allocates
+ * nothing.  Arguments and results are those of dmgs_raster_bwd without the
+ * scratch pair; g->P above the limit returns DMGS_ERR_ARG.  The first call on
+ * a device looks up the array's address (cudaGetSymbolAddress), so make it
+ * before any stream capture begins.  All calls share the array: calls whose
+ * work overlaps on the GPU race. */
+#define DMGS_NOALLOC_MAX_GAUSSIANS 262144
+int dmgs_raster_bwd_noalloc(const DmgsView *view, const DmgsGaussians *g,
+                            const float *dL_dout_color, const void *geom_state,
+                            size_t geom_bytes, const void *binning_state,
+                            size_t binning_bytes, int64_t num_rendered,
+                            const void *image_state, size_t image_bytes,
+                            const DmgsGrads *grads, dmgs_stream_t stream);
+
 /* Frustum test (replaces `mark_visible`): present[i] = 1 iff point i lies in
  * front of view-space z = 0.2.  present: [P] uint8 device. */
 int dmgs_mark_visible(int32_t P, const float *means3D, const float *viewmatrix,
