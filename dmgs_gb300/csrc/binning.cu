@@ -1,130 +1,351 @@
-// binning.cu — (tile, Gaussian) instance emission and per-tile depth sort.
+// binning.cu — (tile, Gaussian) lists ordered by depth, without sorting the
+// instance list.
 //
-// The reference pipeline (duplicateWithKeys -> radix sort of 64-bit
-// (tile << 32 | depth_bits) keys -> identifyTileRanges) produces, for each
-// tile, the list of covering Gaussians ordered by depth with ties in
-// Gaussian-index order.  Here the tile boundaries are known before any
-// instance is written (tile_start from the difference-grid counts), so:
-//   1. scatter: every visible Gaussian claims one slot per covered tile
-//      inside that tile's segment (atomic cursor per tile) and writes the
-//      unique sort key (depth_bits << 32 | index);
-//   2. segment sort: one CTA per tile sorts its segment in shared memory
-//      (bitonic network; segments longer than the shared capacity are
-//      sorted in chunks and merged through global memory) and writes the
-//      Gaussian indices (point_list) and the tile range.
-// The result equals the reference's sorted value list and ranges exactly:
-// within a tile the key (depth_bits, index) is unique, so the order does
-// not depend on which slot an instance claimed.
+// The reference pipeline (duplicateWithKeys -> radix sort of the 64-bit
+// (tile << 32 | depth_bits) instance keys -> identifyTileRanges) yields, per
+// tile, the covering Gaussians in depth order, ties in Gaussian-index order.
+// The same lists are produced here with work linear in the number of visible
+// Gaussians V plus the instances K:
+//
+//   1. compact   the visible Gaussians in index order: (depth_bits, index)
+//   2. sort      them by depth bits with a stable LSD radix sort (4 x 8-bit
+//                digits) -> depth order, ties in index order;
+//   3. count     the sorted list is cut into C chunks of S Gaussians; each
+//                chunk counts its instances per tile -> count matrix [T][C];
+//   4. scan      the matrix in (tile, chunk) order -> the first slot of every
+//                (tile, chunk) pair, the tile ranges and K;
+//   5. emit      each chunk walks its Gaussians in depth order and appends
+//                each Gaussian index to the lists of the tiles it covers.
+//
+// Because every chunk appends in depth order and chunks are laid out in
+// depth order within every tile, each tile's list is exactly the reference's
+// sorted list.  Nothing of size K is read back or sorted; K is written once.
+// The count matrix (T x C x 4 B, at most 16.6 MB at 4056 tiles) stays in L2.
 #include "kernels.cuh"
 
 namespace dmgs {
 
 namespace {
 
-constexpr int SORT_THREADS = 256;
-constexpr int SORT_CAP = 4096;  // keys sorted in shared memory at once (32 KB)
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Block-wide exclusive scan of one value per thread (u64 accumulation).
+template <int THREADS>
+__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long v,
+                                                                   unsigned long long *total) {
+  __shared__ unsigned long long warp_sums[THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long u = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) warp_sums[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long s = lane < THREADS / 32 ? warp_sums[lane] : 0ull;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long u = __shfl_up_sync(FULL, s, o);
+      if (lane >= o) s += u;
+    }
+    if (lane < THREADS / 32) warp_sums[lane] = s;  // inclusive
+  }
+  __syncthreads();
+  const unsigned long long before = (wid > 0 ? warp_sums[wid - 1] : 0ull) + inc - v;
+  if (total) *total = warp_sums[THREADS / 32 - 1];
+  __syncthreads();
+  return before;
+}
+
+__device__ __forceinline__ uint32_t scan_len(const uint32_t *n_dev, uint32_t n_max) {
+  return n_dev ? min(*n_dev, n_max) : n_max;
+}
+
+// ---- generic exclusive scan (u32, in place), three phases ----------------
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_reduce_kernel(const uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev,
+                   uint32_t n_max, uint32_t *__restrict__ part) {
+  const uint32_t n = scan_len(n_dev, n_max);
+  const uint32_t base = blockIdx.x * SCAN_TILE;
+  if (base >= n) return;
+  unsigned long long s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    const uint32_t k = base + i * SCAN_THREADS + threadIdx.x;
+    if (k < n) s += data[k];
+  }
+  unsigned long long tot;
+  block_exclusive_scan<SCAN_THREADS>(s, &tot);
+  if (threadIdx.x == 0) part[blockIdx.x] = (uint32_t)tot;
+}
+
+// One block: exclusive scan of the per-block partials (or of the whole
+// array when it fits one block); total to *total_out, overflow flagged.
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_single_kernel(uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev, uint32_t n_max,
+                   int partials_of_tiles, uint32_t *__restrict__ total_out,
+                   uint32_t *__restrict__ status) {
+  uint32_t n = scan_len(n_dev, n_max);
+  if (partials_of_tiles) n = (n + SCAN_TILE - 1) / SCAN_TILE;
+  const uint32_t per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
+  const uint32_t beg = min(n, threadIdx.x * per), end = min(n, beg + per);
+  unsigned long long s = 0;
+  for (uint32_t k = beg; k < end; ++k) s += data[k];
+  unsigned long long tot;
+  unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, &tot);
+  for (uint32_t k = beg; k < end; ++k) {
+    const uint32_t v = data[k];
+    data[k] = (uint32_t)run;
+    run += v;
+  }
+  if (threadIdx.x == 0) {
+    if (total_out) *total_out = (uint32_t)tot;
+    if (tot > 0xffffffffull && status) atomicOr(status, ST_OVERFLOW);
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_down_kernel(uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev, uint32_t n_max,
+                 const uint32_t *__restrict__ part) {
+  const uint32_t n = scan_len(n_dev, n_max);
+  const uint32_t base = blockIdx.x * SCAN_TILE;
+  if (base >= n) return;
+  // blocked: thread i owns elements base + i*ITEMS .. +ITEMS-1
+  uint32_t v[SCAN_ITEMS];
+  unsigned long long s = 0;
+  const uint32_t k0 = base + threadIdx.x * SCAN_ITEMS;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    v[i] = (k0 + i < n) ? data[k0 + i] : 0u;
+    s += v[i];
+  }
+  unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, nullptr) + part[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    if (k0 + i < n) data[k0 + i] = (uint32_t)run;
+    run += v[i];
+  }
+}
+
+// ---- compaction of visible Gaussians (index order) ----------------------
+
+__global__ void __launch_bounds__(PRE_BLOCK)
+compact_kernel(int P, const int32_t *__restrict__ radii, const float4 *__restrict__ feat,
+               const uint32_t *__restrict__ blkoff, uint32_t *__restrict__ dkey,
+               uint32_t *__restrict__ dval) {
+  const int idx = blockIdx.x * PRE_BLOCK + threadIdx.x;
+  const bool v = idx < P && radii[idx] > 0;
+  __shared__ uint32_t wcount[PRE_BLOCK / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned b = __ballot_sync(FULL, v);
+  if (lane == 0) wcount[wid] = __popc(b);
+  __syncthreads();
+  uint32_t before = 0;
+  for (int w = 0; w < wid; ++w) before += wcount[w];
+  if (v) {
+    const uint32_t pos = blkoff[blockIdx.x] + before + __popc(b & lanemask_lt());
+    dkey[pos] = __float_as_uint(feat[3 * idx + 2].y);
+    dval[pos] = (uint32_t)idx;
+  }
+}
+
+// One thread: derived sizes from V.
+__global__ void params_kernel(int T, uint32_t *__restrict__ counters) {
+  const uint32_t V = counters[CI_V];
+  const uint32_t nbr = (V + RADIX_TILE - 1) / RADIX_TILE;
+  uint32_t S = (V + CHUNK_COUNT_MAX - 1) / CHUNK_COUNT_MAX;
+  if (S < CHUNK_MIN) S = CHUNK_MIN;
+  const uint32_t C = (V + S - 1) / S;
+  counters[CI_NBR] = nbr;
+  counters[CI_NRH] = 256u * nbr;
+  counters[CI_S] = S;
+  counters[CI_C] = C;
+  counters[CI_NCM] = (uint32_t)T * C;
+}
+
+// ---- stable LSD radix sort of (depth_bits, index), 8 bits per pass -------
+
+__global__ void __launch_bounds__(RADIX_BLOCK)
+radix_hist_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ counters,
+                  int shift, uint32_t *__restrict__ rhist) {
+  const uint32_t V = counters[CI_V], nbr = counters[CI_NBR];
+  const uint32_t b = blockIdx.x;
+  if (b >= nbr) return;
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < RADIX_ITEMS; ++i) {
+    const uint32_t k = b * RADIX_TILE + i * RADIX_BLOCK + threadIdx.x;
+    if (k < V) atomicAdd(&h[(keys[k] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  rhist[threadIdx.x * nbr + b] = h[threadIdx.x];  // digit-major
+}
+
+// Warp w of block b owns keys [b*2048 + w*256, +256), visited in 8 rounds
+// of 32 (round-major, then lane) — the input order, so the pass is stable.
+__global__ void __launch_bounds__(RADIX_BLOCK)
+radix_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
+                     const uint32_t *__restrict__ counters, int shift,
+                     const uint32_t *__restrict__ rhist_scanned) {
+  const uint32_t V = counters[CI_V], nbr = counters[CI_NBR];
+  const uint32_t b = blockIdx.x;
+  if (b >= nbr) return;
+  __shared__ uint32_t wh[RADIX_BLOCK / 32][256];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < (RADIX_BLOCK / 32) * 256; i += RADIX_BLOCK) (&wh[0][0])[i] = 0u;
+  __syncthreads();
+  uint32_t key[RADIX_ITEMS], val[RADIX_ITEMS];
+  int dig[RADIX_ITEMS];
+  const uint32_t base = b * RADIX_TILE + w * (32 * RADIX_ITEMS);
+#pragma unroll
+  for (int r = 0; r < RADIX_ITEMS; ++r) {
+    const uint32_t k = base + r * 32 + lane;
+    const bool ok = k < V;
+    key[r] = ok ? kin[k] : 0u;
+    val[r] = ok ? vin[k] : 0u;
+    dig[r] = ok ? (int)((key[r] >> shift) & 255u) : 256;
+    const unsigned peers = __match_any_sync(FULL, dig[r]);
+    if (dig[r] < 256 && lane == __ffs(peers) - 1) wh[w][dig[r]] += __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;  // RADIX_BLOCK == 256 digits
+    uint32_t run = rhist_scanned[d * nbr + b];
+#pragma unroll
+    for (int w2 = 0; w2 < RADIX_BLOCK / 32; ++w2) {
+      const uint32_t c = wh[w2][d];
+      wh[w2][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RADIX_ITEMS; ++r) {
+    const unsigned peers = __match_any_sync(FULL, dig[r]);
+    uint32_t pos = 0;
+    if (dig[r] < 256) pos = wh[w][dig[r]] + __popc(peers & lanemask_lt());
+    __syncwarp();
+    if (dig[r] < 256) {
+      kout[pos] = key[r];
+      vout[pos] = val[r];
+      if (lane == __ffs(peers) - 1) wh[w][dig[r]] += __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// ---- per-(tile, chunk) counts --------------------------------------------
+
+__device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1, int &y1) {
+  const uint32_t lo = __float_as_uint(f2.z), hi = __float_as_uint(f2.w);
+  x0 = lo & 0xffff; y0 = lo >> 16; x1 = hi & 0xffff; y1 = hi >> 16;
+}
 
 __global__ void __launch_bounds__(256)
-scatter_kernel(int P, int gx, const float4 *__restrict__ feat,
-               uint32_t *__restrict__ cursor, uint64_t *__restrict__ keys, uint32_t K,
-               uint32_t *__restrict__ counters) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= P) return;
-  const float4 f2 = feat[3 * idx + 2];
-  const uint32_t lo = __float_as_uint(f2.z), hi = __float_as_uint(f2.w);
-  const int x0 = lo & 0xffff, y0 = lo >> 16, x1 = hi & 0xffff, y1 = hi >> 16;
-  if (x1 <= x0 || y1 <= y0) return;
-  const uint64_t key = ((uint64_t)__float_as_uint(f2.y) << 32) | (uint32_t)idx;
-  for (int y = y0; y < y1; ++y)
-    for (int x = x0; x < x1; ++x) {
-      const uint32_t pos = atomicAdd(cursor + y * gx + x, 1u);
-      if (pos < K) keys[pos] = key;
-      else atomicOr(counters, ST_BOUNDS);
-    }
+tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
+                  const uint32_t *__restrict__ order, const uint32_t *__restrict__ counters,
+                  uint32_t *__restrict__ cmat) {
+  extern __shared__ uint32_t cnt[];
+  const uint32_t V = counters[CI_V], S = counters[CI_S], C = counters[CI_C];
+  const uint32_t c = blockIdx.x;
+  if (c >= C) return;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = 0u;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t s0 = c * S, s1 = min(V, s0 + S);
+  for (uint32_t s = s0 + w; s < s1; s += nw) {
+    const uint32_t g = order[s];
+    int x0, y0, x1, y1;
+    unpack_rect(feat[3 * g + 2], x0, y0, x1, y1);
+    const int rw = x1 - x0, area = rw * (y1 - y0);
+    for (int j = lane; j < area; j += 32) atomicAdd(&cnt[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < T; t += blockDim.x) cmat[(size_t)t * C + c] = cnt[t];
 }
 
-__global__ void init_cursor_kernel(int T, const uint32_t *__restrict__ tile_start,
-                                   uint32_t *__restrict__ cursor) {
+__global__ void ranges_kernel(int T, const uint32_t *__restrict__ cmat_scanned,
+                              uint32_t *__restrict__ counters, uint2 *__restrict__ ranges) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < T) cursor[t] = tile_start[t];
-}
-
-// Ascending bitonic sort of n2 (power of two) keys in shared memory.
-__device__ __forceinline__ void bitonic_smem(uint64_t *s, int n2) {
-  for (int k = 2; k <= n2; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int p = threadIdx.x; p < (n2 >> 1); p += blockDim.x) {
-        const int i = 2 * p - (p & (j - 1));
-        const int l = i + j;
-        const uint64_t a = s[i], b = s[l];
-        const bool up = (i & k) == 0;
-        if ((a > b) == up) { s[i] = b; s[l] = a; }
-      }
-      __syncthreads();
-    }
-  }
-}
-
-__device__ __forceinline__ int lower_bound_u64(const uint64_t *a, int n, uint64_t v) {
-  int lo = 0, hi = n;
-  while (lo < hi) { const int m = (lo + hi) >> 1; if (a[m] < v) lo = m + 1; else hi = m; }
-  return lo;
-}
-__device__ __forceinline__ int upper_bound_u64(const uint64_t *a, int n, uint64_t v) {
-  int lo = 0, hi = n;
-  while (lo < hi) { const int m = (lo + hi) >> 1; if (a[m] <= v) lo = m + 1; else hi = m; }
-  return lo;
-}
-
-__global__ void __launch_bounds__(SORT_THREADS)
-segment_sort_kernel(int T, const uint32_t *__restrict__ tile_start, uint64_t *__restrict__ keys,
-                    uint64_t *__restrict__ keys_alt, uint32_t *__restrict__ point_list,
-                    uint2 *__restrict__ ranges) {
-  __shared__ uint64_t s[SORT_CAP];
-  const int t = blockIdx.x;
   if (t >= T) return;
-  const uint32_t beg = tile_start[t], end = tile_start[t + 1];
-  const int n = (int)(end - beg);
-  if (threadIdx.x == 0) ranges[t] = n > 0 ? make_uint2(beg, end) : make_uint2(0u, 0u);
-  if (n == 0) return;
-  uint64_t *seg = keys + beg;
-  if (n <= SORT_CAP) {
-    int n2 = 2;
-    while (n2 < n) n2 <<= 1;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? seg[i] : ~0ull;
-    __syncthreads();
-    bitonic_smem(s, n2);
-    for (int i = threadIdx.x; i < n; i += blockDim.x) point_list[beg + i] = (uint32_t)s[i];
-    return;
+  const uint32_t C = counters[CI_C], K = counters[CI_K];
+  uint2 r = make_uint2(0u, 0u);
+  if (C > 0) {
+    const uint32_t a = cmat_scanned[(size_t)t * C];
+    const uint32_t e = (t + 1 < T) ? cmat_scanned[(size_t)(t + 1) * C] : K;
+    if (e > a) r = make_uint2(a, e);
+    atomicMax(&counters[CI_MAXLIST], e - a);
   }
-  // Long segment: sort SORT_CAP chunks in place, then merge runs pairwise.
-  for (int c0 = 0; c0 < n; c0 += SORT_CAP) {
-    const int m = min(SORT_CAP, n - c0);
-    int n2 = 2;
-    while (n2 < m) n2 <<= 1;
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < m ? seg[c0 + i] : ~0ull;
-    __syncthreads();
-    bitonic_smem(s, n2);
-    for (int i = threadIdx.x; i < m; i += blockDim.x) seg[c0 + i] = s[i];
-    __syncthreads();
+  ranges[t] = r;
+}
+
+// ---- emission -------------------------------------------------------------
+// Block = chunk; warp w owns a contiguous sub-range of the chunk (depth
+// order).  Shared memory: off[nw][T] (per-warp running slots) + base[T].
+__global__ void __launch_bounds__(256)
+emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__restrict__ order,
+            uint32_t *__restrict__ counters, const uint32_t *__restrict__ cmat_scanned,
+            uint32_t *__restrict__ point_list, uint32_t K_alloc) {
+  extern __shared__ uint32_t sm[];
+  const uint32_t V = counters[CI_V], S = counters[CI_S], C = counters[CI_C];
+  const uint32_t c = blockIdx.x;
+  if (c >= C) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint32_t *off = sm;
+  uint32_t *base = sm + (size_t)nw * T;
+  for (int i = threadIdx.x; i < nw * T; i += blockDim.x) off[i] = 0u;
+  for (int t = threadIdx.x; t < T; t += blockDim.x) base[t] = cmat_scanned[(size_t)t * C + c];
+  __syncthreads();
+  const uint32_t s0 = c * S, s1 = min(V, s0 + S);
+  const uint32_t sub = (s1 - s0 + nw - 1) / nw;
+  const uint32_t a = min(s1, s0 + w * sub), bnd = min(s1, a + sub);
+  uint32_t *my = off + (size_t)w * T;
+  for (uint32_t s = a; s < bnd; ++s) {
+    const uint32_t g = order[s];
+    int x0, y0, x1, y1;
+    unpack_rect(feat[3 * g + 2], x0, y0, x1, y1);
+    const int rw = x1 - x0, area = rw * (y1 - y0);
+    for (int j = lane; j < area; j += 32) atomicAdd(&my[(y0 + j / rw) * gx + x0 + j % rw], 1u);
   }
-  uint64_t *src = seg, *dst = keys_alt + beg;
-  for (int w = SORT_CAP; w < n; w <<= 1) {
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-      const int a0 = (e / (2 * w)) * (2 * w);
-      const int b0 = a0 + w;
-      const int na = min(w, n - a0);
-      const int nb = max(0, min(w, n - b0));
-      const uint64_t v = src[e];
-      int pos;
-      if (e < b0) pos = (e - a0) + lower_bound_u64(src + b0, nb, v);
-      else pos = (e - b0) + upper_bound_u64(src + a0, na, v);
-      dst[a0 + pos] = v;
+  __syncthreads();
+  for (int t = threadIdx.x; t < T; t += blockDim.x) {
+    uint32_t run = base[t];
+    for (int w2 = 0; w2 < nw; ++w2) {
+      const uint32_t n = off[(size_t)w2 * T + t];
+      off[(size_t)w2 * T + t] = run;
+      run += n;
     }
-    __syncthreads();
-    uint64_t *tmp = src; src = dst; dst = tmp;
   }
-  for (int i = threadIdx.x; i < n; i += blockDim.x) point_list[beg + i] = (uint32_t)src[i];
+  __syncthreads();
+  bool bad = false;
+  for (uint32_t s = a; s < bnd; ++s) {
+    const uint32_t g = order[s];
+    int x0, y0, x1, y1;
+    unpack_rect(feat[3 * g + 2], x0, y0, x1, y1);
+    const int rw = x1 - x0, area = rw * (y1 - y0);
+    for (int j = lane; j < area; j += 32) {
+      const int t = (y0 + j / rw) * gx + x0 + j % rw;
+      const uint32_t p = my[t];
+      my[t] = p + 1u;
+      if (p < K_alloc) point_list[p] = g;
+      else bad = true;
+    }
+    __syncwarp();
+  }
+  if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
 }
 
 // Debug view: sorted keys in the reference's form (tile << 32 | depth_bits).
@@ -141,41 +362,125 @@ __global__ void debug_keys_kernel(int T, const uint2 *__restrict__ ranges,
   }
 }
 
+int emit_warps(int T) {
+  // (nw + 1) * T * 4 bytes of shared memory, at most 220 KB
+  const int fit = (int)((220 * 1024 / 4) / (size_t)T) - 1;
+  return fit < 1 ? 0 : (fit > 8 ? 8 : fit);
+}
+
 }  // namespace
 
-int launch_scatter(const GeomLayout &L, const char *geom, const BinLayout &B, char *bin,
-                   int64_t K, cudaStream_t s) {
-  const int T = L.T();
-  uint32_t *cursor = reinterpret_cast<uint32_t *>(bin + B.cursor);
-  DMGS_TIMED(K_INIT_CURSOR, s, init_cursor_kernel<<<(T + 255) / 256, 256, 0, s>>>(
-      T, reinterpret_cast<const uint32_t *>(geom + L.tile_start), cursor));
-  DMGS_LAUNCH_CHECK("init_cursor_kernel");
-  if (L.P > 0 && K > 0) {
-    DMGS_TIMED(K_SCATTER, s, scatter_kernel<<<(L.P + 255) / 256, 256, 0, s>>>(
-        L.P, L.gx, reinterpret_cast<const float4 *>(geom + L.feat), cursor,
-        reinterpret_cast<uint64_t *>(bin + B.keys), (uint32_t)K,
-        reinterpret_cast<uint32_t *>(const_cast<char *>(geom) + L.counters)));
-    DMGS_LAUNCH_CHECK("scatter_kernel");
+int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t *part,
+                uint32_t *total_out, uint32_t *status, cudaStream_t s) {
+  if (n_max <= (uint32_t)SCAN_TILE * 4) {
+    scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, 0, total_out, status);
+    DMGS_LAUNCH_CHECK("scan_single_kernel");
+    return DMGS_OK;
   }
+  const uint32_t nb = (n_max + SCAN_TILE - 1) / SCAN_TILE;
+  scan_reduce_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
+  DMGS_LAUNCH_CHECK("scan_reduce_kernel");
+  scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(part, n_dev, n_max, 1, total_out, status);
+  DMGS_LAUNCH_CHECK("scan_single_kernel");
+  scan_down_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
+  DMGS_LAUNCH_CHECK("scan_down_kernel");
   return DMGS_OK;
 }
 
-int launch_segment_sort(const GeomLayout &L, const char *geom, const BinLayout &B, char *bin,
-                        int64_t K, cudaStream_t s) {
-  (void)K;
+int launch_binning_geometry(const GeomLayout &L, const int32_t *radii, char *geom, cudaStream_t s) {
+  uint32_t *counters = reinterpret_cast<uint32_t *>(geom + L.counters);
+  uint32_t *blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
+  uint32_t *part = reinterpret_cast<uint32_t *>(geom + L.scanpart);
+  uint32_t *k0 = reinterpret_cast<uint32_t *>(geom + L.dkey0);
+  uint32_t *k1 = reinterpret_cast<uint32_t *>(geom + L.dkey1);
+  uint32_t *v0 = reinterpret_cast<uint32_t *>(geom + L.dval0);
+  uint32_t *v1 = reinterpret_cast<uint32_t *>(geom + L.dval1);
+  uint32_t *rhist = reinterpret_cast<uint32_t *>(geom + L.rhist);
+  uint32_t *cmat = reinterpret_cast<uint32_t *>(geom + L.cmat);
+  const float4 *feat = reinterpret_cast<const float4 *>(geom + L.feat);
   const int T = L.T();
-  DMGS_TIMED(K_SEGMENT_SORT, s, segment_sort_kernel<<<T, SORT_THREADS, 0, s>>>(
-      T, reinterpret_cast<const uint32_t *>(geom + L.tile_start),
-      reinterpret_cast<uint64_t *>(bin + B.keys), reinterpret_cast<uint64_t *>(bin + B.keys_alt),
-      reinterpret_cast<uint32_t *>(bin + B.point_list), reinterpret_cast<uint2 *>(bin + B.ranges)));
-  DMGS_LAUNCH_CHECK("segment_sort_kernel");
+  if (L.P > 0) {
+    DMGS_TIMED(K_BIN_COMPACT, s, {
+      int r = launch_scan(blkcnt, nullptr, (uint32_t)L.nb_pre, part, counters + CI_V, counters, s);
+      if (r != DMGS_OK) return r;
+      compact_kernel<<<L.nb_pre, PRE_BLOCK, 0, s>>>(L.P, radii, feat, blkcnt, k0, v0);
+    });
+    DMGS_LAUNCH_CHECK("compact_kernel");
+  }
+  params_kernel<<<1, 1, 0, s>>>(T, counters);
+  DMGS_LAUNCH_CHECK("params_kernel");
+  if (L.P > 0) {
+    DMGS_TIMED(K_BIN_SORT, s, {
+      uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
+      for (int pass = 0; pass < 4; ++pass) {
+        const int shift = 8 * pass;
+        radix_hist_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, counters, shift, rhist);
+        int r = launch_scan(rhist, counters + CI_NRH, (uint32_t)L.n_rhist_max, part, nullptr,
+                            nullptr, s);
+        if (r != DMGS_OK) return r;
+        radix_scatter_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, vi, ko, vo, counters, shift,
+                                                                 rhist);
+        uint32_t *t1 = ki; ki = ko; ko = t1;
+        uint32_t *t2 = vi; vi = vo; vo = t2;
+      }
+    });  // four passes: the sorted order ends in (k0, v0)
+    DMGS_LAUNCH_CHECK("radix_sort");
+  }
+  const size_t csm = (size_t)T * 4;
+  if (csm > 220 * 1024) {
+    dmgs_host::set_error("image too large: %d tiles exceed the binning kernels' shared memory", T);
+    return DMGS_ERR_ARG;
+  }
+  if (L.P > 0) {
+    if (csm > 48 * 1024)
+      DMGS_CUDA(cudaFuncSetAttribute(tile_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)csm));
+    DMGS_TIMED(K_BIN_COUNT, s,
+               tile_count_kernel<<<CHUNK_COUNT_MAX, 256, csm, s>>>(L.gx, T, feat, v0, counters,
+                                                                   cmat));
+    DMGS_LAUNCH_CHECK("tile_count_kernel");
+  }
+  DMGS_TIMED(K_BIN_SCAN, s, {
+    if (L.P > 0) {
+      int r = launch_scan(cmat, counters + CI_NCM, (uint32_t)L.n_cmat_max, part, counters + CI_K,
+                          counters, s);
+      if (r != DMGS_OK) return r;
+    }
+    ranges_kernel<<<(T + 255) / 256, 256, 0, s>>>(T, cmat, counters,
+                                                  reinterpret_cast<uint2 *>(geom + L.ranges));
+  });
+  DMGS_LAUNCH_CHECK("ranges_kernel");
+  return DMGS_OK;
+}
+
+int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, int64_t K,
+                cudaStream_t s) {
+  const int T = L.T();
+  if (L.P <= 0 || K <= 0) return DMGS_OK;
+  const int nw = emit_warps(T);
+  if (nw < 1) {
+    dmgs_host::set_error("image too large: %d tiles exceed the emission kernel's shared memory", T);
+    return DMGS_ERR_ARG;
+  }
+  const size_t smem = (size_t)(nw + 1) * T * 4;
+  if (smem > 48 * 1024)
+    DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+  DMGS_TIMED(K_BIN_EMIT, s,
+             emit_kernel<<<CHUNK_COUNT_MAX, nw * 32, smem, s>>>(
+                 L.gx, T, reinterpret_cast<const float4 *>(geom + L.feat),
+                 reinterpret_cast<const uint32_t *>(geom + L.dval0),
+                 reinterpret_cast<uint32_t *>(geom + L.counters),
+                 reinterpret_cast<const uint32_t *>(geom + L.cmat),
+                 reinterpret_cast<uint32_t *>(bin + B.point_list), (uint32_t)K));
+  DMGS_LAUNCH_CHECK("emit_kernel");
   return DMGS_OK;
 }
 
 int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
                       uint64_t *keys, uint32_t *values, cudaStream_t s) {
   DMGS_TIMED(K_DEBUG, s, debug_keys_kernel<<<L.T(), 256, 0, s>>>(
-      L.T(), reinterpret_cast<const uint2 *>(bin + B.ranges),
+      L.T(), reinterpret_cast<const uint2 *>(geom + L.ranges),
       reinterpret_cast<const uint32_t *>(bin + B.point_list),
       reinterpret_cast<const float4 *>(geom + L.feat), keys, values));
   DMGS_LAUNCH_CHECK("debug_keys_kernel");

@@ -219,7 +219,7 @@ int launch_blend_fwd(const ViewParams &vp, const GeomLayout &L, const char *geom
   const int T = L.T();
   if (T == 0) return DMGS_OK;
   DMGS_TIMED(K_BLEND_FWD, s, blend_fwd_kernel<<<T, TILE_PIX, 0, s>>>(
-      vp.W, vp.H, L.gx, reinterpret_cast<const uint2 *>(bin + B.ranges),
+      vp.W, vp.H, L.gx, reinterpret_cast<const uint2 *>(geom + L.ranges),
       reinterpret_cast<const uint32_t *>(bin + B.point_list),
       reinterpret_cast<const float4 *>(geom + L.feat), bg, out_color,
       reinterpret_cast<float *>(img + I.final_T), reinterpret_cast<uint32_t *>(img + I.n_contrib)));
@@ -234,7 +234,7 @@ int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom
   DMGS_CUDA(cudaMemsetAsync(gacc, 0, (size_t)L.P * 48, s));
   if (T == 0) return DMGS_OK;
   DMGS_TIMED(K_BLEND_BWD, s, blend_bwd_kernel<<<T, TILE_PIX, 0, s>>>(
-      vp.W, vp.H, L.gx, reinterpret_cast<const uint2 *>(bin + B.ranges),
+      vp.W, vp.H, L.gx, reinterpret_cast<const uint2 *>(geom + L.ranges),
       reinterpret_cast<const uint32_t *>(bin + B.point_list),
       reinterpret_cast<const float4 *>(geom + L.feat), bg,
       reinterpret_cast<const float *>(img + I.final_T),

@@ -116,12 +116,12 @@ GaussianPtrs make_gptrs(const DmgsGaussians *g) {
 
 // Reads the kernel status word; returns a DMGS error for set bits.
 int check_status(const char *geom, const GeomLayout &L, cudaStream_t s, uint32_t *host4) {
-  uint32_t h[4] = {0, 0, 0, 0};
-  cudaError_t e = cudaMemcpyAsync(h, geom + L.counters, 16, cudaMemcpyDeviceToHost, s);
+  uint32_t h[CI_WORDS] = {};
+  cudaError_t e = cudaMemcpyAsync(h, geom + L.counters, sizeof(h), cudaMemcpyDeviceToHost, s);
   if (e != cudaSuccess) return dmgs_host::cuda_fail(e, "status copy");
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return dmgs_host::cuda_fail(e, "cudaStreamSynchronize");
-  if (host4) memcpy(host4, h, 16);
+  if (host4) memcpy(host4, h, sizeof(h));
   if (h[0] & ST_PREFILTER) {
     set_error("a point failed the frustum test although prefiltered is set");
     return DMGS_ERR_PREFILTER;
@@ -179,10 +179,10 @@ int dmgs_raster_fwd_geometry(const DmgsView *view, const DmgsGaussians *g, void 
   RET_IF(launch_preprocess(vp, view->viewmatrix, view->projmatrix, view->campos, make_gptrs(g),
                            radii, L, geom, s));
   RET_IF(debug_sync(view, s, "preprocess"));
-  RET_IF(launch_tile_offsets(L, geom, s));
-  uint32_t h[4];
+  RET_IF(launch_binning_geometry(L, radii, geom, s));
+  uint32_t h[CI_WORDS];
   RET_IF(check_status(geom, L, s, h));
-  if (num_rendered) *num_rendered = (int64_t)h[1] | ((int64_t)h[2] << 32);
+  if (num_rendered) *num_rendered = (int64_t)h[CI_K];
   return DMGS_OK;
 }
 
@@ -205,10 +205,8 @@ int dmgs_raster_fwd_render(const DmgsView *view, const DmgsGaussians *g, void *g
   char *bin = static_cast<char *>(binning_state);
   char *img = static_cast<char *>(image_state);
   const ViewParams vp = make_params(view);
-  RET_IF(launch_scatter(L, geom, B, bin, num_rendered, s));
-  RET_IF(debug_sync(view, s, "scatter"));
-  RET_IF(launch_segment_sort(L, geom, B, bin, num_rendered, s));
-  RET_IF(debug_sync(view, s, "segment_sort"));
+  RET_IF(launch_emit(L, geom, B, bin, num_rendered, s));
+  RET_IF(debug_sync(view, s, "emit"));
   RET_IF(launch_blend_fwd(vp, L, geom, B, bin, I, img, view->bg, out_color, s));
   RET_IF(debug_sync(view, s, "blend_fwd"));
   if (view->debug) RET_IF(check_status(geom, L, s, nullptr));
@@ -299,7 +297,7 @@ int dmgs_debug_binning(int32_t P, int32_t width, int32_t height, int64_t num_ren
   if (!binning_state || binning_bytes < B.total) { set_error("binning state too small"); return DMGS_ERR_STATE; }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const char *bin = static_cast<const char *>(binning_state);
-  if (ranges) DMGS_CUDA(cudaMemcpyAsync(ranges, bin + B.ranges, (size_t)L.T() * 8, cudaMemcpyDeviceToDevice, s));
+  if (ranges) DMGS_CUDA(cudaMemcpyAsync(ranges, static_cast<const char *>(geom_state) + L.ranges, (size_t)L.T() * 8, cudaMemcpyDeviceToDevice, s));
   if ((keys || values) && num_rendered > 0)
     return launch_debug_keys(L, static_cast<const char *>(geom_state), B, bin, keys, values, s);
   return DMGS_OK;

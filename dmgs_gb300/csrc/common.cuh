@@ -44,15 +44,44 @@ struct ViewParams {
 };
 
 // ---------------------------------------------------------------------------
-// Geometry state (per Gaussian, 48-byte record = 3 x float4):
+// Geometry state.  Per Gaussian, a 48-byte record = 3 x float4:
 //   f0 = (x, y, conic_a, conic_b)    pixel-space mean, conic (a b; b c)
 //   f1 = (conic_c, opacity, r, g)
 //   f2 = (b, depth, rect_lo, rect_hi) rect packed as 2 x (u16 | u16 << 16)
 // A culled Gaussian has rect_lo == rect_hi == 0 and radius 0.
+// Then the binning working set: per-block visible counts, the visible
+// Gaussians' depth keys / indices (two ping-pong copies for the radix sort),
+// the radix block histograms, the per-(tile, chunk) count matrix, scan
+// partials, per-tile ranges and the counters word block.
 // ---------------------------------------------------------------------------
+constexpr int PRE_BLOCK = 256;           // preprocess / compaction block
+constexpr int RADIX_BLOCK = 256;         // radix sort block (8 warps)
+constexpr int RADIX_ITEMS = 8;           // keys per thread
+constexpr int RADIX_TILE = RADIX_BLOCK * RADIX_ITEMS;  // 2048 keys per block
+constexpr int CHUNK_MIN = 256;           // Gaussians per binning chunk (minimum)
+constexpr int CHUNK_COUNT_MAX = 1024;    // binning chunks (maximum)
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096 elements per block
+
+// counters[] indices
+constexpr int CI_STATUS = 0;   // ST_* bits
+constexpr int CI_K = 1;        // instances (u32; K < 2^32 enforced)
+constexpr int CI_MAXLIST = 3;  // longest tile list
+constexpr int CI_V = 4;        // visible Gaussians
+constexpr int CI_NBR = 5;      // radix blocks in use = ceil(V / RADIX_TILE)
+constexpr int CI_NRH = 6;      // radix histogram entries = 256 * NBR
+constexpr int CI_S = 7;        // Gaussians per chunk
+constexpr int CI_C = 8;        // chunks
+constexpr int CI_NCM = 9;      // count-matrix entries = T * C
+constexpr int CI_WORDS = 16;
+
 struct GeomLayout {
-  size_t feat, clamped, diff, tile_start, counters, total;
+  size_t feat, clamped, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, scanpart, ranges,
+      counters, total;
   int P, gx, gy;
+  int nb_pre, nb_radix;
+  size_t n_rhist_max, n_cmat_max, n_part_max;
   __host__ __device__ int T() const { return gx * gy; }
 };
 
@@ -61,33 +90,42 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.P = P;
   L.gx = (W + TILE - 1) / TILE;
   L.gy = (H + TILE - 1) / TILE;
+  const size_t T = (size_t)L.gx * L.gy;
+  L.nb_pre = (P + PRE_BLOCK - 1) / PRE_BLOCK;
+  L.nb_radix = (P + RADIX_TILE - 1) / RADIX_TILE;
+  L.n_rhist_max = (size_t)256 * L.nb_radix;
+  L.n_cmat_max = T * CHUNK_COUNT_MAX;
+  size_t nmax = L.n_cmat_max > L.n_rhist_max ? L.n_cmat_max : L.n_rhist_max;
+  if ((size_t)L.nb_pre > nmax) nmax = L.nb_pre;
+  L.n_part_max = (nmax + SCAN_TILE - 1) / SCAN_TILE + 1;
   size_t o = 0;
-  L.feat = o;        o = align_up(o + (size_t)P * 48, 256);
-  L.clamped = o;     o = align_up(o + (size_t)P, 256);
-  L.diff = o;        o = align_up(o + (size_t)(L.gx + 1) * (L.gy + 1) * 4, 256);
-  L.tile_start = o;  o = align_up(o + (size_t)(L.gx * L.gy + 1) * 4, 256);
-  L.counters = o;    o = align_up(o + 64, 256);
+  L.feat = o;      o = align_up(o + (size_t)P * 48, 256);
+  L.clamped = o;   o = align_up(o + (size_t)P, 256);
+  L.blkcnt = o;    o = align_up(o + (size_t)L.nb_pre * 4 + 4, 256);
+  L.dkey0 = o;     o = align_up(o + (size_t)P * 4, 256);
+  L.dkey1 = o;     o = align_up(o + (size_t)P * 4, 256);
+  L.dval0 = o;     o = align_up(o + (size_t)P * 4, 256);
+  L.dval1 = o;     o = align_up(o + (size_t)P * 4, 256);
+  L.rhist = o;     o = align_up(o + L.n_rhist_max * 4 + 4, 256);
+  L.cmat = o;      o = align_up(o + L.n_cmat_max * 4, 256);
+  L.scanpart = o;  o = align_up(o + L.n_part_max * 4, 256);
+  L.ranges = o;    o = align_up(o + T * 8, 256);
+  L.counters = o;  o = align_up(o + CI_WORDS * 4, 256);
   L.total = o;
   return L;
 }
 
-// counters[0] = status bits, counters[1] = num_rendered (low 32),
-// counters[2] = num_rendered (high 32), counters[3] = longest tile list
+// Binning state: the per-tile Gaussian index lists, concatenated in tile
+// order (K entries).
 struct BinLayout {
-  size_t keys, keys_alt, point_list, cursor, ranges, total;
+  size_t point_list, total;
 };
 
 __host__ __device__ inline BinLayout bin_layout(int64_t K, int W, int H) {
+  (void)W; (void)H;
   BinLayout L;
-  int gx = (W + TILE - 1) / TILE, gy = (H + TILE - 1) / TILE;
-  size_t T = (size_t)gx * gy;
-  size_t o = 0;
-  L.keys = o;       o = align_up(o + (size_t)K * 8, 256);
-  L.keys_alt = o;   o = align_up(o + (size_t)K * 8, 256);
-  L.point_list = o; o = align_up(o + (size_t)K * 4, 256);
-  L.cursor = o;     o = align_up(o + T * 4, 256);
-  L.ranges = o;     o = align_up(o + T * 8, 256);
-  L.total = o;
+  L.point_list = 0;
+  L.total = align_up((size_t)(K > 0 ? K : 0) * 4, 256) + 256;
   return L;
 }
 
@@ -147,7 +185,7 @@ int cuda_fail(cudaError_t e, const char *what);
 
 // Kernel timing registry (timing.cu).  Kernel ids index kKernelNames.
 enum KernelId {
-  K_PREPROCESS = 0, K_TILE_OFFSETS, K_INIT_CURSOR, K_SCATTER, K_SEGMENT_SORT, K_BLEND_FWD,
+  K_PREPROCESS = 0, K_BIN_COMPACT, K_BIN_SORT, K_BIN_COUNT, K_BIN_SCAN, K_BIN_EMIT, K_BLEND_FWD,
   K_BLEND_BWD, K_PREPROCESS_BWD, K_MARK_VISIBLE, K_BIND_FWD, K_BIND_BWD, K_BIND3_FWD,
   K_BIND3_BWD, K_DEBUG, K_BATCH_PREPROCESS, K_BATCH_BINNING, K_BATCH_BLEND_FWD,
   K_BATCH_BLEND_BWD, K_BATCH_PREPROCESS_BWD, K_COUNT

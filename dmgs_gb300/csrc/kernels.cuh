@@ -14,15 +14,15 @@ struct GaussianPtrs {
 int launch_preprocess(const ViewParams &vp, const float *viewm, const float *projm,
                       const float *campos, const GaussianPtrs &g, int32_t *radii,
                       const GeomLayout &L, char *geom, cudaStream_t s);
-int launch_tile_offsets(const GeomLayout &L, char *geom, cudaStream_t s);
 int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t *present,
                         cudaStream_t s);
 
 // binning.cu
-int launch_scatter(const GeomLayout &L, const char *geom, const BinLayout &B, char *bin,
-                   int64_t K, cudaStream_t s);
-int launch_segment_sort(const GeomLayout &L, const char *geom, const BinLayout &B, char *bin,
-                        int64_t K, cudaStream_t s);
+int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t *part,
+                uint32_t *total_out, uint32_t *status, cudaStream_t s);
+int launch_binning_geometry(const GeomLayout &L, const int32_t *radii, char *geom, cudaStream_t s);
+int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, int64_t K,
+                cudaStream_t s);
 int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
                       uint64_t *keys, uint32_t *values, cudaStream_t s);
 int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,

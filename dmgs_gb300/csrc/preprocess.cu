@@ -8,18 +8,14 @@
 //
 // Design: one thread per Gaussian.  The integer-determining chain (view z,
 // NDC position, 2D covariance, radius, rectangle) uses explicitly rounded
-// IEEE ops so that it is reproducible on the CPU.  Tile counting does not
-// touch every covered tile: each visible Gaussian adds +1/-1 at the four
-// corners of its rectangle in a (gy+1) x (gx+1) difference grid (4 atomics
-// per Gaussian instead of one per tile); a 2D prefix sum then yields the
-// per-tile counts.
+// IEEE ops so that it is reproducible on the CPU.  Each block also records
+// how many of its Gaussians are visible, for the order-preserving
+// compaction that starts the binning (binning.cu).
 #include "kernels.cuh"
 
 namespace dmgs {
 
 namespace {
-
-struct Mat4 { float m[16]; };
 
 __device__ __forceinline__ void load_mat(const float *__restrict__ p, float *m) {
 #pragma unroll
@@ -57,18 +53,17 @@ __device__ __forceinline__ void cov3d_scale_rot(float sx, float sy, float sz, fl
 
 __device__ __forceinline__ int trunc_sat(float v) { return __float2int_rz(v); }
 
-__global__ void __launch_bounds__(256)
-preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
-                  const float *__restrict__ projm_g, const float *__restrict__ campos_g,
-                  int P, int M, const float *__restrict__ means,
-                  const float *__restrict__ opac, const float *__restrict__ shs,
-                  const float *__restrict__ colors, const float *__restrict__ scales,
-                  const float *__restrict__ rots, const float *__restrict__ cov3D,
-                  int32_t *__restrict__ radii, float4 *__restrict__ feat,
-                  uint8_t *__restrict__ clamped, uint32_t *__restrict__ diff,
-                  uint32_t *__restrict__ counters) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= P) return;
+// One Gaussian; returns true when it is visible (radius > 0, non-empty
+// tile rectangle).
+__device__ __forceinline__ bool
+preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
+               const float *__restrict__ projm_g, const float *__restrict__ campos_g, int M,
+               const float *__restrict__ means, const float *__restrict__ opac,
+               const float *__restrict__ shs, const float *__restrict__ colors,
+               const float *__restrict__ scales, const float *__restrict__ rots,
+               const float *__restrict__ cov3D, int32_t *__restrict__ radii,
+               float4 *__restrict__ feat, uint8_t *__restrict__ clamped,
+               uint32_t *__restrict__ counters) {
 
   float V[16], Pm[16];
   load_mat(viewm_g, V);
@@ -87,7 +82,7 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   if (!(vz > 0.2f)) {
     if (vp.prefiltered) atomicOr(counters, ST_PREFILTER);
     cull();
-    return;
+    return false;
   }
   const float hx = add(add(add(mul(Pm[0], x), mul(Pm[4], y)), mul(Pm[8], z)), Pm[12]);
   const float hy = add(add(add(mul(Pm[1], x), mul(Pm[5], y)), mul(Pm[9], z)), Pm[13]);
@@ -141,7 +136,7 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   c00 = add(c00, 0.3f);
   c11 = add(c11, 0.3f);
   const float det = sub(mul(c00, c11), mul(c01, c01));
-  if (det == 0.f) { cull(); return; }
+  if (det == 0.f) { cull(); return false; }
   const float det_inv = dvd(1.f, det);
   const float ca = mul(c11, det_inv), cb = mul(-c01, det_inv), cc = mul(c00, det_inv);
   const float mid = mul(0.5f, add(c00, c11));
@@ -149,13 +144,13 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   const float sq = __fsqrt_rn(disc);
   const float l1 = add(mid, sq), l2 = sub(mid, sq);
   const int rad = trunc_sat(ceilf(mul(3.f, __fsqrt_rn(fmaxf(l1, l2)))));
-  if (rad <= 0) { cull(); return; }
+  if (rad <= 0) { cull(); return false; }
   const float r = (float)rad;
   const int x0 = min(vp.gx, max(0, trunc_sat(dvd(sub(px, r), (float)TILE))));
   const int y0 = min(vp.gy, max(0, trunc_sat(dvd(sub(py, r), (float)TILE))));
   const int x1 = min(vp.gx, max(0, trunc_sat(dvd(add(add(px, r), (float)(TILE - 1)), (float)TILE))));
   const int y1 = min(vp.gy, max(0, trunc_sat(dvd(add(add(py, r), (float)(TILE - 1)), (float)TILE))));
-  if ((x1 - x0) * (y1 - y0) == 0) { cull(); return; }
+  if ((x1 - x0) * (y1 - y0) == 0) { cull(); return false; }
 
   // Colour: precomputed, or SH (degree <= 3) at the view direction, +0.5,
   // clamped at 0 with the clamp recorded for the adjoint.
@@ -213,90 +208,27 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   feat[3 * idx + 2] = make_float4(cbl, vz, __uint_as_float(pack_u16x2(x0, y0)),
                                   __uint_as_float(pack_u16x2(x1, y1)));
 
-  // +1 at (x0,y0), -1 at (x1,y0) and (x0,y1), +1 at (x1,y1).
-  const int stride = vp.gx + 1;
-  atomicAdd(diff + y0 * stride + x0, 1u);
-  atomicAdd(diff + y0 * stride + x1, 0xffffffffu);
-  atomicAdd(diff + y1 * stride + x0, 0xffffffffu);
-  atomicAdd(diff + y1 * stride + x1, 1u);
+  return true;
 }
 
-// One block: 2D prefix sum of the difference grid (in shared memory) ->
-// per-tile counts -> exclusive scan in tile order -> tile_start[T+1].
-// counters[1..2] = total instances (64-bit), counters[3] = longest list.
-__global__ void __launch_bounds__(1024)
-tile_offsets_kernel(int gx, int gy, const uint32_t *__restrict__ diff,
-                    uint32_t *__restrict__ tile_start, uint32_t *__restrict__ counters) {
-  extern __shared__ uint32_t sm[];
-  const int stride = gx + 1;
-  const int n = stride * (gy + 1);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) sm[i] = diff[i];
-  __syncthreads();
-  for (int yrow = threadIdx.x; yrow < gy; yrow += blockDim.x) {
-    uint32_t run = 0;
-    for (int xx = 0; xx < gx; ++xx) { run += sm[yrow * stride + xx]; sm[yrow * stride + xx] = run; }
-  }
-  __syncthreads();
-  for (int xc = threadIdx.x; xc < gx; xc += blockDim.x) {
-    uint32_t run = 0;
-    for (int yy = 0; yy < gy; ++yy) { run += sm[yy * stride + xc]; sm[yy * stride + xc] = run; }
-  }
-  __syncthreads();
-  // Exclusive scan over T counts, each thread a contiguous chunk.
-  const int T = gx * gy;
-  const int per = (T + blockDim.x - 1) / blockDim.x;
-  const int beg = min(T, (int)threadIdx.x * per), end = min(T, beg + per);
-  unsigned long long local = 0;
-  uint32_t lmax = 0;
-  for (int t = beg; t < end; ++t) {
-    const uint32_t c = sm[(t / gx) * stride + (t % gx)];
-    local += c;
-    lmax = max(lmax, c);
-  }
-  __shared__ unsigned long long warp_tot[32];
-  __shared__ uint32_t warp_max[32];
-  // inclusive warp scan of `local`
-  unsigned long long inc = local;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned long long v = __shfl_up_sync(0xffffffffu, inc, o);
-    if (lane >= o) inc += v;
-  }
-  uint32_t wm = lmax;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-  if (lane == 31) warp_tot[wid] = inc;
-  if (lane == 0) warp_max[wid] = wm;
-  __syncthreads();
-  if (wid == 0) {
-    const int nw = blockDim.x >> 5;
-    unsigned long long v = lane < nw ? warp_tot[lane] : 0ull;
-    uint32_t m = lane < nw ? warp_max[lane] : 0u;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long u = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += u;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane < nw) warp_tot[lane] = v;  // inclusive per-warp totals
-    if (lane == 0) warp_max[0] = m;
-  }
-  __syncthreads();
-  unsigned long long base = (wid > 0 ? warp_tot[wid - 1] : 0ull) + inc - local;
-  for (int t = beg; t < end; ++t) {
-    tile_start[t] = (uint32_t)base;
-    base += sm[(t / gx) * stride + (t % gx)];
-  }
-  if (threadIdx.x == blockDim.x - 1) {
-    const unsigned long long total = warp_tot[(blockDim.x >> 5) - 1];
-    tile_start[T] = (uint32_t)total;
-    counters[1] = (uint32_t)(total & 0xffffffffull);
-    counters[2] = (uint32_t)(total >> 32);
-    counters[3] = warp_max[0];
-  }
+__global__ void __launch_bounds__(PRE_BLOCK)
+preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
+                  const float *__restrict__ projm_g, const float *__restrict__ campos_g,
+                  int P, int M, const float *__restrict__ means,
+                  const float *__restrict__ opac, const float *__restrict__ shs,
+                  const float *__restrict__ colors, const float *__restrict__ scales,
+                  const float *__restrict__ rots, const float *__restrict__ cov3D,
+                  int32_t *__restrict__ radii, float4 *__restrict__ feat,
+                  uint8_t *__restrict__ clamped, uint32_t *__restrict__ blkcnt,
+                  uint32_t *__restrict__ counters) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool vis = idx < P &&
+                   preprocess_one(idx, vp, viewm_g, projm_g, campos_g, M, means, opac, shs, colors,
+                                  scales, rots, cov3D, radii, feat, clamped, counters);
+  const int nvis = __syncthreads_count(vis);
+  if (threadIdx.x == 0) blkcnt[blockIdx.x] = (uint32_t)nvis;
 }
+
 
 __global__ void mark_visible_kernel(int P, const float *__restrict__ means,
                                     const float *__restrict__ viewm_g,
@@ -316,36 +248,17 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
                       const GeomLayout &L, char *geom, cudaStream_t s) {
   float4 *feat = reinterpret_cast<float4 *>(geom + L.feat);
   uint8_t *clamped = reinterpret_cast<uint8_t *>(geom + L.clamped);
-  uint32_t *diff = reinterpret_cast<uint32_t *>(geom + L.diff);
+  uint32_t *blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
   uint32_t *counters = reinterpret_cast<uint32_t *>(geom + L.counters);
-  DMGS_CUDA(cudaMemsetAsync(diff, 0, (size_t)(L.gx + 1) * (L.gy + 1) * 4, s));
-  DMGS_CUDA(cudaMemsetAsync(counters, 0, 64, s));
+  DMGS_CUDA(cudaMemsetAsync(counters, 0, CI_WORDS * 4, s));
   if (g.P > 0) {
-    const int threads = 256;
-    const int blocks = (g.P + threads - 1) / threads;
-    DMGS_TIMED(K_PREPROCESS, s, preprocess_kernel<<<blocks, threads, 0, s>>>(vp, viewm, projm, campos, g.P, g.M, g.means3D,
+    const int blocks = L.nb_pre;
+    DMGS_TIMED(K_PREPROCESS, s, preprocess_kernel<<<blocks, PRE_BLOCK, 0, s>>>(vp, viewm, projm, campos, g.P, g.M, g.means3D,
                                                  g.opacities, g.shs, g.colors, g.scales,
-                                                 g.rotations, g.cov3D, radii, feat, clamped, diff,
+                                                 g.rotations, g.cov3D, radii, feat, clamped, blkcnt,
                                                  counters));
     DMGS_LAUNCH_CHECK("preprocess_kernel");
   }
-  return DMGS_OK;
-}
-
-int launch_tile_offsets(const GeomLayout &L, char *geom, cudaStream_t s) {
-  const size_t smem = (size_t)(L.gx + 1) * (L.gy + 1) * 4;
-  if (smem > 200 * 1024) {
-    dmgs_host::set_error("image too large: %d x %d tiles exceeds the tile-offset kernel", L.gx, L.gy);
-    return DMGS_ERR_ARG;
-  }
-  if (smem > 48 * 1024)
-    DMGS_CUDA(cudaFuncSetAttribute(tile_offsets_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-  DMGS_TIMED(K_TILE_OFFSETS, s, tile_offsets_kernel<<<1, 1024, smem, s>>>(
-      L.gx, L.gy, reinterpret_cast<const uint32_t *>(geom + L.diff),
-      reinterpret_cast<uint32_t *>(geom + L.tile_start),
-      reinterpret_cast<uint32_t *>(geom + L.counters)));
-  DMGS_LAUNCH_CHECK("tile_offsets_kernel");
   return DMGS_OK;
 }
 

@@ -12,7 +12,8 @@
 namespace dmgs_host {
 
 static const char *kKernelNames[K_COUNT] = {
-    "preprocess", "tile_offsets", "init_cursor", "scatter", "segment_sort", "blend_fwd",
+    "preprocess", "bin_compact", "bin_depth_sort", "bin_tile_count", "bin_scan", "bin_emit",
+    "blend_fwd",
     "blend_bwd", "preprocess_bwd", "mark_visible", "bind_fwd", "bind_bwd", "bind3_fwd",
     "bind3_bwd", "debug", "batch_preprocess", "batch_binning", "batch_blend_fwd",
     "batch_blend_bwd", "batch_preprocess_bwd"};
