@@ -192,6 +192,19 @@ radix_hist_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict_
   rhist[threadIdx.x * nbr + b] = h[threadIdx.x];  // digit-major
 }
 
+// Lanes whose 8-bit digit equals this lane's (invalid lanes, digit 256, group
+// together): nine ballots instead of match.any.
+__device__ __forceinline__ unsigned digit_peers(int d) {
+  unsigned peers = FULL;
+#pragma unroll
+  for (int b = 0; b < 9; ++b) {
+    const bool bit = (d >> b) & 1;
+    const unsigned m = __ballot_sync(FULL, bit);
+    peers &= bit ? m : ~m;
+  }
+  return peers;
+}
+
 // Warp w of block b owns keys [b*2048 + w*256, +256), visited in 8 rounds
 // of 32 (round-major, then lane) — the input order, so the pass is stable.
 __global__ void __launch_bounds__(RADIX_BLOCK)
@@ -216,7 +229,7 @@ radix_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restric
     key[r] = ok ? kin[k] : 0u;
     val[r] = ok ? vin[k] : 0u;
     dig[r] = ok ? (int)((key[r] >> shift) & 255u) : 256;
-    const unsigned peers = __match_any_sync(FULL, dig[r]);
+    const unsigned peers = digit_peers(dig[r]);
     if (dig[r] < 256 && lane == __ffs(peers) - 1) wh[w][dig[r]] += __popc(peers);
     __syncwarp();
   }
@@ -234,7 +247,7 @@ radix_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restric
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < RADIX_ITEMS; ++r) {
-    const unsigned peers = __match_any_sync(FULL, dig[r]);
+    const unsigned peers = digit_peers(dig[r]);
     uint32_t pos = 0;
     if (dig[r] < 256) pos = wh[w][dig[r]] + __popc(peers & lanemask_lt());
     __syncwarp();
@@ -254,6 +267,43 @@ __device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1
   x0 = lo & 0xffff; y0 = lo >> 16; x1 = hi & 0xffff; y1 = hi >> 16;
 }
 
+// A warp takes up to 32 consecutive Gaussians of the depth-sorted list; lane i
+// loads Gaussian s0 + i's index and tile rectangle (one round of independent
+// loads instead of a dependent load chain per Gaussian).  The warp then
+// visits the Gaussians in order, its lanes spread over each one's tiles.
+struct WarpGroup {
+  uint32_t id;      // this lane's Gaussian index (valid if lane < n)
+  int x0, y0, rw;   // its rectangle origin and width
+  int excl, incl;   // exclusive / inclusive prefix of rectangle areas
+  int total;        // instances of the whole group
+};
+
+__device__ __forceinline__ WarpGroup load_group(const uint32_t *__restrict__ order,
+                                                const float4 *__restrict__ feat, uint32_t s0,
+                                                uint32_t s1, int lane) {
+  WarpGroup G;
+  const uint32_t s = s0 + lane;
+  int area = 0;
+  G.id = 0; G.x0 = 0; G.y0 = 0; G.rw = 1;
+  if (s < s1) {
+    G.id = order[s];
+    int x1, y1;
+    unpack_rect(feat[3 * G.id + 2], G.x0, G.y0, x1, y1);
+    G.rw = max(x1 - G.x0, 1);
+    area = (x1 - G.x0) * (y1 - G.y0);
+  }
+  int inc = area;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(FULL, inc, o);
+    if (lane >= o) inc += u;
+  }
+  G.incl = inc;
+  G.excl = inc - area;
+  G.total = __shfl_sync(FULL, inc, 31);
+  return G;
+}
+
 __global__ void __launch_bounds__(256)
 tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
                   const uint32_t *__restrict__ order, const uint32_t *__restrict__ counters,
@@ -266,12 +316,15 @@ tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t s0 = c * S, s1 = min(V, s0 + S);
-  for (uint32_t s = s0 + w; s < s1; s += nw) {
-    const uint32_t g = order[s];
-    int x0, y0, x1, y1;
-    unpack_rect(feat[3 * g + 2], x0, y0, x1, y1);
-    const int rw = x1 - x0, area = rw * (y1 - y0);
-    for (int j = lane; j < area; j += 32) atomicAdd(&cnt[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+  for (uint32_t g0 = s0 + 32 * w; g0 < s1; g0 += 32 * nw) {
+    const WarpGroup G = load_group(order, feat, g0, s1, lane);
+    const int n = (int)min(32u, s1 - g0);
+    for (int i = 0; i < n; ++i) {
+      const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
+      const int rw = __shfl_sync(FULL, G.rw, i);
+      const int area = __shfl_sync(FULL, G.incl - G.excl, i);
+      for (int j = lane; j < area; j += 32) atomicAdd(&cnt[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+    }
   }
   __syncthreads();
   for (int t = threadIdx.x; t < T; t += blockDim.x) cmat[(size_t)t * C + c] = cnt[t];
@@ -313,12 +366,15 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
   const uint32_t sub = (s1 - s0 + nw - 1) / nw;
   const uint32_t a = min(s1, s0 + w * sub), bnd = min(s1, a + sub);
   uint32_t *my = off + (size_t)w * T;
-  for (uint32_t s = a; s < bnd; ++s) {
-    const uint32_t g = order[s];
-    int x0, y0, x1, y1;
-    unpack_rect(feat[3 * g + 2], x0, y0, x1, y1);
-    const int rw = x1 - x0, area = rw * (y1 - y0);
-    for (int j = lane; j < area; j += 32) atomicAdd(&my[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+  for (uint32_t g0 = a; g0 < bnd; g0 += 32) {
+    const WarpGroup G = load_group(order, feat, g0, bnd, lane);
+    const int n = (int)min(32u, bnd - g0);
+    for (int i = 0; i < n; ++i) {
+      const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
+      const int rw = __shfl_sync(FULL, G.rw, i);
+      const int area = __shfl_sync(FULL, G.incl - G.excl, i);
+      for (int j = lane; j < area; j += 32) atomicAdd(&my[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+    }
   }
   __syncthreads();
   for (int t = threadIdx.x; t < T; t += blockDim.x) {
@@ -331,19 +387,24 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
   }
   __syncthreads();
   bool bad = false;
-  for (uint32_t s = a; s < bnd; ++s) {
-    const uint32_t g = order[s];
-    int x0, y0, x1, y1;
-    unpack_rect(feat[3 * g + 2], x0, y0, x1, y1);
-    const int rw = x1 - x0, area = rw * (y1 - y0);
-    for (int j = lane; j < area; j += 32) {
-      const int t = (y0 + j / rw) * gx + x0 + j % rw;
-      const uint32_t p = my[t];
-      my[t] = p + 1u;
-      if (p < K_alloc) point_list[p] = g;
-      else bad = true;
+  for (uint32_t g0 = a; g0 < bnd; g0 += 32) {
+    const WarpGroup G = load_group(order, feat, g0, bnd, lane);
+    const int n = (int)min(32u, bnd - g0);
+    for (int i = 0; i < n; ++i) {
+      const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
+      const int rw = __shfl_sync(FULL, G.rw, i);
+      const int area = __shfl_sync(FULL, G.incl - G.excl, i);
+      const uint32_t id = __shfl_sync(FULL, G.id, i);
+      // one Gaussian covers each tile once: lanes touch distinct counters
+      for (int j = lane; j < area; j += 32) {
+        const int t = (y0 + j / rw) * gx + x0 + j % rw;
+        const uint32_t p = my[t];
+        my[t] = p + 1u;
+        if (p < K_alloc) point_list[p] = id;
+        else bad = true;
+      }
+      __syncwarp();
     }
-    __syncwarp();
   }
   if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
 }

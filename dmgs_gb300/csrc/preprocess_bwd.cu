@@ -14,37 +14,46 @@
 //   rgb = max(0, SH(dir) + 0.5)      -> dL/dsh, dL/dm through dir = unit(m - campos)
 //   Sigma = (R S)(R S)^T             -> dL/dscale, dL/dquaternion (unnormalised)
 // Culled Gaussians (radius 0, empty rectangle in the geometry state) get
-// zeros in every output.
+// zeros in every output.  Results are staged in shared memory and each
+// block stores its contiguous slice of every output array with coalesced
+// writes (most Gaussians are culled: their outputs are zero-filled at full
+// bandwidth instead of by strided per-thread stores).
 #include "kernels.cuh"
 
 namespace dmgs {
 
 namespace {
 
-__global__ void __launch_bounds__(256)
-preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
-                      const float *__restrict__ projm_g, const float *__restrict__ campos_g,
-                      int P, int M, const float *__restrict__ means,
-                      const float *__restrict__ shs, const float *__restrict__ scales,
-                      const float *__restrict__ rots, const float *__restrict__ cov3D,
-                      const float4 *__restrict__ feat, const uint8_t *__restrict__ clamped,
-                      const float *__restrict__ gacc, DmgsGrads out) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= P) return;
+constexpr int BWD_BLOCK = 128;
+
+// Shared-memory output slots of one block (struct of arrays; thread t owns
+// element t of each).
+struct Slots {
+  float *m2, *col, *op, *m3, *cov, *sc, *rot, *sh;
+};
+
+__device__ __forceinline__ void
+preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict__ viewm_g,
+                   const float *__restrict__ projm_g, const float *__restrict__ campos_g, int M,
+                   const float *__restrict__ means, const float *__restrict__ shs,
+                   const float *__restrict__ scales, const float *__restrict__ rots,
+                   const float *__restrict__ cov3D, const float4 *__restrict__ feat,
+                   const uint8_t *__restrict__ clamped, const float *__restrict__ gacc,
+                   const DmgsGrads &out, const Slots &S_) {
   // visible <=> the forward stored a non-empty tile rectangle (radius > 0)
   const float4 f2 = feat[3 * idx + 2];
   const bool vis = (__float_as_uint(f2.z) | __float_as_uint(f2.w)) != 0u;
   const int nsh = (vp.D + 1) * (vp.D + 1);
 
   if (!vis) {
-    if (out.dL_dmeans2D) { out.dL_dmeans2D[3 * idx] = 0.f; out.dL_dmeans2D[3 * idx + 1] = 0.f; out.dL_dmeans2D[3 * idx + 2] = 0.f; }
-    if (out.dL_dcolors) { out.dL_dcolors[3 * idx] = 0.f; out.dL_dcolors[3 * idx + 1] = 0.f; out.dL_dcolors[3 * idx + 2] = 0.f; }
-    if (out.dL_dopacity) out.dL_dopacity[idx] = 0.f;
-    if (out.dL_dmeans3D) { out.dL_dmeans3D[3 * idx] = 0.f; out.dL_dmeans3D[3 * idx + 1] = 0.f; out.dL_dmeans3D[3 * idx + 2] = 0.f; }
-    if (out.dL_dcov3D) for (int i = 0; i < 6; ++i) out.dL_dcov3D[6 * idx + i] = 0.f;
-    if (out.dL_dsh) for (int i = 0; i < 3 * M; ++i) out.dL_dsh[(size_t)idx * 3 * M + i] = 0.f;
-    if (out.dL_dscales) { out.dL_dscales[3 * idx] = 0.f; out.dL_dscales[3 * idx + 1] = 0.f; out.dL_dscales[3 * idx + 2] = 0.f; }
-    if (out.dL_drotations) reinterpret_cast<float4 *>(out.dL_drotations)[idx] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (out.dL_dmeans2D) { S_.m2[3 * t] = 0.f; S_.m2[3 * t + 1] = 0.f; S_.m2[3 * t + 2] = 0.f; }
+    if (out.dL_dcolors) { S_.col[3 * t] = 0.f; S_.col[3 * t + 1] = 0.f; S_.col[3 * t + 2] = 0.f; }
+    if (out.dL_dopacity) S_.op[t] = 0.f;
+    if (out.dL_dmeans3D) { S_.m3[3 * t] = 0.f; S_.m3[3 * t + 1] = 0.f; S_.m3[3 * t + 2] = 0.f; }
+    if (out.dL_dcov3D) for (int i = 0; i < 6; ++i) S_.cov[6 * t + i] = 0.f;
+    if (out.dL_dsh) for (int i = 0; i < 3 * M; ++i) S_.sh[(size_t)t * 3 * M + i] = 0.f;
+    if (out.dL_dscales) { S_.sc[3 * t] = 0.f; S_.sc[3 * t + 1] = 0.f; S_.sc[3 * t + 2] = 0.f; }
+    if (out.dL_drotations) { S_.rot[4 * t] = 0.f; S_.rot[4 * t + 1] = 0.f; S_.rot[4 * t + 2] = 0.f; S_.rot[4 * t + 3] = 0.f; }
     return;
   }
 
@@ -56,9 +65,9 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   const float dop = gb.y;
   float drgb[3] = {gb.z, gb.w, gblue};
 
-  if (out.dL_dmeans2D) { out.dL_dmeans2D[3 * idx] = dndc_x; out.dL_dmeans2D[3 * idx + 1] = dndc_y; out.dL_dmeans2D[3 * idx + 2] = 0.f; }
-  if (out.dL_dopacity) out.dL_dopacity[idx] = dop;
-  if (out.dL_dcolors) { out.dL_dcolors[3 * idx] = drgb[0]; out.dL_dcolors[3 * idx + 1] = drgb[1]; out.dL_dcolors[3 * idx + 2] = drgb[2]; }
+  if (out.dL_dmeans2D) { S_.m2[3 * t] = dndc_x; S_.m2[3 * t + 1] = dndc_y; S_.m2[3 * t + 2] = 0.f; }
+  if (out.dL_dopacity) S_.op[t] = dop;
+  if (out.dL_dcolors) { S_.col[3 * t] = drgb[0]; S_.col[3 * t + 1] = drgb[1]; S_.col[3 * t + 2] = drgb[2]; }
 
   float V[16], Pm[16];
 #pragma unroll
@@ -150,7 +159,7 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
 #pragma unroll
     for (int j = 0; j < 3; ++j) dS[i * 3 + j] = T[0][i] * GT[0][j] + T[1][i] * GT[1][j];
   if (out.dL_dcov3D) {
-    float *o = out.dL_dcov3D + 6 * idx;
+    float *o = S_.cov + 6 * t;
     o[0] = dS[0]; o[1] = 2.f * dS[1]; o[2] = 2.f * dS[2];
     o[3] = dS[4]; o[4] = 2.f * dS[5]; o[5] = dS[8];
   }
@@ -205,7 +214,7 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
     const float il = 1.f / len;
     const float x = vx_ * il, y = vy_ * il, z = vz_ * il;
     const float *sh = shs + (size_t)idx * M * 3;
-    float *dsh = out.dL_dsh ? out.dL_dsh + (size_t)idx * M * 3 : nullptr;
+    float *dsh = out.dL_dsh ? S_.sh + (size_t)t * M * 3 : nullptr;
     // basis value b_k and its partial derivatives (bx, by, bz) w.r.t. the
     // unnormalised-direction components x, y, z
     float gdx = 0.f, gdy = 0.f, gdz = 0.f;
@@ -253,9 +262,9 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   }
 
   if (out.dL_dmeans3D) {
-    out.dL_dmeans3D[3 * idx] = dm[0];
-    out.dL_dmeans3D[3 * idx + 1] = dm[1];
-    out.dL_dmeans3D[3 * idx + 2] = dm[2];
+    S_.m3[3 * t] = dm[0];
+    S_.m3[3 * t + 1] = dm[1];
+    S_.m3[3 * t + 2] = dm[2];
   }
 
   // --- scale / rotation --------------------------------------------------
@@ -275,7 +284,7 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
     if (out.dL_dscales) {
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        out.dL_dscales[3 * idx + j] =
+        S_.sc[3 * t + j] =
             vp.scale_modifier * (dM[j] * R[j] + dM[3 + j] * R[3 + j] + dM[6 + j] * R[6 + j]);
     }
     if (out.dL_drotations) {
@@ -292,9 +301,54 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
                               z * G[7] - 2.f * y * G[8]);
       const float dz = 2.f * (-2.f * z * G[0] - r * G[1] + x * G[2] + r * G[3] - 2.f * z * G[4] +
                               y * G[5] + x * G[6] + y * G[7]);
-      reinterpret_cast<float4 *>(out.dL_drotations)[idx] = make_float4(dr, dx, dy, dz);
+      { S_.rot[4 * t] = dr; S_.rot[4 * t + 1] = dx; S_.rot[4 * t + 2] = dy; S_.rot[4 * t + 3] = dz; }
     }
   }
+}
+
+
+__global__ void __launch_bounds__(BWD_BLOCK)
+preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
+                      const float *__restrict__ projm_g, const float *__restrict__ campos_g,
+                      int P, int M, const float *__restrict__ means,
+                      const float *__restrict__ shs, const float *__restrict__ scales,
+                      const float *__restrict__ rots, const float *__restrict__ cov3D,
+                      const float4 *__restrict__ feat, const uint8_t *__restrict__ clamped,
+                      const float *__restrict__ gacc, DmgsGrads out) {
+  extern __shared__ float sm[];
+  const int B = BWD_BLOCK;
+  const int t = threadIdx.x;
+  const int start = blockIdx.x * B;
+  const int idx = start + t;
+  Slots S_;
+  S_.m2 = sm;
+  S_.col = S_.m2 + 3 * B;
+  S_.op = S_.col + 3 * B;
+  S_.m3 = S_.op + B;
+  S_.cov = S_.m3 + 3 * B;
+  S_.sc = S_.cov + 6 * B;
+  S_.rot = S_.sc + 3 * B;
+  S_.sh = S_.rot + 4 * B;
+  if (idx < P)
+    preprocess_bwd_one(idx, t, vp, viewm_g, projm_g, campos_g, M, means, shs, scales, rots, cov3D,
+                       feat, clamped, gacc, out, S_);
+  __syncthreads();
+  // Coalesced stores of the block's contiguous output regions.
+  const int nvalid = min(B, P - start);
+  auto store = [&](float *dst, const float *src, int n) {
+    if (!dst) return;
+    float *d = dst + (size_t)start * n;
+    const int cnt = nvalid * n;
+    for (int i = t; i < cnt; i += B) d[i] = src[i];
+  };
+  store(out.dL_dmeans2D, S_.m2, 3);
+  store(out.dL_dcolors, S_.col, 3);
+  store(out.dL_dopacity, S_.op, 1);
+  store(out.dL_dmeans3D, S_.m3, 3);
+  store(out.dL_dcov3D, S_.cov, 6);
+  store(out.dL_dscales, S_.sc, 3);
+  store(out.dL_drotations, S_.rot, 4);
+  store(out.dL_dsh, S_.sh, 3 * M);
 }
 
 }  // namespace
@@ -304,7 +358,15 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
                           const char *geom, const float *gacc, const DmgsGrads &out,
                           cudaStream_t s) {
   if (g.P <= 0) return DMGS_OK;
-  DMGS_TIMED(K_PREPROCESS_BWD, s, preprocess_bwd_kernel<<<(g.P + 255) / 256, 256, 0, s>>>(
+  const size_t smem = (size_t)BWD_BLOCK * (23 + 3 * (size_t)g.M) * 4;
+  if (smem > 200 * 1024) {
+    dmgs_host::set_error("preprocess_bwd: %d SH coefficients per Gaussian exceed shared memory", g.M);
+    return DMGS_ERR_ARG;
+  }
+  if (smem > 48 * 1024)
+    DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DMGS_TIMED(K_PREPROCESS_BWD, s, preprocess_bwd_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
       vp, viewm, projm, campos, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D,
       reinterpret_cast<const float4 *>(geom + L.feat),
       reinterpret_cast<const uint8_t *>(geom + L.clamped), gacc, out));
