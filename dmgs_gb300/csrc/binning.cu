@@ -162,7 +162,7 @@ compact_kernel(int P, const int32_t *__restrict__ radii, const float4 *__restric
 __global__ void params_kernel(int T, uint32_t *__restrict__ counters) {
   const uint32_t V = counters[CI_V];
   const uint32_t nbr = (V + RADIX_TILE - 1) / RADIX_TILE;
-  uint32_t S = (V + CHUNK_COUNT_MAX - 1) / CHUNK_COUNT_MAX;
+  uint32_t S = (V + CHUNK_COUNT_MAX - 1) / CHUNK_COUNT_MAX;  // C <= CHUNK_COUNT_MAX
   if (S < CHUNK_MIN) S = CHUNK_MIN;
   const uint32_t C = (V + S - 1) / S;
   counters[CI_NBR] = nbr;
@@ -304,6 +304,20 @@ __device__ __forceinline__ WarpGroup load_group(const uint32_t *__restrict__ ord
   return G;
 }
 
+// Lane `lane` visits tiles lane, lane+32, ... of a rw-wide rectangle in
+// row-major order; row/column advance incrementally (no per-tile division).
+struct RectWalk {
+  int row, col, dr, dc, rw;
+  __device__ __forceinline__ RectWalk(int lane, int rw_) : rw(rw_) {
+    row = lane / rw; col = lane - row * rw;
+    dr = 32 / rw; dc = 32 - dr * rw;
+  }
+  __device__ __forceinline__ void next() {
+    row += dr; col += dc;
+    if (col >= rw) { col -= rw; ++row; }
+  }
+};
+
 __global__ void __launch_bounds__(256)
 tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
                   const uint32_t *__restrict__ order, const uint32_t *__restrict__ counters,
@@ -323,7 +337,9 @@ tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
       const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
       const int rw = __shfl_sync(FULL, G.rw, i);
       const int area = __shfl_sync(FULL, G.incl - G.excl, i);
-      for (int j = lane; j < area; j += 32) atomicAdd(&cnt[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+      RectWalk it(lane, rw);
+      for (int j = lane; j < area; j += 32, it.next())
+        atomicAdd(&cnt[(y0 + it.row) * gx + x0 + it.col], 1u);
     }
   }
   __syncthreads();
@@ -366,6 +382,8 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
   const uint32_t sub = (s1 - s0 + nw - 1) / nw;
   const uint32_t a = min(s1, s0 + w * sub), bnd = min(s1, a + sub);
   uint32_t *my = off + (size_t)w * T;
+  // one Gaussian covers each tile once: within a Gaussian the lanes touch
+  // distinct counters of this warp's row, so plain read/modify/write suffices
   for (uint32_t g0 = a; g0 < bnd; g0 += 32) {
     const WarpGroup G = load_group(order, feat, g0, bnd, lane);
     const int n = (int)min(32u, bnd - g0);
@@ -373,7 +391,9 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
       const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
       const int rw = __shfl_sync(FULL, G.rw, i);
       const int area = __shfl_sync(FULL, G.incl - G.excl, i);
-      for (int j = lane; j < area; j += 32) atomicAdd(&my[(y0 + j / rw) * gx + x0 + j % rw], 1u);
+      RectWalk it(lane, rw);
+      for (int j = lane; j < area; j += 32, it.next()) ++my[(y0 + it.row) * gx + x0 + it.col];
+      __syncwarp();
     }
   }
   __syncthreads();
@@ -395,11 +415,11 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
       const int rw = __shfl_sync(FULL, G.rw, i);
       const int area = __shfl_sync(FULL, G.incl - G.excl, i);
       const uint32_t id = __shfl_sync(FULL, G.id, i);
-      // one Gaussian covers each tile once: lanes touch distinct counters
-      for (int j = lane; j < area; j += 32) {
-        const int t = (y0 + j / rw) * gx + x0 + j % rw;
-        const uint32_t p = my[t];
-        my[t] = p + 1u;
+      RectWalk it(lane, rw);
+      for (int j = lane; j < area; j += 32, it.next()) {
+        uint32_t *slot = &my[(y0 + it.row) * gx + x0 + it.col];
+        const uint32_t p = *slot;
+        *slot = p + 1u;
         if (p < K_alloc) point_list[p] = id;
         else bad = true;
       }
@@ -423,10 +443,12 @@ __global__ void debug_keys_kernel(int T, const uint2 *__restrict__ ranges,
   }
 }
 
+size_t emit_smem(int nw, int T) { return ((size_t)nw + 1) * T * 4; }
+
 int emit_warps(int T) {
-  // (nw + 1) * T * 4 bytes of shared memory, at most 220 KB
-  const int fit = (int)((220 * 1024 / 4) / (size_t)T) - 1;
-  return fit < 1 ? 0 : (fit > 8 ? 8 : fit);
+  for (int nw = 8; nw >= 1; --nw)
+    if (emit_smem(nw, T) <= 220 * 1024) return nw;
+  return 0;
 }
 
 }  // namespace
@@ -523,7 +545,7 @@ int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, 
     dmgs_host::set_error("image too large: %d tiles exceed the emission kernel's shared memory", T);
     return DMGS_ERR_ARG;
   }
-  const size_t smem = (size_t)(nw + 1) * T * 4;
+  const size_t smem = emit_smem(nw, T);
   if (smem > 48 * 1024)
     DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));

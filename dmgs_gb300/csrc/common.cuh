@@ -59,7 +59,7 @@ constexpr int RADIX_BLOCK = 256;         // radix sort block (8 warps)
 constexpr int RADIX_ITEMS = 8;           // keys per thread
 constexpr int RADIX_TILE = RADIX_BLOCK * RADIX_ITEMS;  // 2048 keys per block
 constexpr int CHUNK_MIN = 256;           // Gaussians per binning chunk (minimum)
-constexpr int CHUNK_COUNT_MAX = 1024;    // binning chunks (maximum)
+constexpr int CHUNK_COUNT_MAX = 1024;    // binning chunks per view (maximum)
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096 elements per block
