@@ -276,6 +276,8 @@ struct WarpGroup {
   int x0, y0, rw;   // its rectangle origin and width
   int excl, incl;   // exclusive / inclusive prefix of rectangle areas
   int total;        // instances of the whole group
+  uint32_t xy;      // x0 | y0 << 16
+  uint32_t wa;      // rw | area << 16 (area of one rectangle < 65536 tiles)
 };
 
 __device__ __forceinline__ WarpGroup load_group(const uint32_t *__restrict__ order,
@@ -301,16 +303,24 @@ __device__ __forceinline__ WarpGroup load_group(const uint32_t *__restrict__ ord
   G.incl = inc;
   G.excl = inc - area;
   G.total = __shfl_sync(FULL, inc, 31);
+  G.xy = (uint32_t)G.x0 | ((uint32_t)G.y0 << 16);
+  G.wa = (uint32_t)G.rw | ((uint32_t)area << 16);
   return G;
 }
 
 // Lane `lane` visits tiles lane, lane+32, ... of a rw-wide rectangle in
-// row-major order; row/column advance incrementally (no per-tile division).
+// row-major order; row/column advance incrementally.  The two divisions by
+// rw use a float reciprocal: for numerators below 33 and rw >= 1 the
+// quotient of (n + 0.5) / rw is at least 1/64 away from an integer, far
+// beyond the reciprocal's error, so truncation gives the exact quotient.
 struct RectWalk {
   int row, col, dr, dc, rw;
   __device__ __forceinline__ RectWalk(int lane, int rw_) : rw(rw_) {
-    row = lane / rw; col = lane - row * rw;
-    dr = 32 / rw; dc = 32 - dr * rw;
+    const float inv = __frcp_rn((float)rw_);
+    row = __float2int_rz(((float)lane + 0.5f) * inv);
+    col = lane - row * rw;
+    dr = __float2int_rz(32.5f * inv);
+    dc = 32 - dr * rw;
   }
   __device__ __forceinline__ void next() {
     row += dr; col += dc;
@@ -334,9 +344,9 @@ tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
     const WarpGroup G = load_group(order, feat, g0, s1, lane);
     const int n = (int)min(32u, s1 - g0);
     for (int i = 0; i < n; ++i) {
-      const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
-      const int rw = __shfl_sync(FULL, G.rw, i);
-      const int area = __shfl_sync(FULL, G.incl - G.excl, i);
+      const uint32_t xy = __shfl_sync(FULL, G.xy, i), wa = __shfl_sync(FULL, G.wa, i);
+      const int x0 = (int)(xy & 0xffffu), y0 = (int)(xy >> 16);
+      const int rw = (int)(wa & 0xffffu), area = (int)(wa >> 16);
       RectWalk it(lane, rw);
       for (int j = lane; j < area; j += 32, it.next())
         atomicAdd(&cnt[(y0 + it.row) * gx + x0 + it.col], 1u);
@@ -388,9 +398,9 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
     const WarpGroup G = load_group(order, feat, g0, bnd, lane);
     const int n = (int)min(32u, bnd - g0);
     for (int i = 0; i < n; ++i) {
-      const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
-      const int rw = __shfl_sync(FULL, G.rw, i);
-      const int area = __shfl_sync(FULL, G.incl - G.excl, i);
+      const uint32_t xy = __shfl_sync(FULL, G.xy, i), wa = __shfl_sync(FULL, G.wa, i);
+      const int x0 = (int)(xy & 0xffffu), y0 = (int)(xy >> 16);
+      const int rw = (int)(wa & 0xffffu), area = (int)(wa >> 16);
       RectWalk it(lane, rw);
       for (int j = lane; j < area; j += 32, it.next()) ++my[(y0 + it.row) * gx + x0 + it.col];
       __syncwarp();
@@ -411,9 +421,9 @@ emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__re
     const WarpGroup G = load_group(order, feat, g0, bnd, lane);
     const int n = (int)min(32u, bnd - g0);
     for (int i = 0; i < n; ++i) {
-      const int x0 = __shfl_sync(FULL, G.x0, i), y0 = __shfl_sync(FULL, G.y0, i);
-      const int rw = __shfl_sync(FULL, G.rw, i);
-      const int area = __shfl_sync(FULL, G.incl - G.excl, i);
+      const uint32_t xy = __shfl_sync(FULL, G.xy, i), wa = __shfl_sync(FULL, G.wa, i);
+      const int x0 = (int)(xy & 0xffffu), y0 = (int)(xy >> 16);
+      const int rw = (int)(wa & 0xffffu), area = (int)(wa >> 16);
       const uint32_t id = __shfl_sync(FULL, G.id, i);
       RectWalk it(lane, rw);
       for (int j = lane; j < area; j += 32, it.next()) {

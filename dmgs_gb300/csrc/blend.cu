@@ -21,6 +21,10 @@
 //   log2(1/(255 o)) is precomputed: a pair below it cannot reach alpha 1/255
 //   and is rejected before the exponential (the alpha test itself is still
 //   applied afterwards);
+// * each staged Gaussian carries row/column masks of the tile pixels its
+//   alpha >= 1/255 ellipse can reach (a superset): a warp skips it with one
+//   uniform test when it misses the warp's rows, a lane when it misses the
+//   lane's column — only pairs the exact test would reject are skipped;
 // * the forward and the adjoint evaluate the exponent with the same
 //   explicitly rounded operations, so their skip/stop decisions agree;
 // * the adjoint sums a Gaussian's nine gradient terms over the thread's two
@@ -48,23 +52,49 @@ __device__ __forceinline__ float ex2_approx(float x) {
   return y;
 }
 
-// Staged Gaussian (forward): s0 = (x, y, A, B), s1 = (C, o, thr, r), s2 = (g, b)
-// with exponent2 = A dx^2 + B dx dy + C dy^2 (A = -a log2e / 2, B = -b log2e,
-// C = -c log2e / 2) and thr = log2(1 / (255 o)).
+// Staged Gaussian (forward): s0 = (x, y, A, B), s1 = (C, o, thr, r),
+// s2 = (g, b, footprint masks, 0) with exponent2 = A dx^2 + B dx dy + C dy^2
+// (A = -a log2e / 2, B = -b log2e, C = -c log2e / 2) and thr = log2(1 / (255 o)).
+// The footprint masks (bits 0-15: tile rows, 16-31: tile columns) cover the
+// pixels of this tile where alpha can reach 1/255: the ellipse
+// (a dx^2 + 2 b dx dy + c dy^2) <= 2 ln(255 o), whose half-extents are
+// sqrt(R^2 c / det) and sqrt(R^2 a / det), inflated by 0.1% + 0.01 px so that
+// the masks are a superset of the pixels the exact test accepts.
 struct Staged {
-  float4 s0, s1;
-  float2 s2;
+  float4 s0, s1, s2;
 };
 
-__device__ __forceinline__ Staged stage(const float4 f0, const float4 f1, const float4 f2) {
+__device__ __forceinline__ uint32_t span_mask(float centre, float ext) {
+  const float lo = fmaxf(ceilf(centre - ext), 0.f);
+  const float hi = fminf(floorf(centre + ext), 15.f);
+  if (!(lo <= hi)) return 0u;
+  const int l = (int)lo, h = (int)hi;
+  return (0xffffu >> (15 - h)) & (0xffffu << l);
+}
+
+__device__ __forceinline__ uint32_t footprint(float a, float b, float c, float o, float cx, float cy) {
+  if (!(o >= ALPHA_MIN)) return 0u;                  // alpha <= o < 1/255 everywhere
+  const float det = a * c - b * b;
+  if (!(det > 0.f) || !(a > 0.f) || !(c > 0.f)) return 0xffffffffu;  // not an ellipse
+  const float R2 = 2.f * (__logf(o) + 5.541263545158426f);  // 2 ln(255 o)
+  if (!(R2 >= 0.f)) return 0u;
+  const float ex = sqrtf(R2 * c / det) * 1.001f + 0.01f;
+  const float ey = sqrtf(R2 * a / det) * 1.001f + 0.01f;
+  return span_mask(cy, ey) | (span_mask(cx, ex) << 16);
+}
+
+// (ox, oy): pixel origin of the tile being blended.
+__device__ __forceinline__ Staged stage(const float4 f0, const float4 f1, const float4 f2,
+                                        float ox, float oy) {
   Staged S;
   const float A = __fmul_rn(-0.5f * LOG2E, f0.z);
   const float B = __fmul_rn(-LOG2E, f0.w);
   const float C = __fmul_rn(-0.5f * LOG2E, f1.x);
   const float thr = -LOG2_255 - __log2f(f1.y);
+  const uint32_t m = footprint(f0.z, f0.w, f1.x, f1.y, f0.x - ox, f0.y - oy);
   S.s0 = make_float4(f0.x, f0.y, A, B);
   S.s1 = make_float4(C, f1.y, thr, f1.z);
-  S.s2 = make_float2(f1.w, f2.x);
+  S.s2 = make_float4(f1.w, f2.x, __uint_as_float(m), 0.f);
   return S;
 }
 
@@ -84,14 +114,14 @@ __device__ __forceinline__ float pair_alpha(float e2, float o, float thr, float 
   return alpha < ALPHA_MIN ? 0.f : alpha;
 }
 
-__global__ void __launch_bounds__(BLEND_THREADS)
+__global__ void __launch_bounds__(BLEND_THREADS, 6)
 blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
                  const uint32_t *__restrict__ point_list, const float4 *__restrict__ feat,
                  const float *__restrict__ bg, float *__restrict__ out_color,
                  float *__restrict__ final_T, uint32_t *__restrict__ n_contrib) {
   __shared__ float4 S0[2][BATCH];
   __shared__ float4 S1[2][BATCH];
-  __shared__ float2 S2[2][BATCH];
+  __shared__ float4 S2[2][BATCH];
   const int tile = blockIdx.x;
   const int tx = tile % gx, ty = tile / gx;
   const int tid = threadIdx.x;
@@ -100,12 +130,18 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
   const int py1 = py0 + 8;
   const bool in0 = px < W && py0 < H, in1 = px < W && py1 < H;
   const float pxf = (float)px, py0f = (float)py0, py1f = (float)py1;
+  const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
   const uint2 range = ranges[tile];
   const int n = (int)(range.y - range.x);
+  // footprint-mask bits of this thread's pixels and of its warp's rows
+  const int r0 = tid >> 4;
+  const uint32_t colbit = 1u << (16 + (tid & 15));
+  const uint32_t row0bit = 1u << r0, row1bit = 1u << (r0 + 8);
+  const uint32_t warp_rows = (3u << ((r0 >> 1) << 1)) | (3u << (((r0 >> 1) << 1) + 8));
 
   bool done0 = !in0, done1 = !in1;
   float T0 = 1.f, T1 = 1.f;
-  float r0 = 0.f, g0 = 0.f, b0 = 0.f, r1 = 0.f, g1 = 0.f, b1 = 0.f;
+  float r0c = 0.f, g0 = 0.f, b0 = 0.f, r1 = 0.f, g1 = 0.f, b1 = 0.f;
   uint32_t last0 = 0, last1 = 0;
 
   // prefetch batch 0 into registers
@@ -126,7 +162,7 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
     for (int k = 0; k < PER_THREAD; ++k) {
       const int i = base + k * BLEND_THREADS + tid;
       if (i < n) {
-        const Staged s = stage(pf0[k], pf1[k], pf2[k]);
+        const Staged s = stage(pf0[k], pf1[k], pf2[k], ox, oy);
         const int slot = k * BLEND_THREADS + tid;
         S0[buf][slot] = s.s0; S1[buf][slot] = s.s1; S2[buf][slot] = s.s2;
       }
@@ -144,10 +180,14 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
     }
     const int cnt = min(BATCH, n - base);
     for (int j = 0; j < cnt && !(done0 && done1); ++j) {
+      const float4 s2 = S2[buf][j];
+      const uint32_t m = __float_as_uint(s2.z);
+      if (!(m & warp_rows)) continue;  // warp-uniform: the footprint misses the warp's rows
+      if (!(m & colbit)) continue;
       const float4 s0 = S0[buf][j];
       const float4 s1 = S1[buf][j];
       const float dx = __fsub_rn(s0.x, pxf);
-      if (!done0) {
+      if (!done0 && (m & row0bit)) {
         float G;
         const float e2 = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, py0f));
         const float alpha = pair_alpha(e2, s1.y, s1.z, G);
@@ -156,15 +196,14 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
           if (test_T < T_EPS) {
             done0 = true;
           } else {
-            const float2 s2 = S2[buf][j];
             const float w = alpha * T0;
-            r0 = fmaf(s1.w, w, r0); g0 = fmaf(s2.x, w, g0); b0 = fmaf(s2.y, w, b0);
+            r0c = fmaf(s1.w, w, r0c); g0 = fmaf(s2.x, w, g0); b0 = fmaf(s2.y, w, b0);
             T0 = test_T;
             last0 = base + j + 1;
           }
         }
       }
-      if (!done1) {
+      if (!done1 && (m & row1bit)) {
         float G;
         const float e2 = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, py1f));
         const float alpha = pair_alpha(e2, s1.y, s1.z, G);
@@ -173,7 +212,6 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
           if (test_T < T_EPS) {
             done1 = true;
           } else {
-            const float2 s2 = S2[buf][j];
             const float w = alpha * T1;
             r1 = fmaf(s1.w, w, r1); g1 = fmaf(s2.x, w, g1); b1 = fmaf(s2.y, w, b1);
             T1 = test_T;
@@ -190,7 +228,7 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
     const int pix = py0 * W + px;
     final_T[pix] = T0;
     n_contrib[pix] = last0;
-    out_color[pix] = r0 + T0 * bgr;
+    out_color[pix] = r0c + T0 * bgr;
     out_color[HW + pix] = g0 + T0 * bgg;
     out_color[2 * HW + pix] = b0 + T0 * bgb;
   }
@@ -207,20 +245,20 @@ blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
 // ------------------------------- adjoint -----------------------------------
 
 // Staged Gaussian (adjoint): s0 = (x, y, A, B), s1 = (C, o, thr, r),
-// s2 = (g, b, ka, kb), s3 = (kc, kd, id bits, 0) with ka = -a W/2,
+// s2 = (g, b, ka, kb), s3 = (kc, kd, id bits, footprint masks) with ka = -a W/2,
 // kb = -b W/2, kc = -c H/2, kd = -b H/2 (the NDC-mean gradient factors).
 struct StagedB {
   float4 s0, s1, s2, s3;
 };
 
 __device__ __forceinline__ StagedB stage_b(const float4 f0, const float4 f1, const float4 f2,
-                                           uint32_t id, float hw, float hh) {
-  const Staged s = stage(f0, f1, f2);
+                                           uint32_t id, float hw, float hh, float ox, float oy) {
+  const Staged s = stage(f0, f1, f2, ox, oy);
   StagedB S;
   S.s0 = s.s0;
   S.s1 = s.s1;
   S.s2 = make_float4(s.s2.x, s.s2.y, -f0.z * hw, -f0.w * hw);
-  S.s3 = make_float4(-f1.x * hh, -f0.w * hh, __uint_as_float(id), 0.f);
+  S.s3 = make_float4(-f1.x * hh, -f0.w * hh, __uint_as_float(id), s.s2.z);
   return S;
 }
 
@@ -332,9 +370,14 @@ blend_bwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
   const int py1 = py0 + 8;
   const bool in0 = px < W && py0 < H, in1 = px < W && py1 < H;
   const float pxf = (float)px, py0f = (float)py0, py1f = (float)py1;
+  const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
   const uint2 range = ranges[tile];
   const int n = (int)(range.y - range.x);
   if (n == 0) return;
+  const int r0 = tid >> 4;
+  const uint32_t colbit = 1u << (16 + (tid & 15));
+  const uint32_t row0bit = 1u << r0, row1bit = 1u << (r0 + 8);
+  const uint32_t warp_rows = (3u << ((r0 >> 1) << 1)) | (3u << (((r0 >> 1) << 1) + 8));
 
   const size_t HW = (size_t)H * W;
   const float bg0 = __ldg(bg), bg1 = __ldg(bg + 1), bg2 = __ldg(bg + 2);
@@ -357,22 +400,26 @@ blend_bwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
       const int slot = k * BLEND_THREADS + tid;
       if (slot < cnt) {
         const uint32_t id = point_list[range.x + top - 1 - slot];  // back to front
-        const StagedB s = stage_b(feat[3 * id], feat[3 * id + 1], feat[3 * id + 2], id, hw, hh);
+        const StagedB s =
+            stage_b(feat[3 * id], feat[3 * id + 1], feat[3 * id + 2], id, hw, hh, ox, oy);
         S0[slot] = s.s0; S1[slot] = s.s1; S2[slot] = s.s2; S3[slot] = s.s3;
       }
     }
     __syncthreads();
     for (int j = 0; j < cnt; ++j) {
       const int li = top - 1 - j;
-      const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j], s3 = S3[j];
+      const float4 s3 = S3[j];
+      const uint32_t m = __float_as_uint(s3.w);
+      if (!(m & warp_rows)) continue;  // warp-uniform: the footprint misses the warp's rows
+      const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j];
       float e[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) e[i] = 0.f;
       const float dx = __fsub_rn(s0.x, pxf);
       bool any = false;
-      if (li < (int)P0.last_contrib)
+      if ((m & colbit) && (m & row0bit) && li < (int)P0.last_contrib)
         any |= adjoint_pair(P0, s0, s1, s2, s3, dx, __fsub_rn(s0.y, py0f), e);
-      if (li < (int)P1.last_contrib)
+      if ((m & colbit) && (m & row1bit) && li < (int)P1.last_contrib)
         any |= adjoint_pair(P1, s0, s1, s2, s3, dx, __fsub_rn(s0.y, py1f), e);
       if (__ballot_sync(FULL, any)) {
         const float sum = warp_reduce_scatter16(e, lane);
