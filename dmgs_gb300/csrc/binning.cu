@@ -139,11 +139,11 @@ scan_down_kernel(uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev
 // ---- compaction of visible Gaussians (index order) ----------------------
 
 __global__ void __launch_bounds__(PRE_BLOCK)
-compact_kernel(int P, const int32_t *__restrict__ radii, const float4 *__restrict__ feat,
+compact_kernel(int P, const uint8_t *__restrict__ flags, const float4 *__restrict__ feat,
                const uint32_t *__restrict__ blkoff, uint32_t *__restrict__ dkey,
                uint32_t *__restrict__ dval) {
   const int idx = blockIdx.x * PRE_BLOCK + threadIdx.x;
-  const bool v = idx < P && radii[idx] > 0;
+  const bool v = idx < P && (flags[idx] & FLAG_VISIBLE);
   __shared__ uint32_t wcount[PRE_BLOCK / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned b = __ballot_sync(FULL, v);
@@ -496,7 +496,7 @@ int launch_binning_geometry(const GeomLayout &L, const int32_t *radii, char *geo
     DMGS_TIMED(K_BIN_COMPACT, s, {
       int r = launch_scan(blkcnt, nullptr, (uint32_t)L.nb_pre, part, counters + CI_V, counters, s);
       if (r != DMGS_OK) return r;
-      compact_kernel<<<L.nb_pre, PRE_BLOCK, 0, s>>>(L.P, radii, feat, blkcnt, k0, v0);
+      compact_kernel<<<L.nb_pre, PRE_BLOCK, 0, s>>>(L.P, reinterpret_cast<const uint8_t *>(geom + L.flags), feat, blkcnt, k0, v0);
     });
     DMGS_LAUNCH_CHECK("compact_kernel");
   }

@@ -49,11 +49,13 @@ struct ViewParams {
 //   f1 = (conic_c, opacity, r, g)
 //   f2 = (b, depth, rect_lo, rect_hi) rect packed as 2 x (u16 | u16 << 16)
 // A culled Gaussian has rect_lo == rect_hi == 0 and radius 0.
+// Per Gaussian also one flags byte: FLAG_VISIBLE | SH clamp bits (r, g, b).
 // Then the binning working set: per-block visible counts, the visible
 // Gaussians' depth keys / indices (two ping-pong copies for the radix sort),
 // the radix block histograms, the per-(tile, chunk) count matrix, scan
 // partials, per-tile ranges and the counters word block.
 // ---------------------------------------------------------------------------
+constexpr uint8_t FLAG_VISIBLE = 8;      // flags byte: radius > 0, tile rectangle non-empty
 constexpr int PRE_BLOCK = 256;           // preprocess / compaction block
 constexpr int RADIX_BLOCK = 256;         // radix sort block (8 warps)
 constexpr int RADIX_ITEMS = 8;           // keys per thread
@@ -77,7 +79,7 @@ constexpr int CI_NCM = 9;      // count-matrix entries = T * C
 constexpr int CI_WORDS = 16;
 
 struct GeomLayout {
-  size_t feat, clamped, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, scanpart, ranges,
+  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, scanpart, ranges,
       counters, total;
   int P, gx, gy;
   int nb_pre, nb_radix;
@@ -100,7 +102,7 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.n_part_max = (nmax + SCAN_TILE - 1) / SCAN_TILE + 1;
   size_t o = 0;
   L.feat = o;      o = align_up(o + (size_t)P * 48, 256);
-  L.clamped = o;   o = align_up(o + (size_t)P, 256);
+  L.flags = o;     o = align_up(o + (size_t)P, 256);
   L.blkcnt = o;    o = align_up(o + (size_t)L.nb_pre * 4 + 4, 256);
   L.dkey0 = o;     o = align_up(o + (size_t)P * 4, 256);
   L.dkey1 = o;     o = align_up(o + (size_t)P * 4, 256);

@@ -62,7 +62,7 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
                const float *__restrict__ shs, const float *__restrict__ colors,
                const float *__restrict__ scales, const float *__restrict__ rots,
                const float *__restrict__ cov3D, int32_t *__restrict__ radii,
-               float4 *__restrict__ feat, uint8_t *__restrict__ clamped,
+               float4 *__restrict__ feat, uint8_t *__restrict__ flags,
                uint32_t *__restrict__ counters) {
 
   float V[16], Pm[16];
@@ -77,6 +77,7 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
 
   auto cull = [&]() {
     radii[idx] = 0;
+    flags[idx] = 0;
     feat[3 * idx + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
   };
   if (!(vz > 0.2f)) {
@@ -198,8 +199,8 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
     rr += 0.5f; gg += 0.5f; bb += 0.5f;
     clampbits = (rr < 0.f ? 1 : 0) | (gg < 0.f ? 2 : 0) | (bb < 0.f ? 4 : 0);
     cr = fmaxf(rr, 0.f); cg = fmaxf(gg, 0.f); cbl = fmaxf(bb, 0.f);
-    clamped[idx] = clampbits;
   }
+  flags[idx] = FLAG_VISIBLE | clampbits;
 
   const float o = __ldg(opac + idx);
   radii[idx] = rad;
@@ -219,12 +220,12 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
                   const float *__restrict__ colors, const float *__restrict__ scales,
                   const float *__restrict__ rots, const float *__restrict__ cov3D,
                   int32_t *__restrict__ radii, float4 *__restrict__ feat,
-                  uint8_t *__restrict__ clamped, uint32_t *__restrict__ blkcnt,
+                  uint8_t *__restrict__ flags, uint32_t *__restrict__ blkcnt,
                   uint32_t *__restrict__ counters) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   const bool vis = idx < P &&
                    preprocess_one(idx, vp, viewm_g, projm_g, campos_g, M, means, opac, shs, colors,
-                                  scales, rots, cov3D, radii, feat, clamped, counters);
+                                  scales, rots, cov3D, radii, feat, flags, counters);
   const int nvis = __syncthreads_count(vis);
   if (threadIdx.x == 0) blkcnt[blockIdx.x] = (uint32_t)nvis;
 }
@@ -247,7 +248,7 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
                       const float *campos, const GaussianPtrs &g, int32_t *radii,
                       const GeomLayout &L, char *geom, cudaStream_t s) {
   float4 *feat = reinterpret_cast<float4 *>(geom + L.feat);
-  uint8_t *clamped = reinterpret_cast<uint8_t *>(geom + L.clamped);
+  uint8_t *flags = reinterpret_cast<uint8_t *>(geom + L.flags);
   uint32_t *blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
   uint32_t *counters = reinterpret_cast<uint32_t *>(geom + L.counters);
   DMGS_CUDA(cudaMemsetAsync(counters, 0, CI_WORDS * 4, s));
@@ -255,7 +256,7 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
     const int blocks = L.nb_pre;
     DMGS_TIMED(K_PREPROCESS, s, preprocess_kernel<<<blocks, PRE_BLOCK, 0, s>>>(vp, viewm, projm, campos, g.P, g.M, g.means3D,
                                                  g.opacities, g.shs, g.colors, g.scales,
-                                                 g.rotations, g.cov3D, radii, feat, clamped, blkcnt,
+                                                 g.rotations, g.cov3D, radii, feat, flags, blkcnt,
                                                  counters));
     DMGS_LAUNCH_CHECK("preprocess_kernel");
   }

@@ -37,26 +37,9 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
                    const float *__restrict__ projm_g, const float *__restrict__ campos_g, int M,
                    const float *__restrict__ means, const float *__restrict__ shs,
                    const float *__restrict__ scales, const float *__restrict__ rots,
-                   const float *__restrict__ cov3D, const float4 *__restrict__ feat,
-                   const uint8_t *__restrict__ clamped, const float *__restrict__ gacc,
-                   const DmgsGrads &out, const Slots &S_) {
-  // visible <=> the forward stored a non-empty tile rectangle (radius > 0)
-  const float4 f2 = feat[3 * idx + 2];
-  const bool vis = (__float_as_uint(f2.z) | __float_as_uint(f2.w)) != 0u;
+                   const float *__restrict__ cov3D, const uint8_t *__restrict__ flags,
+                   const float *__restrict__ gacc, const DmgsGrads &out, const Slots &S_) {
   const int nsh = (vp.D + 1) * (vp.D + 1);
-
-  if (!vis) {
-    if (out.dL_dmeans2D) { S_.m2[3 * t] = 0.f; S_.m2[3 * t + 1] = 0.f; S_.m2[3 * t + 2] = 0.f; }
-    if (out.dL_dcolors) { S_.col[3 * t] = 0.f; S_.col[3 * t + 1] = 0.f; S_.col[3 * t + 2] = 0.f; }
-    if (out.dL_dopacity) S_.op[t] = 0.f;
-    if (out.dL_dmeans3D) { S_.m3[3 * t] = 0.f; S_.m3[3 * t + 1] = 0.f; S_.m3[3 * t + 2] = 0.f; }
-    if (out.dL_dcov3D) for (int i = 0; i < 6; ++i) S_.cov[6 * t + i] = 0.f;
-    if (out.dL_dsh) for (int i = 0; i < 3 * M; ++i) S_.sh[(size_t)t * 3 * M + i] = 0.f;
-    if (out.dL_dscales) { S_.sc[3 * t] = 0.f; S_.sc[3 * t + 1] = 0.f; S_.sc[3 * t + 2] = 0.f; }
-    if (out.dL_drotations) { S_.rot[4 * t] = 0.f; S_.rot[4 * t + 1] = 0.f; S_.rot[4 * t + 2] = 0.f; S_.rot[4 * t + 3] = 0.f; }
-    return;
-  }
-
   const float4 ga = reinterpret_cast<const float4 *>(gacc)[3 * idx];
   const float4 gb = reinterpret_cast<const float4 *>(gacc)[3 * idx + 1];
   const float gblue = gacc[12 * idx + 8];
@@ -205,7 +188,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
 
   // --- SH colour ---------------------------------------------------------
   if (shs != nullptr) {
-    const uint8_t cl = clamped[idx];
+    const uint8_t cl = flags[idx];
     if (cl & 1) drgb[0] = 0.f;
     if (cl & 2) drgb[1] = 0.f;
     if (cl & 4) drgb[2] = 0.f;
@@ -307,15 +290,41 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
 }
 
 
+// Stores the block's contiguous slice of one output array: element i of the
+// slice belongs to Gaussian i / n of the block; culled Gaussians get zeros
+// (their shared-memory slots are never written).
+__device__ __forceinline__ void store_slice(float *dst, const float *src, int n, int start,
+                                            int nvalid, const uint32_t *vmask) {
+  if (!dst) return;
+  float *d = dst + (size_t)start * n;
+  const int cnt = nvalid * n;
+  // ceil(2^32 / n) for n >= 2; i / n = umulhi(i, magic) exactly for i, n < 2^16
+  const uint32_t magic = n > 1 ? (uint32_t)(0xffffffffull / (uint32_t)n) + 1u : 0u;
+  auto vis = [&](int i) {
+    const uint32_t g = n > 1 ? __umulhi((uint32_t)i, magic) : (uint32_t)i;
+    return (vmask[g >> 5] >> (g & 31)) & 1u;
+  };
+  if ((n & 3) == 0 && (cnt & 3) == 0 && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+    // whole float4s never straddle two Gaussians when n % 4 == 0
+    float4 *d4 = reinterpret_cast<float4 *>(d);
+    const float4 *s4 = reinterpret_cast<const float4 *>(src);
+    for (int i = threadIdx.x; i < (cnt >> 2); i += BWD_BLOCK)
+      d4[i] = vis(i << 2) ? s4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  } else {
+    for (int i = threadIdx.x; i < cnt; i += BWD_BLOCK) d[i] = vis(i) ? src[i] : 0.f;
+  }
+}
+
 __global__ void __launch_bounds__(BWD_BLOCK)
 preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
                       const float *__restrict__ projm_g, const float *__restrict__ campos_g,
                       int P, int M, const float *__restrict__ means,
                       const float *__restrict__ shs, const float *__restrict__ scales,
                       const float *__restrict__ rots, const float *__restrict__ cov3D,
-                      const float4 *__restrict__ feat, const uint8_t *__restrict__ clamped,
-                      const float *__restrict__ gacc, DmgsGrads out) {
+                      const uint8_t *__restrict__ flags, const float *__restrict__ gacc,
+                      DmgsGrads out) {
   extern __shared__ float sm[];
+  __shared__ uint32_t vmask[BWD_BLOCK / 32];
   const int B = BWD_BLOCK;
   const int t = threadIdx.x;
   const int start = blockIdx.x * B;
@@ -329,26 +338,22 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   S_.sc = S_.cov + 6 * B;
   S_.rot = S_.sc + 3 * B;
   S_.sh = S_.rot + 4 * B;
-  if (idx < P)
+  const bool vis = idx < P && (flags[idx] & FLAG_VISIBLE);
+  const uint32_t bal = __ballot_sync(0xffffffffu, vis);
+  if ((t & 31) == 0) vmask[t >> 5] = bal;
+  if (vis)
     preprocess_bwd_one(idx, t, vp, viewm_g, projm_g, campos_g, M, means, shs, scales, rots, cov3D,
-                       feat, clamped, gacc, out, S_);
+                       flags, gacc, out, S_);
   __syncthreads();
-  // Coalesced stores of the block's contiguous output regions.
   const int nvalid = min(B, P - start);
-  auto store = [&](float *dst, const float *src, int n) {
-    if (!dst) return;
-    float *d = dst + (size_t)start * n;
-    const int cnt = nvalid * n;
-    for (int i = t; i < cnt; i += B) d[i] = src[i];
-  };
-  store(out.dL_dmeans2D, S_.m2, 3);
-  store(out.dL_dcolors, S_.col, 3);
-  store(out.dL_dopacity, S_.op, 1);
-  store(out.dL_dmeans3D, S_.m3, 3);
-  store(out.dL_dcov3D, S_.cov, 6);
-  store(out.dL_dscales, S_.sc, 3);
-  store(out.dL_drotations, S_.rot, 4);
-  store(out.dL_dsh, S_.sh, 3 * M);
+  store_slice(out.dL_dmeans2D, S_.m2, 3, start, nvalid, vmask);
+  store_slice(out.dL_dcolors, S_.col, 3, start, nvalid, vmask);
+  store_slice(out.dL_dopacity, S_.op, 1, start, nvalid, vmask);
+  store_slice(out.dL_dmeans3D, S_.m3, 3, start, nvalid, vmask);
+  store_slice(out.dL_dcov3D, S_.cov, 6, start, nvalid, vmask);
+  store_slice(out.dL_dscales, S_.sc, 3, start, nvalid, vmask);
+  store_slice(out.dL_drotations, S_.rot, 4, start, nvalid, vmask);
+  store_slice(out.dL_dsh, S_.sh, 3 * M, start, nvalid, vmask);
 }
 
 }  // namespace
@@ -368,8 +373,7 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   DMGS_TIMED(K_PREPROCESS_BWD, s, preprocess_bwd_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
       vp, viewm, projm, campos, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D,
-      reinterpret_cast<const float4 *>(geom + L.feat),
-      reinterpret_cast<const uint8_t *>(geom + L.clamped), gacc, out));
+      reinterpret_cast<const uint8_t *>(geom + L.flags), gacc, out));
   DMGS_LAUNCH_CHECK("preprocess_bwd_kernel");
   return DMGS_OK;
 }
