@@ -50,6 +50,13 @@ class DmgsFaceBinding3(C.Structure):
                 ("verts", vp), ("faces", vp), ("bc", vp), ("scaling2d", vp), ("rotation2d", vp)]
 
 
+class DmgsBatch(C.Structure):
+    _fields_ = [("nviews", C.c_int32), ("views", C.POINTER(DmgsView)),
+                ("out_color", C.POINTER(vp)), ("radii", C.POINTER(vp)),
+                ("capacity", C.POINTER(C.c_int64)), ("pixels_per_thread", C.c_int32),
+                ("gaussians_per_batch", C.c_int32)]
+
+
 DMGS_ERRORS = {-1: "DMGS_ERR_ARG", -2: "DMGS_ERR_CUDA", -3: "DMGS_ERR_STATE",
                -4: "DMGS_ERR_PREFILTER", -5: "DMGS_ERR_OVERFLOW", -6: "DMGS_ERR_DEVICE"}
 
@@ -72,6 +79,14 @@ SIGNATURES = [
     ("dmgs_raster_bwd_noalloc", C.c_int, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians), vp,
                                           vp, C.c_size_t, vp, C.c_size_t, C.c_int64, vp,
                                           C.c_size_t, C.POINTER(DmgsGrads), vp]),
+    ("dmgs_batch_state_bytes", C.c_size_t, [C.POINTER(DmgsBatch), C.c_int32]),
+    ("dmgs_raster_fwd_batched", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians), vp,
+                                          C.c_size_t, vp]),
+    ("dmgs_raster_bwd_batched", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians),
+                                          C.POINTER(vp), vp, C.c_size_t, C.POINTER(DmgsGrads),
+                                          C.POINTER(vp), vp]),
+    ("dmgs_batch_status", C.c_int, [C.POINTER(DmgsBatch), C.c_int32, vp, C.c_size_t,
+                                    C.POINTER(C.c_int64), vp]),
     ("dmgs_mark_visible", C.c_int, [C.c_int32, vp, vp, vp, vp, vp]),
     ("dmgs_debug_geometry", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, C.c_size_t, vp, vp,
                                       vp, vp, vp, vp, vp]),

@@ -1,0 +1,269 @@
+"""Multi-view batched rendering: many views of one Gaussian set per launch.
+
+The reference renders one view per call (``render_and_eval.py:42-44``,
+``train_geo_stage2.py:101``).  Here a batch of up to 16 views of possibly
+different resolutions is rendered forward and backward by one preprocess
+pass (inputs read once), per-view binning into capacity-bounded lists, one
+persistent blend launch over every view's tiles, and an adjoint that sums
+the views' gradients (written once).  The calls never synchronise with the
+host, so a whole step can be captured in a CUDA graph (:meth:`capture`).
+
+:func:`autotune` picks the blend kernels' pixels-per-thread (1, 2, 4) and
+Gaussians-per-batch (128, 256, 512) by timing.  (The binning tile stays
+16 x 16: it defines which Gaussians reach which pixels, so another tile shape
+would change the image relative to the reference.)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import time
+
+import torch
+
+from . import _lib
+from ._lib import DmgsBatch, DmgsError, DmgsGaussians, DmgsGrads, DmgsView, check, ptr
+from .rasterizer import GaussianRasterizationSettings, _f32
+
+MAX_VIEWS = 16
+TUNE_SPACE = [(p, b) for p in (1, 2, 4) for b in (128, 256, 512)]
+
+
+def _view_struct(rs: GaussianRasterizationSettings, device, keep):
+    bg = _f32(rs.bg, device)
+    vm = _f32(rs.viewmatrix, device)
+    pm = _f32(rs.projmatrix, device)
+    cp = _f32(rs.campos, device)
+    keep.extend([bg, vm, pm, cp])
+    return DmgsView(int(rs.image_width), int(rs.image_height), float(rs.tanfovx),
+                    float(rs.tanfovy), float(rs.scale_modifier), int(rs.sh_degree),
+                    int(bool(rs.prefiltered)), int(bool(rs.debug)), ptr(bg), ptr(vm), ptr(pm),
+                    ptr(cp))
+
+
+class BatchedRasterizer:
+    """Forward + backward of a fixed batch of views.
+
+    ``gaussians``: dict of contiguous fp32 CUDA tensors with the reference's
+    names (means3D, opacities, and shs or colors_precomp, and scales +
+    rotations or cov3D_precomp).  Their storage is read at every call, so
+    parameters updated in place are picked up (also by graph replays).
+    """
+
+    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(2, 256)):
+        if not 1 <= len(settings) <= MAX_VIEWS:
+            raise ValueError(f"a batch holds 1..{MAX_VIEWS} views")
+        self.lib = _lib.load()
+        self.settings = list(settings)
+        self.g = {k: (None if v is None else _f32(v, v.device)) for k, v in gaussians.items()}
+        self.device = self.g["means3D"].device
+        self.P = self.g["means3D"].shape[0]
+        self.M = self.g["shs"].shape[1] if self.g.get("shs") is not None else 0
+        self.n = len(self.settings)
+        if self.g.get("rotations") is not None and self.g["rotations"].data_ptr() % 16:
+            self.g["rotations"] = self.g["rotations"].clone()
+        self._keep = []
+        self.views = (DmgsView * self.n)(*[_view_struct(s, self.device, self._keep)
+                                           for s in self.settings])
+        self.gauss = DmgsGaussians(self.P, self.M, ptr(self.g["means3D"]), ptr(self.g["opacities"]),
+                                   ptr(self.g.get("shs")), ptr(self.g.get("colors_precomp")),
+                                   ptr(self.g.get("scales")), ptr(self.g.get("rotations")),
+                                   ptr(self.g.get("cov3D_precomp")))
+        d = self.device
+        self.images = [torch.empty(3, s.image_height, s.image_width, device=d) for s in self.settings]
+        self.radii = [torch.empty(self.P, dtype=torch.int32, device=d) for _ in self.settings]
+        self.dL_dout = [torch.zeros(3, s.image_height, s.image_width, device=d) for s in self.settings]
+        self.grads = self._grad_buffers()
+        self.means2D_grads = [torch.empty(self.P, 3, device=d) for _ in self.settings]
+        self.cfg = tuple(cfg)
+        self.graph = None
+        if capacity is None:
+            capacity = [int(k * margin) + 1024 for k in self.count_instances()]
+        self._set_capacity(capacity)
+
+    # -- set-up ------------------------------------------------------------
+    def _grad_buffers(self):
+        d, P, g = self.device, self.P, self.g
+        z = lambda *s: torch.empty(*s, device=d)  # noqa: E731
+        return {"means3D": z(P, 3), "opacities": z(P, 1),
+                "shs": z(P, self.M, 3) if g.get("shs") is not None else None,
+                "colors_precomp": z(P, 3) if g.get("colors_precomp") is not None else None,
+                "scales": z(P, 3) if g.get("scales") is not None and g.get("cov3D_precomp") is None else None,
+                "rotations": z(P, 4) if g.get("rotations") is not None and g.get("cov3D_precomp") is None else None,
+                "cov3D_precomp": z(P, 6) if g.get("cov3D_precomp") is not None else None}
+
+    def count_instances(self):
+        """Exact instance count of every view (one geometry pass per view;
+        synchronises)."""
+        lib, out = self.lib, []
+        stream = _lib.stream_of(self.device)
+        for v in range(self.n):
+            s = self.settings[v]
+            geom = torch.empty(lib.dmgs_geom_state_bytes(self.P, s.image_width, s.image_height),
+                               dtype=torch.uint8, device=self.device)
+            radii = torch.empty(max(self.P, 1), dtype=torch.int32, device=self.device)
+            K = C.c_int64(0)
+            check(lib.dmgs_raster_fwd_geometry(C.byref(self.views[v]), C.byref(self.gauss),
+                                               geom.data_ptr(), geom.numel(), radii.data_ptr(),
+                                               C.byref(K), stream), "batch count")
+            out.append(int(K.value))
+        return out
+
+    def _set_capacity(self, capacity):
+        self.capacity = [int(c) for c in capacity]
+        self._cap = (C.c_int64 * self.n)(*self.capacity)
+        self._out = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.images])
+        self._rad = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.radii])
+        self._dout = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.dL_dout])
+        self._m2 = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.means2D_grads])
+        self.batch = DmgsBatch(self.n, self.views, self._out, self._rad, self._cap, self.cfg[0],
+                               self.cfg[1])
+        nbytes = self.lib.dmgs_batch_state_bytes(C.byref(self.batch), self.P)
+        if nbytes == 0:
+            raise DmgsError(-1, "batch", self.lib.dmgs_last_error().decode())
+        self.state = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        g = self.grads
+        self._grads = DmgsGrads(None, ptr(g["colors_precomp"]), ptr(g["opacities"]), ptr(g["means3D"]),
+                                ptr(g["cov3D_precomp"]), ptr(g["shs"]), ptr(g["scales"]),
+                                ptr(g["rotations"]))
+        self.graph = None
+
+    def set_config(self, ppt, batch):
+        self.cfg = (int(ppt), int(batch))
+        self.batch.pixels_per_thread = self.cfg[0]
+        self.batch.gaussians_per_batch = self.cfg[1]
+        self.graph = None
+
+    # -- work ---------------------------------------------------------------
+    def _enqueue_forward(self):
+        check(self.lib.dmgs_raster_fwd_batched(C.byref(self.batch), C.byref(self.gauss),
+                                               self.state.data_ptr(), self.state.numel(),
+                                               _lib.stream_of(self.device)), "fwd_batched")
+
+    def _enqueue_backward(self):
+        check(self.lib.dmgs_raster_bwd_batched(C.byref(self.batch), C.byref(self.gauss), self._dout,
+                                               self.state.data_ptr(), self.state.numel(),
+                                               C.byref(self._grads), self._m2,
+                                               _lib.stream_of(self.device)), "bwd_batched")
+
+    def forward(self):
+        """Render every view into ``self.images`` (asynchronous)."""
+        self._enqueue_forward()
+        return self.images
+
+    def backward(self, dL_dimages=None):
+        """Adjoint of the last forward; ``dL_dimages`` (optional list) is
+        copied into the static gradient buffers first.  Gradients (summed
+        over views) land in ``self.grads``."""
+        if dL_dimages is not None:
+            for dst, src in zip(self.dL_dout, dL_dimages):
+                dst.copy_(src)
+        self._enqueue_backward()
+        return self.grads
+
+    def step(self):
+        """Forward + backward with the current ``dL_dout`` buffers; replays
+        the captured graph when there is one."""
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._enqueue_forward()
+            self._enqueue_backward()
+
+    def capture(self):
+        """Capture forward + backward in a CUDA graph (replayed by step())."""
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):  # warm the kernels' one-time attribute set-up
+            self._enqueue_forward()
+            self._enqueue_backward()
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._enqueue_forward()
+            self._enqueue_backward()
+        self.graph = g
+        return g
+
+    def status(self):
+        """Per-view instance counts; raises DmgsError on capacity overflow
+        (grow with :meth:`grow`)."""
+        K = (C.c_int64 * self.n)()
+        code = self.lib.dmgs_batch_status(C.byref(self.batch), self.P, self.state.data_ptr(),
+                                          self.state.numel(), K, _lib.stream_of(self.device))
+        counts = [int(k) for k in K]
+        check(code, "batch_status")
+        return counts
+
+    def grow(self, factor=1.5):
+        """Re-plan capacities from exact counts (after an overflow)."""
+        self._set_capacity([int(k * factor) + 1024 for k in self.count_instances()])
+
+
+def autotune(br: BatchedRasterizer, space=TUNE_SPACE, iters=5, cache_path=None):
+    """Time forward + backward for every (pixels/thread, batch) pair and
+    keep the fastest; the choice is cached in JSON at ``cache_path`` (default
+    ``$DMGS_AUTOTUNE_CACHE`` if set) keyed by device, P and resolutions."""
+    key = json.dumps([torch.cuda.get_device_name(br.device), br.P,
+                      [(s.image_width, s.image_height) for s in br.settings]])
+    cache_path = cache_path or os.environ.get("DMGS_AUTOTUNE_CACHE")
+    cache = {}
+    if cache_path and os.path.exists(cache_path):
+        try:
+            cache = json.load(open(cache_path))
+        except Exception:
+            cache = {}
+    if key in cache:
+        br.set_config(*cache[key]["best"])
+        return cache[key]
+    times = {}
+    for ppt, b in space:
+        br.set_config(ppt, b)
+        br.step()
+        torch.cuda.synchronize(br.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(iters):
+            br.step()
+        e1.record()
+        torch.cuda.synchronize(br.device)
+        times[f"{ppt}x{b}"] = e0.elapsed_time(e1) / iters
+    best = min(times, key=times.get)
+    ppt, b = (int(x) for x in best.split("x"))
+    br.set_config(ppt, b)
+    result = {"best": [ppt, b], "ms": times, "when": time.time()}
+    if cache_path:
+        cache[key] = result
+        os.makedirs(os.path.dirname(os.path.abspath(cache_path)), exist_ok=True)
+        json.dump(cache, open(cache_path, "w"), indent=1)
+    return result
+
+
+class _RasterizeBatched(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, br, means3D, opacities, shs, colors, scales, rotations, cov3D):
+        br.forward()
+        ctx.br = br
+        return tuple(img.clone() for img in br.images)
+
+    @staticmethod
+    def backward(ctx, *dimgs):
+        br = ctx.br
+        br.backward([d if d is not None else torch.zeros_like(i) for d, i in zip(dimgs, br.images)])
+        g = br.grads
+        return (None, g["means3D"].clone(), g["opacities"].clone(),
+                None if g["shs"] is None else g["shs"].clone(),
+                None if g["colors_precomp"] is None else g["colors_precomp"].clone(),
+                None if g["scales"] is None else g["scales"].clone(),
+                None if g["rotations"] is None else g["rotations"].clone(),
+                None if g["cov3D_precomp"] is None else g["cov3D_precomp"].clone())
+
+
+def rasterize_batched(br: BatchedRasterizer, means3D, opacities, shs=None, colors_precomp=None,
+                      scales=None, rotations=None, cov3D_precomp=None):
+    """Autograd entry: images of every view of ``br``; the inputs must be the
+    tensors ``br`` was built on (their gradients are the sums over views)."""
+    return _RasterizeBatched.apply(br, means3D, opacities, shs, colors_precomp, scales, rotations,
+                                   cov3D_precomp)

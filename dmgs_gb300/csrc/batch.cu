@@ -1,0 +1,285 @@
+// batch.cu — the multi-view batched form (C ABI in include/dmgs.h).
+//
+// State buffer (one caller allocation): for every view its geometry state,
+// instance list (capacity-bounded), image state, 2D-gradient accumulators
+// and radii scratch, then two work-queue counters for the persistent blend
+// launches.  Nothing here synchronises with the host, so a forward +
+// backward step can be captured in a CUDA graph and replayed; the only
+// host-visible result besides the outputs is the per-view status word read
+// by dmgs_batch_status.
+#include <cstring>
+
+#include "kernels.cuh"
+
+using namespace dmgs;
+using dmgs_host::set_error;
+
+namespace {
+
+struct ViewLayout {
+  size_t geom, bin, img, gacc, radii;
+  GeomLayout G;
+  BinLayout B;
+  ImgLayout I;
+};
+
+struct BatchLayout {
+  int n;
+  ViewLayout v[MAX_BATCH_VIEWS];
+  size_t queue, total;
+};
+
+int make_layout(const DmgsBatch *b, int P, BatchLayout &L) {
+  if (!b || b->nviews < 1 || b->nviews > MAX_BATCH_VIEWS || !b->views || !b->capacity) {
+    set_error("batch: nviews must be 1..%d with views and capacity arrays", MAX_BATCH_VIEWS);
+    return DMGS_ERR_ARG;
+  }
+  L.n = b->nviews;
+  size_t o = 0;
+  for (int v = 0; v < L.n; ++v) {
+    const DmgsView &view = b->views[v];
+    if (view.width <= 0 || view.height <= 0) {
+      set_error("batch: view %d has an invalid size", v);
+      return DMGS_ERR_ARG;
+    }
+    const int64_t cap = b->capacity[v];
+    if (cap < 0 || cap > 0xfffffffell) {
+      set_error("batch: view %d capacity out of range", v);
+      return DMGS_ERR_ARG;
+    }
+    ViewLayout &V = L.v[v];
+    V.G = geom_layout(P, view.width, view.height);
+    V.B = bin_layout(cap, view.width, view.height);
+    V.I = img_layout(view.width, view.height);
+    V.geom = o;  o = align_up(o + V.G.total, 256);
+    V.bin = o;   o = align_up(o + V.B.total, 256);
+    V.img = o;   o = align_up(o + V.I.total, 256);
+    V.gacc = o;  o = align_up(o + bwd_scratch_bytes(P), 256);
+    V.radii = o; o = align_up(o + (size_t)P * 4 + 4, 256);
+  }
+  L.queue = o;
+  o = align_up(o + 64, 256);
+  L.total = o;
+  return DMGS_OK;
+}
+
+ViewParams params_of(const DmgsView *v) {
+  ViewParams p;
+  p.W = v->width;
+  p.H = v->height;
+  p.gx = (v->width + TILE - 1) / TILE;
+  p.gy = (v->height + TILE - 1) / TILE;
+  volatile float two_tx = 2.0f * v->tanfovx;
+  volatile float two_ty = 2.0f * v->tanfovy;
+  volatile float fx = (float)v->width / two_tx;
+  volatile float fy = (float)v->height / two_ty;
+  p.fx = fx;
+  p.fy = fy;
+  p.tanfovx = v->tanfovx;
+  p.tanfovy = v->tanfovy;
+  p.scale_modifier = v->scale_modifier;
+  p.D = v->sh_degree;
+  p.prefiltered = v->prefiltered;
+  return p;
+}
+
+GaussianPtrs gptrs_of(const DmgsGaussians *g) {
+  GaussianPtrs p;
+  p.P = g->P;
+  p.M = g->M;
+  p.means3D = g->means3D;
+  p.opacities = g->opacities;
+  p.shs = g->shs;
+  p.colors = g->colors_precomp;
+  p.scales = g->cov3D_precomp ? nullptr : g->scales;
+  p.rotations = g->cov3D_precomp ? nullptr : g->rotations;
+  p.cov3D = g->cov3D_precomp;
+  return p;
+}
+
+int check_common(const DmgsBatch *b, const DmgsGaussians *g, void *state, size_t bytes,
+                 BatchLayout &L) {
+  if (!g || g->P < 0) { set_error("batch: invalid Gaussians"); return DMGS_ERR_ARG; }
+  int r = make_layout(b, g->P, L);
+  if (r != DMGS_OK) return r;
+  if (!state || bytes < L.total) {
+    set_error("batch: state too small: %zu < %zu bytes", bytes, L.total);
+    return DMGS_ERR_STATE;
+  }
+  for (int v = 0; v < b->nviews; ++v) {
+    const DmgsView &w = b->views[v];
+    if (!w.bg || !w.viewmatrix || !w.projmatrix || !w.campos || w.sh_degree < 0 ||
+        w.sh_degree > 3 || !(w.tanfovx > 0.f) || !(w.tanfovy > 0.f)) {
+      set_error("batch: view %d is invalid", v);
+      return DMGS_ERR_ARG;
+    }
+  }
+  if (g->P > 0) {
+    if (!g->means3D || !g->opacities ||
+        (g->shs == nullptr) == (g->colors_precomp == nullptr) ||
+        ((g->scales == nullptr || g->rotations == nullptr) && g->cov3D_precomp == nullptr) ||
+        ((g->scales != nullptr || g->rotations != nullptr) && g->cov3D_precomp != nullptr)) {
+      set_error("batch: give exactly one colour source and one covariance source");
+      return DMGS_ERR_ARG;
+    }
+    for (int v = 0; v < b->nviews; ++v)
+      if (g->shs && g->M < (b->views[v].sh_degree + 1) * (b->views[v].sh_degree + 1)) {
+        set_error("batch: too few SH coefficients for view %d", v);
+        return DMGS_ERR_ARG;
+      }
+    if (g->rotations && (reinterpret_cast<uintptr_t>(g->rotations) & 15)) {
+      set_error("rotations must be 16-byte aligned");
+      return DMGS_ERR_ARG;
+    }
+  }
+  return DMGS_OK;
+}
+
+BlendCfg cfg_of(const DmgsBatch *b) {
+  BlendCfg c = default_blend_cfg();
+  if (b->pixels_per_thread) c.ppt = b->pixels_per_thread;
+  if (b->gaussians_per_batch) c.batch = b->gaussians_per_batch;
+  return c;
+}
+
+void fill_views(const DmgsBatch *b, const BatchLayout &L, char *st, BatchViews &bv) {
+  bv.nviews = b->nviews;
+  for (int v = 0; v < b->nviews; ++v) {
+    const ViewLayout &V = L.v[v];
+    char *geom = st + V.geom;
+    BatchView &o = bv.v[v];
+    o.vp = params_of(&b->views[v]);
+    o.viewm = b->views[v].viewmatrix;
+    o.projm = b->views[v].projmatrix;
+    o.campos = b->views[v].campos;
+    o.radii = (b->radii && b->radii[v]) ? b->radii[v] : reinterpret_cast<int32_t *>(st + V.radii);
+    o.feat = reinterpret_cast<float4 *>(geom + V.G.feat);
+    o.flags = reinterpret_cast<uint8_t *>(geom + V.G.flags);
+    o.blkcnt = reinterpret_cast<uint32_t *>(geom + V.G.blkcnt);
+    o.counters = reinterpret_cast<uint32_t *>(geom + V.G.counters);
+    o.gacc = reinterpret_cast<const float *>(st + V.gacc);
+    o.dL_dmeans2D = nullptr;
+  }
+}
+
+void fill_blend(const DmgsBatch *b, const BatchLayout &L, char *st, BlendBatch &bb) {
+  bb.nviews = b->nviews;
+  int base = 0;
+  for (int v = 0; v < b->nviews; ++v) {
+    const ViewLayout &V = L.v[v];
+    char *geom = st + V.geom, *bin = st + V.bin, *img = st + V.img;
+    BlendView &o = bb.v[v];
+    o.W = b->views[v].width;
+    o.H = b->views[v].height;
+    o.gx = V.G.gx;
+    o.T = V.G.T();
+    o.tile_base = base;
+    base += o.T;
+    o.ranges = reinterpret_cast<const uint2 *>(geom + V.G.ranges);
+    o.point_list = reinterpret_cast<const uint32_t *>(bin + V.B.point_list);
+    o.feat = reinterpret_cast<const float4 *>(geom + V.G.feat);
+    o.bg = b->views[v].bg;
+    o.out_color = b->out_color ? b->out_color[v] : nullptr;
+    o.final_T = reinterpret_cast<float *>(img + V.I.final_T);
+    o.n_contrib = reinterpret_cast<uint32_t *>(img + V.I.n_contrib);
+    o.dL_dout = nullptr;
+    o.gacc = reinterpret_cast<float *>(st + V.gacc);
+  }
+  bb.total = base;
+}
+
+#define RET_IF(x)                 \
+  do {                            \
+    int r_ = (x);                 \
+    if (r_ != DMGS_OK) return r_; \
+  } while (0)
+
+}  // namespace
+
+extern "C" size_t dmgs_batch_state_bytes(const DmgsBatch *b, int32_t P) {
+  BatchLayout L;
+  if (P < 0 || make_layout(b, P, L) != DMGS_OK) return 0;
+  return L.total;
+}
+
+extern "C" int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *g, void *state,
+                                       size_t state_bytes, dmgs_stream_t stream) {
+  BatchLayout L;
+  RET_IF(check_common(b, g, state, state_bytes, L));
+  if (!b->out_color) { set_error("batch: out_color is NULL"); return DMGS_ERR_ARG; }
+  for (int v = 0; v < b->nviews; ++v)
+    if (!b->out_color[v]) { set_error("batch: out_color[%d] is NULL", v); return DMGS_ERR_ARG; }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char *st = static_cast<char *>(state);
+  BatchViews bv;
+  fill_views(b, L, st, bv);
+  RET_IF(launch_preprocess_batched(bv, gptrs_of(g), s));
+  for (int v = 0; v < b->nviews; ++v) {
+    const ViewLayout &V = L.v[v];
+    RET_IF(launch_binning_geometry(V.G, st + V.geom, (uint32_t)b->capacity[v], s));
+    RET_IF(launch_emit(V.G, st + V.geom, V.B, st + V.bin, b->capacity[v], s));
+  }
+  BlendBatch bb;
+  fill_blend(b, L, st, bb);
+  uint32_t *queue = reinterpret_cast<uint32_t *>(st + L.queue);
+  DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));
+  RET_IF(launch_blend_batch_fwd(bb, cfg_of(b), queue, s));
+  return DMGS_OK;
+}
+
+extern "C" int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
+                                       const float *const *dL_dout_color, void *state,
+                                       size_t state_bytes, const DmgsGrads *grads,
+                                       float *const *dL_dmeans2D, dmgs_stream_t stream) {
+  BatchLayout L;
+  RET_IF(check_common(b, g, state, state_bytes, L));
+  if (!dL_dout_color || !grads) { set_error("batch: dL_dout_color / grads is NULL"); return DMGS_ERR_ARG; }
+  for (int v = 0; v < b->nviews; ++v)
+    if (!dL_dout_color[v]) { set_error("batch: dL_dout_color[%d] is NULL", v); return DMGS_ERR_ARG; }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char *st = static_cast<char *>(state);
+  BlendBatch bb;
+  fill_blend(b, L, st, bb);
+  for (int v = 0; v < b->nviews; ++v) {
+    bb.v[v].dL_dout = dL_dout_color[v];
+    DMGS_CUDA(cudaMemsetAsync(bb.v[v].gacc, 0, (size_t)g->P * 48, s));
+  }
+  uint32_t *queue = reinterpret_cast<uint32_t *>(st + L.queue) + 1;
+  DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));
+  RET_IF(launch_blend_batch_bwd(bb, cfg_of(b), queue, s));
+  BatchViews bv;
+  fill_views(b, L, st, bv);
+  for (int v = 0; v < b->nviews; ++v) bv.v[v].dL_dmeans2D = dL_dmeans2D ? dL_dmeans2D[v] : nullptr;
+  RET_IF(launch_preprocess_bwd_batched(bv, gptrs_of(g), *grads, s));
+  return DMGS_OK;
+}
+
+extern "C" int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *state,
+                                 size_t state_bytes, int64_t *num_rendered, dmgs_stream_t stream) {
+  BatchLayout L;
+  RET_IF(make_layout(b, P, L));
+  if (!state || state_bytes < L.total) { set_error("batch: state too small"); return DMGS_ERR_STATE; }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const char *st = static_cast<const char *>(state);
+  uint32_t h[MAX_BATCH_VIEWS][CI_WORDS];
+  for (int v = 0; v < b->nviews; ++v)
+    DMGS_CUDA(cudaMemcpyAsync(h[v], st + L.v[v].geom + L.v[v].G.counters, CI_WORDS * 4,
+                              cudaMemcpyDeviceToHost, s));
+  DMGS_CUDA(cudaStreamSynchronize(s));
+  int rc = DMGS_OK;
+  for (int v = 0; v < b->nviews; ++v) {
+    if (num_rendered) num_rendered[v] = (int64_t)h[v][CI_K];
+    if (h[v][CI_STATUS] & ST_OVERFLOW) {
+      set_error("batch: view %d needs %u instances, capacity %lld", v, h[v][CI_K],
+                (long long)b->capacity[v]);
+      rc = DMGS_ERR_OVERFLOW;
+    } else if ((h[v][CI_STATUS] & ST_PREFILTER) && rc == DMGS_OK) {
+      set_error("batch: view %d: a point failed the frustum test although prefiltered is set", v);
+      rc = DMGS_ERR_PREFILTER;
+    } else if ((h[v][CI_STATUS] & ST_BOUNDS) && rc == DMGS_OK) {
+      set_error("batch: view %d: a kernel index left its buffer", v);
+      rc = DMGS_ERR_DEVICE;
+    }
+  }
+  return rc;
+}

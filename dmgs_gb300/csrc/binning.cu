@@ -356,13 +356,19 @@ tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
   for (int t = threadIdx.x; t < T; t += blockDim.x) cmat[(size_t)t * C + c] = cnt[t];
 }
 
+// Tile ranges from the scanned count matrix.  When the instances exceed the
+// list capacity (capacity-bounded callers), every range is left empty and
+// the overflow bit is set, so no kernel reads past the list buffer.
 __global__ void ranges_kernel(int T, const uint32_t *__restrict__ cmat_scanned,
-                              uint32_t *__restrict__ counters, uint2 *__restrict__ ranges) {
+                              uint32_t *__restrict__ counters, uint2 *__restrict__ ranges,
+                              uint32_t K_cap) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   const uint32_t C = counters[CI_C], K = counters[CI_K];
+  const bool over = K > K_cap || (counters[CI_STATUS] & ST_OVERFLOW);
+  if (over && t == 0) atomicOr(&counters[CI_STATUS], ST_OVERFLOW);
   uint2 r = make_uint2(0u, 0u);
-  if (C > 0) {
+  if (C > 0 && !over) {
     const uint32_t a = cmat_scanned[(size_t)t * C];
     const uint32_t e = (t + 1 < T) ? cmat_scanned[(size_t)(t + 1) * C] : K;
     if (e > a) r = make_uint2(a, e);
@@ -480,7 +486,7 @@ int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t 
   return DMGS_OK;
 }
 
-int launch_binning_geometry(const GeomLayout &L, const int32_t *radii, char *geom, cudaStream_t s) {
+int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cudaStream_t s) {
   uint32_t *counters = reinterpret_cast<uint32_t *>(geom + L.counters);
   uint32_t *blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
   uint32_t *part = reinterpret_cast<uint32_t *>(geom + L.scanpart);
@@ -540,7 +546,7 @@ int launch_binning_geometry(const GeomLayout &L, const int32_t *radii, char *geo
       if (r != DMGS_OK) return r;
     }
     ranges_kernel<<<(T + 255) / 256, 256, 0, s>>>(T, cmat, counters,
-                                                  reinterpret_cast<uint2 *>(geom + L.ranges));
+                                                  reinterpret_cast<uint2 *>(geom + L.ranges), K_cap);
   });
   DMGS_LAUNCH_CHECK("ranges_kernel");
   return DMGS_OK;

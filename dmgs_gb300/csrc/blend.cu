@@ -11,11 +11,15 @@
 //
 // Design (both kernels are instruction-issue bound: the visible Gaussians'
 // records and the tile lists are L2-resident):
-// * one 128-thread CTA per 16x16 tile; thread t owns pixels (t%16, t/16)
-//   and (t%16, t/16 + 8), which share dx and every shared-memory load;
-// * Gaussians are staged in shared memory in batches of 256; in the forward
-//   the next batch's global loads are in flight while the current batch is
-//   blended (double buffer);
+// * a CTA blends one 16x16 tile at a time with 256/PPT threads; thread t
+//   owns the PPT pixels (t%16, t/16 + k*16/PPT), which share dx and every
+//   shared-memory load (PPT = 1, 2 or 4, a tuning parameter);
+// * work items are the (view, tile) pairs of one or several views (the
+//   multi-view batched form renders many views in one launch); CTAs either
+//   take one item each or, persistent, pull items from an atomic counter;
+// * Gaussians are staged in shared memory in batches of BATCH (128, 256 or
+//   512, a tuning parameter); in the forward the next batch's global loads
+//   are in flight while the current batch is blended (double buffer);
 // * at staging, the conic is scaled by -log2(e)/2 (so the falloff is one
 //   ex2 instruction) and a per-Gaussian exponent threshold
 //   log2(1/(255 o)) is precomputed: a pair below it cannot reach alpha 1/255
@@ -36,9 +40,6 @@ namespace dmgs {
 
 namespace {
 
-constexpr int BLEND_THREADS = 128;
-constexpr int BATCH = 256;
-constexpr int PER_THREAD = BATCH / BLEND_THREADS;  // Gaussians staged per thread
 constexpr float ALPHA_MIN = 1.0f / 255.0f;
 constexpr float ALPHA_MAX = 0.99f;
 constexpr float T_EPS = 0.0001f;
@@ -114,131 +115,154 @@ __device__ __forceinline__ float pair_alpha(float e2, float o, float thr, float 
   return alpha < ALPHA_MIN ? 0.f : alpha;
 }
 
-__global__ void __launch_bounds__(BLEND_THREADS, 6)
-blend_fwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
-                 const uint32_t *__restrict__ point_list, const float4 *__restrict__ feat,
-                 const float *__restrict__ bg, float *__restrict__ out_color,
-                 float *__restrict__ final_T, uint32_t *__restrict__ n_contrib) {
+
+// Work item -> (view, tile).
+__device__ __forceinline__ int find_view(const BlendBatch &bb, int item) {
+  int v = 0;
+  while (v + 1 < bb.nviews && item >= bb.v[v + 1].tile_base) ++v;
+  return v;
+}
+
+// Next work item of this CTA (all threads receive the same value).
+__device__ __forceinline__ int next_item(uint32_t *queue, int &slot, int *s_item) {
+  if (queue == nullptr) return slot++ == 0 ? (int)blockIdx.x : INT_MAX;
+  __syncthreads();
+  if (threadIdx.x == 0) *s_item = (int)atomicAdd(queue, 1u);
+  __syncthreads();
+  return *s_item;
+}
+
+template <int PPT>
+struct PixelLayout {
+  static constexpr int THREADS = 256 / PPT;
+  static constexpr int RSTEP = 16 / PPT;  // rows between one thread's pixels
+  int col, r0;
+  uint32_t colbit, warp_rows;
+  __device__ __forceinline__ PixelLayout() {
+    const int tid = threadIdx.x;
+    col = tid & 15;
+    r0 = tid >> 4;
+    colbit = 1u << (16 + col);
+    const int w = tid >> 5;
+    uint32_t m = 0;
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) m |= 3u << (2 * w + k * RSTEP);
+    warp_rows = m;
+  }
+  __device__ __forceinline__ int row(int k) const { return r0 + k * RSTEP; }
+};
+
+template <int PPT, int BATCH>
+__global__ void __launch_bounds__(256 / PPT)
+blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
+  constexpr int THREADS = 256 / PPT;
+  constexpr int LOADS = (BATCH + THREADS - 1) / THREADS;
   __shared__ float4 S0[2][BATCH];
   __shared__ float4 S1[2][BATCH];
   __shared__ float4 S2[2][BATCH];
-  const int tile = blockIdx.x;
-  const int tx = tile % gx, ty = tile / gx;
+  __shared__ int s_item;
   const int tid = threadIdx.x;
-  const int px = tx * TILE + (tid & (TILE - 1));
-  const int py0 = ty * TILE + (tid >> 4);
-  const int py1 = py0 + 8;
-  const bool in0 = px < W && py0 < H, in1 = px < W && py1 < H;
-  const float pxf = (float)px, py0f = (float)py0, py1f = (float)py1;
-  const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
-  const uint2 range = ranges[tile];
-  const int n = (int)(range.y - range.x);
-  // footprint-mask bits of this thread's pixels and of its warp's rows
-  const int r0 = tid >> 4;
-  const uint32_t colbit = 1u << (16 + (tid & 15));
-  const uint32_t row0bit = 1u << r0, row1bit = 1u << (r0 + 8);
-  const uint32_t warp_rows = (3u << ((r0 >> 1) << 1)) | (3u << (((r0 >> 1) << 1) + 8));
-
-  bool done0 = !in0, done1 = !in1;
-  float T0 = 1.f, T1 = 1.f;
-  float r0c = 0.f, g0 = 0.f, b0 = 0.f, r1 = 0.f, g1 = 0.f, b1 = 0.f;
-  uint32_t last0 = 0, last1 = 0;
-
-  // prefetch batch 0 into registers
-  float4 pf0[PER_THREAD], pf1[PER_THREAD], pf2[PER_THREAD];
+  const PixelLayout<PPT> lay;
+  int slot = 0;
+  for (int item = next_item(queue, slot, &s_item); item < bb.total;
+       item = next_item(queue, slot, &s_item)) {
+    const BlendView &V = bb.v[find_view(bb, item)];
+    const int tile = item - V.tile_base;
+    const int tx = tile % V.gx, ty = tile / V.gx;
+    const int px = tx * TILE + lay.col;
+    const float pxf = (float)px;
+    const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
+    const uint2 range = V.ranges[tile];
+    const int n = (int)(range.y - range.x);
+    bool done[PPT], inside[PPT];
+    float T[PPT], cr[PPT], cg[PPT], cb[PPT], pyf[PPT];
+    uint32_t last[PPT];
 #pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) {
-    const int i = k * BLEND_THREADS + tid;
-    if (i < n) {
-      const uint32_t id = point_list[range.x + i];
-      pf0[k] = feat[3 * id]; pf1[k] = feat[3 * id + 1]; pf2[k] = feat[3 * id + 2];
+    for (int k = 0; k < PPT; ++k) {
+      const int py = ty * TILE + lay.row(k);
+      inside[k] = px < V.W && py < V.H;
+      done[k] = !inside[k];
+      pyf[k] = (float)py;
+      T[k] = 1.f; cr[k] = cg[k] = cb[k] = 0.f; last[k] = 0;
     }
-  }
-  int buf = 0;
-  for (int base = 0; base < n; base += BATCH) {
-    // stage the prefetched batch (buffer `buf` was last read two batches ago,
-    // before the barrier below of the previous iteration)
+    auto all_done = [&]() {
+      bool d = true;
 #pragma unroll
-    for (int k = 0; k < PER_THREAD; ++k) {
-      const int i = base + k * BLEND_THREADS + tid;
-      if (i < n) {
-        const Staged s = stage(pf0[k], pf1[k], pf2[k], ox, oy);
-        const int slot = k * BLEND_THREADS + tid;
-        S0[buf][slot] = s.s0; S1[buf][slot] = s.s1; S2[buf][slot] = s.s2;
+      for (int k = 0; k < PPT; ++k) d = d && done[k];
+      return d;
+    };
+    float4 pf0[LOADS], pf1[LOADS], pf2[LOADS];
+#pragma unroll
+    for (int l = 0; l < LOADS; ++l) {
+      const int i = l * THREADS + tid;
+      if (i < n && i < BATCH) {
+        const uint32_t id = V.point_list[range.x + i];
+        pf0[l] = V.feat[3 * id]; pf1[l] = V.feat[3 * id + 1]; pf2[l] = V.feat[3 * id + 2];
       }
     }
-    if (__syncthreads_count(done0 && done1) == BLEND_THREADS) break;
-    // prefetch the next batch while this one is blended
-    const int nbase = base + BATCH;
+    int buf = 0;
+    for (int base = 0; base < n; base += BATCH) {
 #pragma unroll
-    for (int k = 0; k < PER_THREAD; ++k) {
-      const int i = nbase + k * BLEND_THREADS + tid;
-      if (i < n) {
-        const uint32_t id = point_list[range.x + i];
-        pf0[k] = feat[3 * id]; pf1[k] = feat[3 * id + 1]; pf2[k] = feat[3 * id + 2];
+      for (int l = 0; l < LOADS; ++l) {
+        const int sl = l * THREADS + tid;
+        if (sl < BATCH && base + sl < n) {
+          const Staged st = stage(pf0[l], pf1[l], pf2[l], ox, oy);
+          S0[buf][sl] = st.s0; S1[buf][sl] = st.s1; S2[buf][sl] = st.s2;
+        }
       }
-    }
-    const int cnt = min(BATCH, n - base);
-    for (int j = 0; j < cnt && !(done0 && done1); ++j) {
-      const float4 s2 = S2[buf][j];
-      const uint32_t m = __float_as_uint(s2.z);
-      if (!(m & warp_rows)) continue;  // warp-uniform: the footprint misses the warp's rows
-      if (!(m & colbit)) continue;
-      const float4 s0 = S0[buf][j];
-      const float4 s1 = S1[buf][j];
-      const float dx = __fsub_rn(s0.x, pxf);
-      if (!done0 && (m & row0bit)) {
-        float G;
-        const float e2 = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, py0f));
-        const float alpha = pair_alpha(e2, s1.y, s1.z, G);
-        if (alpha > 0.f) {
-          const float test_T = T0 * (1.f - alpha);
-          if (test_T < T_EPS) {
-            done0 = true;
-          } else {
-            const float w = alpha * T0;
-            r0c = fmaf(s1.w, w, r0c); g0 = fmaf(s2.x, w, g0); b0 = fmaf(s2.y, w, b0);
-            T0 = test_T;
-            last0 = base + j + 1;
+      if (__syncthreads_count(all_done()) == THREADS) break;
+      const int nbase = base + BATCH;
+#pragma unroll
+      for (int l = 0; l < LOADS; ++l) {
+        const int sl = l * THREADS + tid;
+        if (sl < BATCH && nbase + sl < n) {
+          const uint32_t id = V.point_list[range.x + nbase + sl];
+          pf0[l] = V.feat[3 * id]; pf1[l] = V.feat[3 * id + 1]; pf2[l] = V.feat[3 * id + 2];
+        }
+      }
+      const int cnt = min(BATCH, n - base);
+      for (int j = 0; j < cnt && !all_done(); ++j) {
+        const float4 s2 = S2[buf][j];
+        const uint32_t m = __float_as_uint(s2.z);
+        if (!(m & lay.warp_rows)) continue;  // warp-uniform: footprint misses the warp's rows
+        if (!(m & lay.colbit)) continue;
+        const float4 s0 = S0[buf][j];
+        const float4 s1 = S1[buf][j];
+        const float dx = __fsub_rn(s0.x, pxf);
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          if (done[k] || !(m & (1u << lay.row(k)))) continue;
+          float G;
+          const float e2 = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, pyf[k]));
+          const float alpha = pair_alpha(e2, s1.y, s1.z, G);
+          if (alpha > 0.f) {
+            const float test_T = T[k] * (1.f - alpha);
+            if (test_T < T_EPS) {
+              done[k] = true;
+            } else {
+              const float w = alpha * T[k];
+              cr[k] = fmaf(s1.w, w, cr[k]); cg[k] = fmaf(s2.x, w, cg[k]); cb[k] = fmaf(s2.y, w, cb[k]);
+              T[k] = test_T;
+              last[k] = base + j + 1;
+            }
           }
         }
       }
-      if (!done1 && (m & row1bit)) {
-        float G;
-        const float e2 = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, py1f));
-        const float alpha = pair_alpha(e2, s1.y, s1.z, G);
-        if (alpha > 0.f) {
-          const float test_T = T1 * (1.f - alpha);
-          if (test_T < T_EPS) {
-            done1 = true;
-          } else {
-            const float w = alpha * T1;
-            r1 = fmaf(s1.w, w, r1); g1 = fmaf(s2.x, w, g1); b1 = fmaf(s2.y, w, b1);
-            T1 = test_T;
-            last1 = base + j + 1;
-          }
-        }
-      }
+      buf ^= 1;
     }
-    buf ^= 1;
-  }
-  const size_t HW = (size_t)H * W;
-  const float bgr = __ldg(bg), bgg = __ldg(bg + 1), bgb = __ldg(bg + 2);
-  if (in0) {
-    const int pix = py0 * W + px;
-    final_T[pix] = T0;
-    n_contrib[pix] = last0;
-    out_color[pix] = r0c + T0 * bgr;
-    out_color[HW + pix] = g0 + T0 * bgg;
-    out_color[2 * HW + pix] = b0 + T0 * bgb;
-  }
-  if (in1) {
-    const int pix = py1 * W + px;
-    final_T[pix] = T1;
-    n_contrib[pix] = last1;
-    out_color[pix] = r1 + T1 * bgr;
-    out_color[HW + pix] = g1 + T1 * bgg;
-    out_color[2 * HW + pix] = b1 + T1 * bgb;
+    const size_t HW = (size_t)V.H * V.W;
+    const float bgr = __ldg(V.bg), bgg = __ldg(V.bg + 1), bgb = __ldg(V.bg + 2);
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      if (!inside[k]) continue;
+      const int pix = (int)pyf[k] * V.W + px;
+      V.final_T[pix] = T[k];
+      V.n_contrib[pix] = last[k];
+      V.out_color[pix] = cr[k] + T[k] * bgr;
+      V.out_color[HW + pix] = cg[k] + T[k] * bgg;
+      V.out_color[2 * HW + pix] = cb[k] + T[k] * bgb;
+    }
+    __syncthreads();  // shared buffers are reused by the next item
   }
 }
 
@@ -353,116 +377,201 @@ __device__ __forceinline__ float warp_reduce_scatter16(float v[16], int lane) {
   return v[0] + __shfl_xor_sync(FULL, v[0], 1);
 }
 
-__global__ void __launch_bounds__(BLEND_THREADS)
-blend_bwd_kernel(int W, int H, int gx, const uint2 *__restrict__ ranges,
-                 const uint32_t *__restrict__ point_list, const float4 *__restrict__ feat,
-                 const float *__restrict__ bg, const float *__restrict__ final_Ts,
-                 const uint32_t *__restrict__ n_contrib, const float *__restrict__ dL_dout,
-                 float *__restrict__ gacc) {
+
+template <int PPT, int BATCH>
+__global__ void __launch_bounds__(256 / PPT)
+blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
+  constexpr int THREADS = 256 / PPT;
   __shared__ float4 S0[BATCH], S1[BATCH], S2[BATCH], S3[BATCH];
   __shared__ uint32_t sMaxLast;
-  const int tile = blockIdx.x;
-  const int tx = tile % gx, ty = tile / gx;
+  __shared__ int s_item;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  const int px = tx * TILE + (tid & (TILE - 1));
-  const int py0 = ty * TILE + (tid >> 4);
-  const int py1 = py0 + 8;
-  const bool in0 = px < W && py0 < H, in1 = px < W && py1 < H;
-  const float pxf = (float)px, py0f = (float)py0, py1f = (float)py1;
-  const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
-  const uint2 range = ranges[tile];
-  const int n = (int)(range.y - range.x);
-  if (n == 0) return;
-  const int r0 = tid >> 4;
-  const uint32_t colbit = 1u << (16 + (tid & 15));
-  const uint32_t row0bit = 1u << r0, row1bit = 1u << (r0 + 8);
-  const uint32_t warp_rows = (3u << ((r0 >> 1) << 1)) | (3u << (((r0 >> 1) << 1) + 8));
-
-  const size_t HW = (size_t)H * W;
-  const float bg0 = __ldg(bg), bg1 = __ldg(bg + 1), bg2 = __ldg(bg + 2);
-  PixelState P0, P1;
-  init_pixel(P0, in0, py0 * W + px, HW, final_Ts, n_contrib, dL_dout, bg0, bg1, bg2);
-  init_pixel(P1, in1, py1 * W + px, HW, final_Ts, n_contrib, dL_dout, bg0, bg1, bg2);
-  if (tid == 0) sMaxLast = 0;
-  __syncthreads();
-  atomicMax(&sMaxLast, max(P0.last_contrib, P1.last_contrib));
-  __syncthreads();
-  const int max_last = (int)sMaxLast;  // list positions >= max_last are never blended
-  const float hw = 0.5f * (float)W, hh = 0.5f * (float)H;
-
-  // Walk list positions max_last-1 down to 0 in batches of BATCH.
-  for (int top = max_last; top > 0; top -= BATCH) {
-    const int cnt = min(BATCH, top);
-    __syncthreads();
+  const PixelLayout<PPT> lay;
+  int slot_ = 0;
+  for (int item = next_item(queue, slot_, &s_item); item < bb.total;
+       item = next_item(queue, slot_, &s_item)) {
+    const BlendView &V = bb.v[find_view(bb, item)];
+    const int tile = item - V.tile_base;
+    const int tx = tile % V.gx, ty = tile / V.gx;
+    const int px = tx * TILE + lay.col;
+    const float pxf = (float)px;
+    const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
+    const uint2 range = V.ranges[tile];
+    const int n = (int)(range.y - range.x);
+    if (n == 0) continue;  // block-uniform
+    const size_t HW = (size_t)V.H * V.W;
+    const float bg0 = __ldg(V.bg), bg1 = __ldg(V.bg + 1), bg2 = __ldg(V.bg + 2);
+    PixelState ps[PPT];
+    float pyf[PPT];
+    uint32_t mylast = 0;
 #pragma unroll
-    for (int k = 0; k < PER_THREAD; ++k) {
-      const int slot = k * BLEND_THREADS + tid;
-      if (slot < cnt) {
-        const uint32_t id = point_list[range.x + top - 1 - slot];  // back to front
-        const StagedB s =
-            stage_b(feat[3 * id], feat[3 * id + 1], feat[3 * id + 2], id, hw, hh, ox, oy);
-        S0[slot] = s.s0; S1[slot] = s.s1; S2[slot] = s.s2; S3[slot] = s.s3;
-      }
+    for (int k = 0; k < PPT; ++k) {
+      const int py = ty * TILE + lay.row(k);
+      pyf[k] = (float)py;
+      const bool in = px < V.W && py < V.H;
+      init_pixel(ps[k], in, py * V.W + px, HW, V.final_T, V.n_contrib, V.dL_dout, bg0, bg1, bg2);
+      mylast = max(mylast, ps[k].last_contrib);
     }
+    if (tid == 0) sMaxLast = 0;
     __syncthreads();
-    for (int j = 0; j < cnt; ++j) {
-      const int li = top - 1 - j;
-      const float4 s3 = S3[j];
-      const uint32_t m = __float_as_uint(s3.w);
-      if (!(m & warp_rows)) continue;  // warp-uniform: the footprint misses the warp's rows
-      const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j];
-      float e[16];
+    atomicMax(&sMaxLast, mylast);
+    __syncthreads();
+    const int max_last = (int)sMaxLast;  // list positions >= max_last are never blended
+    const float hw = 0.5f * (float)V.W, hh = 0.5f * (float)V.H;
+    for (int top = max_last; top > 0; top -= BATCH) {
+      const int cnt = min(BATCH, top);
+      __syncthreads();
+      for (int sl = tid; sl < cnt; sl += THREADS) {
+        const uint32_t id = V.point_list[range.x + top - 1 - sl];  // back to front
+        const StagedB st =
+            stage_b(V.feat[3 * id], V.feat[3 * id + 1], V.feat[3 * id + 2], id, hw, hh, ox, oy);
+        S0[sl] = st.s0; S1[sl] = st.s1; S2[sl] = st.s2; S3[sl] = st.s3;
+      }
+      __syncthreads();
+      for (int j = 0; j < cnt; ++j) {
+        const int li = top - 1 - j;
+        const float4 s3 = S3[j];
+        const uint32_t m = __float_as_uint(s3.w);
+        if (!(m & lay.warp_rows)) continue;  // warp-uniform
+        const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j];
+        float e[16];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) e[i] = 0.f;
-      const float dx = __fsub_rn(s0.x, pxf);
-      bool any = false;
-      if ((m & colbit) && (m & row0bit) && li < (int)P0.last_contrib)
-        any |= adjoint_pair(P0, s0, s1, s2, s3, dx, __fsub_rn(s0.y, py0f), e);
-      if ((m & colbit) && (m & row1bit) && li < (int)P1.last_contrib)
-        any |= adjoint_pair(P1, s0, s1, s2, s3, dx, __fsub_rn(s0.y, py1f), e);
-      if (__ballot_sync(FULL, any)) {
-        const float sum = warp_reduce_scatter16(e, lane);
-        const int slot = (lane >> 1) & 15;  // lane bits (4,3,2,1)
-        if (!(lane & 1) && slot < 9) {
-          const float scale = (slot == 2 || slot == 4) ? -0.5f : (slot == 3 ? -1.f : 1.f);
-          atomicAdd(gacc + (size_t)__float_as_uint(s3.z) * 12 + slot, sum * scale);
+        for (int i = 0; i < 16; ++i) e[i] = 0.f;
+        const float dx = __fsub_rn(s0.x, pxf);
+        bool any = false;
+        if (m & lay.colbit) {
+#pragma unroll
+          for (int k = 0; k < PPT; ++k)
+            if ((m & (1u << lay.row(k))) && li < (int)ps[k].last_contrib)
+              any |= adjoint_pair(ps[k], s0, s1, s2, s3, dx, __fsub_rn(s0.y, pyf[k]), e);
+        }
+        if (__ballot_sync(FULL, any)) {
+          const float sum = warp_reduce_scatter16(e, lane);
+          const int slot = (lane >> 1) & 15;  // lane bits (4,3,2,1)
+          if (!(lane & 1) && slot < 9) {
+            const float scale = (slot == 2 || slot == 4) ? -0.5f : (slot == 3 ? -1.f : 1.f);
+            atomicAdd(V.gacc + (size_t)__float_as_uint(s3.z) * 12 + slot, sum * scale);
+          }
         }
       }
     }
   }
 }
 
+// Persistent grid = resident CTAs (SMs x blocks per SM), looked up once per
+// kernel and device (no runtime queries while a graph is being captured
+// after the first call).
+template <typename K>
+int grid_for(K kernel, int threads, int total, bool persistent, int &grid) {
+  if (!persistent) { grid = total; return DMGS_OK; }
+  static int cached_dev = -1, cached_slots = 0;
+  int dev = 0;
+  DMGS_CUDA(cudaGetDevice(&dev));
+  if (dev != cached_dev) {
+    int sms = 0, per = 0;
+    DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0));
+    cached_slots = sms * max(per, 1);
+    cached_dev = dev;
+  }
+  grid = max(1, min(total, cached_slots));
+  return DMGS_OK;
+}
+
+template <int PPT, int BATCH>
+int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
+  int grid;
+  const int r = grid_for(blend_fwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid);
+  if (r != DMGS_OK) return r;
+  blend_fwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  return DMGS_OK;
+}
+
+template <int PPT, int BATCH>
+int run_bwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
+  int grid;
+  const int r = grid_for(blend_bwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid);
+  if (r != DMGS_OK) return r;
+  blend_bwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  return DMGS_OK;
+}
+
+template <bool FWD>
+int dispatch(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *queue, cudaStream_t s) {
+#define DMGS_BLEND_CASE(P_, B_)                                                     \
+  if (cfg.ppt == P_ && cfg.batch == B_)                                             \
+    return FWD ? run_fwd<P_, B_>(bb, queue, s) : run_bwd<P_, B_>(bb, queue, s);
+  DMGS_BLEND_CASE(1, 128) DMGS_BLEND_CASE(1, 256) DMGS_BLEND_CASE(1, 512)
+  DMGS_BLEND_CASE(2, 128) DMGS_BLEND_CASE(2, 256) DMGS_BLEND_CASE(2, 512)
+  DMGS_BLEND_CASE(4, 128) DMGS_BLEND_CASE(4, 256) DMGS_BLEND_CASE(4, 512)
+#undef DMGS_BLEND_CASE
+  dmgs_host::set_error("unsupported blend configuration: %d pixels/thread, batch %d", cfg.ppt,
+                       cfg.batch);
+  return DMGS_ERR_ARG;
+}
+
 }  // namespace
+
+int launch_blend_batch_fwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *queue,
+                           cudaStream_t s) {
+  if (bb.total <= 0) return DMGS_OK;
+  int r = DMGS_OK;
+  DMGS_TIMED(K_BLEND_FWD, s, r = dispatch<true>(bb, cfg, queue, s));
+  if (r != DMGS_OK) return r;
+  DMGS_LAUNCH_CHECK("blend_fwd_kernel");
+  return DMGS_OK;
+}
+
+int launch_blend_batch_bwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *queue,
+                           cudaStream_t s) {
+  if (bb.total <= 0) return DMGS_OK;
+  int r = DMGS_OK;
+  DMGS_TIMED(K_BLEND_BWD, s, r = dispatch<false>(bb, cfg, queue, s));
+  if (r != DMGS_OK) return r;
+  DMGS_LAUNCH_CHECK("blend_bwd_kernel");
+  return DMGS_OK;
+}
+
+BlendView make_blend_view(const ViewParams &vp, const GeomLayout &L, const char *geom,
+                          const BinLayout &B, const char *bin, const ImgLayout &I, char *img,
+                          const float *bg) {
+  BlendView v;
+  v.W = vp.W; v.H = vp.H; v.gx = L.gx; v.T = L.T(); v.tile_base = 0;
+  v.ranges = reinterpret_cast<const uint2 *>(geom + L.ranges);
+  v.point_list = reinterpret_cast<const uint32_t *>(bin + B.point_list);
+  v.feat = reinterpret_cast<const float4 *>(geom + L.feat);
+  v.bg = bg;
+  v.out_color = nullptr;
+  v.final_T = reinterpret_cast<float *>(img + I.final_T);
+  v.n_contrib = reinterpret_cast<uint32_t *>(img + I.n_contrib);
+  v.dL_dout = nullptr;
+  v.gacc = nullptr;
+  return v;
+}
 
 int launch_blend_fwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
                      const BinLayout &B, const char *bin, const ImgLayout &I, char *img,
                      const float *bg, float *out_color, cudaStream_t s) {
-  const int T = L.T();
-  if (T == 0) return DMGS_OK;
-  DMGS_TIMED(K_BLEND_FWD, s, blend_fwd_kernel<<<T, BLEND_THREADS, 0, s>>>(
-      vp.W, vp.H, L.gx, reinterpret_cast<const uint2 *>(geom + L.ranges),
-      reinterpret_cast<const uint32_t *>(bin + B.point_list),
-      reinterpret_cast<const float4 *>(geom + L.feat), bg, out_color,
-      reinterpret_cast<float *>(img + I.final_T), reinterpret_cast<uint32_t *>(img + I.n_contrib)));
-  DMGS_LAUNCH_CHECK("blend_fwd_kernel");
-  return DMGS_OK;
+  BlendBatch bb;
+  bb.nviews = 1;
+  bb.v[0] = make_blend_view(vp, L, geom, B, bin, I, img, bg);
+  bb.v[0].out_color = out_color;
+  bb.total = bb.v[0].T;
+  return launch_blend_batch_fwd(bb, default_blend_cfg(), nullptr, s);
 }
 
 int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
                      const BinLayout &B, const char *bin, const ImgLayout &I, const char *img,
                      const float *bg, const float *dL_dout, float *gacc, cudaStream_t s) {
-  const int T = L.T();
   DMGS_CUDA(cudaMemsetAsync(gacc, 0, (size_t)L.P * 48, s));
-  if (T == 0) return DMGS_OK;
-  DMGS_TIMED(K_BLEND_BWD, s, blend_bwd_kernel<<<T, BLEND_THREADS, 0, s>>>(
-      vp.W, vp.H, L.gx, reinterpret_cast<const uint2 *>(geom + L.ranges),
-      reinterpret_cast<const uint32_t *>(bin + B.point_list),
-      reinterpret_cast<const float4 *>(geom + L.feat), bg,
-      reinterpret_cast<const float *>(img + I.final_T),
-      reinterpret_cast<const uint32_t *>(img + I.n_contrib), dL_dout, gacc));
-  DMGS_LAUNCH_CHECK("blend_bwd_kernel");
-  return DMGS_OK;
+  BlendBatch bb;
+  bb.nviews = 1;
+  bb.v[0] = make_blend_view(vp, L, geom, B, bin, I, const_cast<char *>(img), bg);
+  bb.v[0].dL_dout = dL_dout;
+  bb.v[0].gacc = gacc;
+  bb.total = bb.v[0].T;
+  return launch_blend_batch_bwd(bb, default_blend_cfg(), nullptr, s);
 }
 
 }  // namespace dmgs

@@ -179,7 +179,7 @@ int dmgs_raster_fwd_geometry(const DmgsView *view, const DmgsGaussians *g, void 
   RET_IF(launch_preprocess(vp, view->viewmatrix, view->projmatrix, view->campos, make_gptrs(g),
                            radii, L, geom, s));
   RET_IF(debug_sync(view, s, "preprocess"));
-  RET_IF(launch_binning_geometry(L, radii, geom, s));
+  RET_IF(launch_binning_geometry(L, geom, 0xffffffffu, s));
   uint32_t h[CI_WORDS];
   RET_IF(check_status(geom, L, s, h));
   if (num_rendered) *num_rendered = (int64_t)h[CI_K];

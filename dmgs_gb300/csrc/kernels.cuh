@@ -10,7 +10,26 @@ struct GaussianPtrs {
   const float *means3D, *opacities, *shs, *colors, *scales, *rotations, *cov3D;
 };
 
+// One view of a multi-view batch, as the per-Gaussian kernels see it.
+struct BatchView {
+  ViewParams vp;
+  const float *viewm, *projm, *campos;  // device
+  int32_t *radii;                       // [P] or a [P] scratch when the caller passes none
+  float4 *feat;                         // geometry state of this view
+  uint8_t *flags;
+  uint32_t *blkcnt;
+  uint32_t *counters;
+  const float *gacc;                    // adjoint: this view's 2D gradient records
+  float *dL_dmeans2D;                   // adjoint: optional per-view output [P,3]
+};
+
+struct BatchViews {
+  int nviews;
+  BatchView v[16];
+};
+
 // preprocess.cu
+int launch_preprocess_batched(const BatchViews &bv, const GaussianPtrs &g, cudaStream_t s);
 int launch_preprocess(const ViewParams &vp, const float *viewm, const float *projm,
                       const float *campos, const GaussianPtrs &g, int32_t *radii,
                       const GeomLayout &L, char *geom, cudaStream_t s);
@@ -20,7 +39,9 @@ int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t
 // binning.cu
 int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t *part,
                 uint32_t *total_out, uint32_t *status, cudaStream_t s);
-int launch_binning_geometry(const GeomLayout &L, const int32_t *radii, char *geom, cudaStream_t s);
+// K_cap: capacity of the caller's list buffer (0xffffffff when it is sized
+// after the geometry phase).
+int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cudaStream_t s);
 int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, int64_t K,
                 cudaStream_t s);
 int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
@@ -30,6 +51,41 @@ int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,
                           float *rgb, cudaStream_t s);
 
 // blend.cu
+constexpr int MAX_BATCH_VIEWS = 16;
+
+// One view of a blend launch: its tile grid and the buffers of its tiles.
+struct BlendView {
+  int W, H, gx, T;     // image size, tile-grid width, tiles
+  int tile_base;       // first work item of this view
+  const uint2 *ranges;
+  const uint32_t *point_list;
+  const float4 *feat;
+  const float *bg;
+  float *out_color;     // forward outputs
+  float *final_T;
+  uint32_t *n_contrib;
+  const float *dL_dout; // adjoint inputs/outputs
+  float *gacc;
+};
+
+struct BlendBatch {
+  int nviews, total;    // views, work items (sum of tiles)
+  BlendView v[MAX_BATCH_VIEWS];
+};
+
+// Tuning parameters of the blend kernels: pixels per thread (1, 2, 4) and
+// Gaussians staged per batch (128, 256, 512).
+struct BlendCfg {
+  int ppt, batch;
+};
+inline BlendCfg default_blend_cfg() { return BlendCfg{2, 256}; }
+
+// queue == nullptr: one CTA per work item; else a persistent grid pulling
+// items from *queue (which must be zero at launch).
+int launch_blend_batch_fwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *queue,
+                           cudaStream_t s);
+int launch_blend_batch_bwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *queue,
+                           cudaStream_t s);
 int launch_blend_fwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
                      const BinLayout &B, const char *bin, const ImgLayout &I, char *img,
                      const float *bg, float *out_color, cudaStream_t s);
@@ -38,6 +94,8 @@ int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom
                      const float *bg, const float *dL_dout, float *gacc, cudaStream_t s);
 
 // preprocess_bwd.cu
+int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, const DmgsGrads &out,
+                                  cudaStream_t s);
 int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float *projm,
                           const float *campos, const GaussianPtrs &g, const GeomLayout &L,
                           const char *geom, const float *gacc, const DmgsGrads &out,

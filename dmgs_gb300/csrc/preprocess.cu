@@ -231,6 +231,27 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
 }
 
 
+// Multi-view preprocess: one thread per Gaussian computes its geometry for
+// every view of the batch (the inputs are read from DRAM once; the repeated
+// per-view reads hit L1), writing each view's records and per-block visible
+// counts.
+__global__ void __launch_bounds__(PRE_BLOCK)
+preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__restrict__ means,
+                          const float *__restrict__ opac, const float *__restrict__ shs,
+                          const float *__restrict__ colors, const float *__restrict__ scales,
+                          const float *__restrict__ rots, const float *__restrict__ cov3D) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int v = 0; v < bv.nviews; ++v) {
+    const BatchView &V = bv.v[v];
+    const bool vis = idx < P &&
+                     preprocess_one(idx, V.vp, V.viewm, V.projm, V.campos, M, means, opac, shs,
+                                    colors, scales, rots, cov3D, V.radii, V.feat, V.flags,
+                                    V.counters);
+    const int nvis = __syncthreads_count(vis);
+    if (threadIdx.x == 0) V.blkcnt[blockIdx.x] = (uint32_t)nvis;
+  }
+}
+
 __global__ void mark_visible_kernel(int P, const float *__restrict__ means,
                                     const float *__restrict__ viewm_g,
                                     uint8_t *__restrict__ present) {
@@ -307,4 +328,20 @@ int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,
   DMGS_LAUNCH_CHECK("debug_geometry_kernel");
   return DMGS_OK;
 }
+}  // namespace dmgs
+
+namespace dmgs {
+
+int launch_preprocess_batched(const BatchViews &bv, const GaussianPtrs &g, cudaStream_t s) {
+  for (int v = 0; v < bv.nviews; ++v)
+    DMGS_CUDA(cudaMemsetAsync(bv.v[v].counters, 0, CI_WORDS * 4, s));
+  if (g.P <= 0) return DMGS_OK;
+  DMGS_TIMED(K_BATCH_PREPROCESS, s,
+             preprocess_batched_kernel<<<(g.P + PRE_BLOCK - 1) / PRE_BLOCK, PRE_BLOCK, 0, s>>>(
+                 bv, g.P, g.M, g.means3D, g.opacities, g.shs, g.colors, g.scales, g.rotations,
+                 g.cov3D));
+  DMGS_LAUNCH_CHECK("preprocess_batched_kernel");
+  return DMGS_OK;
+}
+
 }  // namespace dmgs

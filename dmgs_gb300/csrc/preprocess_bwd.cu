@@ -32,6 +32,14 @@ struct Slots {
   float *m2, *col, *op, *m3, *cov, *sc, *rot, *sh;
 };
 
+// ACC: add into the slots (several views of one Gaussian); else assign.
+template <bool ACC>
+__device__ __forceinline__ void put(float &slot, float v) {
+  if (ACC) slot += v;
+  else slot = v;
+}
+
+template <bool ACC>
 __device__ __forceinline__ void
 preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict__ viewm_g,
                    const float *__restrict__ projm_g, const float *__restrict__ campos_g, int M,
@@ -48,9 +56,9 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
   const float dop = gb.y;
   float drgb[3] = {gb.z, gb.w, gblue};
 
-  if (out.dL_dmeans2D) { S_.m2[3 * t] = dndc_x; S_.m2[3 * t + 1] = dndc_y; S_.m2[3 * t + 2] = 0.f; }
-  if (out.dL_dopacity) S_.op[t] = dop;
-  if (out.dL_dcolors) { S_.col[3 * t] = drgb[0]; S_.col[3 * t + 1] = drgb[1]; S_.col[3 * t + 2] = drgb[2]; }
+  if (out.dL_dmeans2D && !ACC) { S_.m2[3 * t] = dndc_x; S_.m2[3 * t + 1] = dndc_y; S_.m2[3 * t + 2] = 0.f; }
+  if (out.dL_dopacity) put<ACC>(S_.op[t], dop);
+  if (out.dL_dcolors) { put<ACC>(S_.col[3 * t], drgb[0]); put<ACC>(S_.col[3 * t + 1], drgb[1]); put<ACC>(S_.col[3 * t + 2], drgb[2]); }
 
   float V[16], Pm[16];
 #pragma unroll
@@ -143,8 +151,8 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
     for (int j = 0; j < 3; ++j) dS[i * 3 + j] = T[0][i] * GT[0][j] + T[1][i] * GT[1][j];
   if (out.dL_dcov3D) {
     float *o = S_.cov + 6 * t;
-    o[0] = dS[0]; o[1] = 2.f * dS[1]; o[2] = 2.f * dS[2];
-    o[3] = dS[4]; o[4] = 2.f * dS[5]; o[5] = dS[8];
+    put<ACC>(o[0], dS[0]); put<ACC>(o[1], 2.f * dS[1]); put<ACC>(o[2], 2.f * dS[2]);
+    put<ACC>(o[3], dS[4]); put<ACC>(o[4], 2.f * dS[5]); put<ACC>(o[5], dS[8]);
   }
 
   // dL/dT = 2 Gs T Sigma
@@ -203,7 +211,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
     float gdx = 0.f, gdy = 0.f, gdz = 0.f;
     auto term = [&](int k, float b, float bx, float by, float bz) {
       const float s0 = sh[3 * k], s1 = sh[3 * k + 1], s2 = sh[3 * k + 2];
-      if (dsh) { dsh[3 * k] = b * drgb[0]; dsh[3 * k + 1] = b * drgb[1]; dsh[3 * k + 2] = b * drgb[2]; }
+      if (dsh) { put<ACC>(dsh[3 * k], b * drgb[0]); put<ACC>(dsh[3 * k + 1], b * drgb[1]); put<ACC>(dsh[3 * k + 2], b * drgb[2]); }
       const float dot = s0 * drgb[0] + s1 * drgb[1] + s2 * drgb[2];
       gdx += bx * dot; gdy += by * dot; gdz += bz * dot;
     };
@@ -236,7 +244,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
       }
     }
     if (dsh)
-      for (int i = 3 * nsh; i < 3 * M; ++i) dsh[i] = 0.f;
+      if (!ACC) for (int i = 3 * nsh; i < 3 * M; ++i) dsh[i] = 0.f;
     // d unit(v)/dv . g = (g - u (u . g)) / |v|
     const float ug = x * gdx + y * gdy + z * gdz;
     dm[0] += (gdx - x * ug) * il;
@@ -245,9 +253,9 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
   }
 
   if (out.dL_dmeans3D) {
-    S_.m3[3 * t] = dm[0];
-    S_.m3[3 * t + 1] = dm[1];
-    S_.m3[3 * t + 2] = dm[2];
+    put<ACC>(S_.m3[3 * t], dm[0]);
+    put<ACC>(S_.m3[3 * t + 1], dm[1]);
+    put<ACC>(S_.m3[3 * t + 2], dm[2]);
   }
 
   // --- scale / rotation --------------------------------------------------
@@ -267,8 +275,8 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
     if (out.dL_dscales) {
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        S_.sc[3 * t + j] =
-            vp.scale_modifier * (dM[j] * R[j] + dM[3 + j] * R[3 + j] + dM[6 + j] * R[6 + j]);
+        put<ACC>(S_.sc[3 * t + j],
+                 vp.scale_modifier * (dM[j] * R[j] + dM[3 + j] * R[3 + j] + dM[6 + j] * R[6 + j]));
     }
     if (out.dL_drotations) {
       float G[9];
@@ -284,7 +292,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
                               z * G[7] - 2.f * y * G[8]);
       const float dz = 2.f * (-2.f * z * G[0] - r * G[1] + x * G[2] + r * G[3] - 2.f * z * G[4] +
                               y * G[5] + x * G[6] + y * G[7]);
-      { S_.rot[4 * t] = dr; S_.rot[4 * t + 1] = dx; S_.rot[4 * t + 2] = dy; S_.rot[4 * t + 3] = dz; }
+      { put<ACC>(S_.rot[4 * t], dr); put<ACC>(S_.rot[4 * t + 1], dx); put<ACC>(S_.rot[4 * t + 2], dy); put<ACC>(S_.rot[4 * t + 3], dz); }
     }
   }
 }
@@ -342,11 +350,66 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   const uint32_t bal = __ballot_sync(0xffffffffu, vis);
   if ((t & 31) == 0) vmask[t >> 5] = bal;
   if (vis)
-    preprocess_bwd_one(idx, t, vp, viewm_g, projm_g, campos_g, M, means, shs, scales, rots, cov3D,
-                       flags, gacc, out, S_);
+    preprocess_bwd_one<false>(idx, t, vp, viewm_g, projm_g, campos_g, M, means, shs, scales, rots,
+                              cov3D, flags, gacc, out, S_);
   __syncthreads();
   const int nvalid = min(B, P - start);
   store_slice(out.dL_dmeans2D, S_.m2, 3, start, nvalid, vmask);
+  store_slice(out.dL_dcolors, S_.col, 3, start, nvalid, vmask);
+  store_slice(out.dL_dopacity, S_.op, 1, start, nvalid, vmask);
+  store_slice(out.dL_dmeans3D, S_.m3, 3, start, nvalid, vmask);
+  store_slice(out.dL_dcov3D, S_.cov, 6, start, nvalid, vmask);
+  store_slice(out.dL_dscales, S_.sc, 3, start, nvalid, vmask);
+  store_slice(out.dL_drotations, S_.rot, 4, start, nvalid, vmask);
+  store_slice(out.dL_dsh, S_.sh, 3 * M, start, nvalid, vmask);
+}
+
+// Multi-view adjoint: the gradients of all views of a batch, summed.  Each
+// thread handles one Gaussian for every view it is visible in, accumulating
+// in its shared-memory slots; the block then stores its slices once.
+__global__ void __launch_bounds__(BWD_BLOCK)
+preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__restrict__ means,
+                              const float *__restrict__ shs, const float *__restrict__ scales,
+                              const float *__restrict__ rots, const float *__restrict__ cov3D,
+                              DmgsGrads out) {
+  extern __shared__ float sm[];
+  __shared__ uint32_t vmask[BWD_BLOCK / 32];
+  const int B = BWD_BLOCK;
+  const int t = threadIdx.x;
+  const int start = blockIdx.x * B;
+  const int idx = start + t;
+  Slots S_;
+  S_.m2 = sm;
+  S_.col = S_.m2 + 3 * B;
+  S_.op = S_.col + 3 * B;
+  S_.m3 = S_.op + B;
+  S_.cov = S_.m3 + 3 * B;
+  S_.sc = S_.cov + 6 * B;
+  S_.rot = S_.sc + 3 * B;
+  S_.sh = S_.rot + 4 * B;
+  const int per_g = 23 + 3 * M;
+  for (int i = t; i < B * per_g; i += B) sm[i] = 0.f;
+  __syncthreads();
+  bool any = false;
+  if (idx < P) {
+    for (int v = 0; v < bv.nviews; ++v) {
+      const BatchView &V = bv.v[v];
+      if (!(V.flags[idx] & FLAG_VISIBLE)) continue;
+      any = true;
+      preprocess_bwd_one<true>(idx, t, V.vp, V.viewm, V.projm, V.campos, M, means, shs, scales,
+                               rots, cov3D, V.flags, V.gacc, out, S_);
+      if (V.dL_dmeans2D) {  // per-view screen-space gradient (NDC)
+        const float4 ga = reinterpret_cast<const float4 *>(V.gacc)[3 * idx];
+        V.dL_dmeans2D[3 * idx] = ga.x;
+        V.dL_dmeans2D[3 * idx + 1] = ga.y;
+        V.dL_dmeans2D[3 * idx + 2] = 0.f;
+      }
+    }
+  }
+  const uint32_t bal = __ballot_sync(0xffffffffu, any);
+  if ((t & 31) == 0) vmask[t >> 5] = bal;
+  __syncthreads();
+  const int nvalid = min(B, P - start);
   store_slice(out.dL_dcolors, S_.col, 3, start, nvalid, vmask);
   store_slice(out.dL_dopacity, S_.op, 1, start, nvalid, vmask);
   store_slice(out.dL_dmeans3D, S_.m3, 3, start, nvalid, vmask);
@@ -375,6 +438,28 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
       vp, viewm, projm, campos, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D,
       reinterpret_cast<const uint8_t *>(geom + L.flags), gacc, out));
   DMGS_LAUNCH_CHECK("preprocess_bwd_kernel");
+  return DMGS_OK;
+}
+
+}  // namespace dmgs
+
+namespace dmgs {
+
+int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, const DmgsGrads &out,
+                                  cudaStream_t s) {
+  if (g.P <= 0) return DMGS_OK;
+  const size_t smem = (size_t)BWD_BLOCK * (23 + 3 * (size_t)g.M) * 4;
+  if (smem > 200 * 1024) {
+    dmgs_host::set_error("preprocess_bwd: %d SH coefficients per Gaussian exceed shared memory", g.M);
+    return DMGS_ERR_ARG;
+  }
+  if (smem > 48 * 1024)
+    DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_batched_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DMGS_TIMED(K_BATCH_PREPROCESS_BWD, s,
+             preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
+                 bv, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D, out));
+  DMGS_LAUNCH_CHECK("preprocess_bwd_batched_kernel");
   return DMGS_OK;
 }
 

@@ -157,6 +157,46 @@ int dmgs_raster_bwd_noalloc(const DmgsView *view, const DmgsGaussians *g,
                             const void *image_state, size_t image_bytes,
                             const DmgsGrads *grads, dmgs_stream_t stream);
 
+/* ---------------------------------------------------------------------- *
+ * Multi-view batched form (no counterpart in the reference, which renders
+ * one view per call: render_and_eval.py:42-44, train_geo_stage2.py:101).
+ * A batch of views of one Gaussian set: one preprocess pass for all views,
+ * per-view binning into capacity-bounded instance lists (no host
+ * synchronisation, so the calls can be captured in a CUDA graph), blending
+ * of every view's tiles by one persistent launch, and an adjoint that sums
+ * the views' gradients and writes them once.  A view whose instances exceed
+ * its capacity renders background and is reported by dmgs_batch_status.
+ * ---------------------------------------------------------------------- */
+#define DMGS_MAX_BATCH_VIEWS 16
+typedef struct DmgsBatch {
+  int32_t nviews;                  /* 1..DMGS_MAX_BATCH_VIEWS */
+  const DmgsView *views;           /* [nviews] host array */
+  float *const *out_color;         /* [nviews] device pointers, [3,H,W] each */
+  int32_t *const *radii;           /* [nviews] device pointers to [P], or NULL */
+  const int64_t *capacity;         /* [nviews] instance-list capacity per view */
+  int32_t pixels_per_thread;       /* blend tuning: 1, 2 or 4 (0: 2) */
+  int32_t gaussians_per_batch;     /* blend tuning: 128, 256 or 512 (0: 256) */
+} DmgsBatch;
+
+size_t dmgs_batch_state_bytes(const DmgsBatch *b, int32_t P);
+/* Forward of every view; asynchronous, no host synchronisation. */
+int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
+                            void *state, size_t state_bytes,
+                            dmgs_stream_t stream);
+/* Adjoint of the batch: dL_dout_color[v] [3,H,W] per view; `grads` receive
+ * the sum over views (its dL_dmeans2D is unused); dL_dmeans2D[v] (may be
+ * NULL, or have NULL entries) receives view v's NDC-mean gradient [P,3]. */
+int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
+                            const float *const *dL_dout_color, void *state,
+                            size_t state_bytes, const DmgsGrads *grads,
+                            float *const *dL_dmeans2D, dmgs_stream_t stream);
+/* Synchronises the stream, writes each view's instance count to
+ * num_rendered[v] and returns DMGS_ERR_OVERFLOW when a view exceeded its
+ * capacity (or another DMGS_ERR_* from a view's status word). */
+int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *state,
+                      size_t state_bytes, int64_t *num_rendered,
+                      dmgs_stream_t stream);
+
 /* Frustum test (replaces `mark_visible`): present[i] = 1 iff point i lies in
  * front of view-space z = 0.2.  present: [P] uint8 device. */
 int dmgs_mark_visible(int32_t P, const float *means3D, const float *viewmatrix,
