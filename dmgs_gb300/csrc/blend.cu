@@ -463,9 +463,9 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
 // kernel and device (no runtime queries while a graph is being captured
 // after the first call).
 template <typename K>
-int grid_for(K kernel, int threads, int total, bool persistent, int &grid) {
+int grid_for(K kernel, int threads, int total, bool persistent, int &grid, int &cached_dev,
+             int &cached_slots) {
   if (!persistent) { grid = total; return DMGS_OK; }
-  static int cached_dev = -1, cached_slots = 0;
   int dev = 0;
   DMGS_CUDA(cudaGetDevice(&dev));
   if (dev != cached_dev) {
@@ -481,8 +481,10 @@ int grid_for(K kernel, int threads, int total, bool persistent, int &grid) {
 
 template <int PPT, int BATCH>
 int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
+  static int cdev = -1, cslots = 0;  // per kernel instantiation
   int grid;
-  const int r = grid_for(blend_fwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid);
+  const int r = grid_for(blend_fwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
+                         cdev, cslots);
   if (r != DMGS_OK) return r;
   blend_fwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
@@ -490,8 +492,10 @@ int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
 
 template <int PPT, int BATCH>
 int run_bwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
+  static int cdev = -1, cslots = 0;  // per kernel instantiation
   int grid;
-  const int r = grid_for(blend_bwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid);
+  const int r = grid_for(blend_bwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
+                         cdev, cslots);
   if (r != DMGS_OK) return r;
   blend_bwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
