@@ -1,15 +1,20 @@
 """Benchmark: forward+backward views/s of the Gaussian rasteriser on the
-large-scene workload (3M Gaussians, 1237x822, SH degree 3, scale/rotation
-inputs), one view per step.
+large-scene workload (3M Gaussians, SH degree 3, scale/rotation inputs).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl dmgs|reference]
 
-Prints one JSON line (rank 0).  `value` is device-resident throughput;
-`e2e` is the same metric through the drop-in API with the step's inputs
-copied from pinned host memory and its image + gradients copied back inside
-the timed region.  The reference arm (--impl reference) times the CPU oracle
-(FP64 torch restatement of the reference algorithm) on a bounded sample of
-the same workload on the host cores.
+A step is one batch of 16 views at 1237x822 rendered forward and backward by
+the multi-view batched form (one CUDA-graph replay).  The JSON line (rank 0)
+also carries the plain drop-in path on the same scene (one view per call,
+the reference's call pattern) and the mixed-resolution batch (16 views of
+400x400 / 800x800 / 1237x822 / 1600x900 round-robin) against the plain path
+on the same views.  `value` is device-resident throughput; `e2e` is the same
+step through the public Python API with the Gaussians and the image
+gradients copied from pinned host memory and the images and parameter
+gradients copied back inside the timed region.  The reference arm
+(--impl reference) times the CPU oracle (FP64 torch restatement of the
+reference algorithm) on a bounded sample of the same workload on the host
+cores.
 """
 from __future__ import annotations
 
@@ -29,8 +34,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "fwd+bwd views/s at 3M Gaussians 1237x822"
+MIXED = [(400, 400), (800, 800), (1237, 822), (1600, 900)]
 UNIT = "views/s"
-WORKLOAD = "large-scene fwd+bwd: 3M Gaussians, 1237x822, SH3, scale/rotation inputs, 1 view/step"
+WORKLOAD = ("large-scene fwd+bwd: 3M Gaussians, SH3, scale/rotation inputs; step = 16 views at "
+            "1237x822, multi-view batched form in a CUDA graph")
 
 
 def parse():
@@ -42,7 +49,9 @@ def parse():
     ap.add_argument("--P", type=int, default=3_000_000)
     ap.add_argument("--width", type=int, default=1237)
     ap.add_argument("--height", type=int, default=822)
-    ap.add_argument("--views", type=int, default=8, help="distinct camera poses cycled over steps")
+    ap.add_argument("--views", type=int, default=16, help="views per batch (<= 16)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-resolution batch")
+    ap.add_argument("--no-graph", action="store_true", help="replay without CUDA-graph capture")
     ap.add_argument("--cpu-tiles", type=int, default=24, help="tiles blended in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
@@ -171,8 +180,13 @@ def cpu_oracle_sample(scene, view, n_tiles):
 
 
 # ----------------------------------------------------------------------------
-def bytes_model(name, P, V, K, npix):
-    """Algorithmic DRAM bytes per launch (SH3, scale/rotation inputs)."""
+def bytes_model(name, P, V, K, npix, nviews=1):
+    """Algorithmic DRAM bytes per launch (SH3, scale/rotation inputs).  For
+    a batched launch V, K, npix are sums over the views."""
+    if name == "batch_preprocess":
+        return P * (12 + 16 + 12 + 4 + 192) + nviews * P * 4 + V * 48
+    if name == "batch_preprocess_bwd":
+        return P * (236 + 236) + V * 48
     if name == "preprocess":
         return P * 12 + V * (12 + 16 + 4 + 192) + P * 4 + V * 48
     if name == "blend_fwd":
@@ -188,6 +202,36 @@ def bytes_model(name, P, V, K, npix):
     return None
 
 
+
+def timed(fn, steps, warmup, sync_dev):
+    """Run fn(i) warmup times, then time `steps` calls with CUDA events."""
+    import torch
+    for i in range(warmup):
+        fn(i)
+    torch.cuda.synchronize(sync_dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(steps):
+        fn(i)
+    e1.record()
+    torch.cuda.synchronize(sync_dev)
+    return e0.elapsed_time(e1)
+
+
+def kernel_table(kt, model_args):
+    kernels = {}
+    tot_all = sum(x[0] for x in kt.values()) or 1e-9
+    for name, (tot, n) in kt.items():
+        avg = tot / max(n, 1)
+        b = bytes_model(name, *model_args)
+        kernels[name] = {"launches": n, "total_ms": round(tot, 4), "avg_ms": round(avg, 5),
+                         "share": round(tot / tot_all, 4)}
+        if b is not None:
+            kernels[name]["alg_bytes"] = int(b)
+            kernels[name]["achieved_gbs"] = round(b / (avg / 1e3) / 1e9, 1)
+    return kernels
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -198,8 +242,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        scene = large_scene(P=args.P, seed=0, n_views=max(args.views, 1), width=args.width,
-                            height=args.height)
+        scene = large_scene(P=args.P, seed=0, n_views=4, width=args.width, height=args.height)
         times = []
         desc = ""
         for i in range(args.warmup + args.steps):
@@ -212,7 +255,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "P": args.P, "width": args.width, "height": args.height},
+            "config": {"workload": "large-scene fwd+bwd: 3M Gaussians, 1237x822, SH3, one view "
+                                   "(CPU oracle, bounded sample)", "P": args.P,
+                       "width": args.width, "height": args.height},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                              "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
@@ -221,6 +266,8 @@ def main():
     import torch
     import dmgs_gb300
     from dmgs_gb300 import _lib
+    from dmgs_gb300.batched import BatchedRasterizer, autotune
+    from dmgs_gb300.scenes import random_inside_view
 
     if world > 1:
         import torch.distributed as dist
@@ -228,101 +275,103 @@ def main():
         torch.cuda.set_device(local)
     dev = torch.device("cuda", local if world > 1 else 0)
     torch.cuda.set_device(dev)
-    _lib.load()
+    lib = _lib.load()
+    nv = max(1, min(16, args.views))
 
-    scene = large_scene(P=args.P, seed=rank, n_views=args.views, width=args.width, height=args.height)
+    scene = large_scene(P=args.P, seed=rank, n_views=nv, width=args.width, height=args.height)
     P = scene.P
     t = lambda a: torch.tensor(a, device=dev)  # noqa: E731
-    xyz = t(scene.means3D).requires_grad_(True)
-    opac = t(scene.opacities).requires_grad_(True)
-    shs = t(scene.shs).requires_grad_(True)
-    scales = t(scene.scales).requires_grad_(True)
-    rots = t(scene.rotations).requires_grad_(True)
-    settings = []
-    for v in scene.views:
-        settings.append(dmgs_gb300.GaussianRasterizationSettings(
+    g = {"means3D": t(scene.means3D), "opacities": t(scene.opacities), "shs": t(scene.shs),
+         "scales": t(scene.scales), "rotations": t(scene.rotations)}
+
+    def settings_of(v):
+        return dmgs_gb300.GaussianRasterizationSettings(
             image_height=v.height, image_width=v.width, tanfovx=v.tanfovx, tanfovy=v.tanfovy,
             bg=torch.zeros(3, device=dev), scale_modifier=1.0, viewmatrix=t(v.viewmatrix),
             projmatrix=t(v.projmatrix), sh_degree=3, campos=t(v.campos), prefiltered=False,
-            debug=False))
-    gen = torch.Generator(device=dev)
-    gen.manual_seed(0)
-    dimg = torch.randn(3, args.height, args.width, device=dev, generator=gen)
+            debug=False)
 
-    def step(i, tensors=None):
-        x, o, s, sc, r = tensors if tensors is not None else (xyz, opac, shs, scales, rots)
-        m2 = torch.zeros_like(x, requires_grad=True)
-        img, radii = dmgs_gb300.GaussianRasterizer(settings[i % len(settings)])(
-            means3D=x, means2D=m2, opacities=o, shs=s, scales=sc, rotations=r)
-        img.backward(dimg)
-        return img, radii, m2
+    settings = [settings_of(v) for v in scene.views]
+    gen = torch.Generator(device=dev).manual_seed(0)
+    dimgs = [torch.randn(3, s.image_height, s.image_width, device=dev, generator=gen) for s in settings]
+    leaves = {k: v.clone().requires_grad_(True) for k, v in g.items()}
 
-    def zero_grads(ts):
-        for p in ts:
+    def plain_step(i, sets, douts, tensors=leaves):
+        m2 = torch.zeros_like(tensors["means3D"], requires_grad=True)
+        img, radii = dmgs_gb300.GaussianRasterizer(sets[i % len(sets)])(
+            means3D=tensors["means3D"], means2D=m2, opacities=tensors["opacities"],
+            shs=tensors["shs"], scales=tensors["scales"], rotations=tensors["rotations"])
+        img.backward(douts[i % len(douts)])
+        for p in tensors.values():
             p.grad = None
+        return img, m2
 
-    for i in range(args.warmup):
-        step(i)
-        zero_grads([xyz, opac, shs, scales, rots])
-    torch.cuda.synchronize()
-
-    # per-view instance counts (for the byte model)
-    stats = []
-    for i in range(len(settings)):
-        with torch.no_grad():
-            img, radii = dmgs_gb300.GaussianRasterizer(settings[i])(
-                means3D=xyz.detach(), means2D=torch.zeros_like(xyz), opacities=opac.detach(),
-                shs=shs.detach(), scales=scales.detach(), rotations=rots.detach())
-        stats.append(int((radii > 0).sum()))
-    torch.cuda.synchronize()
-
-    # ---------------- timed region: device-resident inputs ----------------
-    if world > 1:
-        torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
+    # ---------------- plain drop-in path: one view per call ----------------
+    lib.dmgs_timing_enable(0)
     _lib.timing_collect()
-    _lib.timing_enable(True)
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for i in range(args.steps):
-        step(i)
-        zero_grads([xyz, opac, shs, scales, rots])
-    ev1.record()
-    torch.cuda.synchronize()
-    _lib.timing_enable(False)
-    kt = _lib.timing_collect()
-    clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
-    value = world * args.steps / (ms / 1e3)
+    lib.dmgs_timing_enable(1)
+    n0 = lib.dmgs_kernel_launches()
+    ms_plain = timed(lambda i: plain_step(i, settings, dimgs), args.steps, args.warmup, dev)
+    lib.dmgs_timing_enable(0)
+    kt_plain = _lib.timing_collect()
+    plain_launches_per_view = (lib.dmgs_kernel_launches() - n0) / (args.steps + args.warmup)
+    plain_vps = args.steps / (ms_plain / 1e3)
 
-    # K per view from the forward state is not exposed by the drop-in; the
-    # byte model uses the measured instance count of each view.
-    Ks = []
-    for i in range(len(settings)):
-        rs = settings[i]
-        from dmgs_gb300._lib import DmgsGaussians, ptr
-        from dmgs_gb300.rasterizer import make_view
-        import ctypes as C
-        keep = []
-        view = make_view(rs, dev, keep)
-        g = DmgsGaussians(P, 16, ptr(xyz), ptr(opac), ptr(shs), None, ptr(scales), ptr(rots), None)
-        lib = _lib.load()
-        geom = torch.empty(lib.dmgs_geom_state_bytes(P, args.width, args.height), dtype=torch.uint8, device=dev)
-        radii = torch.empty(P, dtype=torch.int32, device=dev)
-        K = C.c_int64(0)
-        _lib.check(lib.dmgs_raster_fwd_geometry(view, g, geom.data_ptr(), geom.numel(), radii.data_ptr(),
-                                                C.byref(K), _lib.stream_of(dev)), "bench K")
-        Ks.append(int(K.value))
-    steps_views = [i % len(settings) for i in range(args.steps)]
-    K_avg = statistics.mean(Ks[i] for i in steps_views)
-    V_avg = statistics.mean(stats[i] for i in steps_views)
-    npix = args.width * args.height
+    # ---------------- batched form: 16 views per step, CUDA graph ----------------
+    br = BatchedRasterizer(settings, g)
+    for d, s in zip(br.dL_dout, dimgs):
+        d.copy_(s)
+    tune = autotune(br, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
+    counts = br.count_instances()
+    lib.dmgs_timing_enable(1)
+    _lib.timing_collect()
+    n0 = lib.dmgs_kernel_launches()
+    br.step()  # eager, instrumented: per-kernel times of one batch
+    torch.cuda.synchronize(dev)
+    launches_per_step = lib.dmgs_kernel_launches() - n0
+    lib.dmgs_timing_enable(0)
+    kt_batch = _lib.timing_collect()
+    if not args.no_graph:
+        br.capture()
+    if world > 1:
+        torch.distributed.barrier()
+    ms_batch = timed(lambda i: br.step(), args.steps, args.warmup, dev)
+    br.status()  # raises on a capacity overflow
+    if world > 1:
+        tt = torch.tensor([ms_batch], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms_batch = float(tt.item())
+    value = world * nv * args.steps / (ms_batch / 1e3)
+
+    # ---------------- mixed resolutions (16 views) ----------------
+    mixed = None
+    if not args.no_mixed:
+        rng = np.random.default_rng(1234 + rank)
+        mviews = [random_inside_view(rng, *MIXED[i % len(MIXED)]) for i in range(nv)]
+        msets = [settings_of(v) for v in mviews]
+        mdouts = [torch.randn(3, s.image_height, s.image_width, device=dev, generator=gen) for s in msets]
+        ms_mplain = timed(lambda i: plain_step(i, msets, mdouts), nv, 2, dev)
+        bm = BatchedRasterizer(msets, g)
+        for d, s in zip(bm.dL_dout, mdouts):
+            d.copy_(s)
+        mtune = autotune(bm, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
+        if not args.no_graph:
+            bm.capture()
+        ms_mb = timed(lambda i: bm.step(), args.steps, args.warmup, dev)
+        bm.status()
+        mixed = {"views": nv, "resolutions": MIXED, "plain_views_per_s": nv / (ms_mplain / 1e3),
+                 "batched_views_per_s": nv * args.steps / (ms_mb / 1e3),
+                 "ratio_batched_over_plain": (nv * args.steps / ms_mb) / (nv / ms_mplain),
+                 "autotune": {"best": mtune["best"], "ms": mtune["ms"]}}
+        del bm
+    clk = clocks.stop()
+
+    # ---------------- roofline of the dominant kernel (batched step) ----------------
+    Vs = sum(int((r > 0).sum()) for r in br.radii)
+    npix = sum(s.image_width * s.image_height for s in settings)
+    kernels = kernel_table(kt_batch, (P, Vs, sum(counts), npix, nv))
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -330,63 +379,46 @@ def main():
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    kernels = {}
-    for name, (tot, n) in kt.items():
-        avg = tot / max(n, 1)
-        b = bytes_model(name, P, V_avg, K_avg, npix)
-        kernels[name] = {"launches": n, "total_ms": round(tot, 4), "avg_ms": round(avg, 5),
-                         "share": round(tot / max(sum(x[0] for x in kt.values()), 1e-9), 4)}
-        if b is not None:
-            kernels[name]["alg_bytes"] = int(b)
-            kernels[name]["achieved_gbs"] = round(b / (avg / 1e3) / 1e9, 1)
-    dom = max(kt.items(), key=lambda kv: kv[1][0])[0] if kt else None
     roof = None
-    if dom is not None and kernels[dom].get("alg_bytes"):
-        ach = kernels[dom]["achieved_gbs"]
+    if kt_batch:
+        dom = max(kt_batch.items(), key=lambda kv: kv[1][0])[0]
         traffic = None
         try:
-            prof = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-            traffic = prof.get(dom)
+            traffic = json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(dom)
         except Exception:
             pass
-        roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                "frac": round(ach / hbm_peak, 4), "traffic": traffic,
-                "peak_source": peak_src}
-    launches = sum(n for (_, n) in kt.values())
+        if kernels[dom].get("alg_bytes"):
+            ach = kernels[dom]["achieved_gbs"]
+            roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": round(ach / hbm_peak, 4), "traffic": traffic, "peak_source": peak_src}
 
-    # ---------------- e2e: host buffers through the drop-in API ----------------
+    # ---------------- e2e: host buffers through the public API ----------------
     e2e = None
     if not args.no_e2e:
-        host = [torch.tensor(a).pin_memory() for a in
-                (scene.means3D, scene.opacities, scene.shs, scene.scales, scene.rotations)]
-        out_img = torch.empty(3, args.height, args.width).pin_memory()
-        out_g = [torch.empty_like(h).pin_memory() for h in host]
-        h2d = sum(h.numel() * 4 for h in host)
-        d2h = out_img.numel() * 4 + sum(h.numel() * 4 for h in host) + P * 12
-        out_m2 = torch.empty(P, 3).pin_memory()
-        n_e2e = max(3, min(args.steps, 10))
+        names = ["means3D", "opacities", "shs", "scales", "rotations"]
+        host_in = {k: g[k].cpu().pin_memory() for k in names}
+        host_dout = [d.cpu().pin_memory() for d in dimgs]
+        host_img = [torch.empty(i.shape).pin_memory() for i in br.images]
+        host_grad = {k: torch.empty(br.grads[k].shape).pin_memory() for k in names}
 
         def e2e_step(i):
-            dv = [h.to(dev, non_blocking=True).requires_grad_(True) for h in host]
-            img, radii, m2 = step(i, dv)
-            out_img.copy_(img.detach(), non_blocking=True)
-            for o, d in zip(out_g, dv):
-                o.copy_(d.grad, non_blocking=True)
-            out_m2.copy_(m2.grad, non_blocking=True)
+            for k in names:
+                br.g[k].copy_(host_in[k], non_blocking=True)
+            for d, h in zip(br.dL_dout, host_dout):
+                d.copy_(h, non_blocking=True)
+            br.step()
+            for h, d in zip(host_img, br.images):
+                h.copy_(d, non_blocking=True)
+            for k in names:
+                host_grad[k].copy_(br.grads[k], non_blocking=True)
 
-        for i in range(2):
-            e2e_step(i)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for i in range(n_e2e):
-            e2e_step(i)
-        e1.record()
-        torch.cuda.synchronize()
-        ems = e0.elapsed_time(e1)
-        e2e = {"value": world * n_e2e / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "steps": n_e2e,
-               "api": "dmgs_gb300.GaussianRasterizer (drop-in), pinned host buffers"}
+        ems = timed(e2e_step, max(3, min(args.steps, 10)), 2, dev)
+        n_e2e = max(3, min(args.steps, 10))
+        h2d = sum(h.numel() * 4 for h in host_in.values()) + sum(h.numel() * 4 for h in host_dout)
+        d2h = sum(h.numel() * 4 for h in host_img) + sum(h.numel() * 4 for h in host_grad.values())
+        e2e = {"value": world * nv * n_e2e / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": n_e2e, "views_per_step": nv,
+               "api": "dmgs_gb300.batched.BatchedRasterizer, pinned host buffers"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -395,16 +427,24 @@ def main():
                "sample": desc}
 
     if rank == 0:
+        Kp = statistics.mean(counts)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": ms_batch / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "P": P, "width": args.width, "height": args.height,
-                       "views": len(settings), "parallelism": "replicas" if world > 1 else "1 gpu",
-                       "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(K_avg),
-                       "mean_visible": int(V_avg)},
+                       "views_per_step": nv, "parallelism": "replicas" if world > 1 else "1 gpu",
+                       "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
+                       "blend_config": {"pixels_per_thread": br.cfg[0], "gaussians_per_batch": br.cfg[1]},
+                       "graph": not args.no_graph},
+            "plain": {"views_per_s": plain_vps, "ms_per_view": ms_plain / args.steps,
+                      "ratio_batched_over_plain": value / max(plain_vps, 1e-9),
+                      "kernels": kernel_table(kt_plain, (P, Vs / nv, Kp, npix / nv)),
+                      "launches_per_view": plain_launches_per_view},
+            "mixed": mixed,
+            "autotune": {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": launches, "clocks": clk}
+            "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

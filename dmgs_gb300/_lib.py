@@ -98,6 +98,7 @@ SIGNATURES = [
     ("dmgs_bind3_fwd", C.c_int, [C.POINTER(DmgsFaceBinding3), vp, vp, vp, vp]),
     ("dmgs_bind3_bwd", C.c_int, [C.POINTER(DmgsFaceBinding3), vp, vp, vp, vp, vp, vp, vp]),
     ("dmgs_timing_enable", C.c_int, [C.c_int32]),
+    ("dmgs_kernel_launches", C.c_int64, []),
     ("dmgs_timing_collect", C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_char_p),
                                       C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("dmgs_last_error", C.c_char_p, []),

@@ -427,7 +427,7 @@ __global__ void bind3_bwd_kernel(DmgsFaceBinding3 b, const float *__restrict__ d
 int launch_bind_fwd(const DmgsFaceBinding &b, float *xyz, float *cov, float *rot, float *covL,
                     cudaStream_t s) {
   if (b.F <= 0) return DMGS_OK;
-  DMGS_TIMED(K_BIND_FWD, s, bind_fwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, xyz, cov, rot, covL));
+  DMGS_TIMED(K_BIND_FWD, s, dmgs_host::note_launch(), bind_fwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, xyz, cov, rot, covL));
   DMGS_LAUNCH_CHECK("bind_fwd_kernel");
   return DMGS_OK;
 }
@@ -437,7 +437,7 @@ int launch_bind_bwd(const DmgsFaceBinding &b, const float *dxyz, const float *dc
   DMGS_CUDA(cudaMemsetAsync(dverts, 0, (size_t)b.V * 3 * 4, s));
   if (dsf) DMGS_CUDA(cudaMemsetAsync(dsf, 0, 4, s));
   if (b.F <= 0) return DMGS_OK;
-  DMGS_TIMED(K_BIND_BWD, s, bind_bwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, dxyz, dcov, dverts, dsf));
+  DMGS_TIMED(K_BIND_BWD, s, dmgs_host::note_launch(), bind_bwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, dxyz, dcov, dverts, dsf));
   DMGS_LAUNCH_CHECK("bind_bwd_kernel");
   return DMGS_OK;
 }
@@ -445,7 +445,7 @@ int launch_bind_bwd(const DmgsFaceBinding &b, const float *dxyz, const float *dc
 int launch_bind3_fwd(const DmgsFaceBinding3 &b, float *xyz, float *scales, float *rots,
                      cudaStream_t s) {
   if (b.F <= 0) return DMGS_OK;
-  DMGS_TIMED(K_BIND3_FWD, s, bind3_fwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, xyz, scales, rots));
+  DMGS_TIMED(K_BIND3_FWD, s, dmgs_host::note_launch(), bind3_fwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, xyz, scales, rots));
   DMGS_LAUNCH_CHECK("bind3_fwd_kernel");
   return DMGS_OK;
 }
@@ -455,7 +455,7 @@ int launch_bind3_bwd(const DmgsFaceBinding3 &b, const float *dxyz, const float *
                      cudaStream_t s) {
   DMGS_CUDA(cudaMemsetAsync(dverts, 0, (size_t)b.V * 3 * 4, s));
   if (b.F <= 0) return DMGS_OK;
-  DMGS_TIMED(K_BIND3_BWD, s, bind3_bwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, dxyz, dscales, drots, dverts, dscaling,
+  DMGS_TIMED(K_BIND3_BWD, s, dmgs_host::note_launch(), bind3_bwd_kernel<<<(b.F + 255) / 256, 256, 0, s>>>(b, dxyz, dscales, drots, dverts, dscaling,
                                                      drot2d));
   DMGS_LAUNCH_CHECK("bind3_bwd_kernel");
   return DMGS_OK;

@@ -472,16 +472,16 @@ int emit_warps(int T) {
 int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t *part,
                 uint32_t *total_out, uint32_t *status, cudaStream_t s) {
   if (n_max <= (uint32_t)SCAN_TILE * 4) {
-    scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, 0, total_out, status);
+    dmgs_host::note_launch(), scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, 0, total_out, status);
     DMGS_LAUNCH_CHECK("scan_single_kernel");
     return DMGS_OK;
   }
   const uint32_t nb = (n_max + SCAN_TILE - 1) / SCAN_TILE;
-  scan_reduce_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
+  dmgs_host::note_launch(), scan_reduce_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
   DMGS_LAUNCH_CHECK("scan_reduce_kernel");
-  scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(part, n_dev, n_max, 1, total_out, status);
+  dmgs_host::note_launch(), scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(part, n_dev, n_max, 1, total_out, status);
   DMGS_LAUNCH_CHECK("scan_single_kernel");
-  scan_down_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
+  dmgs_host::note_launch(), scan_down_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
   DMGS_LAUNCH_CHECK("scan_down_kernel");
   return DMGS_OK;
 }
@@ -502,22 +502,22 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
     DMGS_TIMED(K_BIN_COMPACT, s, {
       int r = launch_scan(blkcnt, nullptr, (uint32_t)L.nb_pre, part, counters + CI_V, counters, s);
       if (r != DMGS_OK) return r;
-      compact_kernel<<<L.nb_pre, PRE_BLOCK, 0, s>>>(L.P, reinterpret_cast<const uint8_t *>(geom + L.flags), feat, blkcnt, k0, v0);
+      dmgs_host::note_launch(), compact_kernel<<<L.nb_pre, PRE_BLOCK, 0, s>>>(L.P, reinterpret_cast<const uint8_t *>(geom + L.flags), feat, blkcnt, k0, v0);
     });
     DMGS_LAUNCH_CHECK("compact_kernel");
   }
-  params_kernel<<<1, 1, 0, s>>>(T, counters);
+  dmgs_host::note_launch(), params_kernel<<<1, 1, 0, s>>>(T, counters);
   DMGS_LAUNCH_CHECK("params_kernel");
   if (L.P > 0) {
     DMGS_TIMED(K_BIN_SORT, s, {
       uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
       for (int pass = 0; pass < 4; ++pass) {
         const int shift = 8 * pass;
-        radix_hist_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, counters, shift, rhist);
+        dmgs_host::note_launch(), radix_hist_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, counters, shift, rhist);
         int r = launch_scan(rhist, counters + CI_NRH, (uint32_t)L.n_rhist_max, part, nullptr,
                             nullptr, s);
         if (r != DMGS_OK) return r;
-        radix_scatter_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, vi, ko, vo, counters, shift,
+        dmgs_host::note_launch(), radix_scatter_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, vi, ko, vo, counters, shift,
                                                                  rhist);
         uint32_t *t1 = ki; ki = ko; ko = t1;
         uint32_t *t2 = vi; vi = vo; vo = t2;
@@ -535,7 +535,7 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
       DMGS_CUDA(cudaFuncSetAttribute(tile_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)csm));
     DMGS_TIMED(K_BIN_COUNT, s,
-               tile_count_kernel<<<CHUNK_COUNT_MAX, 256, csm, s>>>(L.gx, T, feat, v0, counters,
+               dmgs_host::note_launch(), tile_count_kernel<<<CHUNK_COUNT_MAX, 256, csm, s>>>(L.gx, T, feat, v0, counters,
                                                                    cmat));
     DMGS_LAUNCH_CHECK("tile_count_kernel");
   }
@@ -545,7 +545,7 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
                           counters, s);
       if (r != DMGS_OK) return r;
     }
-    ranges_kernel<<<(T + 255) / 256, 256, 0, s>>>(T, cmat, counters,
+    dmgs_host::note_launch(), ranges_kernel<<<(T + 255) / 256, 256, 0, s>>>(T, cmat, counters,
                                                   reinterpret_cast<uint2 *>(geom + L.ranges), K_cap);
   });
   DMGS_LAUNCH_CHECK("ranges_kernel");
@@ -566,7 +566,7 @@ int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, 
     DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
   DMGS_TIMED(K_BIN_EMIT, s,
-             emit_kernel<<<CHUNK_COUNT_MAX, nw * 32, smem, s>>>(
+             dmgs_host::note_launch(), emit_kernel<<<CHUNK_COUNT_MAX, nw * 32, smem, s>>>(
                  L.gx, T, reinterpret_cast<const float4 *>(geom + L.feat),
                  reinterpret_cast<const uint32_t *>(geom + L.dval0),
                  reinterpret_cast<uint32_t *>(geom + L.counters),
@@ -578,7 +578,7 @@ int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, 
 
 int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
                       uint64_t *keys, uint32_t *values, cudaStream_t s) {
-  DMGS_TIMED(K_DEBUG, s, debug_keys_kernel<<<L.T(), 256, 0, s>>>(
+  DMGS_TIMED(K_DEBUG, s, dmgs_host::note_launch(), debug_keys_kernel<<<L.T(), 256, 0, s>>>(
       L.T(), reinterpret_cast<const uint2 *>(geom + L.ranges),
       reinterpret_cast<const uint32_t *>(bin + B.point_list),
       reinterpret_cast<const float4 *>(geom + L.feat), keys, values));

@@ -486,7 +486,7 @@ int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
   const int r = grid_for(blend_fwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
                          cdev, cslots);
   if (r != DMGS_OK) return r;
-  blend_fwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  dmgs_host::note_launch(), blend_fwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
 }
 
@@ -497,7 +497,7 @@ int run_bwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
   const int r = grid_for(blend_bwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
                          cdev, cslots);
   if (r != DMGS_OK) return r;
-  blend_bwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  dmgs_host::note_launch(), blend_bwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
 }
 

@@ -194,6 +194,7 @@ enum KernelId {
 };
 void timing_begin(int kid, cudaStream_t s);
 void timing_end(int kid, cudaStream_t s);
+void note_launch();  // counts every kernel launch (dmgs_kernel_launches)
 }  // namespace dmgs_host
 
 // Bracket one kernel launch with the timing registry (no-op when disabled).

@@ -275,7 +275,7 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
   DMGS_CUDA(cudaMemsetAsync(counters, 0, CI_WORDS * 4, s));
   if (g.P > 0) {
     const int blocks = L.nb_pre;
-    DMGS_TIMED(K_PREPROCESS, s, preprocess_kernel<<<blocks, PRE_BLOCK, 0, s>>>(vp, viewm, projm, campos, g.P, g.M, g.means3D,
+    DMGS_TIMED(K_PREPROCESS, s, dmgs_host::note_launch(), preprocess_kernel<<<blocks, PRE_BLOCK, 0, s>>>(vp, viewm, projm, campos, g.P, g.M, g.means3D,
                                                  g.opacities, g.shs, g.colors, g.scales,
                                                  g.rotations, g.cov3D, radii, feat, flags, blkcnt,
                                                  counters));
@@ -287,7 +287,7 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
 int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t *present,
                         cudaStream_t s) {
   if (P <= 0) return DMGS_OK;
-  DMGS_TIMED(K_MARK_VISIBLE, s, mark_visible_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, means3D, viewm, present));
+  DMGS_TIMED(K_MARK_VISIBLE, s, dmgs_host::note_launch(), mark_visible_kernel<<<(P + 255) / 256, 256, 0, s>>>(P, means3D, viewm, present));
   DMGS_LAUNCH_CHECK("mark_visible_kernel");
   return DMGS_OK;
 }
@@ -322,7 +322,7 @@ int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,
                           uint32_t *tiles_touched, float *depth, float *xy, float *conic_opacity,
                           float *rgb, cudaStream_t s) {
   if (L.P <= 0) return DMGS_OK;
-  DMGS_TIMED(K_DEBUG, s, debug_geometry_kernel<<<(L.P + 255) / 256, 256, 0, s>>>(
+  DMGS_TIMED(K_DEBUG, s, dmgs_host::note_launch(), debug_geometry_kernel<<<(L.P + 255) / 256, 256, 0, s>>>(
       L.P, L.gx, reinterpret_cast<const float4 *>(geom + L.feat), rect, tiles_touched, depth, xy,
       conic_opacity, rgb));
   DMGS_LAUNCH_CHECK("debug_geometry_kernel");
@@ -337,7 +337,7 @@ int launch_preprocess_batched(const BatchViews &bv, const GaussianPtrs &g, cudaS
     DMGS_CUDA(cudaMemsetAsync(bv.v[v].counters, 0, CI_WORDS * 4, s));
   if (g.P <= 0) return DMGS_OK;
   DMGS_TIMED(K_BATCH_PREPROCESS, s,
-             preprocess_batched_kernel<<<(g.P + PRE_BLOCK - 1) / PRE_BLOCK, PRE_BLOCK, 0, s>>>(
+             dmgs_host::note_launch(), preprocess_batched_kernel<<<(g.P + PRE_BLOCK - 1) / PRE_BLOCK, PRE_BLOCK, 0, s>>>(
                  bv, g.P, g.M, g.means3D, g.opacities, g.shs, g.colors, g.scales, g.rotations,
                  g.cov3D));
   DMGS_LAUNCH_CHECK("preprocess_batched_kernel");

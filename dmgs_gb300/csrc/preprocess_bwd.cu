@@ -434,7 +434,7 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
   if (smem > 48 * 1024)
     DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  DMGS_TIMED(K_PREPROCESS_BWD, s, preprocess_bwd_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
+  DMGS_TIMED(K_PREPROCESS_BWD, s, dmgs_host::note_launch(), preprocess_bwd_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
       vp, viewm, projm, campos, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D,
       reinterpret_cast<const uint8_t *>(geom + L.flags), gacc, out));
   DMGS_LAUNCH_CHECK("preprocess_bwd_kernel");
@@ -457,7 +457,7 @@ int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, c
     DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_batched_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   DMGS_TIMED(K_BATCH_PREPROCESS_BWD, s,
-             preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
+             dmgs_host::note_launch(), preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
                  bv, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D, out));
   DMGS_LAUNCH_CHECK("preprocess_bwd_batched_kernel");
   return DMGS_OK;

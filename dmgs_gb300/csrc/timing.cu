@@ -4,6 +4,7 @@
 // stream around its kernel.  Pairs are kept until dmgs_timing_collect, which
 // waits for them, accumulates elapsed times per kernel and recycles the
 // events.  Disabled (the default) it costs one branch per launch.
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -52,9 +53,14 @@ void timing_end(int kid, cudaStream_t s) {
   g_pending.push_back({kid, g_open[kid], b});
 }
 
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 }  // namespace dmgs_host
 
 using namespace dmgs_host;
+
+extern "C" int64_t dmgs_kernel_launches(void) { return g_launches.load(); }
 
 extern "C" int dmgs_timing_enable(int32_t on) {
   std::lock_guard<std::mutex> lk(g_mu);

@@ -296,6 +296,8 @@ int dmgs_bind3_bwd(const DmgsFaceBinding3 *b, const float *dL_dxyz,
  * to the number written) and resets them.  Names stay valid until unload.
  * ---------------------------------------------------------------------- */
 int dmgs_timing_enable(int32_t on);
+/* Kernels this library has launched (enqueued) since it was loaded. */
+int64_t dmgs_kernel_launches(void);
 int dmgs_timing_collect(int32_t *n, const char **names, double *total_ms,
                         int64_t *launches);
 
