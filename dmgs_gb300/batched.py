@@ -51,7 +51,7 @@ class BatchedRasterizer:
     parameters updated in place are picked up (also by graph replays).
     """
 
-    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(2, 256)):
+    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(4, 128)):
         if not 1 <= len(settings) <= MAX_VIEWS:
             raise ValueError(f"a batch holds 1..{MAX_VIEWS} views")
         self.lib = _lib.load()

@@ -78,7 +78,7 @@ struct BlendBatch {
 struct BlendCfg {
   int ppt, batch;
 };
-inline BlendCfg default_blend_cfg() { return BlendCfg{2, 256}; }
+inline BlendCfg default_blend_cfg() { return BlendCfg{4, 128}; }  // autotuned on GB300
 
 // queue == nullptr: one CTA per work item; else a persistent grid pulling
 // items from *queue (which must be zero at launch).

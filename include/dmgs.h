@@ -174,8 +174,8 @@ typedef struct DmgsBatch {
   float *const *out_color;         /* [nviews] device pointers, [3,H,W] each */
   int32_t *const *radii;           /* [nviews] device pointers to [P], or NULL */
   const int64_t *capacity;         /* [nviews] instance-list capacity per view */
-  int32_t pixels_per_thread;       /* blend tuning: 1, 2 or 4 (0: 2) */
-  int32_t gaussians_per_batch;     /* blend tuning: 128, 256 or 512 (0: 256) */
+  int32_t pixels_per_thread;       /* blend tuning: 1, 2 or 4 (0: 4) */
+  int32_t gaussians_per_batch;     /* blend tuning: 128, 256 or 512 (0: 128) */
 } DmgsBatch;
 
 size_t dmgs_batch_state_bytes(const DmgsBatch *b, int32_t P);
