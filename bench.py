@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-tiles", type=int, default=24, help="tiles blended in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the one-view-per-call leg")
+    ap.add_argument("--no-tune", action="store_true", help="use the default blend configuration")
     return ap.parse_args()
 
 
@@ -309,21 +311,25 @@ def main():
     clocks = ClockSampler(local)
     clocks.start()
     # ---------------- plain drop-in path: one view per call ----------------
-    lib.dmgs_timing_enable(0)
-    _lib.timing_collect()
-    lib.dmgs_timing_enable(1)
-    n0 = lib.dmgs_kernel_launches()
-    ms_plain = timed(lambda i: plain_step(i, settings, dimgs), args.steps, args.warmup, dev)
-    lib.dmgs_timing_enable(0)
-    kt_plain = _lib.timing_collect()
-    plain_launches_per_view = (lib.dmgs_kernel_launches() - n0) / (args.steps + args.warmup)
-    plain_vps = args.steps / (ms_plain / 1e3)
+    plain = None
+    if not args.no_plain:
+        lib.dmgs_timing_enable(0)
+        _lib.timing_collect()
+        lib.dmgs_timing_enable(1)
+        n0 = lib.dmgs_kernel_launches()
+        ms_plain = timed(lambda i: plain_step(i, settings, dimgs), args.steps, args.warmup, dev)
+        lib.dmgs_timing_enable(0)
+        kt_plain = _lib.timing_collect()
+        plain = {"views_per_s": args.steps / (ms_plain / 1e3), "ms_per_view": ms_plain / args.steps,
+                 "launches_per_view": (lib.dmgs_kernel_launches() - n0) / (args.steps + args.warmup)}
 
     # ---------------- batched form: 16 views per step, CUDA graph ----------------
     br = BatchedRasterizer(settings, g)
     for d, s in zip(br.dL_dout, dimgs):
         d.copy_(s)
-    tune = autotune(br, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
+    tune = None
+    if not args.no_tune:
+        tune = autotune(br, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
     counts = br.count_instances()
     lib.dmgs_timing_enable(1)
     _lib.timing_collect()
@@ -352,19 +358,24 @@ def main():
         mviews = [random_inside_view(rng, *MIXED[i % len(MIXED)]) for i in range(nv)]
         msets = [settings_of(v) for v in mviews]
         mdouts = [torch.randn(3, s.image_height, s.image_width, device=dev, generator=gen) for s in msets]
-        ms_mplain = timed(lambda i: plain_step(i, msets, mdouts), nv, 2, dev)
+        ms_mplain = None if args.no_plain else timed(lambda i: plain_step(i, msets, mdouts), nv, 2, dev)
         bm = BatchedRasterizer(msets, g)
         for d, s in zip(bm.dL_dout, mdouts):
             d.copy_(s)
-        mtune = autotune(bm, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
+        mtune = None
+        if not args.no_tune:
+            mtune = autotune(bm, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
         if not args.no_graph:
             bm.capture()
         ms_mb = timed(lambda i: bm.step(), args.steps, args.warmup, dev)
         bm.status()
-        mixed = {"views": nv, "resolutions": MIXED, "plain_views_per_s": nv / (ms_mplain / 1e3),
+        mixed = {"views": nv, "resolutions": MIXED,
                  "batched_views_per_s": nv * args.steps / (ms_mb / 1e3),
-                 "ratio_batched_over_plain": (nv * args.steps / ms_mb) / (nv / ms_mplain),
-                 "autotune": {"best": mtune["best"], "ms": mtune["ms"]}}
+                 "blend_config": {"pixels_per_thread": bm.cfg[0], "gaussians_per_batch": bm.cfg[1]},
+                 "autotune": mtune and {"best": mtune["best"], "ms": mtune["ms"]}}
+        if ms_mplain is not None:
+            mixed["plain_views_per_s"] = nv / (ms_mplain / 1e3)
+            mixed["ratio_batched_over_plain"] = (nv * args.steps / ms_mb) / (nv / ms_mplain)
         del bm
     clk = clocks.stop()
 
@@ -428,6 +439,9 @@ def main():
 
     if rank == 0:
         Kp = statistics.mean(counts)
+        if plain is not None:
+            plain["ratio_batched_over_plain"] = value / max(plain["views_per_s"], 1e-9)
+            plain["kernels"] = kernel_table(kt_plain, (P, Vs / nv, Kp, npix / nv))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batch / args.steps, "higher_is_better": True,
@@ -437,12 +451,9 @@ def main():
                        "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
                        "blend_config": {"pixels_per_thread": br.cfg[0], "gaussians_per_batch": br.cfg[1]},
                        "graph": not args.no_graph},
-            "plain": {"views_per_s": plain_vps, "ms_per_view": ms_plain / args.steps,
-                      "ratio_batched_over_plain": value / max(plain_vps, 1e-9),
-                      "kernels": kernel_table(kt_plain, (P, Vs / nv, Kp, npix / nv)),
-                      "launches_per_view": plain_launches_per_view},
+            "plain": plain,
             "mixed": mixed,
-            "autotune": {"best": tune["best"], "ms": tune["ms"]},
+            "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))

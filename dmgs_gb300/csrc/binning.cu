@@ -10,17 +10,26 @@
 //   1. compact   the visible Gaussians in index order: (depth_bits, index)
 //   2. sort      them by depth bits with a stable LSD radix sort (4 x 8-bit
 //                digits) -> depth order, ties in index order;
-//   3. count     the sorted list is cut into C chunks of S Gaussians; each
-//                chunk counts its instances per tile -> count matrix [T][C];
-//   4. scan      the matrix in (tile, chunk) order -> the first slot of every
+//   3. chunk     the sorted list is cut into C contiguous chunks of equal
+//                work (weight of a Gaussian: CHUNK_W_GAUSS + ceil(tiles/32),
+//                the warp iterations it costs below) -> chunk starts;
+//   4. count     each chunk counts its instances per tile -> count matrix
+//                [T][C];
+//   5. scan      the matrix in (tile, chunk) order -> the first slot of every
 //                (tile, chunk) pair, the tile ranges and K;
-//   5. emit      each chunk walks its Gaussians in depth order and appends
-//                each Gaussian index to the lists of the tiles it covers.
+//   6. emit      one warp per chunk walks its Gaussians in depth order and
+//                appends each Gaussian index to the lists of the tiles it
+//                covers, its running slots in shared memory.
 //
 // Because every chunk appends in depth order and chunks are laid out in
 // depth order within every tile, each tile's list is exactly the reference's
 // sorted list.  Nothing of size K is read back or sorted; K is written once.
-// The count matrix (T x C x 4 B, at most 16.6 MB at 4056 tiles) stays in L2.
+// Near Gaussians cover thousands of tiles and sort together, so chunks of
+// equal Gaussian count would differ in work by an order of magnitude; equal
+// weight keeps one warp per chunk balanced.  The count matrix (T x C x 4 B,
+// 33 MB at 4056 tiles and 2048 chunks) stays in L2.
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace dmgs {
@@ -159,15 +168,12 @@ compact_kernel(int P, const uint8_t *__restrict__ flags, const float4 *__restric
 }
 
 // One thread: derived sizes from V.
-__global__ void params_kernel(int T, uint32_t *__restrict__ counters) {
+__global__ void params_kernel(int T, uint32_t cmax, uint32_t *__restrict__ counters) {
   const uint32_t V = counters[CI_V];
   const uint32_t nbr = (V + RADIX_TILE - 1) / RADIX_TILE;
-  uint32_t S = (V + CHUNK_COUNT_MAX - 1) / CHUNK_COUNT_MAX;  // C <= CHUNK_COUNT_MAX
-  if (S < CHUNK_MIN) S = CHUNK_MIN;
-  const uint32_t C = (V + S - 1) / S;
+  const uint32_t C = min((V + CHUNK_MIN_GAUSS - 1) / CHUNK_MIN_GAUSS, cmax);
   counters[CI_NBR] = nbr;
   counters[CI_NRH] = 256u * nbr;
-  counters[CI_S] = S;
   counters[CI_C] = C;
   counters[CI_NCM] = (uint32_t)T * C;
 }
@@ -267,47 +273,6 @@ __device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1
   x0 = lo & 0xffff; y0 = lo >> 16; x1 = hi & 0xffff; y1 = hi >> 16;
 }
 
-// A warp takes up to 32 consecutive Gaussians of the depth-sorted list; lane i
-// loads Gaussian s0 + i's index and tile rectangle (one round of independent
-// loads instead of a dependent load chain per Gaussian).  The warp then
-// visits the Gaussians in order, its lanes spread over each one's tiles.
-struct WarpGroup {
-  uint32_t id;      // this lane's Gaussian index (valid if lane < n)
-  int x0, y0, rw;   // its rectangle origin and width
-  int excl, incl;   // exclusive / inclusive prefix of rectangle areas
-  int total;        // instances of the whole group
-  uint32_t xy;      // x0 | y0 << 16
-  uint32_t wa;      // rw | area << 16 (area of one rectangle < 65536 tiles)
-};
-
-__device__ __forceinline__ WarpGroup load_group(const uint32_t *__restrict__ order,
-                                                const float4 *__restrict__ feat, uint32_t s0,
-                                                uint32_t s1, int lane) {
-  WarpGroup G;
-  const uint32_t s = s0 + lane;
-  int area = 0;
-  G.id = 0; G.x0 = 0; G.y0 = 0; G.rw = 1;
-  if (s < s1) {
-    G.id = order[s];
-    int x1, y1;
-    unpack_rect(feat[3 * G.id + 2], G.x0, G.y0, x1, y1);
-    G.rw = max(x1 - G.x0, 1);
-    area = (x1 - G.x0) * (y1 - G.y0);
-  }
-  int inc = area;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int u = __shfl_up_sync(FULL, inc, o);
-    if (lane >= o) inc += u;
-  }
-  G.incl = inc;
-  G.excl = inc - area;
-  G.total = __shfl_sync(FULL, inc, 31);
-  G.xy = (uint32_t)G.x0 | ((uint32_t)G.y0 << 16);
-  G.wa = (uint32_t)G.rw | ((uint32_t)area << 16);
-  return G;
-}
-
 // Lane `lane` visits tiles lane, lane+32, ... of a rw-wide rectangle in
 // row-major order; row/column advance incrementally.  The two divisions by
 // rw use a float reciprocal: for numerators below 33 and rw >= 1 the
@@ -328,32 +293,131 @@ struct RectWalk {
   }
 };
 
+// ---- equal-work chunks of the depth-sorted list ---------------------------
+
+// Weight of sorted position s: the warp iterations its Gaussian costs the
+// count and emit kernels (a fixed part plus one per 32 covered tiles).
 __global__ void __launch_bounds__(256)
-tile_count_kernel(int gx, int T, const float4 *__restrict__ feat,
-                  const uint32_t *__restrict__ order, const uint32_t *__restrict__ counters,
-                  uint32_t *__restrict__ cmat) {
-  extern __shared__ uint32_t cnt[];
-  const uint32_t V = counters[CI_V], S = counters[CI_S], C = counters[CI_C];
-  const uint32_t c = blockIdx.x;
+chunk_weight_kernel(const float4 *__restrict__ feat, const uint32_t *__restrict__ order,
+                    const uint32_t *__restrict__ counters, uint32_t *__restrict__ weight) {
+  const uint32_t V = counters[CI_V];
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V) return;
+  int x0, y0, x1, y1;
+  unpack_rect(feat[3 * order[s] + 2], x0, y0, x1, y1);
+  const uint32_t area = (uint32_t)((x1 - x0) * (y1 - y0));
+  weight[s] = CHUNK_W_GAUSS + (area + 31u) / 32u;
+}
+
+// From the exclusive prefix of the weights: chunk c = the positions whose
+// prefix lies in [c W / C, (c + 1) W / C).  Prefixes strictly increase (each
+// weight >= 1), so the chunk of a position never decreases; position s opens
+// the chunks between its predecessor's and its own.  cstart[C] = V.
+__global__ void __launch_bounds__(256)
+chunk_bounds_kernel(const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counters,
+                    uint32_t *__restrict__ cstart) {
+  const uint32_t V = counters[CI_V], C = counters[CI_C];
+  const unsigned long long W = counters[CI_W];
+  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= V || W == 0) return;
+  const uint32_t cs = (uint32_t)((unsigned long long)prefix[s] * C / W);
+  const uint32_t cp = s > 0 ? (uint32_t)((unsigned long long)prefix[s - 1] * C / W) : 0u;
+  for (uint32_t c = (s > 0 ? cp + 1 : 0u); c <= cs; ++c) cstart[c] = s;
+  if (s == V - 1)
+    for (uint32_t c = cs + 1; c <= C; ++c) cstart[c] = V;
+}
+
+// ---- counting and emission: one warp per (chunk, band of tile rows) -------
+// A band is R consecutive rows of tiles; its running slots live in shared
+// memory (R * gx words).  The warp walks its chunk's Gaussians in depth order,
+// 32 at a time (lane i holds Gaussian g0 + i), selects by ballot the ones
+// whose rectangle meets the band and visits each one's tiles within the band,
+// its lanes spread over them.  One Gaussian covers each tile once, so within
+// a Gaussian the lanes touch distinct slots and a plain read/modify/write
+// suffices; __syncwarp orders consecutive Gaussians.  COUNT: slots start at
+// 0 and end as this chunk's per-tile counts (written to the count matrix).
+// EMIT: slots start at the scanned counts (first list position of each
+// (tile, chunk)) and each visit appends the Gaussian index.  Indices and
+// rectangles are loaded two and one groups ahead.
+struct Bands {
+  int gx, gy, R, nb;  // grid, rows per band, bands
+};
+
+template <bool EMIT>
+__global__ void __launch_bounds__(32)
+band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restrict__ order,
+            uint32_t *__restrict__ counters, const uint32_t *__restrict__ cstart,
+            uint32_t *__restrict__ cmat, uint32_t *__restrict__ point_list, uint32_t K_alloc) {
+  extern __shared__ uint32_t slot[];
+  const uint32_t C = counters[CI_C];
+  const uint32_t c = blockIdx.x / (uint32_t)bd.nb;
+  const int b = (int)(blockIdx.x - c * (uint32_t)bd.nb);
   if (c >= C) return;
-  for (int t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = 0u;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const uint32_t s0 = c * S, s1 = min(V, s0 + S);
-  for (uint32_t g0 = s0 + 32 * w; g0 < s1; g0 += 32 * nw) {
-    const WarpGroup G = load_group(order, feat, g0, s1, lane);
-    const int n = (int)min(32u, s1 - g0);
-    for (int i = 0; i < n; ++i) {
-      const uint32_t xy = __shfl_sync(FULL, G.xy, i), wa = __shfl_sync(FULL, G.wa, i);
-      const int x0 = (int)(xy & 0xffffu), y0 = (int)(xy >> 16);
-      const int rw = (int)(wa & 0xffffu), area = (int)(wa >> 16);
+  const int lane = threadIdx.x;
+  const int ys = b * bd.R, ye = min(bd.gy, ys + bd.R);
+  const int t0 = ys * bd.gx, nt = (ye - ys) * bd.gx;
+  const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
+  if (EMIT) {
+    if (s0 >= s1) return;
+    int i = lane;
+    for (; i + 96 < nt; i += 128) {
+      const uint32_t a = cmat[(size_t)(t0 + i) * C + c];
+      const uint32_t e = cmat[(size_t)(t0 + i + 32) * C + c];
+      const uint32_t f = cmat[(size_t)(t0 + i + 64) * C + c];
+      const uint32_t g = cmat[(size_t)(t0 + i + 96) * C + c];
+      slot[i] = a; slot[i + 32] = e; slot[i + 64] = f; slot[i + 96] = g;
+    }
+    for (; i < nt; i += 32) slot[i] = cmat[(size_t)(t0 + i) * C + c];
+  } else {
+    for (int i = lane; i < nt; i += 32) slot[i] = 0u;
+  }
+  __syncwarp();
+  bool bad = false;
+  const float4 none = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool vA = s0 + lane < s1, vB = s0 + 32 + lane < s1;
+  uint32_t idA = vA ? order[s0 + lane] : 0u;
+  uint32_t idB = vB ? order[s0 + 32 + lane] : 0u;
+  float4 rA = vA ? feat[3 * idA + 2] : none;
+  for (uint32_t g0 = s0; g0 < s1; g0 += 32) {
+    const uint32_t id = idA;
+    const float4 r = rA;
+    const bool v = vA;
+    idA = idB; vA = vB;
+    rA = vA ? feat[3 * idA + 2] : none;
+    vB = g0 + 64 + lane < s1;
+    idB = vB ? order[g0 + 64 + lane] : 0u;
+    int x0, y0, x1, y1;
+    unpack_rect(r, x0, y0, x1, y1);
+    const int cy0 = max(y0, ys), cy1 = min(y1, ye);
+    const bool hit = v && cy0 < cy1 && x0 < x1;
+    unsigned m = __ballot_sync(FULL, hit);
+    const uint32_t xy = hit ? ((uint32_t)x0 | ((uint32_t)(cy0 - ys) << 16)) : 0u;
+    const uint32_t wa = hit ? ((uint32_t)(x1 - x0) | ((uint32_t)((x1 - x0) * (cy1 - cy0)) << 16)) : 1u;
+    while (m) {
+      const int i = __ffs(m) - 1;
+      m &= m - 1;
+      const uint32_t xyi = __shfl_sync(FULL, xy, i), wai = __shfl_sync(FULL, wa, i);
+      const uint32_t idi = EMIT ? __shfl_sync(FULL, id, i) : 0u;
+      const int bx = (int)(xyi & 0xffffu), by = (int)(xyi >> 16);
+      const int rw = (int)(wai & 0xffffu), area = (int)(wai >> 16);
       RectWalk it(lane, rw);
-      for (int j = lane; j < area; j += 32, it.next())
-        atomicAdd(&cnt[(y0 + it.row) * gx + x0 + it.col], 1u);
+      for (int j = lane; j < area; j += 32, it.next()) {
+        uint32_t *sl = &slot[(by + it.row) * bd.gx + bx + it.col];
+        const uint32_t p = *sl;
+        *sl = p + 1u;
+        if (EMIT) {
+          if (p < K_alloc) point_list[p] = idi;
+          else bad = true;
+        }
+      }
+      __syncwarp();
     }
   }
-  __syncthreads();
-  for (int t = threadIdx.x; t < T; t += blockDim.x) cmat[(size_t)t * C + c] = cnt[t];
+  if (EMIT) {
+    if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
+  } else {
+    for (int i = lane; i < nt; i += 32) cmat[(size_t)(t0 + i) * C + c] = slot[i];
+  }
 }
 
 // Tile ranges from the scanned count matrix.  When the instances exceed the
@@ -377,74 +441,6 @@ __global__ void ranges_kernel(int T, const uint32_t *__restrict__ cmat_scanned,
   ranges[t] = r;
 }
 
-// ---- emission -------------------------------------------------------------
-// Block = chunk; warp w owns a contiguous sub-range of the chunk (depth
-// order).  Shared memory: off[nw][T] (per-warp running slots) + base[T].
-__global__ void __launch_bounds__(256)
-emit_kernel(int gx, int T, const float4 *__restrict__ feat, const uint32_t *__restrict__ order,
-            uint32_t *__restrict__ counters, const uint32_t *__restrict__ cmat_scanned,
-            uint32_t *__restrict__ point_list, uint32_t K_alloc) {
-  extern __shared__ uint32_t sm[];
-  const uint32_t V = counters[CI_V], S = counters[CI_S], C = counters[CI_C];
-  const uint32_t c = blockIdx.x;
-  if (c >= C) return;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  uint32_t *off = sm;
-  uint32_t *base = sm + (size_t)nw * T;
-  for (int i = threadIdx.x; i < nw * T; i += blockDim.x) off[i] = 0u;
-  for (int t = threadIdx.x; t < T; t += blockDim.x) base[t] = cmat_scanned[(size_t)t * C + c];
-  __syncthreads();
-  const uint32_t s0 = c * S, s1 = min(V, s0 + S);
-  const uint32_t sub = (s1 - s0 + nw - 1) / nw;
-  const uint32_t a = min(s1, s0 + w * sub), bnd = min(s1, a + sub);
-  uint32_t *my = off + (size_t)w * T;
-  // one Gaussian covers each tile once: within a Gaussian the lanes touch
-  // distinct counters of this warp's row, so plain read/modify/write suffices
-  for (uint32_t g0 = a; g0 < bnd; g0 += 32) {
-    const WarpGroup G = load_group(order, feat, g0, bnd, lane);
-    const int n = (int)min(32u, bnd - g0);
-    for (int i = 0; i < n; ++i) {
-      const uint32_t xy = __shfl_sync(FULL, G.xy, i), wa = __shfl_sync(FULL, G.wa, i);
-      const int x0 = (int)(xy & 0xffffu), y0 = (int)(xy >> 16);
-      const int rw = (int)(wa & 0xffffu), area = (int)(wa >> 16);
-      RectWalk it(lane, rw);
-      for (int j = lane; j < area; j += 32, it.next()) ++my[(y0 + it.row) * gx + x0 + it.col];
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < T; t += blockDim.x) {
-    uint32_t run = base[t];
-    for (int w2 = 0; w2 < nw; ++w2) {
-      const uint32_t n = off[(size_t)w2 * T + t];
-      off[(size_t)w2 * T + t] = run;
-      run += n;
-    }
-  }
-  __syncthreads();
-  bool bad = false;
-  for (uint32_t g0 = a; g0 < bnd; g0 += 32) {
-    const WarpGroup G = load_group(order, feat, g0, bnd, lane);
-    const int n = (int)min(32u, bnd - g0);
-    for (int i = 0; i < n; ++i) {
-      const uint32_t xy = __shfl_sync(FULL, G.xy, i), wa = __shfl_sync(FULL, G.wa, i);
-      const int x0 = (int)(xy & 0xffffu), y0 = (int)(xy >> 16);
-      const int rw = (int)(wa & 0xffffu), area = (int)(wa >> 16);
-      const uint32_t id = __shfl_sync(FULL, G.id, i);
-      RectWalk it(lane, rw);
-      for (int j = lane; j < area; j += 32, it.next()) {
-        uint32_t *slot = &my[(y0 + it.row) * gx + x0 + it.col];
-        const uint32_t p = *slot;
-        *slot = p + 1u;
-        if (p < K_alloc) point_list[p] = id;
-        else bad = true;
-      }
-      __syncwarp();
-    }
-  }
-  if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
-}
-
 // Debug view: sorted keys in the reference's form (tile << 32 | depth_bits).
 __global__ void debug_keys_kernel(int T, const uint2 *__restrict__ ranges,
                                   const uint32_t *__restrict__ point_list,
@@ -459,12 +455,54 @@ __global__ void debug_keys_kernel(int T, const uint2 *__restrict__ ranges,
   }
 }
 
-size_t emit_smem(int nw, int T) { return ((size_t)nw + 1) * T * 4; }
 
-int emit_warps(int T) {
-  for (int nw = 8; nw >= 1; --nw)
-    if (emit_smem(nw, T) <= 220 * 1024) return nw;
-  return 0;
+}  // namespace
+
+namespace {
+
+constexpr int BAND_TILES = 1024;  // target slots per band (4 KB of shared memory)
+
+// Bands of tile rows and the chunk count for a gx x gy grid: enough
+// (chunk, band) warps to fill the GPU in one wave, each band's slots small
+// enough for many resident warps per SM.
+struct BandPlan {
+  Bands bd;
+  uint32_t cmax;
+  size_t smem;
+};
+
+int band_plan(int gx, int gy, BandPlan &pl) {
+  pl.bd.gx = gx;
+  pl.bd.gy = gy;
+  pl.bd.R = std::max(1, std::min(gy, BAND_TILES / std::max(gx, 1)));
+  pl.bd.nb = (gy + pl.bd.R - 1) / pl.bd.R;
+  pl.smem = (size_t)pl.bd.R * gx * 4;
+  if (pl.smem > 220 * 1024) {
+    dmgs_host::set_error("image too large: a row of %d tiles exceeds the binning kernels' shared memory", gx);
+    return DMGS_ERR_ARG;
+  }
+  int dev = 0;
+  DMGS_CUDA(cudaGetDevice(&dev));
+  thread_local int cached_dev = -1;
+  thread_local size_t cached_smem = 0;
+  thread_local int cached_resident = 0;
+  if (dev != cached_dev || pl.smem != cached_smem) {
+    if (pl.smem > 48 * 1024) {
+      DMGS_CUDA(cudaFuncSetAttribute(band_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pl.smem));
+      DMGS_CUDA(cudaFuncSetAttribute(band_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pl.smem));
+    }
+    int sms = 0, a = 0, b = 0;
+    DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, band_kernel<false>, 32, pl.smem));
+    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, band_kernel<true>, 32, pl.smem));
+    cached_dev = dev;
+    cached_smem = pl.smem;
+    cached_resident = std::max(1, std::min(a, b)) * sms;
+  }
+  pl.cmax = (uint32_t)std::max(1, std::min(CHUNK_COUNT_MAX, cached_resident / pl.bd.nb));
+  return DMGS_OK;
 }
 
 }  // namespace
@@ -498,6 +536,8 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
   uint32_t *cmat = reinterpret_cast<uint32_t *>(geom + L.cmat);
   const float4 *feat = reinterpret_cast<const float4 *>(geom + L.feat);
   const int T = L.T();
+  BandPlan pl;
+  if (int r = band_plan(L.gx, L.gy, pl)) return r;
   if (L.P > 0) {
     DMGS_TIMED(K_BIN_COMPACT, s, {
       int r = launch_scan(blkcnt, nullptr, (uint32_t)L.nb_pre, part, counters + CI_V, counters, s);
@@ -506,7 +546,7 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
     });
     DMGS_LAUNCH_CHECK("compact_kernel");
   }
-  dmgs_host::note_launch(), params_kernel<<<1, 1, 0, s>>>(T, counters);
+  dmgs_host::note_launch(), params_kernel<<<1, 1, 0, s>>>(T, pl.cmax, counters);
   DMGS_LAUNCH_CHECK("params_kernel");
   if (L.P > 0) {
     DMGS_TIMED(K_BIN_SORT, s, {
@@ -525,19 +565,18 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
     });  // four passes: the sorted order ends in (k0, v0)
     DMGS_LAUNCH_CHECK("radix_sort");
   }
-  const size_t csm = (size_t)T * 4;
-  if (csm > 220 * 1024) {
-    dmgs_host::set_error("image too large: %d tiles exceed the binning kernels' shared memory", T);
-    return DMGS_ERR_ARG;
-  }
   if (L.P > 0) {
-    if (csm > 48 * 1024)
-      DMGS_CUDA(cudaFuncSetAttribute(tile_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)csm));
-    DMGS_TIMED(K_BIN_COUNT, s,
-               dmgs_host::note_launch(), tile_count_kernel<<<CHUNK_COUNT_MAX, 256, csm, s>>>(L.gx, T, feat, v0, counters,
-                                                                   cmat));
-    DMGS_LAUNCH_CHECK("tile_count_kernel");
+    uint32_t *cstart = reinterpret_cast<uint32_t *>(geom + L.cstart);
+    DMGS_TIMED(K_BIN_COUNT, s, {
+      // the sorted keys end in k0, so k1 is free for the chunk weights
+      dmgs_host::note_launch(), chunk_weight_kernel<<<L.nb_pre, 256, 0, s>>>(feat, v0, counters, k1);
+      int r = launch_scan(k1, counters + CI_V, (uint32_t)L.P, part, counters + CI_W, counters, s);
+      if (r != DMGS_OK) return r;
+      dmgs_host::note_launch(), chunk_bounds_kernel<<<L.nb_pre, 256, 0, s>>>(k1, counters, cstart);
+      dmgs_host::note_launch(), band_kernel<false><<<pl.cmax * pl.bd.nb, 32, pl.smem, s>>>(
+          pl.bd, feat, v0, counters, cstart, cmat, nullptr, 0u);
+    });
+    DMGS_LAUNCH_CHECK("tile_count");
   }
   DMGS_TIMED(K_BIN_SCAN, s, {
     if (L.P > 0) {
@@ -554,23 +593,16 @@ int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cud
 
 int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, int64_t K,
                 cudaStream_t s) {
-  const int T = L.T();
   if (L.P <= 0 || K <= 0) return DMGS_OK;
-  const int nw = emit_warps(T);
-  if (nw < 1) {
-    dmgs_host::set_error("image too large: %d tiles exceed the emission kernel's shared memory", T);
-    return DMGS_ERR_ARG;
-  }
-  const size_t smem = emit_smem(nw, T);
-  if (smem > 48 * 1024)
-    DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
+  BandPlan pl;
+  if (int r = band_plan(L.gx, L.gy, pl)) return r;
   DMGS_TIMED(K_BIN_EMIT, s,
-             dmgs_host::note_launch(), emit_kernel<<<CHUNK_COUNT_MAX, nw * 32, smem, s>>>(
-                 L.gx, T, reinterpret_cast<const float4 *>(geom + L.feat),
+             dmgs_host::note_launch(), band_kernel<true><<<pl.cmax * pl.bd.nb, 32, pl.smem, s>>>(
+                 pl.bd, reinterpret_cast<const float4 *>(geom + L.feat),
                  reinterpret_cast<const uint32_t *>(geom + L.dval0),
                  reinterpret_cast<uint32_t *>(geom + L.counters),
-                 reinterpret_cast<const uint32_t *>(geom + L.cmat),
+                 reinterpret_cast<const uint32_t *>(geom + L.cstart),
+                 reinterpret_cast<uint32_t *>(geom + L.cmat),
                  reinterpret_cast<uint32_t *>(bin + B.point_list), (uint32_t)K));
   DMGS_LAUNCH_CHECK("emit_kernel");
   return DMGS_OK;

@@ -60,8 +60,9 @@ constexpr int PRE_BLOCK = 256;           // preprocess / compaction block
 constexpr int RADIX_BLOCK = 256;         // radix sort block (8 warps)
 constexpr int RADIX_ITEMS = 8;           // keys per thread
 constexpr int RADIX_TILE = RADIX_BLOCK * RADIX_ITEMS;  // 2048 keys per block
-constexpr int CHUNK_MIN = 256;           // Gaussians per binning chunk (minimum)
-constexpr int CHUNK_COUNT_MAX = 1024;    // binning chunks per view (maximum)
+constexpr int CHUNK_MIN_GAUSS = 64;     // visible Gaussians per binning chunk (mean, minimum)
+constexpr int CHUNK_COUNT_MAX = 2048;    // binning chunks per view (maximum)
+constexpr int CHUNK_W_GAUSS = 2;         // chunk weight of a Gaussian: this + ceil(tiles / 32)
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096 elements per block
@@ -73,14 +74,14 @@ constexpr int CI_MAXLIST = 3;  // longest tile list
 constexpr int CI_V = 4;        // visible Gaussians
 constexpr int CI_NBR = 5;      // radix blocks in use = ceil(V / RADIX_TILE)
 constexpr int CI_NRH = 6;      // radix histogram entries = 256 * NBR
-constexpr int CI_S = 7;        // Gaussians per chunk
+constexpr int CI_W = 7;        // total chunk weight of the visible Gaussians
 constexpr int CI_C = 8;        // chunks
 constexpr int CI_NCM = 9;      // count-matrix entries = T * C
 constexpr int CI_WORDS = 16;
 
 struct GeomLayout {
-  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, scanpart, ranges,
-      counters, total;
+  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, cstart, scanpart,
+      ranges, counters, total;
   int P, gx, gy;
   int nb_pre, nb_radix;
   size_t n_rhist_max, n_cmat_max, n_part_max;
@@ -99,6 +100,7 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.n_cmat_max = T * CHUNK_COUNT_MAX;
   size_t nmax = L.n_cmat_max > L.n_rhist_max ? L.n_cmat_max : L.n_rhist_max;
   if ((size_t)L.nb_pre > nmax) nmax = L.nb_pre;
+  if ((size_t)P > nmax) nmax = P;
   L.n_part_max = (nmax + SCAN_TILE - 1) / SCAN_TILE + 1;
   size_t o = 0;
   L.feat = o;      o = align_up(o + (size_t)P * 48, 256);
@@ -110,6 +112,7 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.dval1 = o;     o = align_up(o + (size_t)P * 4, 256);
   L.rhist = o;     o = align_up(o + L.n_rhist_max * 4 + 4, 256);
   L.cmat = o;      o = align_up(o + L.n_cmat_max * 4, 256);
+  L.cstart = o;    o = align_up(o + (CHUNK_COUNT_MAX + 1) * 4, 256);
   L.scanpart = o;  o = align_up(o + L.n_part_max * 4, 256);
   L.ranges = o;    o = align_up(o + T * 8, 256);
   L.counters = o;  o = align_up(o + CI_WORDS * 4, 256);
