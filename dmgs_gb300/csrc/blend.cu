@@ -84,6 +84,31 @@ __device__ __forceinline__ uint32_t footprint(float a, float b, float c, float o
   return span_mask(cy, ey) | (span_mask(cx, ex) << 16);
 }
 
+// Row mask refined per row: for pixel row r (dy = cy - r fixed) the exponent
+// A dx^2 + B dx dy + C dy^2 (A < 0) is largest at dx = -B dy / (2A), clamped
+// to the tile's columns (dx in [cx - 15, cx], widened by 0.01); the row is kept
+// when that maximum reaches thr less a margin of 0.01 + 1e-5 x the sum of the
+// terms' magnitudes (far above the rounding of either evaluation).  Rows the
+// bounding-box mask keeps but no pixel of which reaches alpha 1/255 — the
+// ellipse passing the tile's corner — are dropped, so warps skip them.
+__device__ __forceinline__ uint32_t exact_rows(uint32_t m, float A, float B, float C, float thr,
+                                               float cx, float cy) {
+  if (!(A < 0.f) || (m & 0xffffu) == 0u) return m;
+  const float k = -B / (2.f * A);
+  const float lo = cx - 15.01f, hi = cx + 0.01f;
+  uint32_t rows = 0u;
+#pragma unroll
+  for (int r = 0; r < 16; ++r) {
+    const float dy = cy - (float)r;
+    const float dxs = fminf(fmaxf(k * dy, lo), hi);
+    const float t1 = A * dxs * dxs, t2 = B * dxs * dy, t3 = C * dy * dy;
+    const float e = t1 + t2 + t3;
+    const float mag = fabsf(t1) + fabsf(t2) + fabsf(t3);
+    if (e >= thr - (0.01f + 1e-5f * mag)) rows |= 1u << r;
+  }
+  return (m & 0xffff0000u) | (m & rows);
+}
+
 // (ox, oy): pixel origin of the tile being blended.
 __device__ __forceinline__ Staged stage(const float4 f0, const float4 f1, const float4 f2,
                                         float ox, float oy) {
@@ -92,7 +117,8 @@ __device__ __forceinline__ Staged stage(const float4 f0, const float4 f1, const 
   const float B = __fmul_rn(-LOG2E, f0.w);
   const float C = __fmul_rn(-0.5f * LOG2E, f1.x);
   const float thr = -LOG2_255 - __log2f(f1.y);
-  const uint32_t m = footprint(f0.z, f0.w, f1.x, f1.y, f0.x - ox, f0.y - oy);
+  const float cx = f0.x - ox, cy = f0.y - oy;
+  const uint32_t m = exact_rows(footprint(f0.z, f0.w, f1.x, f1.y, cx, cy), A, B, C, thr, cx, cy);
   S.s0 = make_float4(f0.x, f0.y, A, B);
   S.s1 = make_float4(C, f1.y, thr, f1.z);
   S.s2 = make_float4(f1.w, f2.x, __uint_as_float(m), 0.f);
@@ -106,15 +132,6 @@ __device__ __forceinline__ float exponent2(float A, float B, float C, float dx, 
   const float q = __fmul_rn(B, dx);
   return __fmaf_rn(__fmaf_rn(C, dy, q), dy, ax2);
 }
-
-// Returns alpha (>= 1/255) or 0 when the pair is skipped; G = e^power.
-__device__ __forceinline__ float pair_alpha(float e2, float o, float thr, float &G) {
-  if (e2 > 0.f || e2 < thr) return 0.f;
-  G = ex2_approx(e2);
-  const float alpha = fminf(ALPHA_MAX, __fmul_rn(o, G));
-  return alpha < ALPHA_MIN ? 0.f : alpha;
-}
-
 
 // Work item -> (view, tile).
 __device__ __forceinline__ int find_view(const BlendBatch &bb, int item) {
@@ -221,32 +238,43 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
         }
       }
       const int cnt = min(BATCH, n - base);
-      for (int j = 0; j < cnt && !all_done(); ++j) {
+      bool warp_done = __all_sync(FULL, all_done());
+      for (int j = 0; j < cnt && !warp_done; ++j) {
         const float4 s2 = S2[buf][j];
         const uint32_t m = __float_as_uint(s2.z);
         if (!(m & lay.warp_rows)) continue;  // warp-uniform: footprint misses the warp's rows
-        if (!(m & lay.colbit)) continue;
         const float4 s0 = S0[buf][j];
         const float4 s1 = S1[buf][j];
         const float dx = __fsub_rn(s0.x, pxf);
+        const bool col_ok = (m & lay.colbit) != 0u;
+        // pass 1: exponent and range test of every pixel (no branches)
+        float e2[PPT];
+        bool ok[PPT];
+        bool any = false;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
-          if (done[k] || !(m & (1u << lay.row(k)))) continue;
-          float G;
-          const float e2 = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, pyf[k]));
-          const float alpha = pair_alpha(e2, s1.y, s1.z, G);
-          if (alpha > 0.f) {
-            const float test_T = T[k] * (1.f - alpha);
-            if (test_T < T_EPS) {
-              done[k] = true;
-            } else {
-              const float w = alpha * T[k];
-              cr[k] = fmaf(s1.w, w, cr[k]); cg[k] = fmaf(s2.x, w, cg[k]); cb[k] = fmaf(s2.y, w, cb[k]);
-              T[k] = test_T;
-              last[k] = base + j + 1;
-            }
-          }
+          e2[k] = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, pyf[k]));
+          ok[k] = col_ok && !done[k] && ((m >> lay.row(k)) & 1u) && !(e2[k] > 0.f) &&
+                  !(e2[k] < s1.z);
+          any |= ok[k];
         }
+        if (!__any_sync(FULL, any)) continue;  // warp-uniform
+        // pass 2: alpha, stop test and accumulation, predicated
+        const uint32_t pos = (uint32_t)(base + j + 1);
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          const float alpha = fminf(ALPHA_MAX, __fmul_rn(s1.y, ex2_approx(e2[k])));
+          const bool take = ok[k] && !(alpha < ALPHA_MIN);
+          const float test_T = T[k] * (1.f - alpha);
+          const bool stop = take && test_T < T_EPS;
+          const bool blend = take && !stop;
+          const float w = blend ? alpha * T[k] : 0.f;
+          cr[k] = fmaf(s1.w, w, cr[k]); cg[k] = fmaf(s2.x, w, cg[k]); cb[k] = fmaf(s2.y, w, cb[k]);
+          T[k] = blend ? test_T : T[k];
+          last[k] = blend ? pos : last[k];
+          done[k] = done[k] || stop;
+        }
+        warp_done = __all_sync(FULL, all_done());
       }
       buf ^= 1;
     }
@@ -308,40 +336,45 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, bool inside, int pix,
   ps.last_alpha = ps.last_r = ps.last_g = ps.last_b = 0.f;
 }
 
-// One (pixel, Gaussian) term of the adjoint, accumulated into e[0..8];
-// returns whether the pair contributed.
-__device__ __forceinline__ bool adjoint_pair(PixelState &ps, const float4 &s0, const float4 &s1,
-                                             const float4 &s2, const float4 &s3, float dx,
-                                             float dy, float *e) {
-  float G;
-  const float e2 = exponent2(s0.z, s0.w, s1.x, dx, dy);
-  const float alpha = pair_alpha(e2, s1.y, s1.z, G);
-  if (alpha == 0.f) return false;
+// One (pixel, Gaussian) term of the adjoint, accumulated into e[0..8] when
+// `take` (the pair was blended in the forward); otherwise the state and e[]
+// are left as they are.  Evaluated without branches: the state updates are
+// selects and the gradient terms are scaled by a factor selected to 0, so a
+// warp whose lanes differ in `take` runs one straight-line path.
+__device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float alpha, float G,
+                                             const float4 &s1, const float4 &s2, const float4 &s3,
+                                             float dx, float dy, float *e) {
   const float inv = __frcp_rn(1.f - alpha);
-  ps.T = ps.T * inv;
-  const float w = alpha * ps.T;
-  ps.acc_r = ps.last_alpha * ps.last_r + (1.f - ps.last_alpha) * ps.acc_r;
-  ps.acc_g = ps.last_alpha * ps.last_g + (1.f - ps.last_alpha) * ps.acc_g;
-  ps.acc_b = ps.last_alpha * ps.last_b + (1.f - ps.last_alpha) * ps.acc_b;
+  const float Tn = ps.T * inv;
+  const float w = alpha * Tn;
+  const float la = ps.last_alpha, nla = 1.f - ps.last_alpha;
+  const float acc_r = la * ps.last_r + nla * ps.acc_r;
+  const float acc_g = la * ps.last_g + nla * ps.acc_g;
+  const float acc_b = la * ps.last_b + nla * ps.acc_b;
   const float cr = s1.w, cg = s2.x, cb = s2.y;
-  ps.last_r = cr; ps.last_g = cg; ps.last_b = cb;
-  ps.last_alpha = alpha;
-  float dL_dalpha =
-      ((cr - ps.acc_r) * ps.g0 + (cg - ps.acc_g) * ps.g1 + (cb - ps.acc_b) * ps.g2) * ps.T;
+  float dL_dalpha = ((cr - acc_r) * ps.g0 + (cg - acc_g) * ps.g1 + (cb - acc_b) * ps.g2) * Tn;
   dL_dalpha -= ps.T_final * inv * ps.bg_dot;
-  const float Gd = G * dL_dalpha;  // dL/dopacity term
-  const float u = s1.y * Gd;       // dL/dpower = o G dL/dalpha
+  const float Gd = take ? G * dL_dalpha : 0.f;  // dL/dopacity term
+  const float wt = take ? w : 0.f;
+  const float u = s1.y * Gd;                    // dL/dpower = o G dL/dalpha
   const float ux = u * dx, uy = u * dy;
-  e[0] += ux * s2.z + uy * s2.w;   // dL/dndc_x
-  e[1] += uy * s3.x + ux * s3.y;   // dL/dndc_y
-  e[2] += ux * dx;                 // x -1/2 -> dL/dconic_a
-  e[3] += ux * dy;                 // x -1   -> dL/dconic_b
-  e[4] += uy * dy;                 // x -1/2 -> dL/dconic_c
-  e[5] += Gd;                      // dL/dopacity
-  e[6] += w * ps.g0;               // dL/drgb
-  e[7] += w * ps.g1;
-  e[8] += w * ps.g2;
-  return true;
+  e[0] += ux * s2.z + uy * s2.w;  // dL/dndc_x
+  e[1] += uy * s3.x + ux * s3.y;  // dL/dndc_y
+  e[2] += ux * dx;                // x -1/2 -> dL/dconic_a
+  e[3] += ux * dy;                // x -1   -> dL/dconic_b
+  e[4] += uy * dy;                // x -1/2 -> dL/dconic_c
+  e[5] += Gd;                     // dL/dopacity
+  e[6] += wt * ps.g0;             // dL/drgb
+  e[7] += wt * ps.g1;
+  e[8] += wt * ps.g2;
+  ps.T = take ? Tn : ps.T;
+  ps.acc_r = take ? acc_r : ps.acc_r;
+  ps.acc_g = take ? acc_g : ps.acc_g;
+  ps.acc_b = take ? acc_b : ps.acc_b;
+  ps.last_r = take ? cr : ps.last_r;
+  ps.last_g = take ? cg : ps.last_g;
+  ps.last_b = take ? cb : ps.last_b;
+  ps.last_alpha = take ? alpha : ps.last_alpha;
 }
 
 // Transposed reduce-scatter of 16 slots over the warp: afterwards the lane
@@ -435,16 +468,30 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
         const uint32_t m = __float_as_uint(s3.w);
         if (!(m & lay.warp_rows)) continue;  // warp-uniform
         const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j];
+        const float dx = __fsub_rn(s0.x, pxf);
+        const bool col_ok = (m & lay.colbit) != 0u;
+        float e2[PPT];
+        bool ok[PPT];
+        bool cand = false;
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          e2[k] = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, pyf[k]));
+          ok[k] = col_ok && ((m >> lay.row(k)) & 1u) && li < (int)ps[k].last_contrib &&
+                  !(e2[k] > 0.f) && !(e2[k] < s1.z);
+          cand |= ok[k];
+        }
+        if (!__any_sync(FULL, cand)) continue;  // warp-uniform
         float e[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) e[i] = 0.f;
-        const float dx = __fsub_rn(s0.x, pxf);
         bool any = false;
-        if (m & lay.colbit) {
 #pragma unroll
-          for (int k = 0; k < PPT; ++k)
-            if ((m & (1u << lay.row(k))) && li < (int)ps[k].last_contrib)
-              any |= adjoint_pair(ps[k], s0, s1, s2, s3, dx, __fsub_rn(s0.y, pyf[k]), e);
+        for (int k = 0; k < PPT; ++k) {
+          const float G = ex2_approx(e2[k]);
+          const float alpha = fminf(ALPHA_MAX, __fmul_rn(s1.y, G));
+          const bool take = ok[k] && !(alpha < ALPHA_MIN);
+          adjoint_pair(ps[k], take, alpha, G, s1, s2, s3, dx, __fsub_rn(s0.y, pyf[k]), e);
+          any |= take;
         }
         if (__ballot_sync(FULL, any)) {
           const float sum = warp_reduce_scatter16(e, lane);
