@@ -324,7 +324,7 @@ def main():
                  "launches_per_view": (lib.dmgs_kernel_launches() - n0) / (args.steps + args.warmup)}
 
     # ---------------- batched form: 16 views per step, CUDA graph ----------------
-    br = BatchedRasterizer(settings, g)
+    br = BatchedRasterizer(settings, g, means2D_grads=False, densify_stats=True)
     for d, s in zip(br.dL_dout, dimgs):
         d.copy_(s)
     tune = None
@@ -359,7 +359,7 @@ def main():
         msets = [settings_of(v) for v in mviews]
         mdouts = [torch.randn(3, s.image_height, s.image_width, device=dev, generator=gen) for s in msets]
         ms_mplain = None if args.no_plain else timed(lambda i: plain_step(i, msets, mdouts), nv, 2, dev)
-        bm = BatchedRasterizer(msets, g)
+        bm = BatchedRasterizer(msets, g, means2D_grads=False, densify_stats=True)
         for d, s in zip(bm.dL_dout, mdouts):
             d.copy_(s)
         mtune = None
@@ -448,6 +448,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "P": P, "width": args.width, "height": args.height,
                        "views_per_step": nv, "parallelism": "replicas" if world > 1 else "1 gpu",
+                       "outputs": "images, parameter gradients summed over views, densification "
+                                  "statistics (fused add_densification_stats)",
                        "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
                        "blend_config": {"pixels_per_thread": br.cfg[0], "gaussians_per_batch": br.cfg[1]},
                        "graph": not args.no_graph},

@@ -84,7 +84,7 @@ SIGNATURES = [
                                           C.c_size_t, vp]),
     ("dmgs_raster_bwd_batched", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians),
                                           C.POINTER(vp), vp, C.c_size_t, C.POINTER(DmgsGrads),
-                                          C.POINTER(vp), vp]),
+                                          C.POINTER(vp), vp, vp, vp]),
     ("dmgs_batch_status", C.c_int, [C.POINTER(DmgsBatch), C.c_int32, vp, C.c_size_t,
                                     C.POINTER(C.c_int64), vp]),
     ("dmgs_mark_visible", C.c_int, [C.c_int32, vp, vp, vp, vp, vp]),

@@ -49,9 +49,19 @@ class BatchedRasterizer:
     names (means3D, opacities, and shs or colors_precomp, and scales +
     rotations or cov3D_precomp).  Their storage is read at every call, so
     parameters updated in place are picked up (also by graph replays).
+
+    ``means2D_grads``: keep each view's screen-space (NDC) mean gradient in
+    ``self.means2D_grads[v]`` ([P, 3], the reference's
+    ``viewspace_point_tensor.grad``).  ``densify_stats``: accumulate the
+    reference's densification statistics (``add_densification_stats``,
+    scene/gaussian_model.py:405-407) over every view of every backward into
+    ``self.densify_accum`` / ``self.densify_count`` ([P] each; zeroed by
+    :meth:`reset_densify_stats`) — the same information as the per-view
+    gradients for training, without writing [P, 3] per view.
     """
 
-    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(4, 128)):
+    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(4, 128),
+                 means2D_grads=True, densify_stats=False):
         if not 1 <= len(settings) <= MAX_VIEWS:
             raise ValueError(f"a batch holds 1..{MAX_VIEWS} views")
         self.lib = _lib.load()
@@ -75,7 +85,10 @@ class BatchedRasterizer:
         self.radii = [torch.empty(self.P, dtype=torch.int32, device=d) for _ in self.settings]
         self.dL_dout = [torch.zeros(3, s.image_height, s.image_width, device=d) for s in self.settings]
         self.grads = self._grad_buffers()
-        self.means2D_grads = [torch.empty(self.P, 3, device=d) for _ in self.settings]
+        self.means2D_grads = ([torch.empty(self.P, 3, device=d) for _ in self.settings]
+                              if means2D_grads else None)
+        self.densify_accum = torch.zeros(self.P, device=d) if densify_stats else None
+        self.densify_count = torch.zeros(self.P, device=d) if densify_stats else None
         self.cfg = tuple(cfg)
         self.graph = None
         if capacity is None:
@@ -116,7 +129,8 @@ class BatchedRasterizer:
         self._out = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.images])
         self._rad = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.radii])
         self._dout = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.dL_dout])
-        self._m2 = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.means2D_grads])
+        self._m2 = ((C.c_void_p * self.n)(*[t.data_ptr() for t in self.means2D_grads])
+                    if self.means2D_grads is not None else None)
         self.batch = DmgsBatch(self.n, self.views, self._out, self._rad, self._cap, self.cfg[0],
                                self.cfg[1])
         nbytes = self.lib.dmgs_batch_state_bytes(C.byref(self.batch), self.P)
@@ -145,7 +159,15 @@ class BatchedRasterizer:
         check(self.lib.dmgs_raster_bwd_batched(C.byref(self.batch), C.byref(self.gauss), self._dout,
                                                self.state.data_ptr(), self.state.numel(),
                                                C.byref(self._grads), self._m2,
+                                               ptr(self.densify_accum), ptr(self.densify_count),
                                                _lib.stream_of(self.device)), "bwd_batched")
+
+    def reset_densify_stats(self):
+        """Zero the densification accumulators (the reference re-creates
+        them after each densification step)."""
+        if self.densify_accum is not None:
+            self.densify_accum.zero_()
+            self.densify_count.zero_()
 
     def forward(self):
         """Render every view into ``self.images`` (asynchronous)."""

@@ -230,10 +230,15 @@ extern "C" int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *
 extern "C" int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
                                        const float *const *dL_dout_color, void *state,
                                        size_t state_bytes, const DmgsGrads *grads,
-                                       float *const *dL_dmeans2D, dmgs_stream_t stream) {
+                                       float *const *dL_dmeans2D, float *densify_accum,
+                                       float *densify_count, dmgs_stream_t stream) {
   BatchLayout L;
   RET_IF(check_common(b, g, state, state_bytes, L));
   if (!dL_dout_color || !grads) { set_error("batch: dL_dout_color / grads is NULL"); return DMGS_ERR_ARG; }
+  if ((densify_accum == nullptr) != (densify_count == nullptr)) {
+    set_error("batch: densify_accum and densify_count must both be given or both be NULL");
+    return DMGS_ERR_ARG;
+  }
   for (int v = 0; v < b->nviews; ++v)
     if (!dL_dout_color[v]) { set_error("batch: dL_dout_color[%d] is NULL", v); return DMGS_ERR_ARG; }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -250,7 +255,7 @@ extern "C" int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *
   BatchViews bv;
   fill_views(b, L, st, bv);
   for (int v = 0; v < b->nviews; ++v) bv.v[v].dL_dmeans2D = dL_dmeans2D ? dL_dmeans2D[v] : nullptr;
-  RET_IF(launch_preprocess_bwd_batched(bv, gptrs_of(g), *grads, s));
+  RET_IF(launch_preprocess_bwd_batched(bv, gptrs_of(g), *grads, densify_accum, densify_count, s));
   return DMGS_OK;
 }
 

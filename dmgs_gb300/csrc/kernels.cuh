@@ -95,7 +95,7 @@ int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom
 
 // preprocess_bwd.cu
 int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, const DmgsGrads &out,
-                                  cudaStream_t s);
+                                  float *densify_accum, float *densify_count, cudaStream_t s);
 int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float *projm,
                           const float *campos, const GaussianPtrs &g, const GeomLayout &L,
                           const char *geom, const float *gacc, const DmgsGrads &out,

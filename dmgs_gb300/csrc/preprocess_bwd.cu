@@ -25,17 +25,36 @@ namespace dmgs {
 namespace {
 
 constexpr int BWD_BLOCK = 128;
+constexpr int SP = BWD_BLOCK + 1;  // shared-memory row pitch of the output slots
 
-// Shared-memory output slots of one block (struct of arrays; thread t owns
-// element t of each).
+// Shared-memory output slots of one block: element k of Gaussian g of a
+// field lives at field[k * SP + g].  Lanes writing element k of different
+// Gaussians hit consecutive banks, and the pitch of BWD_BLOCK + 1 keeps the
+// Gaussian-major reads of the stores (consecutive k of one g) conflict-free.
 struct Slots {
   float *m2, *col, *op, *m3, *cov, *sc, *rot, *sh;
 };
 
-// ACC: add into the slots (several views of one Gaussian); else assign.
+__host__ __device__ constexpr size_t slot_floats(int M) { return (size_t)(23 + 3 * M) * SP; }
+
+__device__ __forceinline__ Slots make_slots(float *sm) {
+  Slots S;
+  S.m2 = sm;
+  S.col = S.m2 + 3 * SP;
+  S.op = S.col + 3 * SP;
+  S.m3 = S.op + SP;
+  S.cov = S.m3 + 3 * SP;
+  S.sc = S.cov + 6 * SP;
+  S.rot = S.sc + 3 * SP;
+  S.sh = S.rot + 4 * SP;
+  return S;
+}
+
+// ACC: add into the slots (several views of one Gaussian, possibly from
+// several threads at once: a shared-memory atomic add); else assign.
 template <bool ACC>
 __device__ __forceinline__ void put(float &slot, float v) {
-  if (ACC) slot += v;
+  if (ACC) atomicAdd(&slot, v);
   else slot = v;
 }
 
@@ -56,9 +75,9 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
   const float dop = gb.y;
   float drgb[3] = {gb.z, gb.w, gblue};
 
-  if (out.dL_dmeans2D && !ACC) { S_.m2[3 * t] = dndc_x; S_.m2[3 * t + 1] = dndc_y; S_.m2[3 * t + 2] = 0.f; }
+  if (out.dL_dmeans2D && !ACC) { S_.m2[t] = dndc_x; S_.m2[SP + t] = dndc_y; S_.m2[2 * SP + t] = 0.f; }
   if (out.dL_dopacity) put<ACC>(S_.op[t], dop);
-  if (out.dL_dcolors) { put<ACC>(S_.col[3 * t], drgb[0]); put<ACC>(S_.col[3 * t + 1], drgb[1]); put<ACC>(S_.col[3 * t + 2], drgb[2]); }
+  if (out.dL_dcolors) { put<ACC>(S_.col[t], drgb[0]); put<ACC>(S_.col[SP + t], drgb[1]); put<ACC>(S_.col[2 * SP + t], drgb[2]); }
 
   float V[16], Pm[16];
 #pragma unroll
@@ -150,9 +169,9 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
 #pragma unroll
     for (int j = 0; j < 3; ++j) dS[i * 3 + j] = T[0][i] * GT[0][j] + T[1][i] * GT[1][j];
   if (out.dL_dcov3D) {
-    float *o = S_.cov + 6 * t;
-    put<ACC>(o[0], dS[0]); put<ACC>(o[1], 2.f * dS[1]); put<ACC>(o[2], 2.f * dS[2]);
-    put<ACC>(o[3], dS[4]); put<ACC>(o[4], 2.f * dS[5]); put<ACC>(o[5], dS[8]);
+    float *o = S_.cov + t;
+    put<ACC>(o[0], dS[0]); put<ACC>(o[SP], 2.f * dS[1]); put<ACC>(o[2 * SP], 2.f * dS[2]);
+    put<ACC>(o[3 * SP], dS[4]); put<ACC>(o[4 * SP], 2.f * dS[5]); put<ACC>(o[5 * SP], dS[8]);
   }
 
   // dL/dT = 2 Gs T Sigma
@@ -205,13 +224,13 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
     const float il = 1.f / len;
     const float x = vx_ * il, y = vy_ * il, z = vz_ * il;
     const float *sh = shs + (size_t)idx * M * 3;
-    float *dsh = out.dL_dsh ? S_.sh + (size_t)t * M * 3 : nullptr;
+    float *dsh = out.dL_dsh ? S_.sh + t : nullptr;
     // basis value b_k and its partial derivatives (bx, by, bz) w.r.t. the
     // unnormalised-direction components x, y, z
     float gdx = 0.f, gdy = 0.f, gdz = 0.f;
     auto term = [&](int k, float b, float bx, float by, float bz) {
       const float s0 = sh[3 * k], s1 = sh[3 * k + 1], s2 = sh[3 * k + 2];
-      if (dsh) { put<ACC>(dsh[3 * k], b * drgb[0]); put<ACC>(dsh[3 * k + 1], b * drgb[1]); put<ACC>(dsh[3 * k + 2], b * drgb[2]); }
+      if (dsh) { put<ACC>(dsh[3 * k * SP], b * drgb[0]); put<ACC>(dsh[(3 * k + 1) * SP], b * drgb[1]); put<ACC>(dsh[(3 * k + 2) * SP], b * drgb[2]); }
       const float dot = s0 * drgb[0] + s1 * drgb[1] + s2 * drgb[2];
       gdx += bx * dot; gdy += by * dot; gdz += bz * dot;
     };
@@ -244,7 +263,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
       }
     }
     if (dsh)
-      if (!ACC) for (int i = 3 * nsh; i < 3 * M; ++i) dsh[i] = 0.f;
+      if (!ACC) for (int i = 3 * nsh; i < 3 * M; ++i) dsh[i * SP] = 0.f;
     // d unit(v)/dv . g = (g - u (u . g)) / |v|
     const float ug = x * gdx + y * gdy + z * gdz;
     dm[0] += (gdx - x * ug) * il;
@@ -253,9 +272,9 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
   }
 
   if (out.dL_dmeans3D) {
-    put<ACC>(S_.m3[3 * t], dm[0]);
-    put<ACC>(S_.m3[3 * t + 1], dm[1]);
-    put<ACC>(S_.m3[3 * t + 2], dm[2]);
+    put<ACC>(S_.m3[t], dm[0]);
+    put<ACC>(S_.m3[SP + t], dm[1]);
+    put<ACC>(S_.m3[2 * SP + t], dm[2]);
   }
 
   // --- scale / rotation --------------------------------------------------
@@ -275,7 +294,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
     if (out.dL_dscales) {
 #pragma unroll
       for (int j = 0; j < 3; ++j)
-        put<ACC>(S_.sc[3 * t + j],
+        put<ACC>(S_.sc[j * SP + t],
                  vp.scale_modifier * (dM[j] * R[j] + dM[3 + j] * R[3 + j] + dM[6 + j] * R[6 + j]));
     }
     if (out.dL_drotations) {
@@ -292,15 +311,15 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
                               z * G[7] - 2.f * y * G[8]);
       const float dz = 2.f * (-2.f * z * G[0] - r * G[1] + x * G[2] + r * G[3] - 2.f * z * G[4] +
                               y * G[5] + x * G[6] + y * G[7]);
-      { put<ACC>(S_.rot[4 * t], dr); put<ACC>(S_.rot[4 * t + 1], dx); put<ACC>(S_.rot[4 * t + 2], dy); put<ACC>(S_.rot[4 * t + 3], dz); }
+      { put<ACC>(S_.rot[t], dr); put<ACC>(S_.rot[SP + t], dx); put<ACC>(S_.rot[2 * SP + t], dy); put<ACC>(S_.rot[3 * SP + t], dz); }
     }
   }
 }
 
 
-// Stores the block's contiguous slice of one output array: element i of the
-// slice belongs to Gaussian i / n of the block; culled Gaussians get zeros
-// (their shared-memory slots are never written).
+// Stores the block's contiguous slice of one output array (n elements per
+// Gaussian): element i of the slice is element i % n of Gaussian i / n;
+// Gaussians culled in every view get zeros (their slots are never written).
 __device__ __forceinline__ void store_slice(float *dst, const float *src, int n, int start,
                                             int nvalid, const uint32_t *vmask) {
   if (!dst) return;
@@ -308,18 +327,21 @@ __device__ __forceinline__ void store_slice(float *dst, const float *src, int n,
   const int cnt = nvalid * n;
   // ceil(2^32 / n) for n >= 2; i / n = umulhi(i, magic) exactly for i, n < 2^16
   const uint32_t magic = n > 1 ? (uint32_t)(0xffffffffull / (uint32_t)n) + 1u : 0u;
-  auto vis = [&](int i) {
-    const uint32_t g = n > 1 ? __umulhi((uint32_t)i, magic) : (uint32_t)i;
-    return (vmask[g >> 5] >> (g & 31)) & 1u;
-  };
+  auto gauss = [&](int i) { return n > 1 ? (int)__umulhi((uint32_t)i, magic) : i; };
+  auto vis = [&](int g) { return (vmask[g >> 5] >> (g & 31)) & 1u; };
   if ((n & 3) == 0 && (cnt & 3) == 0 && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
     // whole float4s never straddle two Gaussians when n % 4 == 0
     float4 *d4 = reinterpret_cast<float4 *>(d);
-    const float4 *s4 = reinterpret_cast<const float4 *>(src);
-    for (int i = threadIdx.x; i < (cnt >> 2); i += BWD_BLOCK)
-      d4[i] = vis(i << 2) ? s4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = threadIdx.x; i < (cnt >> 2); i += BWD_BLOCK) {
+      const int g = gauss(i << 2), k = (i << 2) - g * n;
+      const float *s = src + k * SP + g;
+      d4[i] = vis(g) ? make_float4(s[0], s[SP], s[2 * SP], s[3 * SP]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
   } else {
-    for (int i = threadIdx.x; i < cnt; i += BWD_BLOCK) d[i] = vis(i) ? src[i] : 0.f;
+    for (int i = threadIdx.x; i < cnt; i += BWD_BLOCK) {
+      const int g = gauss(i), k = i - g * n;
+      d[i] = vis(g) ? src[k * SP + g] : 0.f;
+    }
   }
 }
 
@@ -337,15 +359,7 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   const int t = threadIdx.x;
   const int start = blockIdx.x * B;
   const int idx = start + t;
-  Slots S_;
-  S_.m2 = sm;
-  S_.col = S_.m2 + 3 * B;
-  S_.op = S_.col + 3 * B;
-  S_.m3 = S_.op + B;
-  S_.cov = S_.m3 + 3 * B;
-  S_.sc = S_.cov + 6 * B;
-  S_.rot = S_.sc + 3 * B;
-  S_.sh = S_.rot + 4 * B;
+  const Slots S_ = make_slots(sm);
   const bool vis = idx < P && (flags[idx] & FLAG_VISIBLE);
   const uint32_t bal = __ballot_sync(0xffffffffu, vis);
   if ((t & 31) == 0) vmask[t >> 5] = bal;
@@ -364,50 +378,92 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   store_slice(out.dL_dsh, S_.sh, 3 * M, start, nvalid, vmask);
 }
 
-// Multi-view adjoint: the gradients of all views of a batch, summed.  Each
-// thread handles one Gaussian for every view it is visible in, accumulating
-// in its shared-memory slots; the block then stores its slices once.
+// Multi-view adjoint: the gradients of all views of a batch, summed.  A
+// Gaussian is visible in few of the views, so a thread per Gaussian looping
+// over the views would leave most lanes idle.  Instead the block lists its
+// (Gaussian, view) pairs — thread t's Gaussian contributes one pair per view
+// it is visible in, placed by a block-wide scan — and the threads take the
+// pairs in turn, adding each view's gradients into the Gaussian's shared-
+// memory slots with atomic adds; the block then stores its slices once.  The
+// per-view screen-space gradient and the densification statistics (optional
+// outputs) are handled by each Gaussian's own thread: all views' visibility
+// bytes and 2D gradients are loaded at once (independent loads), then
+// written out, zero where the Gaussian is not visible.
 __global__ void __launch_bounds__(BWD_BLOCK)
 preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__restrict__ means,
                               const float *__restrict__ shs, const float *__restrict__ scales,
                               const float *__restrict__ rots, const float *__restrict__ cov3D,
-                              DmgsGrads out) {
+                              DmgsGrads out, int want_xy, float *__restrict__ densify_accum,
+                              float *__restrict__ densify_count) {
   extern __shared__ float sm[];
   __shared__ uint32_t vmask[BWD_BLOCK / 32];
+  __shared__ uint32_t wsum[BWD_BLOCK / 32];
+  __shared__ uint16_t pairs[BWD_BLOCK * MAX_BATCH_VIEWS];
   const int B = BWD_BLOCK;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const int start = blockIdx.x * B;
   const int idx = start + t;
-  Slots S_;
-  S_.m2 = sm;
-  S_.col = S_.m2 + 3 * B;
-  S_.op = S_.col + 3 * B;
-  S_.m3 = S_.op + B;
-  S_.cov = S_.m3 + 3 * B;
-  S_.sc = S_.cov + 6 * B;
-  S_.rot = S_.sc + 3 * B;
-  S_.sh = S_.rot + 4 * B;
-  const int per_g = 23 + 3 * M;
-  for (int i = t; i < B * per_g; i += B) sm[i] = 0.f;
-  __syncthreads();
-  bool any = false;
+  const Slots S_ = make_slots(sm);
+  const int nslot = (int)slot_floats(M);
+  for (int i = t; i < nslot; i += B) sm[i] = 0.f;
+  uint32_t vm = 0u;
   if (idx < P) {
-    for (int v = 0; v < bv.nviews; ++v) {
-      const BatchView &V = bv.v[v];
-      if (!(V.flags[idx] & FLAG_VISIBLE)) continue;
-      any = true;
-      preprocess_bwd_one<true>(idx, t, V.vp, V.viewm, V.projm, V.campos, M, means, shs, scales,
-                               rots, cov3D, V.flags, V.gacc, out, S_);
-      if (V.dL_dmeans2D) {  // per-view screen-space gradient (NDC)
-        const float4 ga = reinterpret_cast<const float4 *>(V.gacc)[3 * idx];
-        V.dL_dmeans2D[3 * idx] = ga.x;
-        V.dL_dmeans2D[3 * idx + 1] = ga.y;
-        V.dL_dmeans2D[3 * idx + 2] = 0.f;
+    uint32_t f[MAX_BATCH_VIEWS];
+#pragma unroll
+    for (int v = 0; v < MAX_BATCH_VIEWS; ++v) f[v] = v < bv.nviews ? bv.v[v].flags[idx] : 0u;
+#pragma unroll
+    for (int v = 0; v < MAX_BATCH_VIEWS; ++v) vm |= ((f[v] & FLAG_VISIBLE) ? 1u : 0u) << v;
+    if (want_xy) {
+      float2 g2[MAX_BATCH_VIEWS];
+#pragma unroll
+      for (int v = 0; v < MAX_BATCH_VIEWS; ++v)
+        g2[v] = ((vm >> v) & 1u) ? *reinterpret_cast<const float2 *>(bv.v[v].gacc + 12 * (size_t)idx)
+                                 : make_float2(0.f, 0.f);
+      float nsum = 0.f;
+#pragma unroll
+      for (int v = 0; v < MAX_BATCH_VIEWS; ++v) {
+        if (v >= bv.nviews) break;
+        float *d2 = bv.v[v].dL_dmeans2D;
+        if (d2) {
+          d2[3 * (size_t)idx] = g2[v].x;
+          d2[3 * (size_t)idx + 1] = g2[v].y;
+          d2[3 * (size_t)idx + 2] = 0.f;
+        }
+        if ((vm >> v) & 1u) nsum += sqrtf(g2[v].x * g2[v].x + g2[v].y * g2[v].y);
+      }
+      if (densify_accum && vm) {
+        densify_accum[idx] += nsum;
+        densify_count[idx] += (float)__popc(vm);
       }
     }
   }
-  const uint32_t bal = __ballot_sync(0xffffffffu, any);
-  if ((t & 31) == 0) vmask[t >> 5] = bal;
+  // block-wide exclusive scan of the pair counts
+  const uint32_t cnt = __popc(vm);
+  uint32_t inc = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  const uint32_t bal = __ballot_sync(0xffffffffu, vm != 0u);
+  if (lane == 0) vmask[wid] = bal;
+  __syncthreads();
+  uint32_t off = inc - cnt, total = 0;
+#pragma unroll
+  for (int w = 0; w < BWD_BLOCK / 32; ++w) {
+    off += w < wid ? wsum[w] : 0u;
+    total += wsum[w];
+  }
+  for (uint32_t m = vm; m; m &= m - 1) pairs[off++] = (uint16_t)((t << 4) | (__ffs(m) - 1));
+  __syncthreads();
+  for (uint32_t i = t; i < total; i += B) {
+    const uint32_t pr = pairs[i];
+    const int gl = (int)(pr >> 4), v = (int)(pr & 15u);
+    const BatchView &V = bv.v[v];
+    preprocess_bwd_one<true>(start + gl, gl, V.vp, V.viewm, V.projm, V.campos, M, means, shs,
+                             scales, rots, cov3D, V.flags, V.gacc, out, S_);
+  }
   __syncthreads();
   const int nvalid = min(B, P - start);
   store_slice(out.dL_dcolors, S_.col, 3, start, nvalid, vmask);
@@ -426,7 +482,7 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
                           const char *geom, const float *gacc, const DmgsGrads &out,
                           cudaStream_t s) {
   if (g.P <= 0) return DMGS_OK;
-  const size_t smem = (size_t)BWD_BLOCK * (23 + 3 * (size_t)g.M) * 4;
+  const size_t smem = slot_floats(g.M) * 4;
   if (smem > 200 * 1024) {
     dmgs_host::set_error("preprocess_bwd: %d SH coefficients per Gaussian exceed shared memory", g.M);
     return DMGS_ERR_ARG;
@@ -446,19 +502,22 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
 namespace dmgs {
 
 int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, const DmgsGrads &out,
-                                  cudaStream_t s) {
+                                  float *densify_accum, float *densify_count, cudaStream_t s) {
   if (g.P <= 0) return DMGS_OK;
-  const size_t smem = (size_t)BWD_BLOCK * (23 + 3 * (size_t)g.M) * 4;
+  const size_t smem = slot_floats(g.M) * 4;
   if (smem > 200 * 1024) {
     dmgs_host::set_error("preprocess_bwd: %d SH coefficients per Gaussian exceed shared memory", g.M);
     return DMGS_ERR_ARG;
   }
+  int want_xy = densify_accum != nullptr;
+  for (int v = 0; v < bv.nviews; ++v) want_xy |= bv.v[v].dL_dmeans2D != nullptr;
   if (smem > 48 * 1024)
     DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_batched_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   DMGS_TIMED(K_BATCH_PREPROCESS_BWD, s,
              dmgs_host::note_launch(), preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
-                 bv, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D, out));
+                 bv, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D, out, want_xy,
+                 densify_accum, densify_count));
   DMGS_LAUNCH_CHECK("preprocess_bwd_batched_kernel");
   return DMGS_OK;
 }

@@ -185,11 +185,18 @@ int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
                             dmgs_stream_t stream);
 /* Adjoint of the batch: dL_dout_color[v] [3,H,W] per view; `grads` receive
  * the sum over views (its dL_dmeans2D is unused); dL_dmeans2D[v] (may be
- * NULL, or have NULL entries) receives view v's NDC-mean gradient [P,3]. */
+ * NULL, or have NULL entries) receives view v's NDC-mean gradient [P,3].
+ * densify_accum / densify_count ([P] each, both or neither, may be NULL):
+ * the reference's densification statistics fused over the batch
+ * (scene/gaussian_model.py:405-407, called once per view by train.py:116):
+ * for every view v in which Gaussian i is visible, densify_accum[i] +=
+ * |(dL_dmeans2D[v][i][0], dL_dmeans2D[v][i][1])| and densify_count[i] += 1.
+ * They accumulate across calls; the caller zeroes them. */
 int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
                             const float *const *dL_dout_color, void *state,
                             size_t state_bytes, const DmgsGrads *grads,
-                            float *const *dL_dmeans2D, dmgs_stream_t stream);
+                            float *const *dL_dmeans2D, float *densify_accum,
+                            float *densify_count, dmgs_stream_t stream);
 /* Synchronises the stream, writes each view's instance count to
  * num_rendered[v] and returns DMGS_ERR_OVERFLOW when a view exceeded its
  * capacity (or another DMGS_ERR_* from a view's status word). */

@@ -172,3 +172,38 @@ def test_autotune_and_autograd_entry(tmp_path):
     ref = [_plain(g, _settings(v), torch.ones(3, v.height, v.width, device=D)) for v in views[:3]]
     for k in g:
         assert rel_l2(leaves[k].grad.cpu().numpy(), sum(r[1][k] for r in ref).cpu().numpy()) <= 1e-5, k
+
+
+def test_fused_densification_stats_match_per_view_gradients():
+    sc, views = _scene_and_views(P=4000, seed=46)
+    g = _gauss(sc)
+    settings = [_settings(v) for v in views]
+    br = BatchedRasterizer(settings, g, means2D_grads=True, densify_stats=True)
+    gen = torch.Generator(device=D).manual_seed(6)
+    dimgs = [torch.randn(3, v.height, v.width, device=D, generator=gen) for v in views]
+    br.forward()
+    br.backward(dimgs)
+    torch.cuda.synchronize()
+    acc = torch.zeros(br.P, device=D)
+    cnt = torch.zeros(br.P, device=D)
+    for v in range(len(views)):
+        vis = br.radii[v] > 0
+        acc[vis] += br.means2D_grads[v][vis, :2].norm(dim=-1)
+        cnt[vis] += 1
+        assert torch.all(br.means2D_grads[v][~vis] == 0)  # zero where not visible
+    assert torch.equal(br.densify_count, cnt)
+    assert torch.allclose(br.densify_accum, acc, rtol=1e-5, atol=1e-12)
+    br.forward()
+    br.backward()  # same gradients again: the statistics accumulate
+    torch.cuda.synchronize()
+    assert torch.equal(br.densify_count, 2 * cnt)
+    assert torch.allclose(br.densify_accum, 2 * acc, rtol=1e-5, atol=1e-12)
+    br.reset_densify_stats()
+    assert not br.densify_accum.any() and not br.densify_count.any()
+    # without per-view outputs the summed parameter gradients are unchanged
+    lean = BatchedRasterizer(settings, g, means2D_grads=False)
+    lean.forward()
+    lean.backward(dimgs)
+    torch.cuda.synchronize()
+    for k in g:
+        assert rel_l2(lean.grads[k].cpu().numpy(), br.grads[k].cpu().numpy()) <= 1e-5, k
