@@ -53,24 +53,17 @@ __device__ __forceinline__ void cov3d_scale_rot(float sx, float sy, float sz, fl
 
 __device__ __forceinline__ int trunc_sat(float v) { return __float2int_rz(v); }
 
-// One Gaussian; returns true when it is visible (radius > 0, non-empty
-// tile rectangle).
+// Geometry of one Gaussian in one view (position, 3D covariance S and
+// opacity o given): projection, EWA 2D covariance, conic, radius and tile
+// rectangle.  Writes radii[idx] and, when visible, every field of the record
+// but the colour (feat[1].zw, feat[2].x), which color_one adds; a culled
+// Gaussian gets radius 0 and flags 0.  Returns whether it is visible (radius
+// > 0, non-empty tile rectangle).
 __device__ __forceinline__ bool
-preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
-               const float *__restrict__ projm_g, const float *__restrict__ campos_g, int M,
-               const float *__restrict__ means, const float *__restrict__ opac,
-               const float *__restrict__ shs, const float *__restrict__ colors,
-               const float *__restrict__ scales, const float *__restrict__ rots,
-               const float *__restrict__ cov3D, int32_t *__restrict__ radii,
-               float4 *__restrict__ feat, uint8_t *__restrict__ flags,
-               uint32_t *__restrict__ counters) {
-
-  float V[16], Pm[16];
-  load_mat(viewm_g, V);
-  load_mat(projm_g, Pm);
-
-  const float x = __ldg(means + 3 * idx), y = __ldg(means + 3 * idx + 1),
-              z = __ldg(means + 3 * idx + 2);
+geometry_one(int idx, const ViewParams &vp, const float *V, const float *Pm, float x, float y,
+             float z, const float *S, float o, int32_t *__restrict__ radii,
+             float4 *__restrict__ feat, uint8_t *__restrict__ flags,
+             uint32_t *__restrict__ counters) {
   const float vx = add(add(add(mul(V[0], x), mul(V[4], y)), mul(V[8], z)), V[12]);
   const float vy = add(add(add(mul(V[1], x), mul(V[5], y)), mul(V[9], z)), V[13]);
   const float vz = add(add(add(mul(V[2], x), mul(V[6], y)), mul(V[10], z)), V[14]);
@@ -78,7 +71,6 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
   auto cull = [&]() {
     radii[idx] = 0;
     flags[idx] = 0;
-    feat[3 * idx + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
   };
   if (!(vz > 0.2f)) {
     if (vp.prefiltered) atomicOr(counters, ST_PREFILTER);
@@ -93,19 +85,6 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
   const float Wf = (float)vp.W, Hf = (float)vp.H;
   const float px = mul(sub(mul(add(ndcx, 1.f), Wf), 1.f), 0.5f);
   const float py = mul(sub(mul(add(ndcy, 1.f), Hf), 1.f), 0.5f);
-
-  float S[6];
-  if (cov3D != nullptr) {
-#pragma unroll
-    for (int i = 0; i < 6; ++i) S[i] = __ldg(cov3D + 6 * idx + i);
-  } else {
-    const float mod = vp.scale_modifier;
-    const float sx = mul(__ldg(scales + 3 * idx), mod);
-    const float sy = mul(__ldg(scales + 3 * idx + 1), mod);
-    const float sz = mul(__ldg(scales + 3 * idx + 2), mod);
-    const float4 q = __ldg(reinterpret_cast<const float4 *>(rots) + idx);
-    cov3d_scale_rot(sx, sy, sz, q, S);
-  }
 
   // EWA: cov2D = (J W) Sigma (J W)^T with the Jacobian evaluated at the
   // position clamped to 1.3x the field of view.
@@ -153,8 +132,24 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
   const int y1 = min(vp.gy, max(0, trunc_sat(dvd(add(add(py, r), (float)(TILE - 1)), (float)TILE))));
   if ((x1 - x0) * (y1 - y0) == 0) { cull(); return false; }
 
-  // Colour: precomputed, or SH (degree <= 3) at the view direction, +0.5,
-  // clamped at 0 with the clamp recorded for the adjoint.
+  radii[idx] = rad;
+  float *f = reinterpret_cast<float *>(feat + 3 * idx);
+  *reinterpret_cast<float4 *>(f) = make_float4(px, py, ca, cb);
+  *reinterpret_cast<float2 *>(f + 4) = make_float2(cc, o);
+  f[9] = vz;
+  *reinterpret_cast<float2 *>(f + 10) =
+      make_float2(__uint_as_float(pack_u16x2(x0, y0)), __uint_as_float(pack_u16x2(x1, y1)));
+  return true;
+}
+
+// Colour of a visible Gaussian in one view: precomputed, or SH (degree <= 3)
+// at the view direction, +0.5, clamped at 0 with the clamp recorded in the
+// flags for the adjoint.  Completes the record written by geometry_one.
+__device__ __forceinline__ void color_one(int idx, const ViewParams &vp,
+                                          const float *__restrict__ campos_g, int M, float x,
+                                          float y, float z, const float *__restrict__ shs,
+                                          const float *__restrict__ colors,
+                                          float4 *__restrict__ feat, uint8_t *__restrict__ flags) {
   float cr, cg, cbl;
   uint8_t clampbits = 0;
   if (colors != nullptr) {
@@ -191,25 +186,45 @@ preprocess_one(int idx, const ViewParams &vp, const float *__restrict__ viewm_g,
       }
     }
     float rr = 0.f, gg = 0.f, bb = 0.f;
-    for (int k = 0; k < nb; ++k) {
-      rr += b[k] * __ldg(sh + 3 * k);
-      gg += b[k] * __ldg(sh + 3 * k + 1);
-      bb += b[k] * __ldg(sh + 3 * k + 2);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {  // unrolled: b[] stays in registers
+      if (k < nb) {
+        rr += b[k] * __ldg(sh + 3 * k);
+        gg += b[k] * __ldg(sh + 3 * k + 1);
+        bb += b[k] * __ldg(sh + 3 * k + 2);
+      }
     }
     rr += 0.5f; gg += 0.5f; bb += 0.5f;
     clampbits = (rr < 0.f ? 1 : 0) | (gg < 0.f ? 2 : 0) | (bb < 0.f ? 4 : 0);
     cr = fmaxf(rr, 0.f); cg = fmaxf(gg, 0.f); cbl = fmaxf(bb, 0.f);
   }
   flags[idx] = FLAG_VISIBLE | clampbits;
+  float *f = reinterpret_cast<float *>(feat + 3 * idx);
+  *reinterpret_cast<float2 *>(f + 6) = make_float2(cr, cg);
+  f[8] = cbl;
+}
 
-  const float o = __ldg(opac + idx);
-  radii[idx] = rad;
-  feat[3 * idx + 0] = make_float4(px, py, ca, cb);
-  feat[3 * idx + 1] = make_float4(cc, o, cr, cg);
-  feat[3 * idx + 2] = make_float4(cbl, vz, __uint_as_float(pack_u16x2(x0, y0)),
-                                  __uint_as_float(pack_u16x2(x1, y1)));
-
-  return true;
+// View-independent inputs of one Gaussian: position, 3D covariance (given,
+// or from scale and rotation), opacity.
+__device__ __forceinline__ void load_gaussian(int idx, float scale_modifier,
+                                              const float *__restrict__ means,
+                                              const float *__restrict__ opac,
+                                              const float *__restrict__ scales,
+                                              const float *__restrict__ rots,
+                                              const float *__restrict__ cov3D, float &x, float &y,
+                                              float &z, float *S, float &o) {
+  x = __ldg(means + 3 * idx); y = __ldg(means + 3 * idx + 1); z = __ldg(means + 3 * idx + 2);
+  if (cov3D != nullptr) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) S[i] = __ldg(cov3D + 6 * idx + i);
+  } else {
+    const float sx = mul(__ldg(scales + 3 * idx), scale_modifier);
+    const float sy = mul(__ldg(scales + 3 * idx + 1), scale_modifier);
+    const float sz = mul(__ldg(scales + 3 * idx + 2), scale_modifier);
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(rots) + idx);
+    cov3d_scale_rot(sx, sy, sz, q, S);
+  }
+  o = __ldg(opac + idx);
 }
 
 __global__ void __launch_bounds__(PRE_BLOCK)
@@ -223,32 +238,90 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
                   uint8_t *__restrict__ flags, uint32_t *__restrict__ blkcnt,
                   uint32_t *__restrict__ counters) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool vis = idx < P &&
-                   preprocess_one(idx, vp, viewm_g, projm_g, campos_g, M, means, opac, shs, colors,
-                                  scales, rots, cov3D, radii, feat, flags, counters);
+  bool vis = false;
+  if (idx < P) {
+    float V[16], Pm[16], S[6], x, y, z, o;
+    load_mat(viewm_g, V);
+    load_mat(projm_g, Pm);
+    load_gaussian(idx, vp.scale_modifier, means, opac, scales, rots, cov3D, x, y, z, S, o);
+    vis = geometry_one(idx, vp, V, Pm, x, y, z, S, o, radii, feat, flags, counters);
+    if (vis) color_one(idx, vp, campos_g, M, x, y, z, shs, colors, feat, flags);
+  }
   const int nvis = __syncthreads_count(vis);
   if (threadIdx.x == 0) blkcnt[blockIdx.x] = (uint32_t)nvis;
 }
 
-
-// Multi-view preprocess: one thread per Gaussian computes its geometry for
-// every view of the batch (the inputs are read from DRAM once; the repeated
-// per-view reads hit L1), writing each view's records and per-block visible
-// counts.
+// Multi-view preprocess.  Phase 1, one thread per Gaussian: the
+// view-independent inputs are loaded and the 3D covariance formed once, then
+// the geometry of every view is computed (each view's matrices are L1-
+// resident broadcasts).  A Gaussian is visible in few of the views, so the
+// colour (SH evaluation, 48 coefficient loads) is left to phase 2, which
+// takes the block's visible (Gaussian, view) pairs — listed by a block-wide
+// scan of the per-thread visibility masks — with every lane busy.  Each
+// view's per-block visible count feeds its compaction.
 __global__ void __launch_bounds__(PRE_BLOCK)
 preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__restrict__ means,
                           const float *__restrict__ opac, const float *__restrict__ shs,
                           const float *__restrict__ colors, const float *__restrict__ scales,
                           const float *__restrict__ rots, const float *__restrict__ cov3D) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int NW = PRE_BLOCK / 32;
+  __shared__ uint32_t wcnt[NW][MAX_BATCH_VIEWS];
+  __shared__ uint32_t wsum[NW];
+  __shared__ uint16_t pairs[PRE_BLOCK * MAX_BATCH_VIEWS];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int idx = blockIdx.x * PRE_BLOCK + t;
+  uint32_t vm = 0u;
+  if (idx < P) {
+    float S[6], x, y, z, o;
+    const float mod0 = bv.v[0].vp.scale_modifier;
+    load_gaussian(idx, mod0, means, opac, scales, rots, cov3D, x, y, z, S, o);
+    for (int v = 0; v < bv.nviews; ++v) {
+      const BatchView &V = bv.v[v];
+      if (V.vp.scale_modifier != mod0)  // views with another scale modifier (uncommon)
+        load_gaussian(idx, V.vp.scale_modifier, means, opac, scales, rots, cov3D, x, y, z, S, o);
+      float Vm[16], Pm[16];
+      load_mat(V.viewm, Vm);
+      load_mat(V.projm, Pm);
+      if (geometry_one(idx, V.vp, Vm, Pm, x, y, z, S, o, V.radii, V.feat, V.flags, V.counters))
+        vm |= 1u << v;
+      if (V.vp.scale_modifier != mod0)
+        load_gaussian(idx, mod0, means, opac, scales, rots, cov3D, x, y, z, S, o);
+    }
+  }
   for (int v = 0; v < bv.nviews; ++v) {
-    const BatchView &V = bv.v[v];
-    const bool vis = idx < P &&
-                     preprocess_one(idx, V.vp, V.viewm, V.projm, V.campos, M, means, opac, shs,
-                                    colors, scales, rots, cov3D, V.radii, V.feat, V.flags,
-                                    V.counters);
-    const int nvis = __syncthreads_count(vis);
-    if (threadIdx.x == 0) V.blkcnt[blockIdx.x] = (uint32_t)nvis;
+    const uint32_t b = __ballot_sync(0xffffffffu, (vm >> v) & 1u);
+    if (lane == 0) wcnt[wid][v] = __popc(b);
+  }
+  const uint32_t cnt = __popc(vm);
+  uint32_t inc = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off) inc += u;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (t < bv.nviews) {
+    uint32_t n = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) n += wcnt[w][t];
+    bv.v[t].blkcnt[blockIdx.x] = n;
+  }
+  uint32_t off = inc - cnt, total = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    off += w < wid ? wsum[w] : 0u;
+    total += wsum[w];
+  }
+  for (uint32_t m = vm; m; m &= m - 1) pairs[off++] = (uint16_t)((t << 4) | (__ffs(m) - 1));
+  __syncthreads();
+  const int base = blockIdx.x * PRE_BLOCK;
+  for (uint32_t i = t; i < total; i += PRE_BLOCK) {
+    const uint32_t pr = pairs[i];
+    const int g = base + (int)(pr >> 4);
+    const BatchView &V = bv.v[pr & 15u];
+    color_one(g, V.vp, V.campos, M, __ldg(means + 3 * g), __ldg(means + 3 * g + 1),
+              __ldg(means + 3 * g + 2), shs, colors, V.feat, V.flags);
   }
 }
 
@@ -297,14 +370,18 @@ int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t
 namespace dmgs {
 namespace {
 __global__ void debug_geometry_kernel(int P, int gx, const float4 *__restrict__ feat,
-                                      int32_t *rect, uint32_t *tiles_touched, float *depth,
-                                      float *xy, float *conic_opacity, float *rgb) {
+                                      const uint8_t *__restrict__ flags, int32_t *rect,
+                                      uint32_t *tiles_touched, float *depth, float *xy,
+                                      float *conic_opacity, float *rgb) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= P) return;
-  const float4 f0 = feat[3 * idx], f1 = feat[3 * idx + 1], f2 = feat[3 * idx + 2];
+  // the record of a culled Gaussian is not written: read it only when visible
+  const bool vis = flags[idx] & FLAG_VISIBLE;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 f0 = vis ? feat[3 * idx] : zero, f1 = vis ? feat[3 * idx + 1] : zero;
+  const float4 f2 = vis ? feat[3 * idx + 2] : zero;
   const uint32_t lo = __float_as_uint(f2.z), hi = __float_as_uint(f2.w);
   const int x0 = lo & 0xffff, y0 = lo >> 16, x1 = hi & 0xffff, y1 = hi >> 16;
-  const bool vis = (lo | hi) != 0u;
   if (rect) { rect[4 * idx] = x0; rect[4 * idx + 1] = y0; rect[4 * idx + 2] = x1; rect[4 * idx + 3] = y1; }
   if (tiles_touched) tiles_touched[idx] = vis ? (uint32_t)((x1 - x0) * (y1 - y0)) : 0u;
   if (depth) depth[idx] = vis ? f2.y : 0.f;
@@ -323,7 +400,8 @@ int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,
                           float *rgb, cudaStream_t s) {
   if (L.P <= 0) return DMGS_OK;
   DMGS_TIMED(K_DEBUG, s, dmgs_host::note_launch(), debug_geometry_kernel<<<(L.P + 255) / 256, 256, 0, s>>>(
-      L.P, L.gx, reinterpret_cast<const float4 *>(geom + L.feat), rect, tiles_touched, depth, xy,
+      L.P, L.gx, reinterpret_cast<const float4 *>(geom + L.feat),
+      reinterpret_cast<const uint8_t *>(geom + L.flags), rect, tiles_touched, depth, xy,
       conic_opacity, rgb));
   DMGS_LAUNCH_CHECK("debug_geometry_kernel");
   return DMGS_OK;
