@@ -314,49 +314,54 @@ __device__ __forceinline__ StagedB stage_b(const float4 f0, const float4 f1, con
   return S;
 }
 
+// Adjoint state of one pixel.  acc = colour accumulated behind the Gaussian
+// being visited (excluding it); after a blended Gaussian with alpha a and
+// colour c it becomes acc + a (c - acc), the reference's one-step-delayed
+// update (last_alpha * last_color + (1 - last_alpha) * accum) done at once.
 struct PixelState {
-  float T, T_final, g0, g1, g2, bg_dot;
-  float acc_r, acc_g, acc_b, last_alpha, last_r, last_g, last_b;
+  float T, Tfb, g0, g1, g2;  // transmittance, T_final * (bg . dL/dpixel), dL/dpixel
+  float acc_r, acc_g, acc_b;
   uint32_t last_contrib;
 };
+
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 __device__ __forceinline__ void init_pixel(PixelState &ps, bool inside, int pix, size_t HW,
                                            const float *__restrict__ final_Ts,
                                            const uint32_t *__restrict__ n_contrib,
                                            const float *__restrict__ dL_dout, float bg0,
                                            float bg1, float bg2) {
-  ps.T_final = inside ? final_Ts[pix] : 0.f;
+  const float T_final = inside ? final_Ts[pix] : 0.f;
   ps.last_contrib = inside ? n_contrib[pix] : 0u;
   ps.g0 = inside ? dL_dout[pix] : 0.f;
   ps.g1 = inside ? dL_dout[HW + pix] : 0.f;
   ps.g2 = inside ? dL_dout[2 * HW + pix] : 0.f;
-  ps.T = ps.T_final;
-  ps.bg_dot = bg0 * ps.g0 + bg1 * ps.g1 + bg2 * ps.g2;
+  ps.T = T_final;
+  ps.Tfb = T_final * (bg0 * ps.g0 + bg1 * ps.g1 + bg2 * ps.g2);
   ps.acc_r = ps.acc_g = ps.acc_b = 0.f;
-  ps.last_alpha = ps.last_r = ps.last_g = ps.last_b = 0.f;
 }
 
 // One (pixel, Gaussian) term of the adjoint, accumulated into e[0..8] when
 // `take` (the pair was blended in the forward); otherwise the state and e[]
 // are left as they are.  Evaluated without branches: the state updates are
-// selects and the gradient terms are scaled by a factor selected to 0, so a
-// warp whose lanes differ in `take` runs one straight-line path.
+// selects or scaled by a factor selected to 0, so a warp whose lanes differ
+// in `take` runs one straight-line path.  T is recovered by dividing by
+// (1 - alpha) with the hardware reciprocal (alpha <= 0.99).
 __device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float alpha, float G,
                                              const float4 &s1, const float4 &s2, const float4 &s3,
                                              float dx, float dy, float *e) {
-  const float inv = __frcp_rn(1.f - alpha);
+  const float inv = rcp_approx(1.f - alpha);
   const float Tn = ps.T * inv;
-  const float w = alpha * Tn;
-  const float la = ps.last_alpha, nla = 1.f - ps.last_alpha;
-  const float acc_r = la * ps.last_r + nla * ps.acc_r;
-  const float acc_g = la * ps.last_g + nla * ps.acc_g;
-  const float acc_b = la * ps.last_b + nla * ps.acc_b;
-  const float cr = s1.w, cg = s2.x, cb = s2.y;
-  float dL_dalpha = ((cr - acc_r) * ps.g0 + (cg - acc_g) * ps.g1 + (cb - acc_b) * ps.g2) * Tn;
-  dL_dalpha -= ps.T_final * inv * ps.bg_dot;
+  const float dr = s1.w - ps.acc_r, dg = s2.x - ps.acc_g, db = s2.y - ps.acc_b;
+  const float dL_dalpha = (dr * ps.g0 + dg * ps.g1 + db * ps.g2) * Tn - ps.Tfb * inv;
   const float Gd = take ? G * dL_dalpha : 0.f;  // dL/dopacity term
-  const float wt = take ? w : 0.f;
-  const float u = s1.y * Gd;                    // dL/dpower = o G dL/dalpha
+  const float at = take ? alpha : 0.f;
+  const float wt = at * Tn;                      // dL/drgb weight
+  const float u = s1.y * Gd;                     // dL/dpower = o G dL/dalpha
   const float ux = u * dx, uy = u * dy;
   e[0] += ux * s2.z + uy * s2.w;  // dL/dndc_x
   e[1] += uy * s3.x + ux * s3.y;  // dL/dndc_y
@@ -368,13 +373,9 @@ __device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float al
   e[7] += wt * ps.g1;
   e[8] += wt * ps.g2;
   ps.T = take ? Tn : ps.T;
-  ps.acc_r = take ? acc_r : ps.acc_r;
-  ps.acc_g = take ? acc_g : ps.acc_g;
-  ps.acc_b = take ? acc_b : ps.acc_b;
-  ps.last_r = take ? cr : ps.last_r;
-  ps.last_g = take ? cg : ps.last_g;
-  ps.last_b = take ? cb : ps.last_b;
-  ps.last_alpha = take ? alpha : ps.last_alpha;
+  ps.acc_r = fmaf(at, dr, ps.acc_r);
+  ps.acc_g = fmaf(at, dg, ps.acc_g);
+  ps.acc_b = fmaf(at, db, ps.acc_b);
 }
 
 // Transposed reduce-scatter of 16 slots over the warp: afterwards the lane
