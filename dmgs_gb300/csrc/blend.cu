@@ -413,7 +413,7 @@ __device__ __forceinline__ float warp_reduce_scatter16(float v[16], int lane) {
 
 
 template <int PPT, int BATCH>
-__global__ void __launch_bounds__(256 / PPT)
+__global__ void __launch_bounds__(256 / PPT, PPT == 4 ? 10 : (PPT == 2 ? 6 : 4))
 blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
   constexpr int THREADS = 256 / PPT;
   __shared__ float4 S0[BATCH], S1[BATCH], S2[BATCH], S3[BATCH];
