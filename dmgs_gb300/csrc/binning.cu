@@ -274,17 +274,20 @@ __device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1
 }
 
 // Lane `lane` visits tiles lane, lane+32, ... of a rw-wide rectangle in
-// row-major order; row/column advance incrementally.  The two divisions by
-// rw use a float reciprocal: for numerators below 33 and rw >= 1 the
-// quotient of (n + 0.5) / rw is at least 1/64 away from an integer, far
-// beyond the reciprocal's error, so truncation gives the exact quotient.
+// row-major order; row/column advance incrementally.  The divisions by rw
+// (numerators <= 32) use a per-rectangle multiplier M = floor(2^16 / rw) + 1
+// for rw <= 32, exact for numerators below 2^16 / rw (>= 2048), and M = 0
+// for wider rectangles (every quotient is 0).
+__device__ __forceinline__ uint32_t walk_magic(int rw) {
+  return rw <= 32 ? 65536u / (uint32_t)rw + 1u : 0u;
+}
+
 struct RectWalk {
   int row, col, dr, dc, rw;
-  __device__ __forceinline__ RectWalk(int lane, int rw_) : rw(rw_) {
-    const float inv = __frcp_rn((float)rw_);
-    row = __float2int_rz(((float)lane + 0.5f) * inv);
+  __device__ __forceinline__ RectWalk(int lane, int rw_, uint32_t M) : rw(rw_) {
+    row = (int)(((uint32_t)lane * M) >> 16);
     col = lane - row * rw;
-    dr = __float2int_rz(32.5f * inv);
+    dr = (int)((32u * M) >> 16);
     dc = 32 - dr * rw;
   }
   __device__ __forceinline__ void next() {
@@ -393,21 +396,38 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
     unsigned m = __ballot_sync(FULL, hit);
     const uint32_t xy = hit ? ((uint32_t)x0 | ((uint32_t)(cy0 - ys) << 16)) : 0u;
     const uint32_t wa = hit ? ((uint32_t)(x1 - x0) | ((uint32_t)((x1 - x0) * (cy1 - cy0)) << 16)) : 1u;
+    const uint32_t mg = walk_magic(hit ? x1 - x0 : 1);  // lane-parallel, once per group
     while (m) {
       const int i = __ffs(m) - 1;
       m &= m - 1;
       const uint32_t xyi = __shfl_sync(FULL, xy, i), wai = __shfl_sync(FULL, wa, i);
+      const uint32_t mgi = __shfl_sync(FULL, mg, i);
       const uint32_t idi = EMIT ? __shfl_sync(FULL, id, i) : 0u;
       const int bx = (int)(xyi & 0xffffu), by = (int)(xyi >> 16);
       const int rw = (int)(wai & 0xffffu), area = (int)(wai >> 16);
-      RectWalk it(lane, rw);
-      for (int j = lane; j < area; j += 32, it.next()) {
-        uint32_t *sl = &slot[(by + it.row) * bd.gx + bx + it.col];
-        const uint32_t p = *sl;
-        *sl = p + 1u;
+      RectWalk it(lane, rw, mgi);
+      const int o = by * bd.gx + bx;
+      int j = lane;
+      // two tiles per step (distinct slots: independent read/modify/writes)
+      for (; j + 32 < area; j += 64) {
+        const int a0 = o + it.row * bd.gx + it.col;
+        it.next();
+        const int a1 = o + it.row * bd.gx + it.col;
+        it.next();
+        const uint32_t p0 = slot[a0], p1 = slot[a1];
+        slot[a0] = p0 + 1u;
+        slot[a1] = p1 + 1u;
         if (EMIT) {
-          if (p < K_alloc) point_list[p] = idi;
-          else bad = true;
+          if (p0 < K_alloc) point_list[p0] = idi; else bad = true;
+          if (p1 < K_alloc) point_list[p1] = idi; else bad = true;
+        }
+      }
+      if (j < area) {
+        const int a0 = o + it.row * bd.gx + it.col;
+        const uint32_t p0 = slot[a0];
+        slot[a0] = p0 + 1u;
+        if (EMIT) {
+          if (p0 < K_alloc) point_list[p0] = idi; else bad = true;
         }
       }
       __syncwarp();
