@@ -273,6 +273,28 @@ __device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1
   x0 = lo & 0xffff; y0 = lo >> 16; x1 = hi & 0xffff; y1 = hi >> 16;
 }
 
+// L2 eviction-priority hints: the instance list is written 4 bytes at a time
+// by many warps, so its lines should stay in L2 until complete (evict_last);
+// the count-matrix reads of the emission are used once (evict_first).
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_hint(uint32_t *ptr, uint32_t v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(ptr), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_hint(const uint32_t *ptr, uint64_t pol) {
+  uint32_t v;
+  asm volatile("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
+  return v;
+}
+
 // Lane `lane` visits tiles lane, lane+32, ... of a rw-wide rectangle in
 // row-major order; row/column advance incrementally.  The divisions by rw
 // (numerators <= 32) use a per-rectangle multiplier M = floor(2^16 / rw) + 1
@@ -360,17 +382,19 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
   const int ys = b * bd.R, ye = min(bd.gy, ys + bd.R);
   const int t0 = ys * bd.gx, nt = (ye - ys) * bd.gx;
   const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
+  const uint64_t keep = l2_policy_last();
   if (EMIT) {
     if (s0 >= s1) return;
+    const uint64_t once = l2_policy_first();
     int i = lane;
     for (; i + 96 < nt; i += 128) {
-      const uint32_t a = cmat[(size_t)(t0 + i) * C + c];
-      const uint32_t e = cmat[(size_t)(t0 + i + 32) * C + c];
-      const uint32_t f = cmat[(size_t)(t0 + i + 64) * C + c];
-      const uint32_t g = cmat[(size_t)(t0 + i + 96) * C + c];
+      const uint32_t a = ld_hint(cmat + (size_t)(t0 + i) * C + c, once);
+      const uint32_t e = ld_hint(cmat + (size_t)(t0 + i + 32) * C + c, once);
+      const uint32_t f = ld_hint(cmat + (size_t)(t0 + i + 64) * C + c, once);
+      const uint32_t g = ld_hint(cmat + (size_t)(t0 + i + 96) * C + c, once);
       slot[i] = a; slot[i + 32] = e; slot[i + 64] = f; slot[i + 96] = g;
     }
-    for (; i < nt; i += 32) slot[i] = cmat[(size_t)(t0 + i) * C + c];
+    for (; i < nt; i += 32) slot[i] = ld_hint(cmat + (size_t)(t0 + i) * C + c, once);
   } else {
     for (int i = lane; i < nt; i += 32) slot[i] = 0u;
   }
@@ -418,8 +442,8 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
         slot[a0] = p0 + 1u;
         slot[a1] = p1 + 1u;
         if (EMIT) {
-          if (p0 < K_alloc) point_list[p0] = idi; else bad = true;
-          if (p1 < K_alloc) point_list[p1] = idi; else bad = true;
+          if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
+          if (p1 < K_alloc) st_hint(point_list + p1, idi, keep); else bad = true;
         }
       }
       if (j < area) {
@@ -427,7 +451,7 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
         const uint32_t p0 = slot[a0];
         slot[a0] = p0 + 1u;
         if (EMIT) {
-          if (p0 < K_alloc) point_list[p0] = idi; else bad = true;
+          if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
         }
       }
       __syncwarp();
