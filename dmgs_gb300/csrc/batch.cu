@@ -29,7 +29,10 @@ struct BatchLayout {
   size_t queue, total;
 };
 
-int make_layout(const DmgsBatch *b, int P, BatchLayout &L) {
+// Pv: the Gaussian count of every view (nullptr: P for all); with_adjoint:
+// reserve the 2D-gradient accumulators of the backward.
+int make_layout(const DmgsBatch *b, int P, BatchLayout &L, const int32_t *Pv = nullptr,
+                bool with_adjoint = true) {
   if (!b || b->nviews < 1 || b->nviews > MAX_BATCH_VIEWS || !b->views || !b->capacity) {
     set_error("batch: nviews must be 1..%d with views and capacity arrays", MAX_BATCH_VIEWS);
     return DMGS_ERR_ARG;
@@ -37,6 +40,11 @@ int make_layout(const DmgsBatch *b, int P, BatchLayout &L) {
   L.n = b->nviews;
   size_t o = 0;
   for (int v = 0; v < L.n; ++v) {
+    if (Pv) P = Pv[v];
+    if (P < 0) {
+      set_error("batch: view %d has a negative Gaussian count", v);
+      return DMGS_ERR_ARG;
+    }
     const DmgsView &view = b->views[v];
     if (view.width <= 0 || view.height <= 0) {
       set_error("batch: view %d has an invalid size", v);
@@ -54,7 +62,7 @@ int make_layout(const DmgsBatch *b, int P, BatchLayout &L) {
     V.geom = o;  o = align_up(o + V.G.total, 256);
     V.bin = o;   o = align_up(o + V.B.total, 256);
     V.img = o;   o = align_up(o + V.I.total, 256);
-    V.gacc = o;  o = align_up(o + bwd_scratch_bytes(P), 256);
+    V.gacc = o;  o = align_up(o + (with_adjoint ? bwd_scratch_bytes(P) : 0), 256);
     V.radii = o; o = align_up(o + (size_t)P * 4 + 4, 256);
   }
   L.queue = o;
@@ -97,6 +105,42 @@ GaussianPtrs gptrs_of(const DmgsGaussians *g) {
   return p;
 }
 
+#define RET_IF(x)                 \
+  do {                            \
+    int r_ = (x);                 \
+    if (r_ != DMGS_OK) return r_; \
+  } while (0)
+
+int check_view(const DmgsView &w, int v) {
+  if (!w.bg || !w.viewmatrix || !w.projmatrix || !w.campos || w.sh_degree < 0 ||
+      w.sh_degree > 3 || !(w.tanfovx > 0.f) || !(w.tanfovy > 0.f)) {
+    set_error("batch: view %d is invalid", v);
+    return DMGS_ERR_ARG;
+  }
+  return DMGS_OK;
+}
+
+// The Gaussian set rendered by view v (input-mode rules of the drop-in).
+int check_gaussians(const DmgsGaussians *g, const DmgsView &w, int v) {
+  if (!g || g->P < 0) { set_error("batch: invalid Gaussians for view %d", v); return DMGS_ERR_ARG; }
+  if (g->P == 0) return DMGS_OK;
+  if (!g->means3D || !g->opacities || (g->shs == nullptr) == (g->colors_precomp == nullptr) ||
+      ((g->scales == nullptr || g->rotations == nullptr) && g->cov3D_precomp == nullptr) ||
+      ((g->scales != nullptr || g->rotations != nullptr) && g->cov3D_precomp != nullptr)) {
+    set_error("batch: give exactly one colour source and one covariance source");
+    return DMGS_ERR_ARG;
+  }
+  if (g->shs && g->M < (w.sh_degree + 1) * (w.sh_degree + 1)) {
+    set_error("batch: too few SH coefficients for view %d", v);
+    return DMGS_ERR_ARG;
+  }
+  if (g->rotations && (reinterpret_cast<uintptr_t>(g->rotations) & 15)) {
+    set_error("rotations must be 16-byte aligned");
+    return DMGS_ERR_ARG;
+  }
+  return DMGS_OK;
+}
+
 int check_common(const DmgsBatch *b, const DmgsGaussians *g, void *state, size_t bytes,
                  BatchLayout &L) {
   if (!g || g->P < 0) { set_error("batch: invalid Gaussians"); return DMGS_ERR_ARG; }
@@ -106,32 +150,8 @@ int check_common(const DmgsBatch *b, const DmgsGaussians *g, void *state, size_t
     set_error("batch: state too small: %zu < %zu bytes", bytes, L.total);
     return DMGS_ERR_STATE;
   }
-  for (int v = 0; v < b->nviews; ++v) {
-    const DmgsView &w = b->views[v];
-    if (!w.bg || !w.viewmatrix || !w.projmatrix || !w.campos || w.sh_degree < 0 ||
-        w.sh_degree > 3 || !(w.tanfovx > 0.f) || !(w.tanfovy > 0.f)) {
-      set_error("batch: view %d is invalid", v);
-      return DMGS_ERR_ARG;
-    }
-  }
-  if (g->P > 0) {
-    if (!g->means3D || !g->opacities ||
-        (g->shs == nullptr) == (g->colors_precomp == nullptr) ||
-        ((g->scales == nullptr || g->rotations == nullptr) && g->cov3D_precomp == nullptr) ||
-        ((g->scales != nullptr || g->rotations != nullptr) && g->cov3D_precomp != nullptr)) {
-      set_error("batch: give exactly one colour source and one covariance source");
-      return DMGS_ERR_ARG;
-    }
-    for (int v = 0; v < b->nviews; ++v)
-      if (g->shs && g->M < (b->views[v].sh_degree + 1) * (b->views[v].sh_degree + 1)) {
-        set_error("batch: too few SH coefficients for view %d", v);
-        return DMGS_ERR_ARG;
-      }
-    if (g->rotations && (reinterpret_cast<uintptr_t>(g->rotations) & 15)) {
-      set_error("rotations must be 16-byte aligned");
-      return DMGS_ERR_ARG;
-    }
-  }
+  for (int v = 0; v < b->nviews; ++v) RET_IF(check_view(b->views[v], v));
+  for (int v = 0; v < b->nviews; ++v) RET_IF(check_gaussians(g, b->views[v], v));
   return DMGS_OK;
 }
 
@@ -187,12 +207,6 @@ void fill_blend(const DmgsBatch *b, const BatchLayout &L, char *st, BlendBatch &
   }
   bb.total = base;
 }
-
-#define RET_IF(x)                 \
-  do {                            \
-    int r_ = (x);                 \
-    if (r_ != DMGS_OK) return r_; \
-  } while (0)
 
 }  // namespace
 
@@ -287,4 +301,79 @@ extern "C" int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *stat
     }
   }
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Serving form: every view renders its own Gaussian set (requests for
+// several resident scenes in one launch sequence), forward only.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+int multi_layout(const DmgsBatch *b, const DmgsGaussians *g, BatchLayout &L) {
+  if (!g) { set_error("multi: gaussians is NULL"); return DMGS_ERR_ARG; }
+  if (!b || b->nviews < 1 || b->nviews > MAX_BATCH_VIEWS) {
+    set_error("multi: nviews must be 1..%d", MAX_BATCH_VIEWS);
+    return DMGS_ERR_ARG;
+  }
+  int32_t P[MAX_BATCH_VIEWS];
+  for (int v = 0; v < b->nviews; ++v) P[v] = g[v].P;
+  return make_layout(b, 0, L, P, false);
+}
+
+}  // namespace
+
+extern "C" size_t dmgs_multi_state_bytes(const DmgsBatch *b, const DmgsGaussians *g) {
+  BatchLayout L;
+  if (multi_layout(b, g, L) != DMGS_OK) return 0;
+  return L.total;
+}
+
+extern "C" int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *state,
+                                 size_t state_bytes, dmgs_stream_t stream) {
+  BatchLayout L;
+  RET_IF(multi_layout(b, g, L));
+  if (!state || state_bytes < L.total) {
+    set_error("multi: state too small: %zu < %zu bytes", state_bytes, L.total);
+    return DMGS_ERR_STATE;
+  }
+  if (!b->out_color) { set_error("multi: out_color is NULL"); return DMGS_ERR_ARG; }
+  for (int v = 0; v < b->nviews; ++v) {
+    RET_IF(check_view(b->views[v], v));
+    RET_IF(check_gaussians(&g[v], b->views[v], v));
+    if (!b->out_color[v]) { set_error("multi: out_color[%d] is NULL", v); return DMGS_ERR_ARG; }
+  }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  char *st = static_cast<char *>(state);
+  BatchViews bv;
+  fill_views(b, L, st, bv);
+  for (int v = 0; v < b->nviews; ++v) {
+    const ViewLayout &V = L.v[v];
+    const BatchView &o = bv.v[v];
+    RET_IF(launch_preprocess(o.vp, o.viewm, o.projm, o.campos, gptrs_of(&g[v]), o.radii, V.G,
+                             st + V.geom, s));
+    RET_IF(launch_binning_geometry(V.G, st + V.geom, (uint32_t)b->capacity[v], s));
+    RET_IF(launch_emit(V.G, st + V.geom, V.B, st + V.bin, b->capacity[v], s));
+  }
+  BlendBatch bb;
+  fill_blend(b, L, st, bb);
+  uint32_t *queue = reinterpret_cast<uint32_t *>(st + L.queue);
+  DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));
+  RET_IF(launch_blend_batch_fwd(bb, cfg_of(b), queue, s));
+  return DMGS_OK;
+}
+
+extern "C" int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
+                                       const void *state, size_t state_bytes,
+                                       uint32_t *host_words, dmgs_stream_t stream) {
+  BatchLayout L;
+  RET_IF(multi_layout(b, g, L));
+  if (!state || state_bytes < L.total) { set_error("multi: state too small"); return DMGS_ERR_STATE; }
+  if (!host_words) { set_error("multi: host_words is NULL"); return DMGS_ERR_ARG; }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const char *st = static_cast<const char *>(state);
+  for (int v = 0; v < b->nviews; ++v)  // words CI_STATUS, CI_K
+    DMGS_CUDA(cudaMemcpyAsync(host_words + 2 * v, st + L.v[v].geom + L.v[v].G.counters, 8,
+                              cudaMemcpyDeviceToHost, s));
+  return DMGS_OK;
 }

@@ -121,3 +121,36 @@ def hemisphere_views(n, width, height, radius=4.0, fov_deg=50.0, seed=0):
         d /= np.linalg.norm(d)
         out.append(make_view(radius * d, (0.0, 0.0, 0.0), width, height, fovx_deg=fov_deg))
     return out
+
+
+def large_scene_tensors(P, seed, device):
+    """The large-scene distributions of :func:`large_scene`, generated on
+    `device` with torch's generator (for the many-million-Gaussian resident
+    scenes of the serving workload; a different random stream than the
+    numpy generator).  Returns a dict of contiguous fp32 tensors with the
+    reference's names (means3D, scales, rotations, opacities, shs)."""
+    import torch
+
+    g = torch.Generator(device=device).manual_seed(int(seed))
+    f = dict(device=device, dtype=torch.float32, generator=g)
+    n_fg = int(round(P * 0.9))
+    n_bg = P - n_fg
+    centres = torch.randn(64, 3, **f)
+    centres = centres / centres.norm(dim=1, keepdim=True)
+    centres = centres * 5.0 * torch.rand(64, 1, **f) ** (1.0 / 3.0)
+    sig = 0.2 + 1.3 * torch.rand(64, **f)
+    which = torch.randint(0, 64, (n_fg,), device=device, generator=g)
+    fg = centres[which] + torch.randn(n_fg, 3, **f) * sig[which, None]
+    d = torch.randn(n_bg, 3, **f)
+    d = d / d.norm(dim=1, keepdim=True)
+    bg = d * (20.0 + 20.0 * torch.rand(n_bg, 1, **f))
+    means = torch.cat([fg, bg], 0)[torch.randperm(P, device=device, generator=g)]
+    q = torch.randn(P, 4, **f)
+    sh = torch.empty(P, 16, 3, device=device)
+    sh[:, 0, :] = 0.5 + 0.2 * torch.randn(P, 3, **f)
+    sh[:, 1:, :] = 0.05 * torch.randn(P, 15, 3, **f)
+    return {"means3D": means.contiguous(),
+            "scales": torch.exp(-4.0 + torch.randn(P, 3, **f)).contiguous(),
+            "rotations": (q / q.norm(dim=1, keepdim=True)).contiguous(),
+            "opacities": torch.sigmoid(1.5 * torch.randn(P, 1, **f)).contiguous(),
+            "shs": sh.contiguous()}

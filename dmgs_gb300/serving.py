@@ -1,0 +1,450 @@
+"""Serving loop: continuous batching of render requests for resident scenes.
+
+The reference has no serving path (it renders one view per call,
+``render_and_eval.py:42-44``).  Here several scenes stay resident on the
+device and render requests (scene, camera, resolution) arrive over time.
+The scheduler keeps a FIFO of arrived requests and, whenever a slot and
+enough of the HBM budget are free, admits the next ones into a *wave*: one
+``dmgs_render_multi`` launch sequence renders every request of the wave
+(each with its own scene) — per-request preprocess and capacity-bounded
+binning, then one persistent blend over all the wave's tiles.  Waves go to
+several CUDA streams in turn, so a wave admitted while others run overlaps
+with them on the device.  Completion is observed through events; a request
+whose instance list overflowed its capacity is re-admitted at the head of
+the queue with the exact count the device reported.  Memory is accounted per
+request (its state bytes plus its image), released when its wave completes.
+
+The scheduler is independent of the device: :class:`Scheduler` drives a
+backend (``footprint``/``launch``/``ready``/``results``/``release``), so its
+admission, ordering and retry logic is tested on the CPU with a fake one.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+ST_OVERFLOW = 2
+ST_ERRORS = 1 | 4  # prefiltered point culled, index out of its buffer
+
+
+@dataclass
+class Request:
+    rid: int
+    scene: int
+    view: object          # camera.ViewSpec
+    arrival: float        # seconds after the start of the run
+    capacity: int = 0     # instance-list capacity of the current attempt
+    attempts: int = 0
+    t_admit: float = -1.0
+    t_done: float = -1.0
+    result: object = None  # the image (host copy when the backend copies out)
+
+    @property
+    def key(self):
+        return (self.scene, self.view.width, self.view.height)
+
+    @property
+    def latency(self):
+        return self.t_done - self.arrival
+
+
+class CapacityEstimator:
+    """Instance-list capacity per (scene, width, height): the largest count
+    seen times `margin`, plus `slack`; `default(req)` before any
+    observation."""
+
+    def __init__(self, margin=1.3, slack=4096, default=None):
+        self.margin, self.slack = margin, slack
+        self.seen = {}
+        self.default = default or (lambda req: 1 << 20)
+
+    def observe(self, req, K):
+        self.seen[req.key] = max(self.seen.get(req.key, 0), int(K))
+
+    def capacity(self, req):
+        k = self.seen.get(req.key)
+        if k is None:
+            return int(self.default(req))
+        return int(k * self.margin) + self.slack
+
+
+@dataclass
+class Wave:
+    reqs: list
+    nbytes: int
+    handle: object
+    stream: int
+
+
+@dataclass
+class ServeStats:
+    latencies_ms: list = field(default_factory=list)
+    waves: int = 0
+    retries: int = 0
+    peak_bytes: int = 0
+    peak_inflight: int = 0
+    wall_s: float = 0.0
+
+    def summary(self):
+        lat = np.asarray(self.latencies_ms)
+        n = len(lat)
+        return {"requests": n,
+                "p50_ms": float(np.percentile(lat, 50)) if n else None,
+                "p99_ms": float(np.percentile(lat, 99)) if n else None,
+                "mean_ms": float(lat.mean()) if n else None,
+                "max_ms": float(lat.max()) if n else None,
+                "views_per_s": n / self.wall_s if self.wall_s > 0 else None,
+                "waves": self.waves, "mean_wave": n / self.waves if self.waves else None,
+                "retries": self.retries, "peak_bytes": self.peak_bytes,
+                "peak_inflight": self.peak_inflight, "wall_s": self.wall_s}
+
+
+class Scheduler:
+    """Admission and continuous batching over a backend.
+
+    budget_bytes: HBM the in-flight requests may hold; max_inflight: request
+    slots; max_wave: requests per launch (<= 16); n_streams: waves in flight
+    rotate over this many streams.  `clock()` returns seconds; `idle()` is
+    called when there is nothing to do (the real loop sleeps briefly)."""
+
+    def __init__(self, backend, budget_bytes, max_inflight=64, max_wave=16, n_streams=4,
+                 estimator=None, clock=time.perf_counter, idle=None):
+        if not 1 <= max_wave <= 16:
+            raise ValueError("a wave holds 1..16 requests")
+        self.backend = backend
+        self.budget = int(budget_bytes)
+        self.max_inflight = max_inflight
+        self.max_wave = max_wave
+        self.n_streams = n_streams
+        self.estimator = estimator or CapacityEstimator()
+        self.clock = clock
+        self.idle = idle or (lambda: time.sleep(50e-6))
+
+    def run(self, requests, deliver=None):
+        """Serve `requests` (arrival times in seconds from the start) in real
+        time; returns ServeStats.  Each request gets t_admit, t_done and
+        result; `deliver(request)`, if given, is called as each completes
+        (a client taking the image; it may recycle the buffer)."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        be, est = self.backend, self.estimator
+        pending, inflight = deque(), []
+        st = ServeStats()
+        used = n_in = done = nxt = 0
+        stream = 0
+        t0 = self.clock()
+        while done < len(reqs):
+            now = self.clock() - t0
+            while nxt < len(reqs) and reqs[nxt].arrival <= now:
+                pending.append(reqs[nxt])
+                nxt += 1
+            progressed = False
+            for w in list(inflight):
+                if not be.ready(w.handle):
+                    continue
+                progressed = True
+                t_obs = self.clock() - t0
+                retry = []
+                for r, (status, K) in zip(w.reqs, be.results(w.handle)):
+                    est.observe(r, K)
+                    if status & ST_ERRORS:
+                        raise RuntimeError(f"request {r.rid}: device status {status}")
+                    if status & ST_OVERFLOW:
+                        r.capacity = int(K) + est.slack
+                        r.result = None
+                        retry.append(r)
+                        st.retries += 1
+                    else:
+                        r.t_done = t_obs
+                        st.latencies_ms.append(1e3 * r.latency)
+                        done += 1
+                        if deliver is not None:
+                            deliver(r)
+                for r in reversed(retry):  # back at the head of the queue, in order
+                    pending.appendleft(r)
+                be.release(w.handle)
+                used -= w.nbytes
+                n_in -= len(w.reqs)
+                inflight.remove(w)
+            wave, wbytes = [], 0
+            while pending and len(wave) < self.max_wave and n_in + len(wave) < self.max_inflight:
+                r = pending[0]
+                cap = r.capacity or est.capacity(r)
+                fb = be.footprint(r, cap)
+                if fb > self.budget:
+                    raise RuntimeError(f"request {r.rid} needs {fb} bytes, above the budget")
+                if used + wbytes + fb > self.budget:
+                    break
+                pending.popleft()
+                r.capacity = cap
+                r.attempts += 1
+                r.t_admit = self.clock() - t0
+                wave.append(r)
+                wbytes += fb
+            if wave:
+                handle = be.launch(wave, [r.capacity for r in wave], stream)
+                inflight.append(Wave(wave, wbytes, handle, stream))
+                stream = (stream + 1) % self.n_streams
+                used += wbytes
+                n_in += len(wave)
+                st.waves += 1
+                st.peak_bytes = max(st.peak_bytes, used)
+                st.peak_inflight = max(st.peak_inflight, n_in)
+                progressed = True
+            if not progressed:
+                self.idle()
+        st.wall_s = max(r.t_done for r in reqs) - min(r.arrival for r in reqs) if reqs else 0.0
+        return st
+
+
+def poisson_trace(rate, seconds, n_scenes, resolutions, seed=0, view_fn=None):
+    """Requests with Poisson arrivals at `rate` per second for `seconds`,
+    scene uniform over n_scenes, resolution uniform over `resolutions`,
+    camera from view_fn(rng, width, height)."""
+    from .scenes import random_inside_view
+    view_fn = view_fn or random_inside_view
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            break
+        w, h = resolutions[rng.integers(len(resolutions))]
+        out.append(Request(len(out), int(rng.integers(n_scenes)), view_fn(rng, w, h), t))
+    return out
+
+
+# --------------------------------------------------------------------------
+# GPU backends
+# --------------------------------------------------------------------------
+
+class _PinnedPool:
+    """Reusable page-locked host buffers by element count."""
+
+    def __init__(self, torch, dtype):
+        self.torch, self.dtype, self.free = torch, dtype, {}
+
+    def get(self, n):
+        lst = self.free.get(n)
+        if lst:
+            return lst.pop()
+        return self.torch.empty(n, dtype=self.dtype, pin_memory=True)
+
+    def put(self, buf):
+        self.free.setdefault(buf.numel(), []).append(buf)
+
+
+class ResidentScene:
+    """A scene kept on the device: the reference's tensors (means3D,
+    opacities, shs, scales, rotations) and the C-ABI view of them."""
+
+    def __init__(self, tensors, sh_degree=3):
+        from . import _lib
+        self.t = {k: v.contiguous().float() for k, v in tensors.items()}
+        self.P = self.t["means3D"].shape[0]
+        self.M = self.t["shs"].shape[1]
+        self.sh_degree = sh_degree
+        p = _lib.ptr
+        self.gauss = _lib.DmgsGaussians(self.P, self.M, p(self.t["means3D"]), p(self.t["opacities"]),
+                                        p(self.t["shs"]), None, p(self.t["scales"]),
+                                        p(self.t["rotations"]), None)
+        self.nbytes = sum(v.numel() * v.element_size() for v in self.t.values())
+
+
+class GpuBackend:
+    """Waves rendered by dmgs_render_multi on a set of streams; camera
+    constants go up in one copy per wave, status words (and, with
+    copy_out, the images) come back into pinned host memory."""
+
+    CAM = 16 + 16 + 3 + 3  # view matrix, full projection, campos, background
+
+    def __init__(self, scenes, n_streams=4, cfg=(4, 128), copy_out=True, device=None):
+        import torch
+        from . import _lib
+        self.torch, self._lib = torch, _lib
+        self.lib = _lib.load()
+        self.scenes = scenes
+        self.device = device or torch.device("cuda")
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(n_streams)]
+        self.cfg = cfg
+        self.copy_out = copy_out
+        self.f32 = _PinnedPool(torch, torch.float32)
+        self.u32 = _PinnedPool(torch, torch.int32)
+        self._fp_cache = {}
+
+    def _batch(self, reqs, caps, cam_dev, outs):
+        L = self._lib
+        n = len(reqs)
+        views = (L.DmgsView * n)()
+        base = cam_dev.data_ptr()
+        for i, r in enumerate(reqs):
+            v = r.view
+            o = base + 4 * i * self.CAM
+            views[i] = L.DmgsView(v.width, v.height, float(v.tanfovx), float(v.tanfovy), 1.0,
+                                  self.scenes[r.scene].sh_degree, 0, 0, o + 4 * 35, o, o + 4 * 16,
+                                  o + 4 * 32)
+        out = (C.c_void_p * n)(*[t.data_ptr() if t is not None else 0 for t in outs]) if outs else None
+        capa = (C.c_int64 * n)(*caps)
+        gauss = (L.DmgsGaussians * n)(*[self.scenes[r.scene].gauss for r in reqs])
+        b = L.DmgsBatch(n, views, out, None, capa, self.cfg[0], self.cfg[1])
+        return b, gauss, (views, out, capa)
+
+    def footprint(self, req, cap):
+        key = (req.scene, req.view.width, req.view.height, int(cap))
+        fb = self._fp_cache.get(key)
+        if fb is None:
+            b, gauss, _ = self._batch([req], [cap], self.torch.empty(0), None)
+            b.out_color = None
+            fb = int(self.lib.dmgs_multi_state_bytes(C.byref(b), gauss)) + 12 * req.view.width * req.view.height
+            self._fp_cache[key] = fb
+        return fb
+
+    def launch(self, reqs, caps, stream):
+        torch = self.torch
+        s = self.streams[stream]
+        n = len(reqs)
+        cam_host = self.f32.get(n * self.CAM)
+        ch = cam_host.numpy().reshape(n, self.CAM)
+        for i, r in enumerate(reqs):
+            v = r.view
+            ch[i, 0:16] = np.asarray(v.viewmatrix, np.float32).reshape(16)
+            ch[i, 16:32] = np.asarray(v.projmatrix, np.float32).reshape(16)
+            ch[i, 32:35] = v.campos
+            ch[i, 35:38] = 0.0
+        status = self.u32.get(2 * n)
+        with torch.cuda.stream(s):
+            cam_dev = torch.empty(n * self.CAM, device=self.device)
+            cam_dev.copy_(cam_host, non_blocking=True)
+            images = [torch.empty(3, r.view.height, r.view.width, device=self.device) for r in reqs]
+            b, gauss, keep = self._batch(reqs, caps, cam_dev, images)
+            nbytes = int(self.lib.dmgs_multi_state_bytes(C.byref(b), gauss))
+            state = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._lib.check(self.lib.dmgs_render_multi(C.byref(b), gauss, state.data_ptr(), nbytes,
+                                                       s.cuda_stream), "render_multi")
+            self._lib.check(self.lib.dmgs_multi_status_async(C.byref(b), gauss, state.data_ptr(),
+                                                             nbytes, status.data_ptr(),
+                                                             s.cuda_stream), "multi_status")
+            host_imgs = None
+            if self.copy_out:
+                host_imgs = [self.f32.get(im.numel()) for im in images]
+                for h, im in zip(host_imgs, images):
+                    h.copy_(im.view(-1), non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(s)
+        return {"ev": ev, "status": status, "cam": cam_host, "state": state, "cam_dev": cam_dev,
+                "images": images, "host": host_imgs, "reqs": reqs, "keep": keep}
+
+    def ready(self, h):
+        return h["ev"].query()
+
+    def results(self, h):
+        s = h["status"].numpy()
+        out = []
+        for i, r in enumerate(h["reqs"]):
+            out.append((int(s[2 * i]) & 0xffffffff, int(s[2 * i + 1]) & 0xffffffff))
+            if self.copy_out:
+                r.result = h["host"][i].view(3, r.view.height, r.view.width)
+            else:
+                r.result = h["images"][i]
+        return out
+
+    def release(self, h):
+        self.f32.put(h["cam"])
+        self.u32.put(h["status"])
+        h.clear()
+
+    def recycle(self, req):
+        """Return a delivered request's pinned result buffer to the pool."""
+        if self.copy_out and req.result is not None:
+            self.f32.put(req.result.view(-1))
+            req.result = None
+
+
+class PlainBackend:
+    """One request at a time through the drop-in rasteriser (the reference's
+    call pattern: GaussianRasterizer forward per view, host-synchronising
+    on its instance count), with the same result copy as GpuBackend."""
+
+    def __init__(self, scenes, copy_out=True, device=None):
+        import torch
+        self.torch = torch
+        self.scenes = scenes
+        self.device = device or torch.device("cuda")
+        self.copy_out = copy_out
+        self.f32 = _PinnedPool(torch, torch.float32)
+
+    def footprint(self, req, cap):
+        return 1
+
+    def launch(self, reqs, caps, stream):
+        import torch
+        from .rasterizer import GaussianRasterizationSettings, GaussianRasterizer
+        r = reqs[0]
+        sc, v = self.scenes[r.scene], r.view
+        t = lambda a: torch.as_tensor(np.asarray(a, np.float32)).to(self.device, non_blocking=True)  # noqa: E731
+        rs = GaussianRasterizationSettings(
+            image_height=v.height, image_width=v.width, tanfovx=v.tanfovx,
+            tanfovy=v.tanfovy, bg=torch.zeros(3, device=self.device),
+            scale_modifier=1.0, viewmatrix=t(v.viewmatrix), projmatrix=t(v.projmatrix),
+            sh_degree=sc.sh_degree, campos=t(v.campos), prefiltered=False, debug=False)
+        with torch.no_grad():
+            img, _ = GaussianRasterizer(rs)(means3D=sc.t["means3D"], means2D=None,
+                                             opacities=sc.t["opacities"], shs=sc.t["shs"],
+                                             scales=sc.t["scales"], rotations=sc.t["rotations"])
+        host = None
+        if self.copy_out:
+            host = self.f32.get(img.numel())
+            host.copy_(img.reshape(-1), non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        return {"ev": ev, "img": img, "host": host, "reqs": reqs}
+
+    def ready(self, h):
+        return h["ev"].query()
+
+    def results(self, h):
+        r = h["reqs"][0]
+        r.result = h["host"].view(3, r.view.height, r.view.width) if self.copy_out else h["img"]
+        return [(0, 0)]
+
+    def release(self, h):
+        h.clear()
+
+    def recycle(self, req):
+        if self.copy_out and req.result is not None:
+            self.f32.put(req.result.view(-1))
+            req.result = None
+
+
+def profile_capacity(backend_scenes, resolutions, n_views=4, seed=0, margin=1.3):
+    """Seed a CapacityEstimator with exact instance counts of a few random
+    views per (scene, resolution) (one geometry pass each)."""
+    import torch
+    from . import _lib
+    from .scenes import random_inside_view
+    lib = _lib.load()
+    est = CapacityEstimator(margin=margin)
+    rng = np.random.default_rng(seed)
+    dev = torch.device("cuda")
+    stream = _lib.stream_of(dev)
+    for si, sc in enumerate(backend_scenes):
+        for (w, h) in resolutions:
+            for _ in range(n_views):
+                v = random_inside_view(rng, w, h)
+                keep = [torch.as_tensor(np.asarray(a, np.float32)).to(dev)
+                        for a in (np.zeros(3), v.viewmatrix, v.projmatrix, v.campos)]
+                view = _lib.DmgsView(w, h, v.tanfovx, v.tanfovy, 1.0, sc.sh_degree, 0, 0,
+                                     *[k.data_ptr() for k in keep])
+                geom = torch.empty(lib.dmgs_geom_state_bytes(sc.P, w, h), dtype=torch.uint8,
+                                   device=dev)
+                radii = torch.empty(max(sc.P, 1), dtype=torch.int32, device=dev)
+                K = C.c_int64(0)
+                _lib.check(lib.dmgs_raster_fwd_geometry(C.byref(view), C.byref(sc.gauss),
+                                                        geom.data_ptr(), geom.numel(),
+                                                        radii.data_ptr(), C.byref(K), stream),
+                           "profile")
+                est.observe(Request(-1, si, v, 0.0), K.value)
+    return est

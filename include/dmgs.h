@@ -204,6 +204,27 @@ int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *state,
                       size_t state_bytes, int64_t *num_rendered,
                       dmgs_stream_t stream);
 
+/* ---------------------------------------------------------------------- *
+ * Serving form (no counterpart in the reference): a batch whose views each
+ * render their own Gaussian set — render requests for several resident
+ * scenes — forward only, in one launch sequence: per-view preprocess and
+ * capacity-bounded binning, then one persistent blend over every view's
+ * tiles.  `g` points to nviews Gaussian sets (g[v] is rendered by view v).
+ * No host synchronisation; the state holds no adjoint scratch.
+ * ---------------------------------------------------------------------- */
+size_t dmgs_multi_state_bytes(const DmgsBatch *b, const DmgsGaussians *g);
+int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *state,
+                      size_t state_bytes, dmgs_stream_t stream);
+/* Enqueues on `stream` the copy of view v's status word and instance count
+ * into host_words[2v] and host_words[2v+1] (host memory, pinned for the copy
+ * to stay asynchronous); read them once the stream has passed this point.
+ * Status bits: 1 prefiltered point culled, 2 capacity overflow (the view
+ * rendered background; the count is the capacity it needs), 4 index out of
+ * its buffer. */
+int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
+                            const void *state, size_t state_bytes,
+                            uint32_t *host_words, dmgs_stream_t stream);
+
 /* Frustum test (replaces `mark_visible`): present[i] = 1 iff point i lies in
  * front of view-space z = 0.2.  present: [P] uint8 device. */
 int dmgs_mark_visible(int32_t P, const float *means3D, const float *viewmatrix,

@@ -1,0 +1,131 @@
+"""Serving scheduler on the CPU with a fake device backend and a fake clock:
+FIFO admission under the HBM budget and the slot limit, waves of at most
+16 requests, overlap of waves in flight, and re-admission of a request whose
+instance list overflowed with the exact count the device reported."""
+import pytest
+
+from dmgs_gb300.serving import CapacityEstimator, Request, Scheduler, poisson_trace
+
+
+class View:
+    def __init__(self, w, h):
+        self.width, self.height = w, h
+
+
+class FakeClock:
+    def __init__(self):
+        self.t = 0.0
+
+    def __call__(self):
+        return self.t
+
+    def idle(self):
+        self.t += 1e-4
+
+
+class FakeBackend:
+    """A wave completes `delay` seconds after launch; request r needs K(r)
+    instances and overflows when its capacity is smaller."""
+
+    def __init__(self, clock, delay=2e-3, bytes_per_pixel=10, K=lambda r: 1000 + 10 * r.scene):
+        self.clock, self.delay, self.bpp, self.K = clock, delay, bytes_per_pixel, K
+        self.launched, self.live_bytes, self.peak_live = [], 0, 0
+        self.concurrent, self.peak_concurrent = 0, 0
+
+    def footprint(self, r, cap):
+        return self.bpp * r.view.width * r.view.height + 4 * cap
+
+    def launch(self, reqs, caps, stream):
+        nb = sum(self.footprint(r, c) for r, c in zip(reqs, caps))
+        self.live_bytes += nb
+        self.peak_live = max(self.peak_live, self.live_bytes)
+        self.concurrent += 1
+        self.peak_concurrent = max(self.peak_concurrent, self.concurrent)
+        h = {"t": self.clock(), "reqs": list(reqs), "caps": list(caps), "bytes": nb, "stream": stream}
+        self.launched.append(h)
+        return h
+
+    def ready(self, h):
+        return self.clock() >= h["t"] + self.delay
+
+    def results(self, h):
+        out = []
+        for r, c in zip(h["reqs"], h["caps"]):
+            k = self.K(r)
+            out.append((2 if k > c else 0, k))
+            r.result = ("img", r.rid)
+        return out
+
+    def release(self, h):
+        self.live_bytes -= h["bytes"]
+        self.concurrent -= 1
+
+
+def _reqs(n, t_step=1e-3, res=(64, 64), scenes=3):
+    return [Request(i, i % scenes, View(*res), i * t_step) for i in range(n)]
+
+
+def _sched(be, clk, **kw):
+    est = kw.pop("estimator", CapacityEstimator(margin=1.0, slack=0, default=lambda r: 10**6))
+    return Scheduler(be, clock=clk, idle=clk.idle, estimator=est, **kw)
+
+
+def test_all_served_in_arrival_order_within_budget():
+    clk = FakeClock()
+    be = FakeBackend(clk)
+    reqs = _reqs(200)
+    budget = 5 * be.footprint(reqs[0], 10**6)
+    st = _sched(be, clk, budget_bytes=budget).run(reqs)
+    assert all(r.t_done >= r.arrival and r.result == ("img", r.rid) for r in reqs)
+    admits = [r.t_admit for r in sorted(reqs, key=lambda r: r.arrival)]
+    assert admits == sorted(admits)  # FIFO: never admitted ahead of an earlier arrival
+    assert be.peak_live <= budget
+    s = st.summary()
+    assert s["requests"] == 200 and s["retries"] == 0 and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_bursts_are_batched_into_waves_of_at_most_16_and_overlap():
+    clk = FakeClock()
+    be = FakeBackend(clk, delay=5e-3)
+    reqs = [Request(i, i % 4, View(32, 32), 0.0) for i in range(40)]  # one burst
+    st = _sched(be, clk, budget_bytes=10**12, max_inflight=64, n_streams=4).run(reqs)
+    sizes = [len(h["reqs"]) for h in be.launched]
+    assert sizes == [16, 16, 8] and st.waves == 3
+    assert be.peak_concurrent == 3  # all three waves in flight at once
+    assert {h["stream"] for h in be.launched} == {0, 1, 2}
+
+
+def test_slot_limit_bounds_requests_in_flight():
+    clk = FakeClock()
+    be = FakeBackend(clk, delay=5e-3)
+    reqs = [Request(i, 0, View(32, 32), 0.0) for i in range(30)]
+    st = _sched(be, clk, budget_bytes=10**12, max_inflight=8).run(reqs)
+    assert st.peak_inflight == 8 and all(len(h["reqs"]) <= 8 for h in be.launched)
+
+
+def test_overflow_is_retried_with_the_reported_count():
+    clk = FakeClock()
+    be = FakeBackend(clk, K=lambda r: 5000)
+    est = CapacityEstimator(margin=1.0, slack=0, default=lambda r: 100)  # too small at first
+    reqs = _reqs(10, t_step=1e-2, scenes=1)
+    st = _sched(be, clk, budget_bytes=10**9, estimator=est).run(reqs)
+    assert st.retries == 1  # the first request; later ones use the observed count
+    assert reqs[0].attempts == 2 and all(r.attempts == 1 for r in reqs[1:])
+    assert [c for h in be.launched for c in h["caps"]][:2] == [100, 5000]
+    assert all(r.result is not None for r in reqs)
+
+
+def test_request_above_the_budget_is_refused():
+    clk = FakeClock()
+    be = FakeBackend(clk)
+    with pytest.raises(RuntimeError, match="above the budget"):
+        _sched(be, clk, budget_bytes=100).run(_reqs(2))
+
+
+def test_poisson_trace_rate_and_mix():
+    reqs = poisson_trace(200.0, 5.0, 8, [(256, 256), (800, 800)], seed=3,
+                         view_fn=lambda rng, w, h: View(w, h))
+    assert 850 < len(reqs) < 1150
+    assert sorted(r.arrival for r in reqs) == [r.arrival for r in reqs]
+    assert {r.scene for r in reqs} == set(range(8))
+    assert {(r.view.width, r.view.height) for r in reqs} == {(256, 256), (800, 800)}
