@@ -57,6 +57,11 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the one-view-per-call leg")
     ap.add_argument("--no-tune", action="store_true", help="use the default blend configuration")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop leg")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="requests per second")
+    ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of in-flight requests")
+    ap.add_argument("--serve-burst", type=int, default=800, help="requests of the saturation run")
     return ap.parse_args()
 
 
@@ -182,6 +187,55 @@ def cpu_oracle_sample(scene, view, n_tiles):
 
 
 # ----------------------------------------------------------------------------
+SERVE_SIZES = [200_000, 500_000, 1_000_000, 1_000_000, 2_000_000, 2_000_000, 3_000_000, 3_000_000]
+SERVE_RES = [(256, 256), (800, 800), (1237, 822), (1920, 1080)]
+
+
+def serving_leg(args, dev):
+    """Serving loop: 8 resident scenes (the large-scene generator, on the
+    device), Poisson arrivals at --serve-rate for --serve-seconds, scene and
+    resolution uniform; continuous batching (waves over 4 streams, HBM-budget
+    admission) against one-at-a-time plain rendering of the same trace.  A
+    saturation run (--serve-burst requests at t=0) gives each mode's
+    throughput capacity.  Latency = arrival to the image in host memory."""
+    import copy
+
+    from dmgs_gb300.scenes import large_scene_tensors
+    from dmgs_gb300.serving import (GpuBackend, PlainBackend, Request, ResidentScene, Scheduler,
+                                    poisson_trace, profile_capacity)
+    scenes = [ResidentScene(large_scene_tensors(P, 100 + i, dev)) for i, P in enumerate(SERVE_SIZES)]
+    est = profile_capacity(scenes, SERVE_RES, n_views=4, seed=5)
+    budget = int(args.serve_budget_gb * (1 << 30))
+    trace = poisson_trace(args.serve_rate, args.serve_seconds, len(scenes), SERVE_RES, seed=7)
+    burst = [Request(i, r.scene, r.view, 0.0)
+             for i, r in enumerate(poisson_trace(1000.0, args.serve_burst / 1000.0, len(scenes),
+                                                 SERVE_RES, seed=9))]
+    fresh = lambda rs: [Request(r.rid, r.scene, r.view, r.arrival) for r in rs]  # noqa: E731
+    out = {"scenes_gaussians": SERVE_SIZES, "resolutions": SERVE_RES, "rate_per_s": args.serve_rate,
+           "seconds": args.serve_seconds, "requests": len(trace), "budget_gb": args.serve_budget_gb,
+           "latency": "arrival to image in pinned host memory"}
+    gb = GpuBackend(scenes, arena_bytes=budget, n_streams=4)
+    warm = poisson_trace(args.serve_rate, 1.0, len(scenes), SERVE_RES, seed=8)
+    Scheduler(gb, budget, estimator=copy.deepcopy(est)).run(warm, deliver=gb.recycle)
+    st = Scheduler(gb, budget, estimator=copy.deepcopy(est)).run(fresh(trace), deliver=gb.recycle)
+    out["batched"] = st.summary()
+    st = Scheduler(gb, budget, estimator=copy.deepcopy(est)).run(fresh(burst), deliver=gb.recycle)
+    out["batched_saturated"] = st.summary()
+    pb = PlainBackend(scenes)
+    one = dict(max_wave=1, max_inflight=1, n_streams=1)
+    Scheduler(pb, budget, **one).run(fresh(warm), deliver=pb.recycle)
+    st = Scheduler(pb, budget, **one).run(fresh(trace), deliver=pb.recycle)
+    out["plain"] = st.summary()
+    st = Scheduler(pb, budget, **one).run(fresh(burst), deliver=pb.recycle)
+    out["plain_saturated"] = st.summary()
+    for k in ("plain", "plain_saturated"):
+        out[k].pop("peak_bytes", None)
+    out["saturated_ratio_batched_over_plain"] = (out["batched_saturated"]["views_per_s"] /
+                                                 out["plain_saturated"]["views_per_s"])
+    del scenes, gb, pb
+    return out
+
+
 def bytes_model(name, P, V, K, npix, nviews=1):
     """Algorithmic DRAM bytes per launch (SH3, scale/rotation inputs).  For
     a batched launch V, K, npix are sums over the views."""
@@ -431,6 +485,16 @@ def main():
                "d2h_bytes_per_step": int(d2h), "steps": n_e2e, "views_per_step": nv,
                "api": "dmgs_gb300.batched.BatchedRasterizer, pinned host buffers"}
 
+    br_cfg = br.cfg
+    serving = None
+    if not args.no_serve:
+        del br
+        torch.cuda.empty_cache()
+        clocks_s = ClockSampler(local)
+        clocks_s.start()
+        serving = serving_leg(args, dev)
+        serving["clocks"] = clocks_s.stop()
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         est, desc = cpu_oracle_sample(scene, scene.views[0], args.cpu_tiles)
@@ -451,12 +515,13 @@ def main():
                        "outputs": "images, parameter gradients summed over views, densification "
                                   "statistics (fused add_densification_stats)",
                        "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
-                       "blend_config": {"pixels_per_thread": br.cfg[0], "gaussians_per_batch": br.cfg[1]},
+                       "blend_config": {"pixels_per_thread": br_cfg[0], "gaussians_per_batch": br_cfg[1]},
                        "graph": not args.no_graph},
             "plain": plain,
             "mixed": mixed,
             "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+            "serving": serving,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))
     if world > 1:

@@ -87,11 +87,12 @@ SIGNATURES = [
                                           C.POINTER(vp), vp, vp, vp]),
     ("dmgs_batch_status", C.c_int, [C.POINTER(DmgsBatch), C.c_int32, vp, C.c_size_t,
                                     C.POINTER(C.c_int64), vp]),
-    ("dmgs_multi_state_bytes", C.c_size_t, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians)]),
-    ("dmgs_render_multi", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians), vp, C.c_size_t,
-                                    vp]),
-    ("dmgs_multi_status_async", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians), vp,
-                                          C.c_size_t, vp, vp]),
+    ("dmgs_multi_view_state_bytes", C.c_size_t, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians),
+                                                 C.c_int64]),
+    ("dmgs_render_multi", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians), C.POINTER(vp),
+                                    C.POINTER(C.c_size_t), vp, vp]),
+    ("dmgs_multi_status_async", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians),
+                                          C.POINTER(vp), C.POINTER(C.c_size_t), vp, vp]),
     ("dmgs_mark_visible", C.c_int, [C.c_int32, vp, vp, vp, vp, vp]),
     ("dmgs_debug_geometry", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, C.c_size_t, vp, vp,
                                       vp, vp, vp, vp, vp]),

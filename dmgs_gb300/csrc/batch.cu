@@ -29,6 +29,20 @@ struct BatchLayout {
   size_t queue, total;
 };
 
+// Layout of one view's state starting at offset o; returns the end offset.
+size_t view_layout(const DmgsView &view, int P, int64_t cap, bool with_adjoint, size_t o,
+                   ViewLayout &V) {
+  V.G = geom_layout(P, view.width, view.height);
+  V.B = bin_layout(cap, view.width, view.height);
+  V.I = img_layout(view.width, view.height);
+  V.geom = o;  o = align_up(o + V.G.total, 256);
+  V.bin = o;   o = align_up(o + V.B.total, 256);
+  V.img = o;   o = align_up(o + V.I.total, 256);
+  V.gacc = o;  o = align_up(o + (with_adjoint ? bwd_scratch_bytes(P) : 0), 256);
+  V.radii = o; o = align_up(o + (size_t)P * 4 + 4, 256);
+  return o;
+}
+
 // Pv: the Gaussian count of every view (nullptr: P for all); with_adjoint:
 // reserve the 2D-gradient accumulators of the backward.
 int make_layout(const DmgsBatch *b, int P, BatchLayout &L, const int32_t *Pv = nullptr,
@@ -55,15 +69,7 @@ int make_layout(const DmgsBatch *b, int P, BatchLayout &L, const int32_t *Pv = n
       set_error("batch: view %d capacity out of range", v);
       return DMGS_ERR_ARG;
     }
-    ViewLayout &V = L.v[v];
-    V.G = geom_layout(P, view.width, view.height);
-    V.B = bin_layout(cap, view.width, view.height);
-    V.I = img_layout(view.width, view.height);
-    V.geom = o;  o = align_up(o + V.G.total, 256);
-    V.bin = o;   o = align_up(o + V.B.total, 256);
-    V.img = o;   o = align_up(o + V.I.total, 256);
-    V.gacc = o;  o = align_up(o + (with_adjoint ? bwd_scratch_bytes(P) : 0), 256);
-    V.radii = o; o = align_up(o + (size_t)P * 4 + 4, 256);
+    o = view_layout(view, P, cap, with_adjoint, o, L.v[v]);
   }
   L.queue = o;
   o = align_up(o + 64, 256);
@@ -162,10 +168,22 @@ BlendCfg cfg_of(const DmgsBatch *b) {
   return c;
 }
 
-void fill_views(const DmgsBatch *b, const BatchLayout &L, char *st, BatchViews &bv) {
+struct SameBase {
+  char *p[MAX_BATCH_VIEWS];
+  operator char *const *() const { return p; }
+};
+SameBase same_base(char *st) {
+  SameBase b;
+  for (int v = 0; v < MAX_BATCH_VIEWS; ++v) b.p[v] = st;
+  return b;
+}
+
+// base[v]: the buffer view v's layout offsets are relative to.
+void fill_views(const DmgsBatch *b, const BatchLayout &L, char *const *base, BatchViews &bv) {
   bv.nviews = b->nviews;
   for (int v = 0; v < b->nviews; ++v) {
     const ViewLayout &V = L.v[v];
+    char *st = base[v];
     char *geom = st + V.geom;
     BatchView &o = bv.v[v];
     o.vp = params_of(&b->views[v]);
@@ -182,11 +200,12 @@ void fill_views(const DmgsBatch *b, const BatchLayout &L, char *st, BatchViews &
   }
 }
 
-void fill_blend(const DmgsBatch *b, const BatchLayout &L, char *st, BlendBatch &bb) {
+void fill_blend(const DmgsBatch *b, const BatchLayout &L, char *const *bases, BlendBatch &bb) {
   bb.nviews = b->nviews;
   int base = 0;
   for (int v = 0; v < b->nviews; ++v) {
     const ViewLayout &V = L.v[v];
+    char *st = bases[v];
     char *geom = st + V.geom, *bin = st + V.bin, *img = st + V.img;
     BlendView &o = bb.v[v];
     o.W = b->views[v].width;
@@ -226,7 +245,7 @@ extern "C" int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   char *st = static_cast<char *>(state);
   BatchViews bv;
-  fill_views(b, L, st, bv);
+  fill_views(b, L, same_base(st), bv);
   RET_IF(launch_preprocess_batched(bv, gptrs_of(g), s));
   for (int v = 0; v < b->nviews; ++v) {
     const ViewLayout &V = L.v[v];
@@ -234,7 +253,7 @@ extern "C" int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *
     RET_IF(launch_emit(V.G, st + V.geom, V.B, st + V.bin, b->capacity[v], s));
   }
   BlendBatch bb;
-  fill_blend(b, L, st, bb);
+  fill_blend(b, L, same_base(st), bb);
   uint32_t *queue = reinterpret_cast<uint32_t *>(st + L.queue);
   DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));
   RET_IF(launch_blend_batch_fwd(bb, cfg_of(b), queue, s));
@@ -258,7 +277,7 @@ extern "C" int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   char *st = static_cast<char *>(state);
   BlendBatch bb;
-  fill_blend(b, L, st, bb);
+  fill_blend(b, L, same_base(st), bb);
   for (int v = 0; v < b->nviews; ++v) {
     bb.v[v].dL_dout = dL_dout_color[v];
     DMGS_CUDA(cudaMemsetAsync(bb.v[v].gacc, 0, (size_t)g->P * 48, s));
@@ -267,7 +286,7 @@ extern "C" int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *
   DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));
   RET_IF(launch_blend_batch_bwd(bb, cfg_of(b), queue, s));
   BatchViews bv;
-  fill_views(b, L, st, bv);
+  fill_views(b, L, same_base(st), bv);
   for (int v = 0; v < b->nviews; ++v) bv.v[v].dL_dmeans2D = dL_dmeans2D ? dL_dmeans2D[v] : nullptr;
   RET_IF(launch_preprocess_bwd_batched(bv, gptrs_of(g), *grads, densify_accum, densify_count, s));
   return DMGS_OK;
@@ -305,75 +324,86 @@ extern "C" int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *stat
 
 // ---------------------------------------------------------------------------
 // Serving form: every view renders its own Gaussian set (requests for
-// several resident scenes in one launch sequence), forward only.
+// several resident scenes in one launch sequence), forward only, each view
+// in its own state buffer (requests are placed independently in an arena).
 // ---------------------------------------------------------------------------
 
 namespace {
 
-int multi_layout(const DmgsBatch *b, const DmgsGaussians *g, BatchLayout &L) {
-  if (!g) { set_error("multi: gaussians is NULL"); return DMGS_ERR_ARG; }
-  if (!b || b->nviews < 1 || b->nviews > MAX_BATCH_VIEWS) {
-    set_error("multi: nviews must be 1..%d", MAX_BATCH_VIEWS);
+int multi_check(const DmgsBatch *b, const DmgsGaussians *g, void *const *state,
+                const size_t *state_bytes, BatchLayout &L) {
+  if (!g || !state || !state_bytes) {
+    set_error("multi: gaussians, state or state_bytes is NULL");
     return DMGS_ERR_ARG;
   }
-  int32_t P[MAX_BATCH_VIEWS];
-  for (int v = 0; v < b->nviews; ++v) P[v] = g[v].P;
-  return make_layout(b, 0, L, P, false);
+  if (!b || b->nviews < 1 || b->nviews > MAX_BATCH_VIEWS || !b->views || !b->capacity) {
+    set_error("multi: nviews must be 1..%d with views and capacity arrays", MAX_BATCH_VIEWS);
+    return DMGS_ERR_ARG;
+  }
+  L.n = b->nviews;
+  for (int v = 0; v < b->nviews; ++v) {
+    RET_IF(check_view(b->views[v], v));
+    RET_IF(check_gaussians(&g[v], b->views[v], v));
+    const int64_t cap = b->capacity[v];
+    if (cap < 0 || cap > 0xfffffffell || b->views[v].width <= 0 || b->views[v].height <= 0) {
+      set_error("multi: view %d has an invalid size or capacity", v);
+      return DMGS_ERR_ARG;
+    }
+    const size_t need = view_layout(b->views[v], g[v].P, cap, false, 0, L.v[v]);
+    if (!state[v] || state_bytes[v] < need) {
+      set_error("multi: state of view %d too small: %zu < %zu bytes", v, state_bytes[v], need);
+      return DMGS_ERR_STATE;
+    }
+  }
+  return DMGS_OK;
 }
 
 }  // namespace
 
-extern "C" size_t dmgs_multi_state_bytes(const DmgsBatch *b, const DmgsGaussians *g) {
-  BatchLayout L;
-  if (multi_layout(b, g, L) != DMGS_OK) return 0;
-  return L.total;
+extern "C" size_t dmgs_multi_view_state_bytes(const DmgsView *view, const DmgsGaussians *g,
+                                              int64_t capacity) {
+  if (!view || !g || g->P < 0 || capacity < 0 || view->width <= 0 || view->height <= 0) return 0;
+  ViewLayout V;
+  return view_layout(*view, g->P, capacity, false, 0, V);
 }
 
-extern "C" int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *state,
-                                 size_t state_bytes, dmgs_stream_t stream) {
+extern "C" int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *const *state,
+                                 const size_t *state_bytes, uint32_t *queue,
+                                 dmgs_stream_t stream) {
   BatchLayout L;
-  RET_IF(multi_layout(b, g, L));
-  if (!state || state_bytes < L.total) {
-    set_error("multi: state too small: %zu < %zu bytes", state_bytes, L.total);
-    return DMGS_ERR_STATE;
-  }
-  if (!b->out_color) { set_error("multi: out_color is NULL"); return DMGS_ERR_ARG; }
-  for (int v = 0; v < b->nviews; ++v) {
-    RET_IF(check_view(b->views[v], v));
-    RET_IF(check_gaussians(&g[v], b->views[v], v));
+  RET_IF(multi_check(b, g, state, state_bytes, L));
+  if (!b->out_color || !queue) { set_error("multi: out_color or queue is NULL"); return DMGS_ERR_ARG; }
+  for (int v = 0; v < b->nviews; ++v)
     if (!b->out_color[v]) { set_error("multi: out_color[%d] is NULL", v); return DMGS_ERR_ARG; }
-  }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  char *st = static_cast<char *>(state);
+  char *const *base = reinterpret_cast<char *const *>(state);
   BatchViews bv;
-  fill_views(b, L, st, bv);
+  fill_views(b, L, base, bv);
   for (int v = 0; v < b->nviews; ++v) {
     const ViewLayout &V = L.v[v];
     const BatchView &o = bv.v[v];
     RET_IF(launch_preprocess(o.vp, o.viewm, o.projm, o.campos, gptrs_of(&g[v]), o.radii, V.G,
-                             st + V.geom, s));
-    RET_IF(launch_binning_geometry(V.G, st + V.geom, (uint32_t)b->capacity[v], s));
-    RET_IF(launch_emit(V.G, st + V.geom, V.B, st + V.bin, b->capacity[v], s));
+                             base[v] + V.geom, s));
+    RET_IF(launch_binning_geometry(V.G, base[v] + V.geom, (uint32_t)b->capacity[v], s));
+    RET_IF(launch_emit(V.G, base[v] + V.geom, V.B, base[v] + V.bin, b->capacity[v], s));
   }
   BlendBatch bb;
-  fill_blend(b, L, st, bb);
-  uint32_t *queue = reinterpret_cast<uint32_t *>(st + L.queue);
+  fill_blend(b, L, base, bb);
   DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));
   RET_IF(launch_blend_batch_fwd(bb, cfg_of(b), queue, s));
   return DMGS_OK;
 }
 
 extern "C" int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
-                                       const void *state, size_t state_bytes,
+                                       void *const *state, const size_t *state_bytes,
                                        uint32_t *host_words, dmgs_stream_t stream) {
   BatchLayout L;
-  RET_IF(multi_layout(b, g, L));
-  if (!state || state_bytes < L.total) { set_error("multi: state too small"); return DMGS_ERR_STATE; }
+  RET_IF(multi_check(b, g, state, state_bytes, L));
   if (!host_words) { set_error("multi: host_words is NULL"); return DMGS_ERR_ARG; }
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const char *st = static_cast<const char *>(state);
   for (int v = 0; v < b->nviews; ++v)  // words CI_STATUS, CI_K
-    DMGS_CUDA(cudaMemcpyAsync(host_words + 2 * v, st + L.v[v].geom + L.v[v].G.counters, 8,
-                              cudaMemcpyDeviceToHost, s));
+    DMGS_CUDA(cudaMemcpyAsync(host_words + 2 * v,
+                              static_cast<const char *>(state[v]) + L.v[v].geom + L.v[v].G.counters,
+                              8, cudaMemcpyDeviceToHost, s));
   return DMGS_OK;
 }

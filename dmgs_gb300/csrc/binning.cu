@@ -384,7 +384,8 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
   const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
   const uint64_t keep = l2_policy_last();
   if (EMIT) {
-    if (s0 >= s1) return;
+    // an overflowed view (instances above the list capacity) emits nothing
+    if (s0 >= s1 || (counters[CI_STATUS] & ST_OVERFLOW)) return;
     const uint64_t once = l2_policy_first();
     int i = lane;
     for (; i + 96 < nt; i += 128) {

@@ -15,8 +15,11 @@ the queue with the exact count the device reported.  Memory is accounted per
 request (its state bytes plus its image), released when its wave completes.
 
 The scheduler is independent of the device: :class:`Scheduler` drives a
-backend (``footprint``/``launch``/``ready``/``results``/``release``), so its
-admission, ordering and retry logic is tested on the CPU with a fake one.
+backend (``footprint``/``reserve``/``launch``/``ready``/``results``/
+``release``), so its admission, ordering and retry logic is tested on the CPU
+with a fake one.  The GPU backend places every admitted request's state and
+image in one device arena allocated up front (first fit, coalescing frees),
+so serving does no device allocation.
 """
 from __future__ import annotations
 
@@ -42,6 +45,7 @@ class Request:
     t_admit: float = -1.0
     t_done: float = -1.0
     result: object = None  # the image (host copy when the backend copies out)
+    blocks: object = None  # backend placement while admitted
 
     @property
     def key(self):
@@ -111,7 +115,7 @@ class Scheduler:
     rotate over this many streams.  `clock()` returns seconds; `idle()` is
     called when there is nothing to do (the real loop sleeps briefly)."""
 
-    def __init__(self, backend, budget_bytes, max_inflight=64, max_wave=16, n_streams=4,
+    def __init__(self, backend, budget_bytes, max_inflight=64, max_wave=16, n_streams=None,
                  estimator=None, clock=time.perf_counter, idle=None):
         if not 1 <= max_wave <= 16:
             raise ValueError("a wave holds 1..16 requests")
@@ -119,7 +123,7 @@ class Scheduler:
         self.budget = int(budget_bytes)
         self.max_inflight = max_inflight
         self.max_wave = max_wave
-        self.n_streams = n_streams
+        self.n_streams = n_streams or getattr(backend, "n_streams", 4)
         self.estimator = estimator or CapacityEstimator()
         self.clock = clock
         self.idle = idle or (lambda: time.sleep(50e-6))
@@ -177,6 +181,10 @@ class Scheduler:
                 if fb > self.budget:
                     raise RuntimeError(f"request {r.rid} needs {fb} bytes, above the budget")
                 if used + wbytes + fb > self.budget:
+                    break
+                if not be.reserve(r, cap):  # the backend could not place it (fragmentation)
+                    if n_in == 0 and not wave:
+                        raise RuntimeError(f"request {r.rid} cannot be placed in the backend's memory")
                     break
                 pending.popleft()
                 r.capacity = cap
@@ -237,6 +245,54 @@ class _PinnedPool:
         self.free.setdefault(buf.numel(), []).append(buf)
 
 
+class DeviceArena:
+    """One device buffer carved into 256-byte-aligned blocks: first fit over
+    an offset-sorted free list, neighbours coalesced on release."""
+
+    ALIGN = 256
+
+    def __init__(self, nbytes, device):
+        import torch
+        self.size = int(nbytes) // self.ALIGN * self.ALIGN
+        self.buf = torch.empty(self.size, dtype=torch.uint8, device=device)
+        self.base = self.buf.data_ptr()
+        self.free = [(0, self.size)]
+        self.used = 0
+
+    def _round(self, n):
+        return (int(n) + self.ALIGN - 1) // self.ALIGN * self.ALIGN
+
+    def alloc(self, n):
+        n = self._round(max(int(n), 1))
+        for i, (o, sz) in enumerate(self.free):
+            if sz >= n:
+                if sz == n:
+                    del self.free[i]
+                else:
+                    self.free[i] = (o + n, sz - n)
+                self.used += n
+                return o
+        return None
+
+    def release(self, o, n):
+        import bisect
+        n = self._round(max(int(n), 1))
+        self.used -= n
+        i = bisect.bisect_left(self.free, (o, 0))
+        self.free.insert(i, (o, n))
+        if i + 1 < len(self.free) and o + n == self.free[i + 1][0]:  # merge right
+            self.free[i] = (o, n + self.free[i + 1][1])
+            del self.free[i + 1]
+        if i > 0 and self.free[i - 1][0] + self.free[i - 1][1] == o:  # merge left
+            self.free[i - 1] = (self.free[i - 1][0], self.free[i - 1][1] + self.free[i][1])
+            del self.free[i]
+
+    def tensor(self, o, n, dtype, shape):
+        import torch
+        esz = torch.tensor([], dtype=dtype).element_size()
+        return self.buf[o:o + n * esz].view(dtype).view(*shape)
+
+
 class ResidentScene:
     """A scene kept on the device: the reference's tensors (means3D,
     opacities, shs, scales, rotations) and the C-ABI view of them."""
@@ -255,56 +311,70 @@ class ResidentScene:
 
 
 class GpuBackend:
-    """Waves rendered by dmgs_render_multi on a set of streams; camera
-    constants go up in one copy per wave, status words (and, with
-    copy_out, the images) come back into pinned host memory."""
+    """Waves rendered by dmgs_render_multi on a set of streams.  Each
+    admitted request holds two arena blocks (its state and its image) from
+    reserve() until its wave is released; camera constants go up in one copy
+    per wave, status words (and, with copy_out, the images) come back into
+    pinned host memory."""
 
     CAM = 16 + 16 + 3 + 3  # view matrix, full projection, campos, background
 
-    def __init__(self, scenes, n_streams=4, cfg=(4, 128), copy_out=True, device=None):
+    def __init__(self, scenes, arena_bytes=8 << 30, n_streams=4, cfg=(4, 128), copy_out=True,
+                 device=None, max_waves=256):
         import torch
         from . import _lib
         self.torch, self._lib = torch, _lib
         self.lib = _lib.load()
         self.scenes = scenes
         self.device = device or torch.device("cuda")
+        self.arena = DeviceArena(arena_bytes, self.device)
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(n_streams)]
+        self.n_streams = n_streams
         self.cfg = cfg
         self.copy_out = copy_out
         self.f32 = _PinnedPool(torch, torch.float32)
         self.u32 = _PinnedPool(torch, torch.int32)
-        self._fp_cache = {}
+        self.queues = torch.zeros(max_waves * 64, dtype=torch.int32, device=self.device)
+        self.free_queues = list(range(max_waves))
+        self._sb_cache = {}
 
-    def _batch(self, reqs, caps, cam_dev, outs):
-        L = self._lib
-        n = len(reqs)
-        views = (L.DmgsView * n)()
-        base = cam_dev.data_ptr()
-        for i, r in enumerate(reqs):
-            v = r.view
-            o = base + 4 * i * self.CAM
-            views[i] = L.DmgsView(v.width, v.height, float(v.tanfovx), float(v.tanfovy), 1.0,
-                                  self.scenes[r.scene].sh_degree, 0, 0, o + 4 * 35, o, o + 4 * 16,
-                                  o + 4 * 32)
-        out = (C.c_void_p * n)(*[t.data_ptr() if t is not None else 0 for t in outs]) if outs else None
-        capa = (C.c_int64 * n)(*caps)
-        gauss = (L.DmgsGaussians * n)(*[self.scenes[r.scene].gauss for r in reqs])
-        b = L.DmgsBatch(n, views, out, None, capa, self.cfg[0], self.cfg[1])
-        return b, gauss, (views, out, capa)
+    def _view(self, r, cam_ptr):
+        v = r.view
+        return self._lib.DmgsView(v.width, v.height, float(v.tanfovx), float(v.tanfovy), 1.0,
+                                  self.scenes[r.scene].sh_degree, 0, 0, cam_ptr + 4 * 35, cam_ptr,
+                                  cam_ptr + 4 * 16, cam_ptr + 4 * 32)
 
-    def footprint(self, req, cap):
-        key = (req.scene, req.view.width, req.view.height, int(cap))
-        fb = self._fp_cache.get(key)
-        if fb is None:
-            b, gauss, _ = self._batch([req], [cap], self.torch.empty(0), None)
-            b.out_color = None
-            fb = int(self.lib.dmgs_multi_state_bytes(C.byref(b), gauss)) + 12 * req.view.width * req.view.height
-            self._fp_cache[key] = fb
-        return fb
+    def _state_bytes(self, r, cap):
+        key = (r.scene, r.view.width, r.view.height, int(cap))
+        sb = self._sb_cache.get(key)
+        if sb is None:
+            view = self._view(r, 0)
+            sb = int(self.lib.dmgs_multi_view_state_bytes(C.byref(view),
+                                                          C.byref(self.scenes[r.scene].gauss),
+                                                          int(cap)))
+            self._sb_cache[key] = sb
+        return sb
+
+    def footprint(self, r, cap):
+        return self.arena._round(self._state_bytes(r, cap)) + self.arena._round(
+            12 * r.view.width * r.view.height)
+
+    def reserve(self, r, cap):
+        sb = self._state_bytes(r, cap)
+        ib = 12 * r.view.width * r.view.height
+        o1 = self.arena.alloc(sb)
+        if o1 is None:
+            return False
+        o2 = self.arena.alloc(ib)
+        if o2 is None:
+            self.arena.release(o1, sb)
+            return False
+        r.blocks = (o1, sb, o2, ib)
+        return True
 
     def launch(self, reqs, caps, stream):
-        torch = self.torch
-        s = self.streams[stream]
+        torch, L = self.torch, self._lib
+        s = self.streams[stream % len(self.streams)]
         n = len(reqs)
         cam_host = self.f32.get(n * self.CAM)
         ch = cam_host.numpy().reshape(n, self.CAM)
@@ -315,18 +385,28 @@ class GpuBackend:
             ch[i, 32:35] = v.campos
             ch[i, 35:38] = 0.0
         status = self.u32.get(2 * n)
+        q = self.free_queues.pop()
+        ar = self.arena
         with torch.cuda.stream(s):
             cam_dev = torch.empty(n * self.CAM, device=self.device)
             cam_dev.copy_(cam_host, non_blocking=True)
-            images = [torch.empty(3, r.view.height, r.view.width, device=self.device) for r in reqs]
-            b, gauss, keep = self._batch(reqs, caps, cam_dev, images)
-            nbytes = int(self.lib.dmgs_multi_state_bytes(C.byref(b), gauss))
-            state = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
-            self._lib.check(self.lib.dmgs_render_multi(C.byref(b), gauss, state.data_ptr(), nbytes,
-                                                       s.cuda_stream), "render_multi")
-            self._lib.check(self.lib.dmgs_multi_status_async(C.byref(b), gauss, state.data_ptr(),
-                                                             nbytes, status.data_ptr(),
-                                                             s.cuda_stream), "multi_status")
+            base = cam_dev.data_ptr()
+            views = (L.DmgsView * n)(*[self._view(r, base + 4 * i * self.CAM)
+                                       for i, r in enumerate(reqs)])
+            images = [ar.tensor(r.blocks[2], 3 * r.view.width * r.view.height, torch.float32,
+                                (3, r.view.height, r.view.width)) for r in reqs]
+            out = (C.c_void_p * n)(*[im.data_ptr() for im in images])
+            states = (C.c_void_p * n)(*[ar.base + r.blocks[0] for r in reqs])
+            sizes = (C.c_size_t * n)(*[r.blocks[1] for r in reqs])
+            capa = (C.c_int64 * n)(*caps)
+            gauss = (L.DmgsGaussians * n)(*[self.scenes[r.scene].gauss for r in reqs])
+            b = L.DmgsBatch(n, views, out, None, capa, self.cfg[0], self.cfg[1])
+            queue = self.queues.data_ptr() + 256 * q
+            L.check(self.lib.dmgs_render_multi(C.byref(b), gauss, states, sizes, queue,
+                                               s.cuda_stream), "render_multi")
+            L.check(self.lib.dmgs_multi_status_async(C.byref(b), gauss, states, sizes,
+                                                     status.data_ptr(), s.cuda_stream),
+                    "multi_status")
             host_imgs = None
             if self.copy_out:
                 host_imgs = [self.f32.get(im.numel()) for im in images]
@@ -334,8 +414,8 @@ class GpuBackend:
                     h.copy_(im.view(-1), non_blocking=True)
             ev = torch.cuda.Event()
             ev.record(s)
-        return {"ev": ev, "status": status, "cam": cam_host, "state": state, "cam_dev": cam_dev,
-                "images": images, "host": host_imgs, "reqs": reqs, "keep": keep}
+        return {"ev": ev, "status": status, "cam": cam_host, "cam_dev": cam_dev, "q": q,
+                "images": images, "host": host_imgs, "reqs": reqs}
 
     def ready(self, h):
         return h["ev"].query()
@@ -348,12 +428,18 @@ class GpuBackend:
             if self.copy_out:
                 r.result = h["host"][i].view(3, r.view.height, r.view.width)
             else:
-                r.result = h["images"][i]
+                r.result = h["images"][i].clone()
         return out
 
     def release(self, h):
+        for r in h["reqs"]:
+            o1, sb, o2, ib = r.blocks
+            self.arena.release(o1, sb)
+            self.arena.release(o2, ib)
+            r.blocks = None
         self.f32.put(h["cam"])
         self.u32.put(h["status"])
+        self.free_queues.append(h["q"])
         h.clear()
 
     def recycle(self, req):
@@ -378,6 +464,9 @@ class PlainBackend:
 
     def footprint(self, req, cap):
         return 1
+
+    def reserve(self, req, cap):
+        return True
 
     def launch(self, reqs, caps, stream):
         import torch

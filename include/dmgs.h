@@ -209,12 +209,18 @@ int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *state,
  * render their own Gaussian set — render requests for several resident
  * scenes — forward only, in one launch sequence: per-view preprocess and
  * capacity-bounded binning, then one persistent blend over every view's
- * tiles.  `g` points to nviews Gaussian sets (g[v] is rendered by view v).
- * No host synchronisation; the state holds no adjoint scratch.
+ * tiles.  `g` points to nviews Gaussian sets (g[v] is rendered by view v);
+ * each view has its own state buffer state[v] of state_bytes[v] >=
+ * dmgs_multi_view_state_bytes(view, g, capacity) bytes (so requests can be
+ * placed independently in a device arena); `queue` is 4 bytes of device
+ * memory for the blend's work counter.  b->radii may be NULL (the state
+ * holds a radii scratch).  No host synchronisation, no adjoint scratch.
  * ---------------------------------------------------------------------- */
-size_t dmgs_multi_state_bytes(const DmgsBatch *b, const DmgsGaussians *g);
-int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *state,
-                      size_t state_bytes, dmgs_stream_t stream);
+size_t dmgs_multi_view_state_bytes(const DmgsView *view, const DmgsGaussians *g,
+                                   int64_t capacity);
+int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *const *state,
+                      const size_t *state_bytes, uint32_t *queue,
+                      dmgs_stream_t stream);
 /* Enqueues on `stream` the copy of view v's status word and instance count
  * into host_words[2v] and host_words[2v+1] (host memory, pinned for the copy
  * to stay asynchronous); read them once the stream has passed this point.
@@ -222,7 +228,7 @@ int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, void *state,
  * rendered background; the count is the capacity it needs), 4 index out of
  * its buffer. */
 int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
-                            const void *state, size_t state_bytes,
+                            void *const *state, const size_t *state_bytes,
                             uint32_t *host_words, dmgs_stream_t stream);
 
 /* Frustum test (replaces `mark_visible`): present[i] = 1 iff point i lies in

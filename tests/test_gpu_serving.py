@@ -42,7 +42,7 @@ def _plain(scene, v):
 
 def _serve(scenes, views, est, **kw):
     reqs = [Request(i, s, v, 0.0) for i, (s, v) in enumerate(views)]
-    st = Scheduler(GpuBackend(scenes, n_streams=3), 1 << 34, estimator=est, **kw).run(reqs)
+    st = Scheduler(GpuBackend(scenes, 1 << 31, n_streams=3), 1 << 31, estimator=est, **kw).run(reqs)
     return reqs, st
 
 
@@ -70,8 +70,8 @@ def test_overflow_retry_gives_the_same_images(scenes):
 def test_poisson_trace_in_real_time(scenes):
     reqs = poisson_trace(400.0, 0.25, len(scenes), RES, seed=2)
     est = profile_capacity(scenes, RES, n_views=2)
-    be = GpuBackend(scenes, n_streams=4)
-    st = Scheduler(be, 1 << 33, estimator=est).run(reqs, deliver=be.recycle)
+    be = GpuBackend(scenes, 1 << 31, n_streams=4)
+    st = Scheduler(be, 1 << 31, estimator=est).run(reqs, deliver=be.recycle)
     s = st.summary()
     assert s["requests"] == len(reqs) > 50
     assert 0 < s["p50_ms"] <= s["p99_ms"] < 1000

@@ -35,6 +35,9 @@ class FakeBackend:
     def footprint(self, r, cap):
         return self.bpp * r.view.width * r.view.height + 4 * cap
 
+    def reserve(self, r, cap):
+        return True
+
     def launch(self, reqs, caps, stream):
         nb = sum(self.footprint(r, c) for r, c in zip(reqs, caps))
         self.live_bytes += nb
@@ -129,3 +132,23 @@ def test_poisson_trace_rate_and_mix():
     assert sorted(r.arrival for r in reqs) == [r.arrival for r in reqs]
     assert {r.scene for r in reqs} == set(range(8))
     assert {(r.view.width, r.view.height) for r in reqs} == {(256, 256), (800, 800)}
+
+
+def test_device_arena_first_fit_and_coalescing():
+    torch = pytest.importorskip("torch")
+    from dmgs_gb300.serving import DeviceArena
+    a = DeviceArena(4096, torch.device("cpu"))
+    x = a.alloc(1000)   # 1024
+    y = a.alloc(100)    # 256
+    z = a.alloc(2000)   # 2048
+    assert (x, y, z) == (0, 1024, 1280) and a.alloc(1024) is None  # 768 left
+    a.release(y, 100)
+    assert a.alloc(300) == 3328 and a.alloc(200) == 1024  # first fit: tail, then the hole
+    assert a.alloc(256) == 3840 and a.alloc(1) is None
+    for o, n in [(1024, 200), (3328, 300), (3840, 256)]:
+        a.release(o, n)
+    a.release(x, 1000)
+    a.release(z, 2000)
+    assert a.free == [(0, 4096)] and a.used == 0
+    t = a.tensor(256, 6, torch.float32, (2, 3))
+    assert t.shape == (2, 3) and t.data_ptr() == a.base + 256
