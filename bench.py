@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the one-view-per-call leg")
     ap.add_argument("--no-tune", action="store_true", help="use the default blend configuration")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop leg")
+    ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-bound training leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="requests per second")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of in-flight requests")
@@ -233,6 +234,63 @@ def serving_leg(args, dev):
     out["saturated_ratio_batched_over_plain"] = (out["batched_saturated"]["views_per_s"] /
                                                  out["plain_saturated"]["views_per_s"])
     del scenes, gb, pb
+    return out
+
+
+def mesh_leg(args, dev):
+    """Configuration 2: one stage-2 training step (binding -> SH colour ->
+    rasteriser with precomputed covariance and colours -> L1 + 0.2 (1 - SSIM)
+    -> backward) on the 45,304-face sphere-union-torus mesh, 6 Gaussians per
+    face, 800x800, 100 hemisphere cameras, targets rendered from a perturbed
+    copy.  Reports steps/s and the binding kernels' achieved GB/s."""
+    import torch
+    from dmgs_gb300 import _lib
+    from dmgs_gb300.meshbound import MeshBoundScene, _gauss_window, sphere_torus_mesh, training_step
+    from dmgs_gb300.scenes import hemisphere_views
+    lib = _lib.load()
+    v, f = sphere_torus_mesh(64)
+    scene = MeshBoundScene(v, f, G=6, seed=0, device=dev)
+    target = MeshBoundScene(v, f, G=6, seed=0, device=dev)
+    gen = torch.Generator(device=dev).manual_seed(11)
+    with torch.no_grad():
+        target.verts.add_(0.005 * torch.randn(target.verts.shape, device=dev, generator=gen))
+        target.features.add_(0.05 * torch.randn(target.features.shape, device=dev, generator=gen))
+    views = hemisphere_views(100, 800, 800, seed=0)
+    bg = torch.zeros(3, device=dev)
+    targets = [target.render(w, bg)[0].detach() for w in views]
+    window = _gauss_window(device=dev)
+    steps = max(args.steps, 20)
+    for i in range(5):
+        training_step(scene, views[i], targets[i], bg, window=window)
+    torch.cuda.synchronize(dev)
+    lib.dmgs_timing_enable(1)
+    _lib.timing_collect()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(steps):
+        training_step(scene, views[i % len(views)], targets[i % len(views)], bg, window=window)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    lib.dmgs_timing_enable(0)
+    kt = _lib.timing_collect()
+    ms = e0.elapsed_time(e1) / steps
+    F, P, Vn = int(f.shape[0]), scene.P, int(v.shape[0])
+    # binding bytes: fwd reads faces (24 B) + 3 vertices (36 B) + per-Gaussian barycentrics
+    # (12 B) and writes xyz + covariance (36 B); bwd reads the same geometry and the 36 B
+    # of gradients per Gaussian and writes 12 B per vertex
+    fwd_bytes = F * (24 + 36) + P * (12 + 36)
+    bwd_bytes = F * (24 + 36) + P * (12 + 36) + Vn * 12
+    out = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "faces": F, "gaussians": P,
+           "resolution": [800, 800], "cameras": len(views), "steps": steps,
+           "loss": "0.8 L1 + 0.2 (1 - SSIM), SSIM and SH colour in torch"}
+    for name, nbytes in (("bind_fwd", fwd_bytes), ("bind_bwd", bwd_bytes)):
+        if name in kt:
+            t = kt[name][0] / kt[name][1]
+            out[name] = {"ms": t, "alg_bytes": nbytes, "achieved_gbs": nbytes / (t * 1e-3) / 1e9}
+    for name in ("preprocess", "blend_fwd", "blend_bwd", "preprocess_bwd"):
+        if name in kt:
+            out.setdefault("kernels_ms", {})[name] = kt[name][0] / kt[name][1]
+    del scene, target, targets
     return out
 
 
@@ -495,6 +553,10 @@ def main():
         serving = serving_leg(args, dev)
         serving["clocks"] = clocks_s.stop()
 
+    mesh = None
+    if not args.no_mesh:
+        mesh = mesh_leg(args, dev)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         est, desc = cpu_oracle_sample(scene, scene.views[0], args.cpu_tiles)
@@ -521,7 +583,7 @@ def main():
             "mixed": mixed,
             "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
-            "serving": serving,
+            "serving": serving, "mesh_training": mesh,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))
     if world > 1:

@@ -247,11 +247,15 @@ extern "C" int dmgs_raster_fwd_batched(const DmgsBatch *b, const DmgsGaussians *
   BatchViews bv;
   fill_views(b, L, same_base(st), bv);
   RET_IF(launch_preprocess_batched(bv, gptrs_of(g), s));
+  BinViews bins;
+  bins.n = b->nviews;
   for (int v = 0; v < b->nviews; ++v) {
     const ViewLayout &V = L.v[v];
-    RET_IF(launch_binning_geometry(V.G, st + V.geom, (uint32_t)b->capacity[v], s));
-    RET_IF(launch_emit(V.G, st + V.geom, V.B, st + V.bin, b->capacity[v], s));
+    RET_IF(make_bin_view(V.G, st + V.geom, (uint32_t)b->capacity[v], st + V.bin + V.B.point_list,
+                         (uint32_t)b->capacity[v], bins.v[v]));
   }
+  RET_IF(launch_binning_geometry(bins, s));
+  RET_IF(launch_emit(bins, s));
   BlendBatch bb;
   fill_blend(b, L, same_base(st), bb);
   uint32_t *queue = reinterpret_cast<uint32_t *>(st + L.queue);
@@ -379,14 +383,18 @@ extern "C" int dmgs_render_multi(const DmgsBatch *b, const DmgsGaussians *g, voi
   char *const *base = reinterpret_cast<char *const *>(state);
   BatchViews bv;
   fill_views(b, L, base, bv);
+  BinViews bins;
+  bins.n = b->nviews;
   for (int v = 0; v < b->nviews; ++v) {
     const ViewLayout &V = L.v[v];
     const BatchView &o = bv.v[v];
     RET_IF(launch_preprocess(o.vp, o.viewm, o.projm, o.campos, gptrs_of(&g[v]), o.radii, V.G,
                              base[v] + V.geom, s));
-    RET_IF(launch_binning_geometry(V.G, base[v] + V.geom, (uint32_t)b->capacity[v], s));
-    RET_IF(launch_emit(V.G, base[v] + V.geom, V.B, base[v] + V.bin, b->capacity[v], s));
+    RET_IF(make_bin_view(V.G, base[v] + V.geom, (uint32_t)b->capacity[v],
+                         base[v] + V.bin + V.B.point_list, (uint32_t)b->capacity[v], bins.v[v]));
   }
+  RET_IF(launch_binning_geometry(bins, s));
+  RET_IF(launch_emit(bins, s));
   BlendBatch bb;
   fill_blend(b, L, base, bb);
   DMGS_CUDA(cudaMemsetAsync(queue, 0, 4, s));

@@ -28,6 +28,10 @@
 // equal Gaussian count would differ in work by an order of magnitude; equal
 // weight keeps one warp per chunk balanced.  The count matrix (T x C x 4 B,
 // 33 MB at 4056 tiles and 2048 chunks) stays in L2.
+//
+// Every kernel bins several views at once (blockIdx.y = view, each view with
+// its own geometry state and sizes): a batch of views fills the GPU with one
+// launch per stage instead of one small launch per stage and view.
 #include <algorithm>
 
 #include "kernels.cuh"
@@ -74,37 +78,40 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long
   return before;
 }
 
-__device__ __forceinline__ uint32_t scan_len(const uint32_t *n_dev, uint32_t n_max) {
-  return n_dev ? min(*n_dev, n_max) : n_max;
+// ---- generic exclusive scan (u32, in place), three phases, per view -----
+
+__device__ __forceinline__ uint32_t scan_len(const ScanView &v) {
+  return v.n_dev ? min(*v.n_dev, v.n_max) : v.n_max;
 }
 
-// ---- generic exclusive scan (u32, in place), three phases ----------------
-
 __global__ void __launch_bounds__(SCAN_THREADS)
-scan_reduce_kernel(const uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev,
-                   uint32_t n_max, uint32_t *__restrict__ part) {
-  const uint32_t n = scan_len(n_dev, n_max);
+scan_reduce_kernel(const ScanViews sv) {
+  const ScanView &v = sv.v[blockIdx.y];
+  const uint32_t n = scan_len(v);
   const uint32_t base = blockIdx.x * SCAN_TILE;
   if (base >= n) return;
   unsigned long long s = 0;
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; ++i) {
     const uint32_t k = base + i * SCAN_THREADS + threadIdx.x;
-    if (k < n) s += data[k];
+    if (k < n) s += v.data[k];
   }
   unsigned long long tot;
   block_exclusive_scan<SCAN_THREADS>(s, &tot);
-  if (threadIdx.x == 0) part[blockIdx.x] = (uint32_t)tot;
+  if (threadIdx.x == 0) v.part[blockIdx.x] = (uint32_t)tot;
 }
 
-// One block: exclusive scan of the per-block partials (or of the whole
-// array when it fits one block); total to *total_out, overflow flagged.
+// One block per view: exclusive scan of the per-block partials (or of the
+// whole array when it fits one block); total to *total_out, overflow flagged.
 __global__ void __launch_bounds__(SCAN_THREADS)
-scan_single_kernel(uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev, uint32_t n_max,
-                   int partials_of_tiles, uint32_t *__restrict__ total_out,
-                   uint32_t *__restrict__ status) {
-  uint32_t n = scan_len(n_dev, n_max);
-  if (partials_of_tiles) n = (n + SCAN_TILE - 1) / SCAN_TILE;
+scan_single_kernel(const ScanViews sv, int partials_of_tiles) {
+  const ScanView &v = sv.v[blockIdx.y];
+  uint32_t n = scan_len(v);
+  uint32_t *data = v.data;
+  if (partials_of_tiles) {
+    n = (n + SCAN_TILE - 1) / SCAN_TILE;
+    data = v.part;
+  }
   const uint32_t per = (n + SCAN_THREADS - 1) / SCAN_THREADS;
   const uint32_t beg = min(n, threadIdx.x * per), end = min(n, beg + per);
   unsigned long long s = 0;
@@ -112,47 +119,47 @@ scan_single_kernel(uint32_t *__restrict__ data, const uint32_t *__restrict__ n_d
   unsigned long long tot;
   unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, &tot);
   for (uint32_t k = beg; k < end; ++k) {
-    const uint32_t v = data[k];
+    const uint32_t x = data[k];
     data[k] = (uint32_t)run;
-    run += v;
+    run += x;
   }
   if (threadIdx.x == 0) {
-    if (total_out) *total_out = (uint32_t)tot;
-    if (tot > 0xffffffffull && status) atomicOr(status, ST_OVERFLOW);
+    if (v.total_out) *v.total_out = (uint32_t)tot;
+    if (tot > 0xffffffffull && v.status) atomicOr(v.status, ST_OVERFLOW);
   }
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS)
-scan_down_kernel(uint32_t *__restrict__ data, const uint32_t *__restrict__ n_dev, uint32_t n_max,
-                 const uint32_t *__restrict__ part) {
-  const uint32_t n = scan_len(n_dev, n_max);
+scan_down_kernel(const ScanViews sv) {
+  const ScanView &v = sv.v[blockIdx.y];
+  const uint32_t n = scan_len(v);
   const uint32_t base = blockIdx.x * SCAN_TILE;
   if (base >= n) return;
   // blocked: thread i owns elements base + i*ITEMS .. +ITEMS-1
-  uint32_t v[SCAN_ITEMS];
+  uint32_t x[SCAN_ITEMS];
   unsigned long long s = 0;
   const uint32_t k0 = base + threadIdx.x * SCAN_ITEMS;
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; ++i) {
-    v[i] = (k0 + i < n) ? data[k0 + i] : 0u;
-    s += v[i];
+    x[i] = (k0 + i < n) ? v.data[k0 + i] : 0u;
+    s += x[i];
   }
-  unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, nullptr) + part[blockIdx.x];
+  unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, nullptr) + v.part[blockIdx.x];
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; ++i) {
-    if (k0 + i < n) data[k0 + i] = (uint32_t)run;
-    run += v[i];
+    if (k0 + i < n) v.data[k0 + i] = (uint32_t)run;
+    run += x[i];
   }
 }
 
 // ---- compaction of visible Gaussians (index order) ----------------------
 
 __global__ void __launch_bounds__(PRE_BLOCK)
-compact_kernel(int P, const uint8_t *__restrict__ flags, const float4 *__restrict__ feat,
-               const uint32_t *__restrict__ blkoff, uint32_t *__restrict__ dkey,
-               uint32_t *__restrict__ dval) {
+compact_kernel(const BinViews bv) {
+  const BinView &B = bv.v[blockIdx.y];
+  if ((int)blockIdx.x >= B.nb_pre) return;
   const int idx = blockIdx.x * PRE_BLOCK + threadIdx.x;
-  const bool v = idx < P && (flags[idx] & FLAG_VISIBLE);
+  const bool v = idx < B.P && (B.flags[idx] & FLAG_VISIBLE);
   __shared__ uint32_t wcount[PRE_BLOCK / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const unsigned b = __ballot_sync(FULL, v);
@@ -161,29 +168,35 @@ compact_kernel(int P, const uint8_t *__restrict__ flags, const float4 *__restric
   uint32_t before = 0;
   for (int w = 0; w < wid; ++w) before += wcount[w];
   if (v) {
-    const uint32_t pos = blkoff[blockIdx.x] + before + __popc(b & lanemask_lt());
-    dkey[pos] = __float_as_uint(feat[3 * idx + 2].y);
-    dval[pos] = (uint32_t)idx;
+    const uint32_t pos = B.blkcnt[blockIdx.x] + before + __popc(b & lanemask_lt());
+    B.k0[pos] = __float_as_uint(B.feat[3 * idx + 2].y);
+    B.v0[pos] = (uint32_t)idx;
   }
 }
 
-// One thread: derived sizes from V.
-__global__ void params_kernel(int T, uint32_t cmax, uint32_t *__restrict__ counters) {
+// One thread per view: derived sizes from V.
+__global__ void params_kernel(const BinViews bv) {
+  const int vi = threadIdx.x;
+  if (vi >= bv.n) return;
+  const BinView &B = bv.v[vi];
+  uint32_t *counters = B.counters;
   const uint32_t V = counters[CI_V];
   const uint32_t nbr = (V + RADIX_TILE - 1) / RADIX_TILE;
-  const uint32_t C = min((V + CHUNK_MIN_GAUSS - 1) / CHUNK_MIN_GAUSS, cmax);
+  const uint32_t C = min((V + CHUNK_MIN_GAUSS - 1) / CHUNK_MIN_GAUSS, B.cmax);
   counters[CI_NBR] = nbr;
   counters[CI_NRH] = 256u * nbr;
   counters[CI_C] = C;
-  counters[CI_NCM] = (uint32_t)T * C;
+  counters[CI_NCM] = (uint32_t)(B.bd.gx * B.bd.gy) * C;
 }
 
 // ---- stable LSD radix sort of (depth_bits, index), 8 bits per pass -------
 
 __global__ void __launch_bounds__(RADIX_BLOCK)
-radix_hist_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ counters,
-                  int shift, uint32_t *__restrict__ rhist) {
-  const uint32_t V = counters[CI_V], nbr = counters[CI_NBR];
+radix_hist_kernel(const BinViews bv, int pass) {
+  const BinView &B = bv.v[blockIdx.y];
+  const uint32_t *keys = (pass & 1) ? B.k1 : B.k0;
+  const int shift = 8 * pass;
+  const uint32_t V = B.counters[CI_V], nbr = B.counters[CI_NBR];
   const uint32_t b = blockIdx.x;
   if (b >= nbr) return;
   __shared__ uint32_t h[256];
@@ -195,7 +208,7 @@ radix_hist_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict_
     if (k < V) atomicAdd(&h[(keys[k] >> shift) & 255u], 1u);
   }
   __syncthreads();
-  rhist[threadIdx.x * nbr + b] = h[threadIdx.x];  // digit-major
+  B.rhist[threadIdx.x * nbr + b] = h[threadIdx.x];  // digit-major
 }
 
 // Lanes whose 8-bit digit equals this lane's (invalid lanes, digit 256, group
@@ -214,11 +227,14 @@ __device__ __forceinline__ unsigned digit_peers(int d) {
 // Warp w of block b owns keys [b*2048 + w*256, +256), visited in 8 rounds
 // of 32 (round-major, then lane) — the input order, so the pass is stable.
 __global__ void __launch_bounds__(RADIX_BLOCK)
-radix_scatter_kernel(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
-                     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout,
-                     const uint32_t *__restrict__ counters, int shift,
-                     const uint32_t *__restrict__ rhist_scanned) {
-  const uint32_t V = counters[CI_V], nbr = counters[CI_NBR];
+radix_scatter_kernel(const BinViews bv, int pass) {
+  const BinView &B = bv.v[blockIdx.y];
+  // pass p reads (k0, v0) when p is even and writes (k1, v1), and back
+  const uint32_t *kin = (pass & 1) ? B.k1 : B.k0, *vin = (pass & 1) ? B.v1 : B.v0;
+  uint32_t *kout = (pass & 1) ? B.k0 : B.k1, *vout = (pass & 1) ? B.v0 : B.v1;
+  const int shift = 8 * pass;
+  const uint32_t *rhist_scanned = B.rhist;
+  const uint32_t V = B.counters[CI_V], nbr = B.counters[CI_NBR];
   const uint32_t b = blockIdx.x;
   if (b >= nbr) return;
   __shared__ uint32_t wh[RADIX_BLOCK / 32][256];
@@ -323,15 +339,15 @@ struct RectWalk {
 // Weight of sorted position s: the warp iterations its Gaussian costs the
 // count and emit kernels (a fixed part plus one per 32 covered tiles).
 __global__ void __launch_bounds__(256)
-chunk_weight_kernel(const float4 *__restrict__ feat, const uint32_t *__restrict__ order,
-                    const uint32_t *__restrict__ counters, uint32_t *__restrict__ weight) {
-  const uint32_t V = counters[CI_V];
+chunk_weight_kernel(const BinViews bv) {
+  const BinView &B = bv.v[blockIdx.y];
+  const uint32_t V = B.counters[CI_V];
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= V) return;
   int x0, y0, x1, y1;
-  unpack_rect(feat[3 * order[s] + 2], x0, y0, x1, y1);
+  unpack_rect(B.feat[3 * B.v0[s] + 2], x0, y0, x1, y1);
   const uint32_t area = (uint32_t)((x1 - x0) * (y1 - y0));
-  weight[s] = CHUNK_W_GAUSS + (area + 31u) / 32u;
+  B.k1[s] = CHUNK_W_GAUSS + (area + 31u) / 32u;  // the sorted keys end in k0: k1 is free
 }
 
 // From the exclusive prefix of the weights: chunk c = the positions whose
@@ -339,10 +355,12 @@ chunk_weight_kernel(const float4 *__restrict__ feat, const uint32_t *__restrict_
 // weight >= 1), so the chunk of a position never decreases; position s opens
 // the chunks between its predecessor's and its own.  cstart[C] = V.
 __global__ void __launch_bounds__(256)
-chunk_bounds_kernel(const uint32_t *__restrict__ prefix, const uint32_t *__restrict__ counters,
-                    uint32_t *__restrict__ cstart) {
-  const uint32_t V = counters[CI_V], C = counters[CI_C];
-  const unsigned long long W = counters[CI_W];
+chunk_bounds_kernel(const BinViews bv) {
+  const BinView &B = bv.v[blockIdx.y];
+  const uint32_t *prefix = B.k1;
+  uint32_t *cstart = B.cstart;
+  const uint32_t V = B.counters[CI_V], C = B.counters[CI_C];
+  const unsigned long long W = B.counters[CI_W];
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= V || W == 0) return;
   const uint32_t cs = (uint32_t)((unsigned long long)prefix[s] * C / W);
@@ -364,16 +382,18 @@ chunk_bounds_kernel(const uint32_t *__restrict__ prefix, const uint32_t *__restr
 // EMIT: slots start at the scanned counts (first list position of each
 // (tile, chunk)) and each visit appends the Gaussian index.  Indices and
 // rectangles are loaded two and one groups ahead.
-struct Bands {
-  int gx, gy, R, nb;  // grid, rows per band, bands
-};
-
 template <bool EMIT>
 __global__ void __launch_bounds__(32)
-band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restrict__ order,
-            uint32_t *__restrict__ counters, const uint32_t *__restrict__ cstart,
-            uint32_t *__restrict__ cmat, uint32_t *__restrict__ point_list, uint32_t K_alloc) {
+band_kernel(const BinViews bv) {
   extern __shared__ uint32_t slot[];
+  const BinView &Bv = bv.v[blockIdx.y];
+  const Bands bd = Bv.bd;
+  const float4 *__restrict__ feat = Bv.feat;
+  const uint32_t *__restrict__ order = Bv.v0;
+  uint32_t *__restrict__ counters = Bv.counters;
+  uint32_t *__restrict__ cmat = Bv.cmat;
+  uint32_t *__restrict__ point_list = Bv.point_list;
+  const uint32_t K_alloc = Bv.K_alloc;
   const uint32_t C = counters[CI_C];
   const uint32_t c = blockIdx.x / (uint32_t)bd.nb;
   const int b = (int)(blockIdx.x - c * (uint32_t)bd.nb);
@@ -381,7 +401,7 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
   const int lane = threadIdx.x;
   const int ys = b * bd.R, ye = min(bd.gy, ys + bd.R);
   const int t0 = ys * bd.gx, nt = (ye - ys) * bd.gx;
-  const uint32_t s0 = cstart[c], s1 = cstart[c + 1];
+  const uint32_t s0 = Bv.cstart[c], s1 = Bv.cstart[c + 1];
   const uint64_t keep = l2_policy_last();
   if (EMIT) {
     // an overflowed view (instances above the list capacity) emits nothing
@@ -468,13 +488,15 @@ band_kernel(Bands bd, const float4 *__restrict__ feat, const uint32_t *__restric
 // Tile ranges from the scanned count matrix.  When the instances exceed the
 // list capacity (capacity-bounded callers), every range is left empty and
 // the overflow bit is set, so no kernel reads past the list buffer.
-__global__ void ranges_kernel(int T, const uint32_t *__restrict__ cmat_scanned,
-                              uint32_t *__restrict__ counters, uint2 *__restrict__ ranges,
-                              uint32_t K_cap) {
+__global__ void ranges_kernel(const BinViews bv) {
+  const BinView &B = bv.v[blockIdx.y];
+  const int T = B.bd.gx * B.bd.gy;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
+  uint32_t *counters = B.counters;
+  const uint32_t *cmat_scanned = B.cmat;
   const uint32_t C = counters[CI_C], K = counters[CI_K];
-  const bool over = K > K_cap || (counters[CI_STATUS] & ST_OVERFLOW);
+  const bool over = K > B.K_cap || (counters[CI_STATUS] & ST_OVERFLOW);
   if (over && t == 0) atomicOr(&counters[CI_STATUS], ST_OVERFLOW);
   uint2 r = make_uint2(0u, 0u);
   if (C > 0 && !over) {
@@ -483,7 +505,7 @@ __global__ void ranges_kernel(int T, const uint32_t *__restrict__ cmat_scanned,
     if (e > a) r = make_uint2(a, e);
     atomicMax(&counters[CI_MAXLIST], e - a);
   }
-  ranges[t] = r;
+  B.ranges[t] = r;
 }
 
 // Debug view: sorted keys in the reference's form (tile << 32 | depth_bits).
@@ -529,14 +551,16 @@ int band_plan(int gx, int gy, BandPlan &pl) {
   int dev = 0;
   DMGS_CUDA(cudaGetDevice(&dev));
   thread_local int cached_dev = -1;
-  thread_local size_t cached_smem = 0;
+  thread_local size_t cached_smem = 0, attr_smem = 48 * 1024;
   thread_local int cached_resident = 0;
+  if (dev != cached_dev) attr_smem = 48 * 1024;
   if (dev != cached_dev || pl.smem != cached_smem) {
-    if (pl.smem > 48 * 1024) {
+    if (pl.smem > attr_smem) {  // only ever raised: a launch uses the largest of its views
       DMGS_CUDA(cudaFuncSetAttribute(band_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)pl.smem));
       DMGS_CUDA(cudaFuncSetAttribute(band_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)pl.smem));
+      attr_smem = pl.smem;
     }
     int sms = 0, a = 0, b = 0;
     DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -552,103 +576,146 @@ int band_plan(int gx, int gy, BandPlan &pl) {
 
 }  // namespace
 
-int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t *part,
-                uint32_t *total_out, uint32_t *status, cudaStream_t s) {
+namespace {
+
+// Scan of one array per view: host bound n_max (the launch size), device
+// length *n_dev when given.
+int launch_scan_views(const ScanViews &sv, cudaStream_t s) {
+  uint32_t n_max = 0;
+  for (int v = 0; v < sv.n; ++v) n_max = std::max(n_max, sv.v[v].n_max);
+  const dim3 one(1, sv.n);
   if (n_max <= (uint32_t)SCAN_TILE * 4) {
-    dmgs_host::note_launch(), scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, 0, total_out, status);
+    dmgs_host::note_launch(), scan_single_kernel<<<one, SCAN_THREADS, 0, s>>>(sv, 0);
     DMGS_LAUNCH_CHECK("scan_single_kernel");
     return DMGS_OK;
   }
-  const uint32_t nb = (n_max + SCAN_TILE - 1) / SCAN_TILE;
-  dmgs_host::note_launch(), scan_reduce_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
+  const dim3 grid((n_max + SCAN_TILE - 1) / SCAN_TILE, sv.n);
+  dmgs_host::note_launch(), scan_reduce_kernel<<<grid, SCAN_THREADS, 0, s>>>(sv);
   DMGS_LAUNCH_CHECK("scan_reduce_kernel");
-  dmgs_host::note_launch(), scan_single_kernel<<<1, SCAN_THREADS, 0, s>>>(part, n_dev, n_max, 1, total_out, status);
+  dmgs_host::note_launch(), scan_single_kernel<<<one, SCAN_THREADS, 0, s>>>(sv, 1);
   DMGS_LAUNCH_CHECK("scan_single_kernel");
-  dmgs_host::note_launch(), scan_down_kernel<<<nb, SCAN_THREADS, 0, s>>>(data, n_dev, n_max, part);
+  dmgs_host::note_launch(), scan_down_kernel<<<grid, SCAN_THREADS, 0, s>>>(sv);
   DMGS_LAUNCH_CHECK("scan_down_kernel");
   return DMGS_OK;
 }
 
-int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cudaStream_t s) {
-  uint32_t *counters = reinterpret_cast<uint32_t *>(geom + L.counters);
-  uint32_t *blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
-  uint32_t *part = reinterpret_cast<uint32_t *>(geom + L.scanpart);
-  uint32_t *k0 = reinterpret_cast<uint32_t *>(geom + L.dkey0);
-  uint32_t *k1 = reinterpret_cast<uint32_t *>(geom + L.dkey1);
-  uint32_t *v0 = reinterpret_cast<uint32_t *>(geom + L.dval0);
-  uint32_t *v1 = reinterpret_cast<uint32_t *>(geom + L.dval1);
-  uint32_t *rhist = reinterpret_cast<uint32_t *>(geom + L.rhist);
-  uint32_t *cmat = reinterpret_cast<uint32_t *>(geom + L.cmat);
-  const float4 *feat = reinterpret_cast<const float4 *>(geom + L.feat);
-  const int T = L.T();
+template <typename F>
+ScanViews scan_views(const BinViews &bv, F &&f) {
+  ScanViews sv;
+  sv.n = bv.n;
+  for (int v = 0; v < bv.n; ++v) sv.v[v] = f(bv.v[v]);
+  return sv;
+}
+
+}  // namespace
+
+int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_list,
+                  uint32_t K_alloc, BinView &B) {
   BandPlan pl;
   if (int r = band_plan(L.gx, L.gy, pl)) return r;
-  if (L.P > 0) {
+  B.P = L.P;
+  B.nb_pre = L.nb_pre;
+  B.nb_radix = L.nb_radix;
+  B.n_rhist_max = (uint32_t)L.n_rhist_max;
+  B.n_cmat_max = (uint32_t)L.n_cmat_max;
+  B.flags = reinterpret_cast<const uint8_t *>(geom + L.flags);
+  B.feat = reinterpret_cast<const float4 *>(geom + L.feat);
+  B.blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
+  B.counters = reinterpret_cast<uint32_t *>(geom + L.counters);
+  B.part = reinterpret_cast<uint32_t *>(geom + L.scanpart);
+  B.k0 = reinterpret_cast<uint32_t *>(geom + L.dkey0);
+  B.k1 = reinterpret_cast<uint32_t *>(geom + L.dkey1);
+  B.v0 = reinterpret_cast<uint32_t *>(geom + L.dval0);
+  B.v1 = reinterpret_cast<uint32_t *>(geom + L.dval1);
+  B.rhist = reinterpret_cast<uint32_t *>(geom + L.rhist);
+  B.cmat = reinterpret_cast<uint32_t *>(geom + L.cmat);
+  B.cstart = reinterpret_cast<uint32_t *>(geom + L.cstart);
+  B.ranges = reinterpret_cast<uint2 *>(geom + L.ranges);
+  B.point_list = reinterpret_cast<uint32_t *>(point_list);
+  B.K_cap = K_cap;
+  B.K_alloc = K_alloc;
+  B.bd = pl.bd;
+  B.cmax = pl.cmax;
+  B.smem = (uint32_t)pl.smem;
+  return DMGS_OK;
+}
+
+int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
+  if (bv.n < 1) return DMGS_OK;
+  int nb_pre = 0, nb_radix = 0, P = 0, T = 0;
+  uint32_t smem = 0, band_blocks = 0;
+  for (int v = 0; v < bv.n; ++v) {
+    const BinView &B = bv.v[v];
+    nb_pre = std::max(nb_pre, B.nb_pre);
+    nb_radix = std::max(nb_radix, B.nb_radix);
+    P = std::max(P, B.P);
+    T = std::max(T, B.bd.gx * B.bd.gy);
+    smem = std::max(smem, B.smem);
+    band_blocks = std::max(band_blocks, B.cmax * (uint32_t)B.bd.nb);
+  }
+  const int nv = bv.n;
+  if (P > 0) {
     DMGS_TIMED(K_BIN_COMPACT, s, {
-      int r = launch_scan(blkcnt, nullptr, (uint32_t)L.nb_pre, part, counters + CI_V, counters, s);
+      int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
+        return ScanView{B.blkcnt, nullptr, (uint32_t)B.nb_pre, B.part, B.counters + CI_V, B.counters};
+      }), s);
       if (r != DMGS_OK) return r;
-      dmgs_host::note_launch(), compact_kernel<<<L.nb_pre, PRE_BLOCK, 0, s>>>(L.P, reinterpret_cast<const uint8_t *>(geom + L.flags), feat, blkcnt, k0, v0);
+      dmgs_host::note_launch(), compact_kernel<<<dim3(nb_pre, nv), PRE_BLOCK, 0, s>>>(bv);
     });
     DMGS_LAUNCH_CHECK("compact_kernel");
   }
-  dmgs_host::note_launch(), params_kernel<<<1, 1, 0, s>>>(T, pl.cmax, counters);
+  dmgs_host::note_launch(), params_kernel<<<1, 32, 0, s>>>(bv);
   DMGS_LAUNCH_CHECK("params_kernel");
-  if (L.P > 0) {
+  if (P > 0) {
     DMGS_TIMED(K_BIN_SORT, s, {
-      uint32_t *ki = k0, *vi = v0, *ko = k1, *vo = v1;
+      const ScanViews hs = scan_views(bv, [](const BinView &B) {
+        return ScanView{B.rhist, B.counters + CI_NRH, B.n_rhist_max, B.part, nullptr, nullptr};
+      });
       for (int pass = 0; pass < 4; ++pass) {
-        const int shift = 8 * pass;
-        dmgs_host::note_launch(), radix_hist_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, counters, shift, rhist);
-        int r = launch_scan(rhist, counters + CI_NRH, (uint32_t)L.n_rhist_max, part, nullptr,
-                            nullptr, s);
+        dmgs_host::note_launch(), radix_hist_kernel<<<dim3(nb_radix, nv), RADIX_BLOCK, 0, s>>>(bv, pass);
+        int r = launch_scan_views(hs, s);
         if (r != DMGS_OK) return r;
-        dmgs_host::note_launch(), radix_scatter_kernel<<<L.nb_radix, RADIX_BLOCK, 0, s>>>(ki, vi, ko, vo, counters, shift,
-                                                                 rhist);
-        uint32_t *t1 = ki; ki = ko; ko = t1;
-        uint32_t *t2 = vi; vi = vo; vo = t2;
+        dmgs_host::note_launch(), radix_scatter_kernel<<<dim3(nb_radix, nv), RADIX_BLOCK, 0, s>>>(bv, pass);
       }
     });  // four passes: the sorted order ends in (k0, v0)
     DMGS_LAUNCH_CHECK("radix_sort");
-  }
-  if (L.P > 0) {
-    uint32_t *cstart = reinterpret_cast<uint32_t *>(geom + L.cstart);
     DMGS_TIMED(K_BIN_COUNT, s, {
-      // the sorted keys end in k0, so k1 is free for the chunk weights
-      dmgs_host::note_launch(), chunk_weight_kernel<<<L.nb_pre, 256, 0, s>>>(feat, v0, counters, k1);
-      int r = launch_scan(k1, counters + CI_V, (uint32_t)L.P, part, counters + CI_W, counters, s);
+      dmgs_host::note_launch(), chunk_weight_kernel<<<dim3(nb_pre, nv), 256, 0, s>>>(bv);
+      int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
+        return ScanView{B.k1, B.counters + CI_V, (uint32_t)B.P, B.part, B.counters + CI_W, B.counters};
+      }), s);
       if (r != DMGS_OK) return r;
-      dmgs_host::note_launch(), chunk_bounds_kernel<<<L.nb_pre, 256, 0, s>>>(k1, counters, cstart);
-      dmgs_host::note_launch(), band_kernel<false><<<pl.cmax * pl.bd.nb, 32, pl.smem, s>>>(
-          pl.bd, feat, v0, counters, cstart, cmat, nullptr, 0u);
+      dmgs_host::note_launch(), chunk_bounds_kernel<<<dim3(nb_pre, nv), 256, 0, s>>>(bv);
+      dmgs_host::note_launch(), band_kernel<false><<<dim3(band_blocks, nv), 32, smem, s>>>(bv);
     });
     DMGS_LAUNCH_CHECK("tile_count");
   }
   DMGS_TIMED(K_BIN_SCAN, s, {
-    if (L.P > 0) {
-      int r = launch_scan(cmat, counters + CI_NCM, (uint32_t)L.n_cmat_max, part, counters + CI_K,
-                          counters, s);
+    if (P > 0) {
+      int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
+        return ScanView{B.cmat, B.counters + CI_NCM, B.n_cmat_max, B.part, B.counters + CI_K, B.counters};
+      }), s);
       if (r != DMGS_OK) return r;
     }
-    dmgs_host::note_launch(), ranges_kernel<<<(T + 255) / 256, 256, 0, s>>>(T, cmat, counters,
-                                                  reinterpret_cast<uint2 *>(geom + L.ranges), K_cap);
+    dmgs_host::note_launch(), ranges_kernel<<<dim3((T + 255) / 256, nv), 256, 0, s>>>(bv);
   });
   DMGS_LAUNCH_CHECK("ranges_kernel");
   return DMGS_OK;
 }
 
-int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, int64_t K,
-                cudaStream_t s) {
-  if (L.P <= 0 || K <= 0) return DMGS_OK;
-  BandPlan pl;
-  if (int r = band_plan(L.gx, L.gy, pl)) return r;
+int launch_emit(const BinViews &bv, cudaStream_t s) {
+  uint32_t smem = 0, band_blocks = 0;
+  bool any = false;
+  for (int v = 0; v < bv.n; ++v) {
+    const BinView &B = bv.v[v];
+    if (B.P <= 0 || B.K_alloc == 0) continue;
+    any = true;
+    smem = std::max(smem, B.smem);
+    band_blocks = std::max(band_blocks, B.cmax * (uint32_t)B.bd.nb);
+  }
+  if (!any) return DMGS_OK;
   DMGS_TIMED(K_BIN_EMIT, s,
-             dmgs_host::note_launch(), band_kernel<true><<<pl.cmax * pl.bd.nb, 32, pl.smem, s>>>(
-                 pl.bd, reinterpret_cast<const float4 *>(geom + L.feat),
-                 reinterpret_cast<const uint32_t *>(geom + L.dval0),
-                 reinterpret_cast<uint32_t *>(geom + L.counters),
-                 reinterpret_cast<const uint32_t *>(geom + L.cstart),
-                 reinterpret_cast<uint32_t *>(geom + L.cmat),
-                 reinterpret_cast<uint32_t *>(bin + B.point_list), (uint32_t)K));
+             dmgs_host::note_launch(), band_kernel<true><<<dim3(band_blocks, bv.n), 32, smem, s>>>(bv));
   DMGS_LAUNCH_CHECK("emit_kernel");
   return DMGS_OK;
 }

@@ -179,7 +179,10 @@ int dmgs_raster_fwd_geometry(const DmgsView *view, const DmgsGaussians *g, void 
   RET_IF(launch_preprocess(vp, view->viewmatrix, view->projmatrix, view->campos, make_gptrs(g),
                            radii, L, geom, s));
   RET_IF(debug_sync(view, s, "preprocess"));
-  RET_IF(launch_binning_geometry(L, geom, 0xffffffffu, s));
+  BinViews bv;
+  bv.n = 1;
+  RET_IF(make_bin_view(L, geom, 0xffffffffu, nullptr, 0u, bv.v[0]));
+  RET_IF(launch_binning_geometry(bv, s));
   uint32_t h[CI_WORDS];
   RET_IF(check_status(geom, L, s, h));
   if (num_rendered) *num_rendered = (int64_t)h[CI_K];
@@ -205,7 +208,10 @@ int dmgs_raster_fwd_render(const DmgsView *view, const DmgsGaussians *g, void *g
   char *bin = static_cast<char *>(binning_state);
   char *img = static_cast<char *>(image_state);
   const ViewParams vp = make_params(view);
-  RET_IF(launch_emit(L, geom, B, bin, num_rendered, s));
+  BinViews bv;
+  bv.n = 1;
+  RET_IF(make_bin_view(L, geom, 0xffffffffu, bin + B.point_list, (uint32_t)num_rendered, bv.v[0]));
+  RET_IF(launch_emit(bv, s));
   RET_IF(debug_sync(view, s, "emit"));
   RET_IF(launch_blend_fwd(vp, L, geom, B, bin, I, img, view->bg, out_color, s));
   RET_IF(debug_sync(view, s, "blend_fwd"));

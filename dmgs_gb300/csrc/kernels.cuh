@@ -36,14 +36,54 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
 int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t *present,
                         cudaStream_t s);
 
-// binning.cu
-int launch_scan(uint32_t *data, const uint32_t *n_dev, uint32_t n_max, uint32_t *part,
-                uint32_t *total_out, uint32_t *status, cudaStream_t s);
-// K_cap: capacity of the caller's list buffer (0xffffffff when it is sized
-// after the geometry phase).
-int launch_binning_geometry(const GeomLayout &L, char *geom, uint32_t K_cap, cudaStream_t s);
-int launch_emit(const GeomLayout &L, char *geom, const BinLayout &B, char *bin, int64_t K,
-                cudaStream_t s);
+// binning.cu — every stage bins a set of views in one launch per stage.
+constexpr int MAX_BIN_VIEWS = 16;
+
+struct Bands {
+  int gx, gy, R, nb;  // tile grid, tile rows per band, bands
+};
+
+// One view's binning: its geometry-state arrays and sizes.
+struct BinView {
+  int P, nb_pre, nb_radix;
+  uint32_t n_rhist_max, n_cmat_max;
+  const uint8_t *flags;
+  const float4 *feat;
+  uint32_t *blkcnt, *counters, *part, *k0, *k1, *v0, *v1, *rhist, *cmat, *cstart;
+  uint2 *ranges;
+  uint32_t *point_list;  // emission target (K_alloc entries)
+  uint32_t K_cap;        // list capacity checked by the ranges (0xffffffff: sized afterwards)
+  uint32_t K_alloc;      // entries of point_list
+  Bands bd;
+  uint32_t cmax, smem;   // chunk bound, band shared memory (bytes)
+};
+
+struct BinViews {
+  int n;
+  BinView v[MAX_BIN_VIEWS];
+};
+
+// One array per view for the generic scan.
+struct ScanView {
+  uint32_t *data;
+  const uint32_t *n_dev;  // device length (nullptr: n_max)
+  uint32_t n_max;
+  uint32_t *part;
+  uint32_t *total_out;
+  uint32_t *status;
+};
+
+struct ScanViews {
+  int n;
+  ScanView v[MAX_BIN_VIEWS];
+};
+
+// Fill one view's binning record from its geometry state; point_list /
+// K_alloc may be set later (after the instance count is known).
+int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_list,
+                  uint32_t K_alloc, BinView &B);
+int launch_binning_geometry(const BinViews &bv, cudaStream_t s);
+int launch_emit(const BinViews &bv, cudaStream_t s);
 int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
                       uint64_t *keys, uint32_t *values, cudaStream_t s);
 int launch_debug_geometry(const GeomLayout &L, const char *geom, int32_t *rect,

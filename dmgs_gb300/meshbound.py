@@ -1,0 +1,227 @@
+"""Mesh-bound Gaussian training step (the stage-2 path of the reference).
+
+The reference's stage-2 step (train_geo_stage2.py:101-116) extracts a mesh
+(FlexiCubes), binds Gaussians to its faces (renew_gaussian /
+get_covariance_dyn, scene/gaussian_geo_model_mlp_flex.py:258-335,370-385),
+evaluates SH colours in torch (gaussian_renderer/__init__.py:165-170:
+eval_sh then sigmoid), rasterises with precomputed covariance and colours
+(render_dyn, :104-193) and optimises L1 + 0.2 (1 - SSIM)
+(utils/loss_utils.py).  Here the binding and the rasteriser are this
+library's kernels; the SH colour and the loss stay in torch as in the
+reference.
+
+The mesh of the workload is built by :func:`sphere_torus_mesh`: a surface of
+the union of a sphere (r 0.6) and a torus (R 0.7, r 0.2) on a 64^3 grid over
+[-1, 1]^3, one vertex per sign-changing cell (the mean of its edge
+crossings) and, for every sign-changing grid edge, the quad of the four
+cells around it split into four triangles about its centre — the face count
+of FlexiCubes' training-mode extraction of the same field (45,304).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+import torch.nn.functional as F_
+
+from .binding import bind_faces
+from .rasterizer import GaussianRasterizationSettings, GaussianRasterizer
+
+# Real SH basis constants (degree <= 3), the standard orthonormal basis.
+_C0 = 0.28209479177387814
+_C1 = 0.4886025119029199
+_C2 = (1.0925484305920792, -1.0925484305920792, 0.31539156525252005, -1.0925484305920792,
+       0.5462742152960396)
+_C3 = (-0.5900435899266435, 2.890611442640554, -0.4570457994644658, 0.3731763325901154,
+       -0.4570457994644658, 1.445305721320277, -0.5900435899266435)
+
+
+def sdf_sphere_torus(p):
+    sph = np.linalg.norm(p, axis=-1) - 0.6
+    q = np.sqrt(p[..., 0] ** 2 + p[..., 2] ** 2) - 0.7
+    tor = np.sqrt(q ** 2 + p[..., 1] ** 2) - 0.2
+    return np.minimum(sph, tor)
+
+
+def sphere_torus_mesh(res=64, lo=-1.0, hi=1.0, sdf=sdf_sphere_torus):
+    """Surface of an SDF on a res^3 grid: (verts [V,3] float32, faces [F,3]
+    int64), outward-facing triangles."""
+    g = np.linspace(lo, hi, res + 1)
+    P = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1)
+    d = sdf(P)
+    inside = d < 0
+    # edge crossings: points where the field changes sign along each grid edge
+    cell_sum = np.zeros((res, res, res, 3))
+    cell_cnt = np.zeros((res, res, res))
+    for axis in range(3):
+        sl0 = [slice(None)] * 3
+        sl1 = [slice(None)] * 3
+        sl0[axis] = slice(0, -1)
+        sl1[axis] = slice(1, None)
+        d0, d1 = d[tuple(sl0)], d[tuple(sl1)]
+        p0, p1 = P[tuple(sl0)], P[tuple(sl1)]
+        cross = (d0 < 0) != (d1 < 0)
+        t = np.where(cross, d0 / np.where(cross, d0 - d1, 1.0), 0.0)
+        pt = p0 + t[..., None] * (p1 - p0)
+        # the edge belongs to the 4 cells around it
+        idx = np.argwhere(cross)
+        for o1 in (0, -1):
+            for o2 in (0, -1):
+                c = idx.copy()
+                other = [a for a in range(3) if a != axis]
+                c[:, other[0]] += o1
+                c[:, other[1]] += o2
+                ok = np.all((c >= 0) & (c < res), axis=1)
+                cc = c[ok]
+                np.add.at(cell_sum, (cc[:, 0], cc[:, 1], cc[:, 2]), pt[tuple(idx[ok].T)])
+                np.add.at(cell_cnt, (cc[:, 0], cc[:, 1], cc[:, 2]), 1.0)
+    has = cell_cnt > 0
+    vid = -np.ones((res, res, res), np.int64)
+    vid[has] = np.arange(has.sum())
+    verts = (cell_sum[has] / cell_cnt[has, None]).astype(np.float32)
+    quads = []
+    for axis in range(3):
+        sl0 = [slice(None)] * 3
+        sl1 = [slice(None)] * 3
+        sl0[axis] = slice(0, -1)
+        sl1[axis] = slice(1, None)
+        cross = inside[tuple(sl0)] != inside[tuple(sl1)]
+        flip = inside[tuple(sl0)]
+        a, b = [x for x in range(3) if x != axis]
+        idx = np.argwhere(cross)
+        ok = (idx[:, a] > 0) & (idx[:, a] < res) & (idx[:, b] > 0) & (idx[:, b] < res)
+        idx = idx[ok]
+        fl = flip[tuple(idx.T)]
+        cells = []
+        for oa, ob in ((0, 0), (-1, 0), (-1, -1), (0, -1)):
+            c = idx.copy()
+            c[:, a] += oa
+            c[:, b] += ob
+            cells.append(vid[c[:, 0], c[:, 1], c[:, 2]])
+        q = np.stack(cells, 1)
+        # orientation: normals point from inside to outside
+        q = np.where(((axis == 1) ^ fl)[:, None], q, q[:, ::-1])
+        quads.append(q)
+    quads = np.concatenate(quads, 0)
+    centre = verts[quads].mean(1)
+    cid = len(verts) + np.arange(len(quads))
+    verts = np.concatenate([verts, centre.astype(np.float32)], 0)
+    faces = np.concatenate([np.stack([quads[:, i], quads[:, (i + 1) % 4], cid], 1)
+                            for i in range(4)], 0)
+    return verts, faces.astype(np.int64)
+
+
+def eval_sh(deg, sh, dirs):
+    """SH colour (degree <= 3) of features sh [P, 3, (deg+1)^2] at unit
+    directions dirs [P, 3] (the real SH polynomial of the 3DGS reference,
+    utils/sh_utils.py:25-110)."""
+    x, y, z = dirs[:, 0:1], dirs[:, 1:2], dirs[:, 2:3]
+    r = _C0 * sh[..., 0]
+    if deg > 0:
+        r = r - _C1 * y * sh[..., 1] + _C1 * z * sh[..., 2] - _C1 * x * sh[..., 3]
+        if deg > 1:
+            xx, yy, zz, xy, yz, xz = x * x, y * y, z * z, x * y, y * z, x * z
+            r = (r + _C2[0] * xy * sh[..., 4] + _C2[1] * yz * sh[..., 5]
+                 + _C2[2] * (2.0 * zz - xx - yy) * sh[..., 6] + _C2[3] * xz * sh[..., 7]
+                 + _C2[4] * (xx - yy) * sh[..., 8])
+            if deg > 2:
+                r = (r + _C3[0] * y * (3 * xx - yy) * sh[..., 9] + _C3[1] * xy * z * sh[..., 10]
+                     + _C3[2] * y * (4 * zz - xx - yy) * sh[..., 11]
+                     + _C3[3] * z * (2 * zz - 3 * xx - 3 * yy) * sh[..., 12]
+                     + _C3[4] * x * (4 * zz - xx - yy) * sh[..., 13]
+                     + _C3[5] * z * (xx - yy) * sh[..., 14]
+                     + _C3[6] * x * (xx - 3 * yy) * sh[..., 15])
+    return r
+
+
+def _gauss_window(size=11, sigma=1.5, channels=3, device="cuda"):
+    g = torch.exp(-((torch.arange(size, device=device) - size // 2) ** 2) / (2 * sigma ** 2))
+    g = g / g.sum()
+    w = (g[:, None] * g[None, :])[None, None]
+    return w.expand(channels, 1, size, size).contiguous()
+
+
+def ssim(img1, img2, window=None):
+    """Mean SSIM (Wang et al. 2004) with an 11x11 Gaussian window (sigma 1.5),
+    C1 = 0.01^2, C2 = 0.03^2, per channel — the form of the reference's
+    utils/loss_utils.py."""
+    C = img1.shape[0]
+    w = window if window is not None else _gauss_window(channels=C, device=img1.device)
+    a, b = img1[None], img2[None]
+    mu1 = F_.conv2d(a, w, padding=5, groups=C)
+    mu2 = F_.conv2d(b, w, padding=5, groups=C)
+    s11 = F_.conv2d(a * a, w, padding=5, groups=C) - mu1 * mu1
+    s22 = F_.conv2d(b * b, w, padding=5, groups=C) - mu2 * mu2
+    s12 = F_.conv2d(a * b, w, padding=5, groups=C) - mu1 * mu2
+    C1, C2 = 0.01 ** 2, 0.03 ** 2
+    m = ((2 * mu1 * mu2 + C1) * (2 * s12 + C2)) / ((mu1 * mu1 + mu2 * mu2 + C1) * (s11 + s22 + C2))
+    return m.mean()
+
+
+class MeshBoundScene:
+    """Gaussians bound to a mesh's faces (stage 2): learnable vertices and
+    scale factor, G Gaussians per face at per-Gaussian Dirichlet(1,1,1)
+    barycentric coordinates, per-Gaussian SH features [P, 3, 16] and
+    opacities."""
+
+    def __init__(self, verts, faces, G=6, seed=0, device="cuda", sh_degree=3):
+        rng = np.random.default_rng(seed)
+        self.device = torch.device(device)
+        self.faces = torch.as_tensor(faces, device=self.device)
+        F = self.faces.shape[0]
+        self.G, self.P = G, F * G
+        self.verts = torch.tensor(verts, device=self.device, requires_grad=True)
+        self.bc = torch.tensor(rng.dirichlet((1.0, 1.0, 1.0), (F, G)).astype(np.float32),
+                               device=self.device)
+        self.rad_base = 1.0 / (4.0 + 2.0 * math.sqrt(3.0))
+        self.max_scale = 2.0  # the reference's initial scale factor: atanh(1 / max_scale)
+        self.scale_factor = torch.full((1,), math.atanh(1.0 / self.max_scale), device=self.device,
+                                       requires_grad=True)
+        sh = np.zeros((self.P, 3, 16), np.float32)
+        sh[:, :, 0] = rng.normal(0.5, 0.2, (self.P, 3))
+        sh[:, :, 1:] = rng.normal(0.0, 0.05, (self.P, 3, 15))
+        self.features = torch.tensor(sh, device=self.device, requires_grad=True)
+        self.opacity = torch.tensor(
+            (1.0 / (1.0 + np.exp(-rng.standard_normal((self.P, 1))))).astype(np.float32),
+            device=self.device, requires_grad=True)
+        self.sh_degree = sh_degree
+        self.spatial_lr_scale = 1.0
+
+    def params(self):
+        return [self.verts, self.scale_factor, self.features, self.opacity]
+
+    def gaussians(self):
+        xyz, cov, _ = bind_faces(self.verts, self.faces, self.bc, self.scale_factor,
+                                 self.rad_base, self.spatial_lr_scale, self.max_scale)
+        return xyz, cov
+
+    def render(self, view, bg):
+        """render_dyn: precomputed covariance and sigmoid(SH) colours."""
+        xyz, cov = self.gaussians()
+        campos = torch.tensor(view.campos, device=self.device)
+        d = xyz - campos
+        d = d / d.norm(dim=1, keepdim=True)
+        colors = torch.sigmoid(eval_sh(self.sh_degree, self.features, d))
+        rs = GaussianRasterizationSettings(
+            image_height=view.height, image_width=view.width, tanfovx=view.tanfovx,
+            tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0,
+            viewmatrix=torch.tensor(view.viewmatrix, device=self.device),
+            projmatrix=torch.tensor(view.projmatrix, device=self.device),
+            sh_degree=self.sh_degree, campos=campos, prefiltered=False, debug=False)
+        means2D = torch.zeros_like(xyz, requires_grad=True)
+        img, radii = GaussianRasterizer(rs)(means3D=xyz, means2D=means2D, opacities=self.opacity,
+                                            colors_precomp=colors, cov3D_precomp=cov)
+        return img, radii, means2D
+
+
+def training_step(scene: MeshBoundScene, view, target, bg, lambda_dssim=0.2, window=None):
+    """One stage-2 step, forward and backward: bind, colour, rasterise,
+    L1 + lambda (1 - SSIM), gradients into the scene's parameters."""
+    for p in scene.params():
+        p.grad = None
+    img, radii, _ = scene.render(view, bg)
+    loss = (1.0 - lambda_dssim) * (img - target).abs().mean() + lambda_dssim * (
+        1.0 - ssim(img, target, window))
+    loss.backward()
+    return loss.detach(), radii
