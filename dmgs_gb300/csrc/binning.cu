@@ -382,6 +382,74 @@ chunk_bounds_kernel(const BinViews bv) {
 // EMIT: slots start at the scanned counts (first list position of each
 // (tile, chunk)) and each visit appends the Gaussian index.  Indices and
 // rectangles are loaded two and one groups ahead.
+// Per-(tile, chunk) counts of one (chunk, band of tile rows) without walking
+// the instances: every Gaussian whose rectangle meets the band adds +1 / -1
+// at the four corners of its rectangle clipped to the band, in a 2D
+// difference grid of (R + 1) x (gx + 1) cells (shared-memory atomics, the 32
+// Gaussians of a group in parallel); inclusive prefix sums along the rows and
+// then the columns turn it into the counts of the band's tiles.  Work per
+// warp: 4 updates per Gaussian plus 2 passes over the band's tiles, instead
+// of one visit per instance.  Indices and rectangles are loaded one group
+// ahead.
+__global__ void __launch_bounds__(32)
+count_kernel(const BinViews bv) {
+  extern __shared__ int dgrid[];
+  const BinView &Bv = bv.v[blockIdx.y];
+  const Bands bd = Bv.bd;
+  const uint32_t C = Bv.counters[CI_C];
+  const uint32_t c = blockIdx.x / (uint32_t)bd.nb;
+  const int b = (int)(blockIdx.x - c * (uint32_t)bd.nb);
+  if (c >= C) return;
+  const int lane = threadIdx.x;
+  const int ys = b * bd.R, ye = min(bd.gy, ys + bd.R), R = ye - ys;
+  const int W = bd.gx + 1;
+  for (int i = lane; i < (R + 1) * W; i += 32) dgrid[i] = 0;
+  __syncwarp();
+  const uint32_t s0 = Bv.cstart[c], s1 = Bv.cstart[c + 1];
+  const float4 none = make_float4(0.f, 0.f, 0.f, 0.f);
+  bool vA = s0 + lane < s1;
+  float4 rA = vA ? Bv.feat[3 * Bv.v0[s0 + lane] + 2] : none;
+  for (uint32_t g0 = s0; g0 < s1; g0 += 32) {
+    const float4 r = rA;
+    const bool v = vA;
+    vA = g0 + 32 + lane < s1;
+    rA = vA ? Bv.feat[3 * Bv.v0[g0 + 32 + lane] + 2] : none;
+    int x0, y0, x1, y1;
+    unpack_rect(r, x0, y0, x1, y1);
+    const int cy0 = max(y0, ys) - ys, cy1 = min(y1, ye) - ys;
+    if (v && cy0 < cy1 && x0 < x1) {
+      atomicAdd(&dgrid[cy0 * W + x0], 1);
+      atomicAdd(&dgrid[cy0 * W + x1], -1);
+      atomicAdd(&dgrid[cy1 * W + x0], -1);
+      atomicAdd(&dgrid[cy1 * W + x1], 1);
+    }
+  }
+  __syncwarp();
+  for (int row = 0; row < R; ++row) {  // inclusive prefix along each row, 32 columns at a time
+    int carry = 0;
+    for (int xb = 0; xb < bd.gx; xb += 32) {
+      const int x = xb + lane;
+      int val = x < bd.gx ? dgrid[row * W + x] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(FULL, val, o);
+        if (lane >= o) val += u;
+      }
+      val += carry;
+      if (x < bd.gx) dgrid[row * W + x] = val;
+      carry = __shfl_sync(FULL, val, 31);
+    }
+  }
+  __syncwarp();
+  for (int x = lane; x < bd.gx; x += 32) {  // inclusive prefix along each column -> counts
+    int run = 0;
+    for (int row = 0; row < R; ++row) {
+      run += dgrid[row * W + x];
+      Bv.cmat[(size_t)((ys + row) * bd.gx + x) * C + c] = (uint32_t)run;
+    }
+  }
+}
+
 template <bool EMIT>
 __global__ void __launch_bounds__(32)
 band_kernel(const BinViews bv) {
@@ -453,7 +521,26 @@ band_kernel(const BinViews bv) {
       RectWalk it(lane, rw, mgi);
       const int o = by * bd.gx + bx;
       int j = lane;
-      // two tiles per step (distinct slots: independent read/modify/writes)
+      // four, then two tiles per step (distinct slots: independent read/modify/writes)
+      for (; j + 96 < area; j += 128) {
+        int a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          a[u] = o + it.row * bd.gx + it.col;
+          it.next();
+        }
+        uint32_t p[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) p[u] = slot[a[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) slot[a[u]] = p[u] + 1u;
+        if (EMIT) {
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (p[u] < K_alloc) st_hint(point_list + p[u], idi, keep); else bad = true;
+          }
+        }
+      }
       for (; j + 32 < area; j += 64) {
         const int a0 = o + it.row * bd.gx + it.col;
         it.next();
@@ -529,6 +616,8 @@ namespace {
 
 constexpr int BAND_TILES = 1024;  // target slots per band (4 KB of shared memory)
 
+uint32_t count_grid_bytes(const Bands &bd) { return (uint32_t)((bd.R + 1) * (bd.gx + 1) * 4); }
+
 // Bands of tile rows and the chunk count for a gx x gy grid: enough
 // (chunk, band) warps to fill the GPU in one wave, each band's slots small
 // enough for many resident warps per SM.
@@ -544,7 +633,7 @@ int band_plan(int gx, int gy, BandPlan &pl) {
   pl.bd.R = std::max(1, std::min(gy, BAND_TILES / std::max(gx, 1)));
   pl.bd.nb = (gy + pl.bd.R - 1) / pl.bd.R;
   pl.smem = (size_t)pl.bd.R * gx * 4;
-  if (pl.smem > 220 * 1024) {
+  if (pl.smem > 220 * 1024 || count_grid_bytes(pl.bd) > 220 * 1024) {
     dmgs_host::set_error("image too large: a row of %d tiles exceeds the binning kernels' shared memory", gx);
     return DMGS_ERR_ARG;
   }
@@ -555,16 +644,17 @@ int band_plan(int gx, int gy, BandPlan &pl) {
   thread_local int cached_resident = 0;
   if (dev != cached_dev) attr_smem = 48 * 1024;
   if (dev != cached_dev || pl.smem != cached_smem) {
-    if (pl.smem > attr_smem) {  // only ever raised: a launch uses the largest of its views
-      DMGS_CUDA(cudaFuncSetAttribute(band_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)pl.smem));
+    const size_t csm = count_grid_bytes(pl.bd);
+    if (std::max(pl.smem, csm) > attr_smem) {  // only ever raised: a launch uses its largest view
+      attr_smem = std::max(pl.smem, csm);
+      DMGS_CUDA(cudaFuncSetAttribute(count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)attr_smem));
       DMGS_CUDA(cudaFuncSetAttribute(band_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)pl.smem));
-      attr_smem = pl.smem;
+                                     (int)attr_smem));
     }
     int sms = 0, a = 0, b = 0;
     DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, band_kernel<false>, 32, pl.smem));
+    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, count_kernel, 32, csm));
     DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, band_kernel<true>, 32, pl.smem));
     cached_dev = dev;
     cached_smem = pl.smem;
@@ -643,7 +733,7 @@ int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_l
 int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
   if (bv.n < 1) return DMGS_OK;
   int nb_pre = 0, nb_radix = 0, P = 0, T = 0;
-  uint32_t smem = 0, band_blocks = 0;
+  uint32_t smem = 0, count_smem = 0, band_blocks = 0;
   for (int v = 0; v < bv.n; ++v) {
     const BinView &B = bv.v[v];
     nb_pre = std::max(nb_pre, B.nb_pre);
@@ -651,6 +741,7 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
     P = std::max(P, B.P);
     T = std::max(T, B.bd.gx * B.bd.gy);
     smem = std::max(smem, B.smem);
+    count_smem = std::max(count_smem, count_grid_bytes(B.bd));
     band_blocks = std::max(band_blocks, B.cmax * (uint32_t)B.bd.nb);
   }
   const int nv = bv.n;
@@ -686,7 +777,7 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
       }), s);
       if (r != DMGS_OK) return r;
       dmgs_host::note_launch(), chunk_bounds_kernel<<<dim3(nb_pre, nv), 256, 0, s>>>(bv);
-      dmgs_host::note_launch(), band_kernel<false><<<dim3(band_blocks, nv), 32, smem, s>>>(bv);
+      dmgs_host::note_launch(), count_kernel<<<dim3(band_blocks, nv), 32, count_smem, s>>>(bv);
     });
     DMGS_LAUNCH_CHECK("tile_count");
   }
