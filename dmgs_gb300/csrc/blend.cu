@@ -149,6 +149,29 @@ __device__ __forceinline__ int next_item(uint32_t *queue, int &slot, int *s_item
   return *s_item;
 }
 
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// The staged Gaussians (of cnt) whose footprint rows meet this warp's rows,
+// in staging order, written to this warp's list; returns their number.  One
+// ballot per 32 staged Gaussians replaces a per-Gaussian test in the loop.
+__device__ __forceinline__ int visit_list(const uint32_t *masks, int cnt, uint32_t warp_rows,
+                                          uint16_t *list, int lane) {
+  int nv = 0;
+  for (int j0 = 0; j0 < cnt; j0 += 32) {
+    const int j = j0 + lane;
+    const bool hit = j < cnt && (masks[j] & warp_rows);
+    const unsigned bal = __ballot_sync(FULL, hit);
+    if (hit) list[nv + __popc(bal & lanemask_lt())] = (uint16_t)j;
+    nv += __popc(bal);
+  }
+  __syncwarp();
+  return nv;
+}
+
 template <int PPT>
 struct PixelLayout {
   static constexpr int THREADS = 256 / PPT;
@@ -177,8 +200,11 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
   __shared__ float4 S0[2][BATCH];
   __shared__ float4 S1[2][BATCH];
   __shared__ float4 S2[2][BATCH];
+  __shared__ uint32_t SM[2][BATCH];              // footprint masks
+  __shared__ uint16_t VL[THREADS / 32][BATCH];   // per-warp visit lists
   __shared__ int s_item;
   const int tid = threadIdx.x;
+  const int lane = tid & 31;
   const PixelLayout<PPT> lay;
   int slot = 0;
   for (int item = next_item(queue, slot, &s_item); item < bb.total;
@@ -225,6 +251,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
         if (sl < BATCH && base + sl < n) {
           const Staged st = stage(pf0[l], pf1[l], pf2[l], ox, oy);
           S0[buf][sl] = st.s0; S1[buf][sl] = st.s1; S2[buf][sl] = st.s2;
+          SM[buf][sl] = __float_as_uint(st.s2.z);
         }
       }
       if (__syncthreads_count(all_done()) == THREADS) break;
@@ -239,10 +266,12 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
       }
       const int cnt = min(BATCH, n - base);
       bool warp_done = __all_sync(FULL, all_done());
-      for (int j = 0; j < cnt && !warp_done; ++j) {
+      uint16_t *vl = VL[tid >> 5];
+      const int nvis = warp_done ? 0 : visit_list(SM[buf], cnt, lay.warp_rows, vl, lane);
+      for (int i = 0; i < nvis && !warp_done; ++i) {
+        const int j = vl[i];
         const float4 s2 = S2[buf][j];
         const uint32_t m = __float_as_uint(s2.z);
-        if (!(m & lay.warp_rows)) continue;  // warp-uniform: footprint misses the warp's rows
         const float4 s0 = S0[buf][j];
         const float4 s1 = S1[buf][j];
         const float dx = __fsub_rn(s0.x, pxf);
@@ -417,6 +446,8 @@ __global__ void __launch_bounds__(256 / PPT, PPT == 4 ? 10 : (PPT == 2 ? 6 : 4))
 blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
   constexpr int THREADS = 256 / PPT;
   __shared__ float4 S0[BATCH], S1[BATCH], S2[BATCH], S3[BATCH];
+  __shared__ uint32_t SM[BATCH];                // footprint masks
+  __shared__ uint16_t VL[THREADS / 32][BATCH];  // per-warp visit lists
   __shared__ uint32_t sMaxLast;
   __shared__ int s_item;
   const int tid = threadIdx.x;
@@ -461,13 +492,16 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
         const StagedB st =
             stage_b(V.feat[3 * id], V.feat[3 * id + 1], V.feat[3 * id + 2], id, hw, hh, ox, oy);
         S0[sl] = st.s0; S1[sl] = st.s1; S2[sl] = st.s2; S3[sl] = st.s3;
+        SM[sl] = __float_as_uint(st.s3.w);
       }
       __syncthreads();
-      for (int j = 0; j < cnt; ++j) {
+      uint16_t *vl = VL[tid >> 5];
+      const int nvis = visit_list(SM, cnt, lay.warp_rows, vl, lane);
+      for (int i = 0; i < nvis; ++i) {
+        const int j = vl[i];
         const int li = top - 1 - j;
         const float4 s3 = S3[j];
         const uint32_t m = __float_as_uint(s3.w);
-        if (!(m & lay.warp_rows)) continue;  // warp-uniform
         const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j];
         const float dx = __fsub_rn(s0.x, pxf);
         const bool col_ok = (m & lay.colbit) != 0u;
