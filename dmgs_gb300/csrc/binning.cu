@@ -13,10 +13,11 @@
 //   3. chunk     the sorted list is cut into C contiguous chunks of equal
 //                work (weight of a Gaussian: CHUNK_W_GAUSS + ceil(tiles/32),
 //                the warp iterations it costs below) -> chunk starts;
-//   4. count     each chunk counts its instances per tile -> count matrix
-//                [T][C];
-//   5. scan      the matrix in (tile, chunk) order -> the first slot of every
-//                (tile, chunk) pair, the tile ranges and K;
+//   4. count     each chunk counts its instances per tile -> count matrix,
+//                stored chunk-major [C][T] (coalesced in every kernel);
+//   5. scan      per tile over the chunks (the within-tile offset of every
+//                (tile, chunk) pair and the tile's total), then over the
+//                tile totals -> tile bases, the tile ranges and K;
 //   6. emit      one warp per chunk walks its Gaussians in depth order and
 //                appends each Gaussian index to the lists of the tiles it
 //                covers, its running slots in shared memory.
@@ -26,8 +27,8 @@
 // sorted list.  Nothing of size K is read back or sorted; K is written once.
 // Near Gaussians cover thousands of tiles and sort together, so chunks of
 // equal Gaussian count would differ in work by an order of magnitude; equal
-// weight keeps one warp per chunk balanced.  The count matrix (T x C x 4 B,
-// 33 MB at 4056 tiles and 2048 chunks) stays in L2.
+// weight keeps one warp per chunk balanced.  The count matrix (C x T x 4 B,
+// 20 MB at 4056 tiles and 1216 chunks) stays in L2.
 //
 // Every kernel bins several views at once (blockIdx.y = view, each view with
 // its own geometry state and sizes): a batch of views fills the GPU with one
@@ -289,6 +290,10 @@ __device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1
   x0 = lo & 0xffff; y0 = lo >> 16; x1 = hi & 0xffff; y1 = hi >> 16;
 }
 
+// Chunk segments of the per-tile offset scan: segment s = chunks
+// [s L, (s + 1) L), L = ceil(C / segs).
+__device__ __forceinline__ uint32_t seg_len(uint32_t C, uint32_t segs) { return (C + segs - 1) / segs; }
+
 // L2 eviction-priority hints: the instance list is written 4 bytes at a time
 // by many warps, so its lines should stay in L2 until complete (evict_last);
 // the count-matrix reads of the emission are used once (evict_first).
@@ -445,7 +450,7 @@ count_kernel(const BinViews bv) {
     int run = 0;
     for (int row = 0; row < R; ++row) {
       run += dgrid[row * W + x];
-      Bv.cmat[(size_t)((ys + row) * bd.gx + x) * C + c] = (uint32_t)run;
+      Bv.cmat[(size_t)c * (bd.gx * bd.gy) + (ys + row) * bd.gx + x] = (uint32_t)run;
     }
   }
 }
@@ -474,16 +479,23 @@ band_kernel(const BinViews bv) {
   if (EMIT) {
     // an overflowed view (instances above the list capacity) emits nothing
     if (s0 >= s1 || (counters[CI_STATUS] & ST_OVERFLOW)) return;
+    // first list position of (tile, this chunk) = tile base + the counts of
+    // the earlier chunk segments + the offset within this chunk's segment
     const uint64_t once = l2_policy_first();
+    const int T = bd.gx * bd.gy;
+    const uint32_t *off = cmat + (size_t)c * T + t0;
+    const uint32_t *tb = Bv.tbase + t0;
+    const uint32_t *sp = Bv.segpre + (size_t)(c / seg_len(C, counters[CI_SEGS])) * T + t0;
     int i = lane;
     for (; i + 96 < nt; i += 128) {
-      const uint32_t a = ld_hint(cmat + (size_t)(t0 + i) * C + c, once);
-      const uint32_t e = ld_hint(cmat + (size_t)(t0 + i + 32) * C + c, once);
-      const uint32_t f = ld_hint(cmat + (size_t)(t0 + i + 64) * C + c, once);
-      const uint32_t g = ld_hint(cmat + (size_t)(t0 + i + 96) * C + c, once);
-      slot[i] = a; slot[i + 32] = e; slot[i + 64] = f; slot[i + 96] = g;
+      uint32_t a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        a[u] = ld_hint(off + i + 32 * u, once) + tb[i + 32 * u] + sp[i + 32 * u];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) slot[i + 32 * u] = a[u];
     }
-    for (; i < nt; i += 32) slot[i] = ld_hint(cmat + (size_t)(t0 + i) * C + c, once);
+    for (; i < nt; i += 32) slot[i] = ld_hint(off + i, once) + tb[i] + sp[i];
   } else {
     for (int i = lane; i < nt; i += 32) slot[i] = 0u;
   }
@@ -575,20 +587,73 @@ band_kernel(const BinViews bv) {
 // Tile ranges from the scanned count matrix.  When the instances exceed the
 // list capacity (capacity-bounded callers), every range is left empty and
 // the overflow bit is set, so no kernel reads past the list buffer.
+// Within-tile offsets of every (tile, chunk): a block takes 32 tiles (the
+// lanes: chunk-major storage makes each step a coalesced 128-byte row
+// segment) and `segs` chunk segments (the warps: 8 when one view fills the
+// launch, 1 when many views already provide the parallelism; a block is 256
+// threads either way).  Each warp
+// writes the exclusive prefix of its segment in place; the segment totals
+// give, per tile, segpre[s][t] (the counts of the earlier segments) and the
+// tile total tbase[t].  Offset of (t, c) = scanned tbase[t] +
+// segpre[seg(c)][t] + cmat[c][t].
+__global__ void __launch_bounds__(256)
+tile_scan_kernel(const BinViews bv, int segs) {
+  __shared__ uint32_t segsum[256];
+  const BinView &B = bv.v[blockIdx.y];
+  const int T = B.bd.gx * B.bd.gy;
+  const int tpb = 256 / segs;  // tiles per block
+  if ((int)blockIdx.x * tpb >= T) return;  // block-uniform
+  const int tl = threadIdx.x % tpb, seg = threadIdx.x / tpb;
+  const int t = blockIdx.x * tpb + tl;
+  if (blockIdx.x == 0 && threadIdx.x == 0) B.counters[CI_SEGS] = (uint32_t)segs;
+  const uint32_t C = B.counters[CI_C], L = seg_len(C, (uint32_t)segs);
+  const uint32_t c0 = min(C, seg * L), c1 = min(C, c0 + L);
+  uint32_t *col = B.cmat + t;
+  uint32_t run = 0;
+  if (t < T) {
+    uint32_t c = c0;
+    for (; c + 8 <= c1; c += 8) {
+      uint32_t x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x[u] = col[(size_t)(c + u) * T];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        col[(size_t)(c + u) * T] = run;
+        run += x[u];
+      }
+    }
+    for (; c < c1; ++c) {
+      const uint32_t x = col[(size_t)c * T];
+      col[(size_t)c * T] = run;
+      run += x;
+    }
+  }
+  segsum[threadIdx.x] = run;
+  __syncthreads();
+  if (t < T) {
+    uint32_t pre = 0;
+    for (int q = 0; q < seg; ++q) pre += segsum[q * tpb + tl];
+    B.segpre[(size_t)seg * T + t] = pre;
+    if (seg == segs - 1) B.tbase[t] = pre + run;
+  }
+}
+
+// Tile ranges from the scanned tile bases.  When the instances exceed the
+// list capacity (capacity-bounded callers), every range is left empty and
+// the overflow bit is set, so no kernel reads past the list buffer.
 __global__ void ranges_kernel(const BinViews bv) {
   const BinView &B = bv.v[blockIdx.y];
   const int T = B.bd.gx * B.bd.gy;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   uint32_t *counters = B.counters;
-  const uint32_t *cmat_scanned = B.cmat;
-  const uint32_t C = counters[CI_C], K = counters[CI_K];
+  const uint32_t K = counters[CI_K];
   const bool over = K > B.K_cap || (counters[CI_STATUS] & ST_OVERFLOW);
   if (over && t == 0) atomicOr(&counters[CI_STATUS], ST_OVERFLOW);
   uint2 r = make_uint2(0u, 0u);
-  if (C > 0 && !over) {
-    const uint32_t a = cmat_scanned[(size_t)t * C];
-    const uint32_t e = (t + 1 < T) ? cmat_scanned[(size_t)(t + 1) * C] : K;
+  if (B.P > 0 && !over) {
+    const uint32_t a = B.tbase[t];
+    const uint32_t e = (t + 1 < T) ? B.tbase[t + 1] : K;
     if (e > a) r = make_uint2(a, e);
     atomicMax(&counters[CI_MAXLIST], e - a);
   }
@@ -720,6 +785,8 @@ int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_l
   B.rhist = reinterpret_cast<uint32_t *>(geom + L.rhist);
   B.cmat = reinterpret_cast<uint32_t *>(geom + L.cmat);
   B.cstart = reinterpret_cast<uint32_t *>(geom + L.cstart);
+  B.tbase = reinterpret_cast<uint32_t *>(geom + L.tbase);
+  B.segpre = reinterpret_cast<uint32_t *>(geom + L.segpre);
   B.ranges = reinterpret_cast<uint2 *>(geom + L.ranges);
   B.point_list = reinterpret_cast<uint32_t *>(point_list);
   B.K_cap = K_cap;
@@ -783,8 +850,11 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
   }
   DMGS_TIMED(K_BIN_SCAN, s, {
     if (P > 0) {
+      const int segs = nv > 1 ? 1 : CHUNK_SEGS, tpb = 256 / segs;
+      dmgs_host::note_launch(), tile_scan_kernel<<<dim3((T + tpb - 1) / tpb, nv), 256, 0, s>>>(bv, segs);
       int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
-        return ScanView{B.cmat, B.counters + CI_NCM, B.n_cmat_max, B.part, B.counters + CI_K, B.counters};
+        return ScanView{B.tbase, nullptr, (uint32_t)(B.bd.gx * B.bd.gy), B.part, B.counters + CI_K,
+                        B.counters};
       }), s);
       if (r != DMGS_OK) return r;
     }

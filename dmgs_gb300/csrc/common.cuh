@@ -62,6 +62,7 @@ constexpr int RADIX_ITEMS = 8;           // keys per thread
 constexpr int RADIX_TILE = RADIX_BLOCK * RADIX_ITEMS;  // 2048 keys per block
 constexpr int CHUNK_MIN_GAUSS = 64;     // visible Gaussians per binning chunk (mean, minimum)
 constexpr int CHUNK_COUNT_MAX = 2048;    // binning chunks per view (maximum)
+constexpr int CHUNK_SEGS = 8;            // chunk segments of the per-tile offset scan
 constexpr int CHUNK_W_GAUSS = 2;         // chunk weight of a Gaussian: this + ceil(tiles / 32)
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
@@ -77,10 +78,12 @@ constexpr int CI_NRH = 6;      // radix histogram entries = 256 * NBR
 constexpr int CI_W = 7;        // total chunk weight of the visible Gaussians
 constexpr int CI_C = 8;        // chunks
 constexpr int CI_NCM = 9;      // count-matrix entries = T * C
+constexpr int CI_SEGS = 10;    // chunk segments of the per-tile offset scan
 constexpr int CI_WORDS = 16;
 
 struct GeomLayout {
-  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, cstart, scanpart,
+  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, cstart, tbase, segpre,
+      scanpart,
       ranges, counters, total;
   int P, gx, gy;
   int nb_pre, nb_radix;
@@ -113,6 +116,8 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.rhist = o;     o = align_up(o + L.n_rhist_max * 4 + 4, 256);
   L.cmat = o;      o = align_up(o + L.n_cmat_max * 4, 256);
   L.cstart = o;    o = align_up(o + (CHUNK_COUNT_MAX + 1) * 4, 256);
+  L.tbase = o;     o = align_up(o + (T + 1) * 4, 256);
+  L.segpre = o;    o = align_up(o + T * CHUNK_SEGS * 4, 256);
   L.scanpart = o;  o = align_up(o + L.n_part_max * 4, 256);
   L.ranges = o;    o = align_up(o + T * 8, 256);
   L.counters = o;  o = align_up(o + CI_WORDS * 4, 256);

@@ -49,7 +49,8 @@ struct BinView {
   uint32_t n_rhist_max, n_cmat_max;
   const uint8_t *flags;
   const float4 *feat;
-  uint32_t *blkcnt, *counters, *part, *k0, *k1, *v0, *v1, *rhist, *cmat, *cstart;
+  uint32_t *blkcnt, *counters, *part, *k0, *k1, *v0, *v1, *rhist, *cmat, *cstart, *tbase,
+      *segpre;
   uint2 *ranges;
   uint32_t *point_list;  // emission target (K_alloc entries)
   uint32_t K_cap;        // list capacity checked by the ranges (0xffffffff: sized afterwards)
