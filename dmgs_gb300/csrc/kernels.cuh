@@ -36,6 +36,11 @@ int launch_preprocess(const ViewParams &vp, const float *viewm, const float *pro
 int launch_mark_visible(int P, const float *means3D, const float *viewm, uint8_t *present,
                         cudaStream_t s);
 
+// loss.cu
+size_t l1_ssim_scratch_bytes(int C, int H, int W);
+int launch_l1_ssim(const float *x, const float *y, int C, int H, int W, float lambda,
+                   float *loss, float *grad, char *scratch, cudaStream_t s);
+
 // binning.cu — every stage bins a set of views in one launch per stage.
 constexpr int MAX_BIN_VIEWS = 16;
 

@@ -26,6 +26,7 @@ import torch
 import torch.nn.functional as F_
 
 from .binding import bind_faces
+from .loss import l1_ssim_loss
 from .rasterizer import GaussianRasterizationSettings, GaussianRasterizer
 
 # Real SH basis constants (degree <= 3), the standard orthonormal basis.
@@ -135,8 +136,9 @@ def eval_sh(deg, sh, dirs):
     return r
 
 
-def _gauss_window(size=11, sigma=1.5, channels=3, device="cuda"):
-    g = torch.exp(-((torch.arange(size, device=device) - size // 2) ** 2) / (2 * sigma ** 2))
+def _gauss_window(size=11, sigma=1.5, channels=3, device="cuda", dtype=torch.float32):
+    g = torch.exp(-((torch.arange(size, device=device, dtype=dtype) - size // 2) ** 2)
+                  / (2 * sigma ** 2))
     g = g / g.sum()
     w = (g[:, None] * g[None, :])[None, None]
     return w.expand(channels, 1, size, size).contiguous()
@@ -147,7 +149,8 @@ def ssim(img1, img2, window=None):
     C1 = 0.01^2, C2 = 0.03^2, per channel — the form of the reference's
     utils/loss_utils.py."""
     C = img1.shape[0]
-    w = window if window is not None else _gauss_window(channels=C, device=img1.device)
+    w = window if window is not None else _gauss_window(channels=C, device=img1.device,
+                                                        dtype=img1.dtype)
     a, b = img1[None], img2[None]
     mu1 = F_.conv2d(a, w, padding=5, groups=C)
     mu2 = F_.conv2d(b, w, padding=5, groups=C)
@@ -215,13 +218,18 @@ class MeshBoundScene:
         return img, radii, means2D
 
 
-def training_step(scene: MeshBoundScene, view, target, bg, lambda_dssim=0.2, window=None):
+def training_step(scene: MeshBoundScene, view, target, bg, lambda_dssim=0.2, window=None,
+                  fused_loss=True):
     """One stage-2 step, forward and backward: bind, colour, rasterise,
-    L1 + lambda (1 - SSIM), gradients into the scene's parameters."""
+    L1 + lambda (1 - SSIM) (the fused loss kernel, or the torch composition
+    with fused_loss=False), gradients into the scene's parameters."""
     for p in scene.params():
         p.grad = None
     img, radii, _ = scene.render(view, bg)
-    loss = (1.0 - lambda_dssim) * (img - target).abs().mean() + lambda_dssim * (
-        1.0 - ssim(img, target, window))
+    if fused_loss:
+        loss = l1_ssim_loss(img, target, lambda_dssim)
+    else:
+        loss = (1.0 - lambda_dssim) * (img - target).abs().mean() + lambda_dssim * (
+            1.0 - ssim(img, target, window))
     loss.backward()
     return loss.detach(), radii

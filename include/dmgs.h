@@ -231,6 +231,20 @@ int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
                             void *const *state, const size_t *state_bytes,
                             uint32_t *host_words, dmgs_stream_t stream);
 
+/* ---------------------------------------------------------------------- *
+ * Fused photometric loss (no counterpart kernel in the reference, which
+ * composes it from torch ops: l1_loss and ssim of utils/loss_utils.py as
+ * used by train_geo_stage2.py:114-116):
+ *   loss = (1 - lambda) mean|image - target| + lambda (1 - mean SSIM),
+ * SSIM with an 11 x 11 Gaussian window (sigma 1.5), zero padding, C1 = 0.01^2,
+ * C2 = 0.03^2, per channel.  image / target: [C,H,W] fp32 device arrays;
+ * writes *loss (device scalar, may be NULL) and grad = dloss/dimage [C,H,W].
+ * ---------------------------------------------------------------------- */
+size_t dmgs_l1_ssim_scratch_bytes(int32_t C, int32_t H, int32_t W);
+int dmgs_l1_ssim(const float *image, const float *target, int32_t C, int32_t H,
+                 int32_t W, float lambda_dssim, float *loss, float *grad,
+                 void *scratch, size_t scratch_bytes, dmgs_stream_t stream);
+
 /* Frustum test (replaces `mark_visible`): present[i] = 1 iff point i lies in
  * front of view-space z = 0.2.  present: [P] uint8 device. */
 int dmgs_mark_visible(int32_t P, const float *means3D, const float *viewmatrix,
