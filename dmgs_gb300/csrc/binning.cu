@@ -376,17 +376,8 @@ chunk_bounds_kernel(const BinViews bv) {
 }
 
 // ---- counting and emission: one warp per (chunk, band of tile rows) -------
-// A band is R consecutive rows of tiles; its running slots live in shared
-// memory (R * gx words).  The warp walks its chunk's Gaussians in depth order,
-// 32 at a time (lane i holds Gaussian g0 + i), selects by ballot the ones
-// whose rectangle meets the band and visits each one's tiles within the band,
-// its lanes spread over them.  One Gaussian covers each tile once, so within
-// a Gaussian the lanes touch distinct slots and a plain read/modify/write
-// suffices; __syncwarp orders consecutive Gaussians.  COUNT: slots start at
-// 0 and end as this chunk's per-tile counts (written to the count matrix).
-// EMIT: slots start at the scanned counts (first list position of each
-// (tile, chunk)) and each visit appends the Gaussian index.  Indices and
-// rectangles are loaded two and one groups ahead.
+// A band is R consecutive rows of tiles (R * gx <= ~1024 tiles).
+
 // Per-(tile, chunk) counts of one (chunk, band of tile rows) without walking
 // the instances: every Gaussian whose rectangle meets the band adds +1 / -1
 // at the four corners of its rectangle clipped to the band, in a 2D
@@ -455,9 +446,18 @@ count_kernel(const BinViews bv) {
   }
 }
 
-template <bool EMIT>
+// Emission.  The band's running slots live in shared memory (R * gx words),
+// starting at the first list position of each (tile, this chunk): tile base
+// + the counts of the earlier chunk segments + the offset within this
+// chunk's segment.  The warp walks its chunk's Gaussians in depth order, 32
+// at a time (lane i holds Gaussian g0 + i; indices and rectangles loaded two
+// and one groups ahead), selects by ballot the ones whose rectangle meets the
+// band and visits each one's tiles within the band, its lanes spread over
+// them, appending the Gaussian index.  One Gaussian covers each tile once, so
+// within a Gaussian the lanes touch distinct slots and a plain
+// read/modify/write suffices; __syncwarp orders consecutive Gaussians.
 __global__ void __launch_bounds__(32)
-band_kernel(const BinViews bv) {
+emit_kernel(const BinViews bv) {
   extern __shared__ uint32_t slot[];
   const BinView &Bv = bv.v[blockIdx.y];
   const Bands bd = Bv.bd;
@@ -476,11 +476,9 @@ band_kernel(const BinViews bv) {
   const int t0 = ys * bd.gx, nt = (ye - ys) * bd.gx;
   const uint32_t s0 = Bv.cstart[c], s1 = Bv.cstart[c + 1];
   const uint64_t keep = l2_policy_last();
-  if (EMIT) {
-    // an overflowed view (instances above the list capacity) emits nothing
-    if (s0 >= s1 || (counters[CI_STATUS] & ST_OVERFLOW)) return;
-    // first list position of (tile, this chunk) = tile base + the counts of
-    // the earlier chunk segments + the offset within this chunk's segment
+  // an overflowed view (instances above the list capacity) emits nothing
+  if (s0 >= s1 || (counters[CI_STATUS] & ST_OVERFLOW)) return;
+  {
     const uint64_t once = l2_policy_first();
     const int T = bd.gx * bd.gy;
     const uint32_t *off = cmat + (size_t)c * T + t0;
@@ -496,8 +494,6 @@ band_kernel(const BinViews bv) {
       for (int u = 0; u < 4; ++u) slot[i + 32 * u] = a[u];
     }
     for (; i < nt; i += 32) slot[i] = ld_hint(off + i, once) + tb[i] + sp[i];
-  } else {
-    for (int i = lane; i < nt; i += 32) slot[i] = 0u;
   }
   __syncwarp();
   bool bad = false;
@@ -527,7 +523,7 @@ band_kernel(const BinViews bv) {
       m &= m - 1;
       const uint32_t xyi = __shfl_sync(FULL, xy, i), wai = __shfl_sync(FULL, wa, i);
       const uint32_t mgi = __shfl_sync(FULL, mg, i);
-      const uint32_t idi = EMIT ? __shfl_sync(FULL, id, i) : 0u;
+      const uint32_t idi = __shfl_sync(FULL, id, i);
       const int bx = (int)(xyi & 0xffffu), by = (int)(xyi >> 16);
       const int rw = (int)(wai & 0xffffu), area = (int)(wai >> 16);
       RectWalk it(lane, rw, mgi);
@@ -546,11 +542,9 @@ band_kernel(const BinViews bv) {
         for (int u = 0; u < 4; ++u) p[u] = slot[a[u]];
 #pragma unroll
         for (int u = 0; u < 4; ++u) slot[a[u]] = p[u] + 1u;
-        if (EMIT) {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            if (p[u] < K_alloc) st_hint(point_list + p[u], idi, keep); else bad = true;
-          }
+        for (int u = 0; u < 4; ++u) {
+          if (p[u] < K_alloc) st_hint(point_list + p[u], idi, keep); else bad = true;
         }
       }
       for (; j + 32 < area; j += 64) {
@@ -561,41 +555,30 @@ band_kernel(const BinViews bv) {
         const uint32_t p0 = slot[a0], p1 = slot[a1];
         slot[a0] = p0 + 1u;
         slot[a1] = p1 + 1u;
-        if (EMIT) {
-          if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
-          if (p1 < K_alloc) st_hint(point_list + p1, idi, keep); else bad = true;
-        }
+        if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
+        if (p1 < K_alloc) st_hint(point_list + p1, idi, keep); else bad = true;
       }
       if (j < area) {
         const int a0 = o + it.row * bd.gx + it.col;
         const uint32_t p0 = slot[a0];
         slot[a0] = p0 + 1u;
-        if (EMIT) {
-          if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
-        }
+        if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
       }
       __syncwarp();
     }
   }
-  if (EMIT) {
-    if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
-  } else {
-    for (int i = lane; i < nt; i += 32) cmat[(size_t)(t0 + i) * C + c] = slot[i];
-  }
+  if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
 }
 
-// Tile ranges from the scanned count matrix.  When the instances exceed the
-// list capacity (capacity-bounded callers), every range is left empty and
-// the overflow bit is set, so no kernel reads past the list buffer.
-// Within-tile offsets of every (tile, chunk): a block takes 32 tiles (the
-// lanes: chunk-major storage makes each step a coalesced 128-byte row
-// segment) and `segs` chunk segments (the warps: 8 when one view fills the
-// launch, 1 when many views already provide the parallelism; a block is 256
-// threads either way).  Each warp
-// writes the exclusive prefix of its segment in place; the segment totals
-// give, per tile, segpre[s][t] (the counts of the earlier segments) and the
-// tile total tbase[t].  Offset of (t, c) = scanned tbase[t] +
-// segpre[seg(c)][t] + cmat[c][t].
+// Within-tile offsets of every (tile, chunk).  A block of 256 threads takes
+// 256 / segs tiles (consecutive threads = consecutive tiles: chunk-major
+// storage makes each step a coalesced row access) and splits the chunks into
+// `segs` contiguous segments (8 when one view fills the launch, 1 when many
+// views already provide the parallelism).  Each thread writes the exclusive
+// prefix of its segment in place; the segment totals give, per tile,
+// segpre[s][t] (the counts of the earlier segments) and the tile total
+// tbase[t].  Offset of (t, c) = scanned tbase[t] + segpre[seg(c)][t] +
+// cmat[c][t].
 __global__ void __launch_bounds__(256)
 tile_scan_kernel(const BinViews bv, int segs) {
   __shared__ uint32_t segsum[256];
@@ -714,13 +697,13 @@ int band_plan(int gx, int gy, BandPlan &pl) {
       attr_smem = std::max(pl.smem, csm);
       DMGS_CUDA(cudaFuncSetAttribute(count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)attr_smem));
-      DMGS_CUDA(cudaFuncSetAttribute(band_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)attr_smem));
     }
     int sms = 0, a = 0, b = 0;
     DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, count_kernel, 32, csm));
-    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, band_kernel<true>, 32, pl.smem));
+    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, emit_kernel, 32, pl.smem));
     cached_dev = dev;
     cached_smem = pl.smem;
     cached_resident = std::max(1, std::min(a, b)) * sms;
@@ -876,7 +859,7 @@ int launch_emit(const BinViews &bv, cudaStream_t s) {
   }
   if (!any) return DMGS_OK;
   DMGS_TIMED(K_BIN_EMIT, s,
-             dmgs_host::note_launch(), band_kernel<true><<<dim3(band_blocks, bv.n), 32, smem, s>>>(bv));
+             dmgs_host::note_launch(), emit_kernel<<<dim3(band_blocks, bv.n), 32, smem, s>>>(bv));
   DMGS_LAUNCH_CHECK("emit_kernel");
   return DMGS_OK;
 }

@@ -381,8 +381,8 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, bool inside, int pix,
 // in `take` runs one straight-line path.  T is recovered by dividing by
 // (1 - alpha) with the hardware reciprocal (alpha <= 0.99).
 __device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float alpha, float G,
-                                             const float4 &s1, const float4 &s2, const float4 &s3,
-                                             float dx, float dy, float *e) {
+                                             const float4 &s1, const float4 &s2, float dy,
+                                             float *e) {
   const float inv = rcp_approx(1.f - alpha);
   const float Tn = ps.T * inv;
   const float dr = s1.w - ps.acc_r, dg = s2.x - ps.acc_g, db = s2.y - ps.acc_b;
@@ -391,12 +391,12 @@ __device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float al
   const float at = take ? alpha : 0.f;
   const float wt = at * Tn;                      // dL/drgb weight
   const float u = s1.y * Gd;                     // dL/dpower = o G dL/dalpha
-  const float ux = u * dx, uy = u * dy;
-  e[0] += ux * s2.z + uy * s2.w;  // dL/dndc_x
-  e[1] += uy * s3.x + ux * s3.y;  // dL/dndc_y
-  e[2] += ux * dx;                // x -1/2 -> dL/dconic_a
-  e[3] += ux * dy;                // x -1   -> dL/dconic_b
-  e[4] += uy * dy;                // x -1/2 -> dL/dconic_c
+  const float uy = u * dy;
+  // the thread's pixels share dx: the mean and conic terms need only
+  // sum u, sum u dy and sum u dy^2 (combined with dx once per Gaussian)
+  e[0] += u;
+  e[1] += uy;
+  e[2] += uy * dy;
   e[5] += Gd;                     // dL/dopacity
   e[6] += wt * ps.g0;             // dL/drgb
   e[7] += wt * ps.g1;
@@ -405,6 +405,21 @@ __device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float al
   ps.acc_r = fmaf(at, dr, ps.acc_r);
   ps.acc_g = fmaf(at, dg, ps.acc_g);
   ps.acc_b = fmaf(at, db, ps.acc_b);
+}
+
+// From the thread's sums (e[0] = sum u, e[1] = sum u dy, e[2] = sum u dy^2
+// over its pixels, u = dL/dpower) to the mean and conic gradient terms:
+// e0 = dL/dndc_x, e1 = dL/dndc_y, e2..e4 = (sum u dx^2, sum u dx dy,
+// sum u dy^2) for the conic (scaled by -1/2, -1, -1/2 at the atomics).
+__device__ __forceinline__ void adjoint_finish(float dx, const float4 &s2, const float4 &s3,
+                                               float *e) {
+  const float su = e[0], suy = e[1], suy2 = e[2];
+  const float sux = dx * su;
+  e[0] = sux * s2.z + suy * s2.w;
+  e[1] = suy * s3.x + sux * s3.y;
+  e[2] = sux * dx;
+  e[3] = suy * dx;
+  e[4] = suy2;
 }
 
 // Transposed reduce-scatter of 16 slots over the warp: afterwards the lane
@@ -525,10 +540,11 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
           const float G = ex2_approx(e2[k]);
           const float alpha = fminf(ALPHA_MAX, __fmul_rn(s1.y, G));
           const bool take = ok[k] && !(alpha < ALPHA_MIN);
-          adjoint_pair(ps[k], take, alpha, G, s1, s2, s3, dx, __fsub_rn(s0.y, pyf[k]), e);
+          adjoint_pair(ps[k], take, alpha, G, s1, s2, __fsub_rn(s0.y, pyf[k]), e);
           any |= take;
         }
         if (__ballot_sync(FULL, any)) {
+          adjoint_finish(dx, s2, s3, e);
           const float sum = warp_reduce_scatter16(e, lane);
           const int slot = (lane >> 1) & 15;  // lane bits (4,3,2,1)
           if (!(lane & 1) && slot < 9) {
