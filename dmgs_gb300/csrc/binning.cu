@@ -483,7 +483,7 @@ emit_kernel(const BinViews bv) {
     const int T = bd.gx * bd.gy;
     const uint32_t *off = cmat + (size_t)c * T + t0;
     const uint32_t *tb = Bv.tbase + t0;
-    const uint32_t *sp = Bv.segpre + (size_t)(c / seg_len(C, counters[CI_SEGS])) * T + t0;
+    const uint32_t *sp = Bv.segpre + (size_t)(c / seg_len(C, CHUNK_SEGS)) * T + t0;
     int i = lane;
     for (; i + 96 < nt; i += 128) {
       uint32_t a[4];
@@ -570,26 +570,23 @@ emit_kernel(const BinViews bv) {
   if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
 }
 
-// Within-tile offsets of every (tile, chunk).  A block of 256 threads takes
-// 256 / segs tiles (consecutive threads = consecutive tiles: chunk-major
-// storage makes each step a coalesced row access) and splits the chunks into
-// `segs` contiguous segments (8 when one view fills the launch, 1 when many
-// views already provide the parallelism).  Each thread writes the exclusive
+// Within-tile offsets of every (tile, chunk).  A block takes 32 tiles (the
+// lanes: chunk-major storage makes each step a coalesced 128-byte row
+// segment) and CHUNK_SEGS contiguous chunk segments (the warps), so a view
+// of 4,056 tiles keeps ~4,000 warps busy.  Each thread writes the exclusive
 // prefix of its segment in place; the segment totals give, per tile,
 // segpre[s][t] (the counts of the earlier segments) and the tile total
 // tbase[t].  Offset of (t, c) = scanned tbase[t] + segpre[seg(c)][t] +
 // cmat[c][t].
-__global__ void __launch_bounds__(256)
-tile_scan_kernel(const BinViews bv, int segs) {
-  __shared__ uint32_t segsum[256];
+__global__ void __launch_bounds__(32 * CHUNK_SEGS)
+tile_scan_kernel(const BinViews bv) {
+  __shared__ uint32_t segsum[CHUNK_SEGS][32];
   const BinView &B = bv.v[blockIdx.y];
   const int T = B.bd.gx * B.bd.gy;
-  const int tpb = 256 / segs;  // tiles per block
-  if ((int)blockIdx.x * tpb >= T) return;  // block-uniform
-  const int tl = threadIdx.x % tpb, seg = threadIdx.x / tpb;
-  const int t = blockIdx.x * tpb + tl;
-  if (blockIdx.x == 0 && threadIdx.x == 0) B.counters[CI_SEGS] = (uint32_t)segs;
-  const uint32_t C = B.counters[CI_C], L = seg_len(C, (uint32_t)segs);
+  if ((int)blockIdx.x * 32 >= T) return;  // block-uniform
+  const int lane = threadIdx.x & 31, seg = threadIdx.x >> 5;
+  const int t = blockIdx.x * 32 + lane;
+  const uint32_t C = B.counters[CI_C], L = seg_len(C, CHUNK_SEGS);
   const uint32_t c0 = min(C, seg * L), c1 = min(C, c0 + L);
   uint32_t *col = B.cmat + t;
   uint32_t run = 0;
@@ -611,13 +608,13 @@ tile_scan_kernel(const BinViews bv, int segs) {
       run += x;
     }
   }
-  segsum[threadIdx.x] = run;
+  segsum[seg][lane] = run;
   __syncthreads();
   if (t < T) {
     uint32_t pre = 0;
-    for (int q = 0; q < seg; ++q) pre += segsum[q * tpb + tl];
+    for (int q = 0; q < seg; ++q) pre += segsum[q][lane];
     B.segpre[(size_t)seg * T + t] = pre;
-    if (seg == segs - 1) B.tbase[t] = pre + run;
+    if (seg == CHUNK_SEGS - 1) B.tbase[t] = pre + run;
   }
 }
 
@@ -833,8 +830,7 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
   }
   DMGS_TIMED(K_BIN_SCAN, s, {
     if (P > 0) {
-      const int segs = nv > 1 ? 1 : CHUNK_SEGS, tpb = 256 / segs;
-      dmgs_host::note_launch(), tile_scan_kernel<<<dim3((T + tpb - 1) / tpb, nv), 256, 0, s>>>(bv, segs);
+      dmgs_host::note_launch(), tile_scan_kernel<<<dim3((T + 31) / 32, nv), 32 * CHUNK_SEGS, 0, s>>>(bv);
       int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
         return ScanView{B.tbase, nullptr, (uint32_t)(B.bd.gx * B.bd.gy), B.part, B.counters + CI_K,
                         B.counters};

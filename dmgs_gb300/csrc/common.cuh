@@ -62,7 +62,7 @@ constexpr int RADIX_ITEMS = 8;           // keys per thread
 constexpr int RADIX_TILE = RADIX_BLOCK * RADIX_ITEMS;  // 2048 keys per block
 constexpr int CHUNK_MIN_GAUSS = 64;     // visible Gaussians per binning chunk (mean, minimum)
 constexpr int CHUNK_COUNT_MAX = 2048;    // binning chunks per view (maximum)
-constexpr int CHUNK_SEGS = 8;            // chunk segments of the per-tile offset scan
+constexpr int CHUNK_SEGS = 32;           // chunk segments of the per-tile offset scan
 constexpr int CHUNK_W_GAUSS = 2;         // chunk weight of a Gaussian: this + ceil(tiles / 32)
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
@@ -78,7 +78,6 @@ constexpr int CI_NRH = 6;      // radix histogram entries = 256 * NBR
 constexpr int CI_W = 7;        // total chunk weight of the visible Gaussians
 constexpr int CI_C = 8;        // chunks
 constexpr int CI_NCM = 9;      // count-matrix entries = T * C
-constexpr int CI_SEGS = 10;    // chunk segments of the per-tile offset scan
 constexpr int CI_WORDS = 16;
 
 struct GeomLayout {
