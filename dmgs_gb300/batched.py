@@ -224,6 +224,85 @@ class BatchedRasterizer:
         self._set_capacity([int(k * factor) + 1024 for k in self.count_instances()])
 
 
+class HostPipeline:
+    """Training steps whose inputs come from host memory and whose results go
+    back to it, overlapped: while step i computes, the upload of step i+1 and
+    the download of step i-1 run on their own copy streams.  Two
+    BatchedRasterizers (ping-pong device buffers, each replaying its own CUDA
+    graph) hold the Gaussians, image gradients and outputs of alternate steps.
+
+    ``names``: the Gaussian tensors uploaded every step (keys of
+    ``gaussians``); the rasteriser options (capacity, cfg, means2D_grads,
+    densify_stats) pass through ``**kw``."""
+
+    def __init__(self, settings, gaussians, names, **kw):
+        self.names = list(names)
+        self.slots = [BatchedRasterizer(settings, {k: v.detach().clone() for k, v in
+                                                   gaussians.items() if v is not None}, **kw)
+                      for _ in range(2)]
+        for br in self.slots:
+            br.capture()
+        dev = self.slots[0].device
+        self.up = torch.cuda.Stream(device=dev)
+        self.comp = torch.cuda.Stream(device=dev)
+        self.down = torch.cuda.Stream(device=dev)
+        self.free = [None, None]  # per slot: its last download done
+        self.last = None
+        self.i = 0
+
+    def set_config(self, ppt, batch):
+        for br in self.slots:
+            br.set_config(ppt, batch)
+            br.capture()
+
+    def start(self):
+        """Order the pipeline after the work already on the current stream."""
+        cur = torch.cuda.current_stream(self.slots[0].device)
+        for st in (self.up, self.comp, self.down):
+            st.wait_stream(cur)
+
+    def submit(self, host_gaussians, host_dout, host_images, host_grads):
+        """Enqueue one step: upload host_gaussians (dict) and host_dout (list
+        of [3,H,W]), forward + backward, download the images into
+        host_images and the gradients named in ``names`` into host_grads.
+        Host buffers must be pinned and stay untouched until the returned
+        event has completed."""
+        k = self.i % 2
+        self.i += 1
+        br = self.slots[k]
+        if self.free[k] is not None:
+            self.up.wait_event(self.free[k])
+        with torch.cuda.stream(self.up):
+            for n in self.names:
+                br.g[n].copy_(host_gaussians[n], non_blocking=True)
+            for d, h in zip(br.dL_dout, host_dout):
+                d.copy_(h, non_blocking=True)
+            uploaded = torch.cuda.Event()
+            uploaded.record(self.up)
+        self.comp.wait_event(uploaded)
+        with torch.cuda.stream(self.comp):
+            br.graph.replay()
+            computed = torch.cuda.Event()
+            computed.record(self.comp)
+        self.down.wait_event(computed)
+        with torch.cuda.stream(self.down):
+            for h, d in zip(host_images, br.images):
+                h.copy_(d, non_blocking=True)
+            for n in self.names:
+                host_grads[n].copy_(br.grads[n], non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(self.down)
+        self.free[k] = done
+        self.last = done
+        return done
+
+    def finish(self):
+        """Make the current stream wait for every submitted step."""
+        cur = torch.cuda.current_stream(self.slots[0].device)
+        for st in (self.up, self.comp, self.down):
+            cur.wait_stream(st)
+
+
 def autotune(br: BatchedRasterizer, space=TUNE_SPACE, iters=5, cache_path=None):
     """Time forward + backward for every (pixels/thread, batch) pair and
     keep the fastest; the choice is cached in JSON at ``cache_path`` (default
