@@ -239,3 +239,24 @@ def test_host_pipeline_overlapped_steps_match_the_direct_step():
             assert torch.equal(a, b.cpu())
         for k in names:
             assert rel_l2(grads[k].numpy(), br.grads[k].cpu().numpy()) <= 1e-5, k
+
+
+def test_view_with_nothing_visible_in_a_batch():
+    from dmgs_gb300.camera import make_view
+    sc, views = _scene_and_views(P=2000, seed=48)
+    g = _gauss(sc)
+    away = make_view((0.0, 0.0, 3.5), (0.0, 0.0, 10.0), 90, 70, fovx_deg=40)  # facing away
+    settings = [_settings(away, bg=(0.2, 0.3, 0.4)), _settings(views[0])]
+    br = BatchedRasterizer(settings, g)
+    assert br.count_instances()[0] == 0
+    br.forward()
+    br.backward([torch.ones_like(i) for i in br.images])
+    torch.cuda.synchronize()
+    br.status()
+    bg = torch.tensor([0.2, 0.3, 0.4], device=D).view(3, 1, 1).expand_as(br.images[0])
+    assert torch.equal(br.images[0], bg)
+    assert torch.count_nonzero(br.radii[0]) == 0
+    plain = _plain(g, settings[1], torch.ones(3, views[0].height, views[0].width, device=D))
+    assert torch.equal(br.images[1], plain[0])
+    for k in g:  # the empty view adds nothing to the summed gradients
+        assert rel_l2(br.grads[k].cpu().numpy(), plain[1][k].cpu().numpy()) <= 1e-5, k

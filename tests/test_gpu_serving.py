@@ -75,3 +75,17 @@ def test_poisson_trace_in_real_time(scenes):
     s = st.summary()
     assert s["requests"] == len(reqs) > 50
     assert 0 < s["p50_ms"] <= s["p99_ms"] < 1000
+
+
+def test_empty_and_culled_scenes_render_background(scenes):
+    from dmgs_gb300.camera import make_view
+    empty = ResidentScene({k: v[:0] for k, v in scenes[0].t.items()})
+    mixed = [scenes[0], empty]
+    away = make_view((0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 64, 48, fovx_deg=1.0)  # a sliver of sky
+    views = [(1, random_inside_view(np.random.default_rng(3), 96, 80)), (0, away), (0, _views(1)[0][1])]
+    est = CapacityEstimator(margin=1.0, slack=1024, default=lambda r: 1 << 16)
+    reqs = [Request(i, s, v, 0.0) for i, (s, v) in enumerate(views)]
+    Scheduler(GpuBackend(mixed, 1 << 30, n_streams=2), 1 << 30, estimator=est).run(reqs)
+    assert torch.count_nonzero(reqs[0].result) == 0  # empty scene: black background
+    for (s, v), r in zip(views[1:], reqs[1:]):
+        assert torch.equal(r.result, _plain(mixed[s], v))
