@@ -93,6 +93,9 @@ SIGNATURES = [
                                     C.POINTER(C.c_size_t), vp, vp]),
     ("dmgs_multi_status_async", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians),
                                           C.POINTER(vp), C.POINTER(C.c_size_t), vp, vp]),
+    ("dmgs_face_cull_scratch_bytes", C.c_size_t, [C.c_int32]),
+    ("dmgs_face_cull", C.c_int, [vp, C.c_int32, vp, C.c_int32, vp, vp, vp, vp, vp, C.c_size_t,
+                                 vp]),
     ("dmgs_l1_ssim_scratch_bytes", C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     ("dmgs_l1_ssim", C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, vp, vp, vp,
                                C.c_size_t, vp]),

@@ -137,3 +137,27 @@ def bind_faces_scale_rot(verts, faces, bc, scaling2d, rotation2d, thin_z):
     """Stage-3 binding.  Returns (xyz, scales, rotations) for the rasteriser's
     scale/rotation input mode."""
     return _Bind3.apply(verts, scaling2d, rotation2d, faces, bc, thin_z)
+
+
+def frustum_faces(verts, faces, full_proj):
+    """Stage-3 frustum face selection (scene/gaussian_geo_model_finetune.py:
+    33-48,404-409): the faces whose centroid lies inside 1.05x the clip volume
+    of the camera's full_proj_transform (stored [4,4], row-vector
+    convention).  Returns (face_mask bool [F], kept faces [F',3] int64, kept
+    face indices [F'] int64); the reference's gs_mask is
+    face_mask.repeat_interleave(G)."""
+    lib = _lib.load()
+    v = _prep(verts)
+    f = faces.detach().to(torch.int64).contiguous()
+    M = _prep(full_proj)
+    F = f.shape[0]
+    dev = v.device
+    mask = torch.empty(F, dtype=torch.uint8, device=dev)
+    kept = torch.empty(max(F, 1), dtype=torch.int32, device=dev)
+    num = torch.zeros(1, dtype=torch.int32, device=dev)
+    scratch = torch.empty(max(int(lib.dmgs_face_cull_scratch_bytes(F)), 1), dtype=torch.uint8,
+                          device=dev)
+    check(lib.dmgs_face_cull(ptr(v), v.shape[0], ptr(f), F, ptr(M), ptr(mask), ptr(kept), ptr(num),
+                             ptr(scratch), scratch.numel(), stream_of(dev)), "face_cull")
+    idx = kept[:int(num.item())].long()
+    return mask.bool(), f[idx], idx

@@ -461,4 +461,100 @@ int launch_bind3_bwd(const DmgsFaceBinding3 &b, const float *dxyz, const float *
   return DMGS_OK;
 }
 
+namespace {
+
+constexpr int CULL_BLOCK = 256;
+
+// Face f is in the frustum when its centroid (the mean of its vertices),
+// taken through the full projection (row-vector convention of the stored
+// matrix: p_j = sum_i c_i M[i][j] + M[3][j]), has |x/w|, |y/w|, |z/w| < 1.05
+// with w = p_3 + 1e-6 > 0 — the stage-3 test of
+// scene/gaussian_geo_model_finetune.py:33-48.  A face with a vertex index
+// outside [0, V) is not kept.
+__device__ __forceinline__ bool face_in_frustum(const float *__restrict__ verts, int V,
+                                                const int64_t *__restrict__ faces, int f,
+                                                const float *__restrict__ M) {
+  int64_t vi[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    vi[k] = faces[3 * (size_t)f + k];
+    if (vi[k] < 0 || vi[k] >= V) return false;
+  }
+  float c[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) c[a] += verts[3 * vi[k] + a];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) c[a] = c[a] / 3.f;
+  float p[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    p[j] = c[0] * __ldg(M + j) + c[1] * __ldg(M + 4 + j) + c[2] * __ldg(M + 8 + j) + __ldg(M + 12 + j);
+  const float w = p[3] + 1e-6f;
+  return w > 0.f && fabsf(p[0] / w) < 1.05f && fabsf(p[1] / w) < 1.05f && fabsf(p[2] / w) < 1.05f;
+}
+
+// The test per face, the per-block count of kept faces (for the
+// order-preserving compaction).
+__global__ void __launch_bounds__(CULL_BLOCK)
+face_cull_test_kernel(const float *__restrict__ verts, int V, const int64_t *__restrict__ faces,
+                      int F, const float *__restrict__ M, uint8_t *__restrict__ mask,
+                      uint32_t *__restrict__ blkcnt) {
+  const int f = blockIdx.x * CULL_BLOCK + threadIdx.x;
+  const bool keep = f < F && face_in_frustum(verts, V, faces, f, M);
+  if (f < F && mask) mask[f] = keep ? 1 : 0;
+  const int n = __syncthreads_count(keep);
+  if (threadIdx.x == 0) blkcnt[blockIdx.x] = (uint32_t)n;
+}
+
+// Kept face indices at their block's scanned offset, in face order (the
+// test is recomputed: cheaper than a round trip of a flag through memory).
+__global__ void __launch_bounds__(CULL_BLOCK)
+face_cull_compact_kernel(const float *__restrict__ verts, int V, const int64_t *__restrict__ faces,
+                         int F, const float *__restrict__ M, const uint32_t *__restrict__ blkoff,
+                         int32_t *__restrict__ kept) {
+  __shared__ uint32_t wcount[CULL_BLOCK / 32];
+  const int f = blockIdx.x * CULL_BLOCK + threadIdx.x;
+  const bool keep = f < F && face_in_frustum(verts, V, faces, f, M);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned b = __ballot_sync(0xffffffffu, keep);
+  if (lane == 0) wcount[wid] = __popc(b);
+  __syncthreads();
+  uint32_t before = 0;
+  for (int w = 0; w < wid; ++w) before += wcount[w];
+  if (keep) {
+    unsigned lt;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+    kept[blkoff[blockIdx.x] + before + __popc(b & lt)] = f;
+  }
+}
+
+}  // namespace
+
+size_t face_cull_scratch_bytes(int F) {
+  const uint32_t nb = (uint32_t)((F + CULL_BLOCK - 1) / CULL_BLOCK);
+  return align_up((size_t)nb * 4 + 4, 256) + scan_part_words(nb) * 4;
+}
+
+int launch_face_cull(const float *verts, int V, const int64_t *faces, int F,
+                     const float *full_proj, uint8_t *face_mask, int32_t *kept, int32_t *num_kept,
+                     char *scratch, cudaStream_t s) {
+  if (F <= 0) {
+    DMGS_CUDA(cudaMemsetAsync(num_kept, 0, 4, s));
+    return DMGS_OK;
+  }
+  const uint32_t nb = (uint32_t)((F + CULL_BLOCK - 1) / CULL_BLOCK);
+  uint32_t *blkcnt = reinterpret_cast<uint32_t *>(scratch);
+  uint32_t *part = reinterpret_cast<uint32_t *>(scratch + align_up((size_t)nb * 4 + 4, 256));
+  DMGS_TIMED(K_FACE_CULL, s, {
+    dmgs_host::note_launch(), face_cull_test_kernel<<<nb, CULL_BLOCK, 0, s>>>(verts, V, faces, F, full_proj, face_mask, blkcnt);
+    int r = launch_scan1(blkcnt, nb, part, reinterpret_cast<uint32_t *>(num_kept), nullptr, s);
+    if (r != DMGS_OK) return r;
+    dmgs_host::note_launch(), face_cull_compact_kernel<<<nb, CULL_BLOCK, 0, s>>>(verts, V, faces, F, full_proj, blkcnt, kept);
+  });
+  DMGS_LAUNCH_CHECK("face_cull");
+  return DMGS_OK;
+}
+
 }  // namespace dmgs

@@ -744,6 +744,16 @@ ScanViews scan_views(const BinViews &bv, F &&f) {
 
 }  // namespace
 
+int launch_scan1(uint32_t *data, uint32_t n, uint32_t *part, uint32_t *total_out,
+                 uint32_t *status, cudaStream_t s) {
+  ScanViews sv;
+  sv.n = 1;
+  sv.v[0] = ScanView{data, nullptr, n, part, total_out, status};
+  return launch_scan_views(sv, s);
+}
+
+size_t scan_part_words(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
+
 int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_list,
                   uint32_t K_alloc, BinView &B) {
   BandPlan pl;

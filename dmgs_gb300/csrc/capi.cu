@@ -363,4 +363,21 @@ int dmgs_bind3_bwd(const DmgsFaceBinding3 *b, const float *dL_dxyz, const float 
                           dL_drotation2d, reinterpret_cast<cudaStream_t>(stream));
 }
 
+size_t dmgs_face_cull_scratch_bytes(int32_t F) { return F < 0 ? 0 : face_cull_scratch_bytes(F); }
+
+int dmgs_face_cull(const float *verts, int32_t V, const int64_t *faces, int32_t F,
+                   const float *full_proj, uint8_t *face_mask, int32_t *kept_faces,
+                   int32_t *num_kept, void *scratch, size_t scratch_bytes, dmgs_stream_t stream) {
+  if (F < 0 || V < 0 || !num_kept || (F > 0 && (!verts || !faces || !full_proj || !kept_faces))) {
+    set_error("face_cull: invalid arguments");
+    return DMGS_ERR_ARG;
+  }
+  if (F > 0 && (!scratch || scratch_bytes < face_cull_scratch_bytes(F))) {
+    set_error("face_cull: scratch too small");
+    return DMGS_ERR_STATE;
+  }
+  return launch_face_cull(verts, V, faces, F, full_proj, face_mask, kept_faces, num_kept,
+                          static_cast<char *>(scratch), reinterpret_cast<cudaStream_t>(stream));
+}
+
 }  // extern "C"

@@ -89,6 +89,11 @@ struct ScanViews {
 int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_list,
                   uint32_t K_alloc, BinView &B);
 int launch_binning_geometry(const BinViews &bv, cudaStream_t s);
+// Exclusive scan of one u32 array of n entries in place (part: scan_part_words(n)
+// words of scratch; total to *total_out, overflow bit into *status when given).
+int launch_scan1(uint32_t *data, uint32_t n, uint32_t *part, uint32_t *total_out,
+                 uint32_t *status, cudaStream_t s);
+size_t scan_part_words(uint32_t n);
 int launch_emit(const BinViews &bv, cudaStream_t s);
 int launch_debug_keys(const GeomLayout &L, const char *geom, const BinLayout &B, const char *bin,
                       uint64_t *keys, uint32_t *values, cudaStream_t s);
@@ -152,6 +157,11 @@ int launch_bind_fwd(const DmgsFaceBinding &b, float *xyz, float *cov, float *rot
                     cudaStream_t s);
 int launch_bind_bwd(const DmgsFaceBinding &b, const float *dxyz, const float *dcov,
                     float *dverts, float *dsf, cudaStream_t s);
+// Frustum face culling (binding.cu): scratch bytes and launcher.
+size_t face_cull_scratch_bytes(int F);
+int launch_face_cull(const float *verts, int V, const int64_t *faces, int F,
+                     const float *full_proj, uint8_t *face_mask, int32_t *kept, int32_t *num_kept,
+                     char *scratch, cudaStream_t s);
 int launch_bind3_fwd(const DmgsFaceBinding3 &b, float *xyz, float *scales, float *rots,
                      cudaStream_t s);
 int launch_bind3_bwd(const DmgsFaceBinding3 &b, const float *dxyz, const float *dscales,

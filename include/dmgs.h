@@ -231,6 +231,20 @@ int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
                             void *const *state, const size_t *state_bytes,
                             uint32_t *host_words, dmgs_stream_t stream);
 
+/* Frustum face culling of the stage-3 binding (replaces in_frustum and the
+ * face selection of scene/gaussian_geo_model_finetune.py:33-48,404-409):
+ * face f is kept when its centroid, taken through full_proj (the camera's
+ * full_proj_transform as stored, 16 floats, device), has |x/w|, |y/w|, |z/w|
+ * < 1.05 with w = p.w + 1e-6 > 0.  face_mask[F] (may be NULL) receives
+ * 1/0 per face; kept_faces receives the kept face indices in order and
+ * *num_kept (device int32) their number.  verts: [V,3], faces: [F,3] int64
+ * (device); a face with a vertex index outside [0, V) is not kept. */
+size_t dmgs_face_cull_scratch_bytes(int32_t F);
+int dmgs_face_cull(const float *verts, int32_t V, const int64_t *faces, int32_t F,
+                   const float *full_proj, uint8_t *face_mask, int32_t *kept_faces,
+                   int32_t *num_kept, void *scratch, size_t scratch_bytes,
+                   dmgs_stream_t stream);
+
 /* ---------------------------------------------------------------------- *
  * Fused photometric loss (no counterpart kernel in the reference, which
  * composes it from torch ops: l1_loss and ssim of utils/loss_utils.py as

@@ -101,3 +101,31 @@ def test_stage3_against_reference_and_oracle():
     assert rel_l2(verts.grad.cpu().numpy(), v64.grad.numpy()) <= 1e-3
     assert rel_l2(s2.grad.cpu().numpy(), s64.grad.numpy()) <= 1e-4
     assert rel_l2(r2.grad.cpu().numpy(), r64.grad.numpy()) <= 1e-3
+
+
+def test_frustum_face_culling_matches_the_reference_rule():
+    import numpy as np
+    from dmgs_gb300.binding import frustum_faces
+    from dmgs_gb300.camera import make_view
+    from dmgs_gb300.meshbound import sphere_torus_mesh
+    v, f = sphere_torus_mesh(32)
+    verts = torch.tensor(v, device="cuda")
+    faces = torch.tensor(f, device="cuda")
+    view = make_view((1.2, 0.4, 1.0), (0.0, 0.0, 0.0), 200, 160, fovx_deg=40)
+    M = torch.tensor(view.projmatrix, device="cuda")
+    mask, kept, idx = frustum_faces(verts, faces, M)
+    # the reference's in_frustum on face centroids, in float64
+    c = verts.double()[faces].mean(dim=1)
+    p = c @ M.double()[:3] + M.double()[3:]
+    w = p[:, 3:] + 1e-6
+    q = p[:, :3] / w
+    ref = (q.abs() < 1.05).all(dim=-1) & (w.squeeze() > 0)
+    near = ((q.abs() - 1.05).abs() < 1e-4).any(dim=-1) | (w.squeeze().abs() < 1e-4)
+    assert torch.equal(mask[~near], ref[~near])
+    assert 0 < int(mask.sum()) < len(f)
+    assert torch.equal(idx, torch.nonzero(mask).squeeze(1))  # kept in face order
+    assert torch.equal(kept, faces[mask])
+    bad = faces.clone()
+    bad[0, 0] = len(v) + 5  # out-of-range vertex: never kept
+    m2, _, _ = frustum_faces(verts, bad, M)
+    assert not bool(m2[0])
