@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="use the default blend configuration")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-bound training leg")
+    ap.add_argument("--no-fc", action="store_true", help="skip the FlexiCubes extraction leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="requests per second")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of in-flight requests")
@@ -302,6 +303,68 @@ def mesh_leg(args, dev):
         if name in kt:
             out.setdefault("kernels_ms", {})[name] = kt[name][0] / kt[name][1]
     del scene, target, targets
+    return out
+
+
+def flexicubes_leg(args, dev):
+    """FlexiCubes extraction as stage 2 runs it every step
+    (scene/gaussian_geo_model_mlp_flex.py:240-255: deformed grid, per-cube
+    weights initialised to ones, training mode) on the sphere-union-torus
+    field over [-1,1]^3: forward and forward+backward ms at 64^3 (the
+    configuration-2 grid) and at 128^3 and 250^3 (the reference configs'
+    res_fg range, 100-300), with the float32 CPU oracle at 64^3 beside it."""
+    import torch
+    from dmgs_gb300 import _lib
+    from dmgs_gb300.flexicubes import FlexiCubes
+    from dmgs_gb300.meshbound import sdf_sphere_torus
+    lib = _lib.load()
+    fc = FlexiCubes(device=dev)
+    out = {"field": "sphere(0.6) union torus(0.7, 0.2) over [-1,1]^3, training mode, "
+                    "deformation tanh(0), raw weights 1 (the reference's initialisation)"}
+    for res in (64, 128, 250):
+        grid, cubes = fc.construct_voxel_grid_v2(res, [-1.0] * 3, [1.0] * 3)
+        s0 = torch.as_tensor(sdf_sphere_torus(grid.double().cpu().numpy()), dtype=torch.float32,
+                             device=dev)
+        sdf = s0.clone().requires_grad_(True)
+        deform = torch.zeros_like(grid, requires_grad=True)
+        w = torch.ones((cubes.shape[0], 21), device=dev, requires_grad=True)
+        maxd = 2.0 / res / 4
+
+        def fwd():
+            x = grid + maxd * torch.tanh(deform)
+            return fc(x, sdf, cubes, res, w[:, :12], w[:, 12:20], w[:, 20], training=True)
+
+        def step(i):
+            v, f, L, se = fwd()
+            (v.square().sum() + L.mean()).backward()
+
+        n = 20
+        l0 = lib.dmgs_kernel_launches()
+        ms_fwd = timed(lambda i: fwd(), n, 3, dev) / n
+        ms_step = timed(step, n, 3, dev) / n
+        launches = (lib.dmgs_kernel_launches() - l0) / (2 * n + 6)
+        v, f, L, se = fwd()
+        out[f"res{res}"] = {"cubes": int(cubes.shape[0]), "faces": int(f.shape[0]),
+                            "vertices": int(v.shape[0]), "surface_edges": int(se.shape[0]),
+                            "fwd_ms": ms_fwd, "fwd_bwd_ms": ms_step,
+                            "own_kernels_per_fwd_bwd": launches}
+        del grid, cubes, s0, sdf, deform, w, v, f, L, se
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu:
+        from oracle import flexicubes as ofc  # CPU baseline only
+        torch.set_num_threads(os.cpu_count())
+        verts, cubes = ofc.voxel_grid(64, (-1, -1, -1), (1, 1, 1))
+        s = torch.tensor(sdf_sphere_torus(verts.double().numpy()), dtype=torch.float32,
+                         requires_grad=True)
+        wc = torch.ones((cubes.shape[0], 21), requires_grad=True)
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            v, f, L, se = ofc.extract(verts, s, cubes, 64, wc[:, :12], wc[:, 12:20], wc[:, 20],
+                                      training=True)
+            (v.square().sum() + L.mean()).backward()
+        out["cpu_baseline"] = {"fwd_bwd_ms": (time.perf_counter() - t0) / reps * 1e3,
+                               "res": 64, "cores": os.cpu_count(), "kind": "port",
+                               "sample": "float32 torch oracle on the host, 3 forward+backward"}
     return out
 
 
@@ -580,6 +643,9 @@ def main():
     mesh = None
     if not args.no_mesh:
         mesh = mesh_leg(args, dev)
+    fcl = None
+    if not args.no_fc:
+        fcl = flexicubes_leg(args, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -607,7 +673,7 @@ def main():
             "mixed": mixed,
             "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
-            "serving": serving, "mesh_training": mesh,
+            "serving": serving, "mesh_training": mesh, "flexicubes": fcl,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))
     if world > 1:

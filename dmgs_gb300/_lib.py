@@ -50,6 +50,11 @@ class DmgsFaceBinding3(C.Structure):
                 ("verts", vp), ("faces", vp), ("bc", vp), ("scaling2d", vp), ("rotation2d", vp)]
 
 
+class DmgsFcGrid(C.Structure):
+    _fields_ = [("x", vp), ("s", vp), ("beta", vp), ("alpha", vp), ("gamma", vp),
+                ("rx", C.c_int32), ("ry", C.c_int32), ("rz", C.c_int32), ("training", C.c_int32)]
+
+
 class DmgsBatch(C.Structure):
     _fields_ = [("nviews", C.c_int32), ("views", C.POINTER(DmgsView)),
                 ("out_color", C.POINTER(vp)), ("radii", C.POINTER(vp)),
@@ -96,6 +101,14 @@ SIGNATURES = [
     ("dmgs_face_cull_scratch_bytes", C.c_size_t, [C.c_int32]),
     ("dmgs_face_cull", C.c_int, [vp, C.c_int32, vp, C.c_int32, vp, vp, vp, vp, vp, C.c_size_t,
                                  vp]),
+    ("dmgs_fc_tables", C.c_int, [vp, vp, vp]),
+    ("dmgs_fc_state_bytes", C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
+    ("dmgs_fc_work_bytes", C.c_size_t, [vp]),
+    ("dmgs_fc_count", C.c_int, [C.POINTER(DmgsFcGrid), vp, C.c_size_t, vp, vp]),
+    ("dmgs_fc_emit", C.c_int, [C.POINTER(DmgsFcGrid), vp, vp, C.c_size_t, vp, C.c_size_t, vp, vp,
+                               vp, vp, vp]),
+    ("dmgs_fc_bwd", C.c_int, [C.POINTER(DmgsFcGrid), vp, vp, C.c_size_t, vp, C.c_size_t, vp, vp,
+                              vp, vp, vp, vp, vp, vp, vp]),
     ("dmgs_l1_ssim_scratch_bytes", C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     ("dmgs_l1_ssim", C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, vp, vp, vp,
                                C.c_size_t, vp]),

@@ -1,0 +1,175 @@
+"""FlexiCubes isosurface extraction on the GPU (csrc/flexicubes.cu).
+
+Drop-in for the reference's ``geo.flexicubes.FlexiCubes`` as stage 2 uses it
+(``scene/gaussian_geo_model_mlp_flex.py:177-181,240-255``): a regular grid
+from ``construct_voxel_grid_v2`` and ``__call__(x_nx3, s_n, cube_fx8, res,
+beta_fx12, alpha_fx8, gamma_f, training=...)`` returning
+``(vertices, faces, L_dev, surf_edges)``, differentiable w.r.t. the vertex
+positions, the scalar field and the three raw weight sets.
+
+Not provided (no DMGS caller uses them): the tetrahedral output
+(``output_tetmesh=True``), the QEF path (``grad_func``) and cube layouts other
+than the regular grid's; each raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib
+from ._lib import check, ptr, stream_of
+
+__all__ = ["FlexiCubes", "flexicubes"]
+
+
+def _grid(x, s, beta, alpha, gamma, res, training):
+    g = _lib.DmgsFcGrid()
+    g.x, g.s = x.data_ptr(), s.data_ptr()
+    g.beta, g.alpha, g.gamma = ptr(beta), ptr(alpha), ptr(gamma)
+    g.rx, g.ry, g.rz = (int(r) for r in res)
+    g.training = 1 if training else 0
+    return g
+
+
+def _f32(t):
+    return None if t is None else t.detach().float().contiguous()
+
+
+class _FlexiCubesFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, s, beta, alpha, gamma, res, training):
+        lib = _lib.load()
+        dev = x.device
+        xs, ss, bs, as_, gs = (_f32(t) for t in (x, s, beta, alpha, gamma))
+        grid = _grid(xs, ss, bs, as_, gs, res, training)
+        state = torch.empty(lib.dmgs_fc_state_bytes(*grid_res(res)), dtype=torch.uint8, device=dev)
+        counts = (C.c_uint32 * 8)()
+        stream = stream_of(dev)
+        check(lib.dmgs_fc_count(C.byref(grid), state.data_ptr(), state.numel(), C.addressof(counts),
+                                stream), "fc_count")
+        n_surf, n_vd, n_ent, n_edges, n_quads = (int(counts[k]) for k in range(5))
+        work = torch.empty(max(1, lib.dmgs_fc_work_bytes(C.addressof(counts))), dtype=torch.uint8,
+                           device=dev)
+        nverts = n_vd + (n_quads if training else 0)
+        vertices = torch.empty((nverts, 3), dtype=torch.float32, device=dev)
+        faces = torch.empty(((4 if training else 2) * n_quads, 3), dtype=torch.int64, device=dev)
+        L_dev = torch.empty((n_ent,), dtype=torch.float32, device=dev)
+        surf_edges = torch.empty((n_edges, 2), dtype=torch.int64, device=dev)
+        if n_surf:
+            check(lib.dmgs_fc_emit(C.byref(grid), C.addressof(counts), state.data_ptr(), state.numel(),
+                                   work.data_ptr(), work.numel(), vertices.data_ptr(), ptr(faces),
+                                   ptr(L_dev), ptr(surf_edges), stream), "fc_emit")
+        ctx.res, ctx.training, ctx.counts = tuple(res), training, bytes(counts)
+        ctx.has = (beta is not None, alpha is not None, gamma is not None)
+        ctx.save_for_backward(xs, ss, bs, as_, gs, state, work, vertices)
+        ctx.mark_non_differentiable(faces, surf_edges)
+        return vertices, faces, L_dev, surf_edges
+
+    @staticmethod
+    def backward(ctx, dvertices, dfaces, dL_dev, dsurf):
+        lib = _lib.load()
+        xs, ss, bs, as_, gs, state, work, vertices = ctx.saved_tensors
+        dev = xs.device
+        counts = (C.c_uint32 * 8).from_buffer_copy(ctx.counts)
+        grid = _grid(xs, ss, bs, as_, gs, ctx.res, ctx.training)
+        dvert = (dvertices.float().contiguous().clone() if dvertices is not None
+                 else torch.zeros_like(vertices))
+        dL = dL_dev.float().contiguous() if dL_dev is not None else \
+            torch.zeros((int(counts[2]),), dtype=torch.float32, device=dev)
+        dx = torch.empty_like(xs)
+        ds = torch.empty_like(ss)
+        db = torch.empty_like(bs) if ctx.has[0] and ctx.needs_input_grad[2] else None
+        da = torch.empty_like(as_) if ctx.has[1] and ctx.needs_input_grad[3] else None
+        dg = torch.empty_like(gs) if ctx.has[2] and ctx.needs_input_grad[4] else None
+        check(lib.dmgs_fc_bwd(C.byref(grid), C.addressof(counts), state.data_ptr(), state.numel(),
+                              work.data_ptr(), work.numel(), ptr(vertices), ptr(dvert), ptr(dL),
+                              dx.data_ptr(), ds.data_ptr(), ptr(db), ptr(da), ptr(dg),
+                              stream_of(dev)), "fc_bwd")
+        return dx, ds, db, da, dg, None, None
+
+
+def grid_res(res):
+    if isinstance(res, int):
+        return (res, res, res)
+    r = tuple(int(v) for v in res)
+    if len(r) != 3 or min(r) <= 0:
+        raise ValueError(f"grid resolution must be 3 positive integers, got {res}")
+    return r
+
+
+def flexicubes(x_nx3, s_n, res, beta_fx12=None, alpha_fx8=None, gamma_f=None, training=False):
+    """FlexiCubes triangle extraction on the regular grid of ``res``; see
+    ``FlexiCubes.__call__``."""
+    res = grid_res(res)
+    N = (res[0] + 1) * (res[1] + 1) * (res[2] + 1)
+    Cn = res[0] * res[1] * res[2]
+    if not x_nx3.is_cuda:
+        raise RuntimeError("flexicubes: inputs must be CUDA tensors (no CPU path)")
+    if tuple(x_nx3.shape) != (N, 3) or tuple(s_n.reshape(-1).shape) != (N,):
+        raise ValueError(f"flexicubes: x [{N},3] and s [{N}] expected for grid {res}")
+    for name, t, shp in (("beta_fx12", beta_fx12, (Cn, 12)), ("alpha_fx8", alpha_fx8, (Cn, 8)),
+                         ("gamma_f", gamma_f, (Cn,))):
+        if t is not None and tuple(t.shape) != shp:
+            raise ValueError(f"flexicubes: {name} must be {list(shp)}, got {list(t.shape)}")
+    v, f, L, se = _FlexiCubesFn.apply(x_nx3, s_n.reshape(-1), beta_fx12, alpha_fx8,
+                                      gamma_f, res, bool(training))
+    if v.shape[0] == 0 and f.shape[0] == 0 and se.shape[0] == 0:
+        return v, f, L, None   # the reference's result for a grid without surface
+    return v, f, L, se
+
+
+class FlexiCubes:
+    """GPU FlexiCubes with the reference class's interface
+    (``geo/flexicubes.py:16-180``) for the regular-grid triangle path."""
+
+    def __init__(self, device="cuda", qef_reg_scale=1e-3, weight_scale=0.99):
+        if abs(weight_scale - 0.99) > 1e-12:
+            raise NotImplementedError("FlexiCubes: only weight_scale=0.99 (the reference default)")
+        self.device = device
+        self.qef_reg_scale = qef_reg_scale
+        self.weight_scale = weight_scale
+        self._regular = {}
+
+    def construct_voxel_grid_v2(self, res, xyz_min=None, xyz_max=None):
+        """Vertices [(rx+1)(ry+1)(rz+1), 3] on linspace axes and the corner
+        indices of each cube [rx ry rz, 8], both in (i, j, k) order
+        (``geo/flexicubes.py:133-157``)."""
+        res = grid_res(res)
+        lo = [-0.5] * 3 if xyz_min is None else [float(v) for v in xyz_min]
+        hi = [0.5] * 3 if xyz_max is None else [float(v) for v in xyz_max]
+        axes = [torch.linspace(lo[d], hi[d], res[d] + 1, device=self.device) for d in range(3)]
+        verts = torch.stack(torch.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+        return verts, self._cubes(res)
+
+    def _cubes(self, res):
+        rx, ry, rz = res
+        dev = self.device
+        i = torch.arange(rx, device=dev).view(-1, 1, 1)
+        j = torch.arange(ry, device=dev).view(1, -1, 1)
+        k = torch.arange(rz, device=dev).view(1, 1, -1)
+        base = ((i * (ry + 1) + j) * (rz + 1) + k).reshape(-1, 1)
+        n = torch.arange(8, device=dev)
+        off = (n & 1) * (ry + 1) * (rz + 1) + ((n >> 1) & 1) * (rz + 1) + ((n >> 2) & 1)
+        return base + off.view(1, 8)   # int64, as the reference's sum over int32 gives
+
+    def _check_regular(self, cube_fx8, res):
+        key = (cube_fx8.data_ptr(), tuple(cube_fx8.shape), cube_fx8._version, res)
+        if key in self._regular:
+            return
+        ok = tuple(cube_fx8.shape) == (res[0] * res[1] * res[2], 8) and bool(
+            torch.equal(cube_fx8.to(torch.int64), self._cubes(res).to(cube_fx8.device).to(torch.int64)))
+        if not ok:
+            raise NotImplementedError("FlexiCubes: cube_fx8 must be the regular grid of "
+                                      "construct_voxel_grid_v2 for this resolution")
+        self._regular = {key: True}
+
+    def __call__(self, x_nx3, s_n, cube_fx8, res, beta_fx12=None, alpha_fx8=None, gamma_f=None,
+                 training=False, output_tetmesh=False, grad_func=None):
+        if output_tetmesh:
+            raise NotImplementedError("FlexiCubes: tetrahedral output is not provided")
+        if grad_func is not None:
+            raise NotImplementedError("FlexiCubes: the grad_func (QEF) path is not provided")
+        res = grid_res(res)
+        self._check_regular(cube_fx8, res)
+        return flexicubes(x_nx3, s_n, res, beta_fx12, alpha_fx8, gamma_f, training)

@@ -10,12 +10,10 @@ eval_sh then sigmoid), rasterises with precomputed covariance and colours
 library's kernels; the SH colour and the loss stay in torch as in the
 reference.
 
-The mesh of the workload is built by :func:`sphere_torus_mesh`: a surface of
-the union of a sphere (r 0.6) and a torus (R 0.7, r 0.2) on a 64^3 grid over
-[-1, 1]^3, one vertex per sign-changing cell (the mean of its edge
-crossings) and, for every sign-changing grid edge, the quad of the four
-cells around it split into four triangles about its centre — the face count
-of FlexiCubes' training-mode extraction of the same field (45,304).
+The mesh of the workload is built by :func:`sphere_torus_mesh`: this
+library's FlexiCubes extraction (csrc/flexicubes.cu) of the union of a
+sphere (r 0.6) and a torus (R 0.7, r 0.2) sampled on a 64^3 grid over
+[-1, 1]^3, in training mode (45,304 faces).
 """
 from __future__ import annotations
 
@@ -26,6 +24,7 @@ import torch
 import torch.nn.functional as F_
 
 from .binding import bind_faces
+from .flexicubes import FlexiCubes
 from .loss import l1_ssim_loss
 from .rasterizer import GaussianRasterizationSettings, GaussianRasterizer
 
@@ -45,72 +44,16 @@ def sdf_sphere_torus(p):
     return np.minimum(sph, tor)
 
 
-def sphere_torus_mesh(res=64, lo=-1.0, hi=1.0, sdf=sdf_sphere_torus):
-    """Surface of an SDF on a res^3 grid: (verts [V,3] float32, faces [F,3]
-    int64), outward-facing triangles."""
-    g = np.linspace(lo, hi, res + 1)
-    P = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1)
-    d = sdf(P)
-    inside = d < 0
-    # edge crossings: points where the field changes sign along each grid edge
-    cell_sum = np.zeros((res, res, res, 3))
-    cell_cnt = np.zeros((res, res, res))
-    for axis in range(3):
-        sl0 = [slice(None)] * 3
-        sl1 = [slice(None)] * 3
-        sl0[axis] = slice(0, -1)
-        sl1[axis] = slice(1, None)
-        d0, d1 = d[tuple(sl0)], d[tuple(sl1)]
-        p0, p1 = P[tuple(sl0)], P[tuple(sl1)]
-        cross = (d0 < 0) != (d1 < 0)
-        t = np.where(cross, d0 / np.where(cross, d0 - d1, 1.0), 0.0)
-        pt = p0 + t[..., None] * (p1 - p0)
-        # the edge belongs to the 4 cells around it
-        idx = np.argwhere(cross)
-        for o1 in (0, -1):
-            for o2 in (0, -1):
-                c = idx.copy()
-                other = [a for a in range(3) if a != axis]
-                c[:, other[0]] += o1
-                c[:, other[1]] += o2
-                ok = np.all((c >= 0) & (c < res), axis=1)
-                cc = c[ok]
-                np.add.at(cell_sum, (cc[:, 0], cc[:, 1], cc[:, 2]), pt[tuple(idx[ok].T)])
-                np.add.at(cell_cnt, (cc[:, 0], cc[:, 1], cc[:, 2]), 1.0)
-    has = cell_cnt > 0
-    vid = -np.ones((res, res, res), np.int64)
-    vid[has] = np.arange(has.sum())
-    verts = (cell_sum[has] / cell_cnt[has, None]).astype(np.float32)
-    quads = []
-    for axis in range(3):
-        sl0 = [slice(None)] * 3
-        sl1 = [slice(None)] * 3
-        sl0[axis] = slice(0, -1)
-        sl1[axis] = slice(1, None)
-        cross = inside[tuple(sl0)] != inside[tuple(sl1)]
-        flip = inside[tuple(sl0)]
-        a, b = [x for x in range(3) if x != axis]
-        idx = np.argwhere(cross)
-        ok = (idx[:, a] > 0) & (idx[:, a] < res) & (idx[:, b] > 0) & (idx[:, b] < res)
-        idx = idx[ok]
-        fl = flip[tuple(idx.T)]
-        cells = []
-        for oa, ob in ((0, 0), (-1, 0), (-1, -1), (0, -1)):
-            c = idx.copy()
-            c[:, a] += oa
-            c[:, b] += ob
-            cells.append(vid[c[:, 0], c[:, 1], c[:, 2]])
-        q = np.stack(cells, 1)
-        # orientation: normals point from inside to outside
-        q = np.where(((axis == 1) ^ fl)[:, None], q, q[:, ::-1])
-        quads.append(q)
-    quads = np.concatenate(quads, 0)
-    centre = verts[quads].mean(1)
-    cid = len(verts) + np.arange(len(quads))
-    verts = np.concatenate([verts, centre.astype(np.float32)], 0)
-    faces = np.concatenate([np.stack([quads[:, i], quads[:, (i + 1) % 4], cid], 1)
-                            for i in range(4)], 0)
-    return verts, faces.astype(np.int64)
+def sphere_torus_mesh(res=64, lo=-1.0, hi=1.0, sdf=sdf_sphere_torus, device="cuda"):
+    """FlexiCubes extraction (training mode, uniform weights, undeformed
+    grid) of an SDF sampled on a res^3 grid over [lo, hi]^3, on the device:
+    (verts [V,3] float32, faces [F,3] int64), consistently outward.  For the
+    sphere-union-torus field at 64^3 that is 45,304 faces."""
+    fc = FlexiCubes(device=device)
+    grid, cubes = fc.construct_voxel_grid_v2(res, [lo] * 3, [hi] * 3)
+    s = torch.as_tensor(sdf(grid.double().cpu().numpy()), dtype=torch.float32, device=device)
+    v, f, _, _ = fc(grid, s, cubes, res, training=True)
+    return v.detach(), f
 
 
 def eval_sh(deg, sh, dirs):
@@ -174,7 +117,8 @@ class MeshBoundScene:
         self.faces = torch.as_tensor(faces, device=self.device)
         F = self.faces.shape[0]
         self.G, self.P = G, F * G
-        self.verts = torch.tensor(verts, device=self.device, requires_grad=True)
+        self.verts = torch.as_tensor(verts, dtype=torch.float32, device=self.device).detach().clone()
+        self.verts.requires_grad_(True)
         self.bc = torch.tensor(rng.dirichlet((1.0, 1.0, 1.0), (F, G)).astype(np.float32),
                                device=self.device)
         self.rad_base = 1.0 / (4.0 + 2.0 * math.sqrt(3.0))

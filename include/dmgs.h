@@ -246,6 +246,60 @@ int dmgs_face_cull(const float *verts, int32_t V, const int64_t *faces, int32_t 
                    dmgs_stream_t stream);
 
 /* ---------------------------------------------------------------------- *
+ * FlexiCubes isosurface extraction on a regular grid (replaces the
+ * triangle path of `FlexiCubes.__call__`, geo/flexicubes.py:180-260, with
+ * grad_func=None and output_tetmesh=False, as stage 2 calls it:
+ * scene/gaussian_geo_model_mlp_flex.py:250-251).  The grid is the one of
+ * `construct_voxel_grid_v2` (geo/flexicubes.py:133-157): vertices in
+ * (i, j, k) lexicographic order, N = (rx+1)(ry+1)(rz+1), cubes likewise,
+ * C = rx ry rz.  Weights are the RAW per-cube parameters (normalised inside
+ * as beta = tanh(b) 0.99 + 1, alpha = tanh(a) 0.99 + 1,
+ * gamma = sigmoid(g) 0.99 + 0.005); NULL means all ones after
+ * normalisation, as in the reference.
+ *
+ * Three calls: dmgs_fc_count runs the classification and the scans and
+ * returns (after synchronising the stream) counts[8] = {surface cubes, dual
+ * vertices, L_dev entries, surface edges, quads, flipped quads, 0, 0};
+ * the caller sizes the outputs from them:
+ *   vertices [n_vd + n_quads (training) | n_vd, 3] f32,
+ *   faces    [4 n_quads (training) | 2 n_quads, 3] int64,
+ *   L_dev    [n_entries] f32, surf_edges [n_edges, 2] int64,
+ *   work     dmgs_fc_work_bytes(counts) bytes (kept for the adjoint);
+ * dmgs_fc_emit writes them in the reference's order; dmgs_fc_bwd takes
+ * dL/dvertices (MODIFIED: the quad centres' gradients are added to the dual
+ * vertices' rows) and dL/dL_dev and writes dense gradients w.r.t. x [N,3],
+ * s [N] and the raw weights [C,12], [C,8], [C] (each optional when its
+ * weight is NULL).
+ * ---------------------------------------------------------------------- */
+typedef struct DmgsFcGrid {
+  const float *x;     /* [N,3] vertex positions (deformed grid) */
+  const float *s;     /* [N] scalar field, s < 0 inside */
+  const float *beta;  /* [C,12] raw edge weights or NULL */
+  const float *alpha; /* [C,8] raw corner weights or NULL */
+  const float *gamma; /* [C] raw quad-split weights or NULL */
+  int32_t rx, ry, rz; /* cubes per axis */
+  int32_t training;   /* 1: four triangles per quad around a centre vertex */
+} DmgsFcGrid;
+
+/* Dual Marching Cubes tables this build derives: groups[256*4] edge masks of
+ * the dual vertices, num_vd[256], check[256*5] (flag, di, dj, dk, complement
+ * case) — the meaning of geo/tables.py's dmc_table / num_vd_table /
+ * check_table.  Host only. */
+int dmgs_fc_tables(uint16_t *groups, uint8_t *num_vd, int8_t *check);
+size_t dmgs_fc_state_bytes(int32_t rx, int32_t ry, int32_t rz);
+size_t dmgs_fc_work_bytes(const uint32_t *counts);
+int dmgs_fc_count(const DmgsFcGrid *g, void *state, size_t state_bytes, uint32_t *counts,
+                  dmgs_stream_t stream);
+int dmgs_fc_emit(const DmgsFcGrid *g, const uint32_t *counts, void *state,
+                 size_t state_bytes, void *work, size_t work_bytes, float *vertices,
+                 int64_t *faces, float *L_dev, int64_t *surf_edges, dmgs_stream_t stream);
+int dmgs_fc_bwd(const DmgsFcGrid *g, const uint32_t *counts, const void *state,
+                size_t state_bytes, const void *work, size_t work_bytes,
+                const float *vertices, float *dL_dvertices, const float *dL_dL_dev,
+                float *dx, float *ds, float *dbeta, float *dalpha, float *dgamma,
+                dmgs_stream_t stream);
+
+/* ---------------------------------------------------------------------- *
  * Fused photometric loss (no counterpart kernel in the reference, which
  * composes it from torch ops: l1_loss and ssim of utils/loss_utils.py as
  * used by train_geo_stage2.py:114-116):

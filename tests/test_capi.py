@@ -93,3 +93,32 @@ def test_state_size_checks(lib):
     assert lib.dmgs_raster_fwd_render(_view(), _gauss(), 16, need, 16, 1 << 30, 5, 16, 0, 16, None) == -3
     assert lib.dmgs_bind_fwd(None, None, None, None, None, None) == -1
     assert lib.dmgs_mark_visible(-1, None, None, None, None, None) == -1
+
+
+def test_flexicubes_tables_match_oracle(lib):
+    """The Dual Marching Cubes tables the library derives (host-only call)
+    equal the oracle's, which are pinned to the reference's tables."""
+    from oracle.flexicubes import derive_tables
+    groups = (C.c_uint16 * 1024)()
+    nvd = (C.c_uint8 * 256)()
+    chk = (C.c_int8 * 1280)()
+    assert lib.dmgs_fc_tables(C.addressof(groups), C.addressof(nvd), C.addressof(chk)) == 0
+    dmc, num_vd, check = derive_tables()
+    for c in range(256):
+        assert nvd[c] == num_vd[c]
+        for l in range(4):
+            edges = [e for e in dmc[c][l] if e != -1]
+            assert groups[4 * c + l] == sum(1 << e for e in edges), (c, l)
+        got = [chk[5 * c + q] for q in range(5)]
+        want = list(check[c])
+        want[4] = want[4] - 256 if want[4] > 127 else want[4]  # int8 storage of the complement
+        assert got == want, c
+
+
+def test_flexicubes_rejects_bad_grid(lib):
+    g = _lib.DmgsFcGrid(x=8, s=8, rx=0, ry=4, rz=4)
+    counts = (C.c_uint32 * 8)()
+    assert lib.dmgs_fc_count(C.byref(g), 8, 1 << 20, C.addressof(counts), None) == -1
+    g = _lib.DmgsFcGrid(x=8, s=8, rx=4, ry=4, rz=4)
+    assert lib.dmgs_fc_count(C.byref(g), 8, 16, C.addressof(counts), None) == -3
+    assert lib.dmgs_fc_state_bytes(4, 4, 4) > 4 * 4 * 4 * 5

@@ -109,8 +109,7 @@ def test_frustum_face_culling_matches_the_reference_rule():
     from dmgs_gb300.camera import make_view
     from dmgs_gb300.meshbound import sphere_torus_mesh
     v, f = sphere_torus_mesh(32)
-    verts = torch.tensor(v, device="cuda")
-    faces = torch.tensor(f, device="cuda")
+    verts, faces = v.to("cuda"), f.to("cuda")
     view = make_view((1.2, 0.4, 1.0), (0.0, 0.0, 0.0), 200, 160, fovx_deg=40)
     M = torch.tensor(view.projmatrix, device="cuda")
     mask, kept, idx = frustum_faces(verts, faces, M)

@@ -4,10 +4,30 @@ reach every parameter, are finite, and a few Adam steps lower the loss."""
 import pytest
 import torch
 
-from dmgs_gb300.meshbound import MeshBoundScene, sphere_torus_mesh, training_step
+import numpy as np
+
+from dmgs_gb300.meshbound import MeshBoundScene, sdf_sphere_torus, sphere_torus_mesh, training_step
 from dmgs_gb300.scenes import hemisphere_views
 
 pytestmark = pytest.mark.gpu
+
+
+def test_configuration_mesh_is_closed_outward_with_the_reference_face_count():
+    """FlexiCubes of the sphere-union-torus field at 64^3 (training mode):
+    45,304 faces, every edge in two faces, normals along the SDF gradient."""
+    v, f = sphere_torus_mesh(64)
+    v, f = v.cpu().numpy().astype(np.float64), f.cpu().numpy()
+    assert f.shape == (45304, 3) and f.min() >= 0 and f.max() < len(v)
+    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
+    _, counts = np.unique(e, axis=0, return_counts=True)
+    assert np.all(counts == 2)
+    c = v[f].mean(1)
+    n = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
+    h = 1e-3
+    grad = np.stack([(sdf_sphere_torus(c + h * np.eye(3)[i]) - sdf_sphere_torus(c - h * np.eye(3)[i]))
+                     / (2 * h) for i in range(3)], 1)
+    assert (((n * grad).sum(1) > 0).mean()) > 0.999
+    assert np.abs(sdf_sphere_torus(v)).max() < 2.0 / 64
 
 
 def test_training_step_gradients_and_descent():

@@ -1,23 +1,7 @@
-"""The configuration-2 mesh: FlexiCubes' training-mode face count of the
-sphere-union-torus field (45,304 at 64^3), closed, consistently outward."""
+"""Host-side pieces of the configuration-2 training step."""
 import numpy as np
 
-from dmgs_gb300.meshbound import eval_sh, sdf_sphere_torus, sphere_torus_mesh
-
-
-def test_sphere_torus_mesh_is_closed_outward_with_the_reference_face_count():
-    v, f = sphere_torus_mesh(64)
-    assert f.shape == (45304, 3) and f.min() >= 0 and f.max() < len(v)
-    e = np.sort(np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]]), axis=1)
-    _, counts = np.unique(e, axis=0, return_counts=True)
-    assert np.all(counts == 2)  # every edge shared by exactly two faces
-    c = v[f].mean(1)
-    n = np.cross(v[f[:, 1]] - v[f[:, 0]], v[f[:, 2]] - v[f[:, 0]])
-    h = 1e-3
-    grad = np.stack([(sdf_sphere_torus(c + h * np.eye(3)[i]) - sdf_sphere_torus(c - h * np.eye(3)[i]))
-                     / (2 * h) for i in range(3)], 1)
-    assert np.all((n * grad).sum(1) > 0)
-    assert np.abs(sdf_sphere_torus(v)).max() < 2.0 / 64
+from dmgs_gb300.meshbound import eval_sh
 
 
 def test_eval_sh_matches_the_oracle_polynomial():
