@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-bound training leg")
     ap.add_argument("--no-fc", action="store_true", help="skip the FlexiCubes extraction leg")
+    ap.add_argument("--no-tex", action="store_true", help="skip the hash-grid texture leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="requests per second")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of in-flight requests")
@@ -368,6 +369,55 @@ def flexicubes_leg(args, dev):
     return out
 
 
+def texture_leg(args, dev):
+    """The stage-2 hash-grid texture query (MLPTexture3D.sample_noact,
+    scene/gaussian_geo_model_mlp_flex.py:313) at the configuration-2
+    Gaussian count: 271,824 points on the 45,304-face FlexiCubes mesh
+    (6 per face at Dirichlet(1,1,1) barycentrics), 48 SH channels, AABB =
+    the mesh bounds x 1.1 (:206-208).  Forward and forward+backward ms."""
+    import torch
+    from dmgs_gb300 import _lib
+    from dmgs_gb300.meshbound import sphere_torus_mesh
+    from dmgs_gb300.texture import MLPTexture3D
+    lib = _lib.load()
+    v, f = sphere_torus_mesh(64)
+    gen = torch.Generator(device=dev).manual_seed(3)
+    bc = torch.distributions.Dirichlet(torch.ones(3, device=dev)).sample((f.shape[0] * 6,))
+    tri = v[f].repeat_interleave(6, 0)
+    xyz = (bc.unsqueeze(2) * tri).sum(1).contiguous().requires_grad_(True)
+    aabb = torch.stack([v.min(0).values, v.max(0).values]) * 1.1
+    tex = MLPTexture3D(aabb, channels=48, device=dev)
+    up = torch.randn((xyz.shape[0], 48), device=dev, generator=gen)
+
+    def step(i):
+        out = tex.sample_noact(xyz)
+        (out * up).sum().backward()
+
+    n = 20
+    with torch.no_grad():
+        ms_fwd = timed(lambda i: tex.sample_noact(xyz), n, 3, dev) / n
+    l0 = lib.dmgs_kernel_launches()
+    ms_step = timed(step, n, 3, dev) / n
+    out = {"points": int(xyz.shape[0]), "channels": 48, "fwd_ms": ms_fwd, "fwd_bwd_ms": ms_step,
+           "own_kernels_per_fwd_bwd": (lib.dmgs_kernel_launches() - l0) / (n + 3),
+           "table_mb": tex.encoder.params.numel() * 4 / 1e6,
+           "encoding": "float32 hash grid (the reference's tiny-cuda-nn default is half)"}
+    if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu:
+        from oracle import texture as otex  # CPU baseline only
+        torch.set_num_threads(os.cpu_count())
+        m = 32768
+        x = xyz[:m].detach().cpu().requires_grad_(True)
+        tb = tex.encoder.params.detach().cpu().view(-1, 2).requires_grad_(True)
+        W = [w.detach().cpu().requires_grad_(True) for w in tex.net.weights()]
+        t0 = time.perf_counter()
+        o = otex.sample_noact(x, aabb.cpu(), tb, W)
+        (o * up[:m].cpu()).sum().backward()
+        out["cpu_baseline"] = {"fwd_bwd_ms_per_271824_points": (time.perf_counter() - t0) * 1e3 *
+                               xyz.shape[0] / m, "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"float32 torch oracle, {m} points, scaled to 271,824"}
+    return out
+
+
 def bytes_model(name, P, V, K, npix, nviews=1):
     """Algorithmic DRAM bytes per launch (SH3, scale/rotation inputs).  For
     a batched launch V, K, npix are sums over the views."""
@@ -646,6 +696,9 @@ def main():
     fcl = None
     if not args.no_fc:
         fcl = flexicubes_leg(args, dev)
+    texl = None
+    if not args.no_tex:
+        texl = texture_leg(args, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -674,6 +727,7 @@ def main():
             "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
             "serving": serving, "mesh_training": mesh, "flexicubes": fcl,
+            "texture": texl,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))
     if world > 1:

@@ -55,6 +55,11 @@ class DmgsFcGrid(C.Structure):
                 ("rx", C.c_int32), ("ry", C.c_int32), ("rz", C.c_int32), ("training", C.c_int32)]
 
 
+class DmgsTexture(C.Structure):
+    _fields_ = [("table", vp), ("W1", vp), ("W2", vp), ("W3", vp), ("channels", C.c_int32),
+                ("aabb", C.c_float * 6), ("per_level_scale", C.c_float)]
+
+
 class DmgsBatch(C.Structure):
     _fields_ = [("nviews", C.c_int32), ("views", C.POINTER(DmgsView)),
                 ("out_color", C.POINTER(vp)), ("radii", C.POINTER(vp)),
@@ -109,6 +114,9 @@ SIGNATURES = [
                                vp, vp, vp]),
     ("dmgs_fc_bwd", C.c_int, [C.POINTER(DmgsFcGrid), vp, vp, C.c_size_t, vp, C.c_size_t, vp, vp,
                               vp, vp, vp, vp, vp, vp, vp]),
+    ("dmgs_tex_table_entries", C.c_int64, [C.c_float]),
+    ("dmgs_tex_fwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp]),
+    ("dmgs_tex_bwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]),
     ("dmgs_l1_ssim_scratch_bytes", C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     ("dmgs_l1_ssim", C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, vp, vp, vp,
                                C.c_size_t, vp]),

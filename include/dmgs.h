@@ -300,6 +300,33 @@ int dmgs_fc_bwd(const DmgsFcGrid *g, const uint32_t *counts, const void *state,
                 dmgs_stream_t stream);
 
 /* ---------------------------------------------------------------------- *
+ * Hash-grid texture (replaces MLPTexture3D.sample_noact, geo/texture.py:
+ * 101-112, whose encoding is tiny-cuda-nn's HashGrid): positions -> features
+ *   t = clamp((xyz - lo) / (hi - lo), 0, 1); enc = 16-level x 2-feature
+ *   hash encoding (base resolution 16, 2^19 entries per level, the given
+ *   per-level scale); out = W3 relu(W2 relu(W1 enc)), no biases.
+ * table: [entries, 2] f32 (dmgs_tex_table_entries); W1, W2: [32,32];
+ * W3: [channels, 32] (torch Linear layout); channels in {3, 12, 27, 48}.
+ * dmgs_tex_bwd writes (overwrites) dW1..dW3, the table gradient (optional)
+ * scaled by 128 and the position gradient (optional) unscaled, as the
+ * reference's two backward hooks (geo/texture.py:72-73) leave them.
+ * ---------------------------------------------------------------------- */
+typedef struct DmgsTexture {
+  const float *table;    /* [entries, 2] */
+  const float *W1, *W2, *W3;
+  int32_t channels;
+  float aabb[6];         /* lo x, y, z, hi x, y, z */
+  float per_level_scale; /* exp(ln(4096 / 16) / 15) in the reference */
+} DmgsTexture;
+
+int64_t dmgs_tex_table_entries(float per_level_scale);
+int dmgs_tex_fwd(const DmgsTexture *t, int64_t n, const float *xyz, float *out,
+                 dmgs_stream_t stream);
+int dmgs_tex_bwd(const DmgsTexture *t, int64_t n, const float *xyz, const float *dout,
+                 float *dxyz, float *dtable, float *dW1, float *dW2, float *dW3,
+                 dmgs_stream_t stream);
+
+/* ---------------------------------------------------------------------- *
  * Fused photometric loss (no counterpart kernel in the reference, which
  * composes it from torch ops: l1_loss and ssim of utils/loss_utils.py as
  * used by train_geo_stage2.py:114-116):

@@ -122,3 +122,10 @@ def test_flexicubes_rejects_bad_grid(lib):
     g = _lib.DmgsFcGrid(x=8, s=8, rx=4, ry=4, rz=4)
     assert lib.dmgs_fc_count(C.byref(g), 8, 16, C.addressof(counts), None) == -3
     assert lib.dmgs_fc_state_bytes(4, 4, 4) > 4 * 4 * 4 * 5
+
+
+def test_texture_table_size_matches_oracle(lib):
+    """The encoding's level layout (host-only): total table entries."""
+    from oracle.texture import per_level_scale, table_entries
+    assert lib.dmgs_tex_table_entries(per_level_scale()) == table_entries()
+    assert lib.dmgs_tex_table_entries(0.5) == -1
