@@ -340,15 +340,24 @@ def flexicubes_leg(args, dev):
             (v.square().sum() + L.mean()).backward()
 
         n = 20
-        l0 = lib.dmgs_kernel_launches()
         ms_fwd = timed(lambda i: fwd(), n, 3, dev) / n
+        l0 = lib.dmgs_kernel_launches()
         ms_step = timed(step, n, 3, dev) / n
-        launches = (lib.dmgs_kernel_launches() - l0) / (2 * n + 6)
+        launches = (lib.dmgs_kernel_launches() - l0) / (n + 3)
+        lib.dmgs_timing_enable(1)
+        _lib.timing_collect()
+        for i in range(5):
+            step(i)
+        torch.cuda.synchronize(dev)
+        lib.dmgs_timing_enable(0)
+        kt = _lib.timing_collect()
         v, f, L, se = fwd()
         out[f"res{res}"] = {"cubes": int(cubes.shape[0]), "faces": int(f.shape[0]),
                             "vertices": int(v.shape[0]), "surface_edges": int(se.shape[0]),
                             "fwd_ms": ms_fwd, "fwd_bwd_ms": ms_step,
-                            "own_kernels_per_fwd_bwd": launches}
+                            "own_kernels_per_fwd_bwd": launches,
+                            "kernel_ms_per_step": {k: kt[k][0] / 5 for k in ("fc_fwd", "fc_bwd")
+                                                   if k in kt}}
         del grid, cubes, s0, sdf, deform, w, v, f, L, se
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu:
         from oracle import flexicubes as ofc  # CPU baseline only
@@ -398,8 +407,17 @@ def texture_leg(args, dev):
         ms_fwd = timed(lambda i: tex.sample_noact(xyz), n, 3, dev) / n
     l0 = lib.dmgs_kernel_launches()
     ms_step = timed(step, n, 3, dev) / n
+    launches = (lib.dmgs_kernel_launches() - l0) / (n + 3)
+    lib.dmgs_timing_enable(1)
+    _lib.timing_collect()
+    for i in range(5):
+        step(i)
+    torch.cuda.synchronize(dev)
+    lib.dmgs_timing_enable(0)
+    kt = _lib.timing_collect()
     out = {"points": int(xyz.shape[0]), "channels": 48, "fwd_ms": ms_fwd, "fwd_bwd_ms": ms_step,
-           "own_kernels_per_fwd_bwd": (lib.dmgs_kernel_launches() - l0) / (n + 3),
+           "own_kernels_per_fwd_bwd": launches,
+           "kernel_ms_per_step": {k: kt[k][0] / 5 for k in ("tex_fwd", "tex_bwd") if k in kt},
            "table_mb": tex.encoder.params.numel() * 4 / 1e6,
            "encoding": "float32 hash grid (the reference's tiny-cuda-nn default is half)"}
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu:

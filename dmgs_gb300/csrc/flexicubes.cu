@@ -8,7 +8,7 @@
 // sorts and a python loop over dual-vertex counts.  On the regular grid of
 // construct_voxel_grid_v2 (geo/flexicubes.py:133-157) every ordering those
 // sorts produce has a closed form, so here the whole forward is four
-// kernels and one small host read:
+// kernels (and a per-surface-cube pass) with one small host read:
 //
 //   1. count   every item i is cube i and grid vertex i; per item it forms
 //              the cube's case (with the C16/C19 re-check against the
@@ -18,9 +18,11 @@
 //              crossing edges, flipped and unflipped quads;
 //   2. scan    one block turns the block counters into exclusive offsets and
 //              totals (the host reads the totals to size the outputs);
-//   3. emit    per item again, now with its global positions: dual
-//              vertices, L_dev entries and the surface-cube record of each
-//              surface cube; surface edges and the quad list of each vertex;
+//   3. emit    per item again, now with its global positions: the record
+//              of each surface cube (cube, first dual vertex, first L_dev
+//              entry, case); surface edges and the quad list of each vertex;
+//      then, one thread per surface cube, its dual vertices and L_dev
+//      entries (kept out of the item pass, which stays light);
 //   4. quads   per quad: the four dual vertices around its edge, winding,
 //              the gamma-weighted centre and four triangles (training) or
 //              the gamma split into two (otherwise).
@@ -182,9 +184,46 @@ constexpr int NVAL = 12;
 // counter slots
 constexpr int V_SURF = 0, V_CUBES = 1 /* +g-1 */, V_ENTS = 5 /* +g-1 */, V_EDGES = 9, V_QF = 10,
               V_QN = 11;
-// header words (state + 0)
+// derived header (from the 12 totals): counts and the first dual vertex /
+// first L_dev entry of each dual-vertex-count group
 constexpr int H_SURF = 0, H_VD = 1, H_ENT = 2, H_EDGES = 3, H_QUADS = 4, H_QF = 5, H_VDB = 6,
               H_ENTB = 10, H_WORDS = 16;
+
+__host__ __device__ inline void derive_header(const uint32_t *tot, uint32_t *h) {
+  uint32_t vdb = 0, entb = 0;
+  for (int g = 1; g <= 4; ++g) {
+    h[H_VDB + g - 1] = vdb;
+    h[H_ENTB + g - 1] = entb;
+    vdb += tot[V_CUBES + g - 1] * (uint32_t)g;
+    entb += tot[V_ENTS + g - 1];
+  }
+  h[H_SURF] = tot[V_SURF];
+  h[H_VD] = vdb;
+  h[H_ENT] = entb;
+  h[H_EDGES] = tot[V_EDGES];
+  h[H_QF] = tot[V_QF];
+  h[H_QUADS] = tot[V_QF] + tot[V_QN];
+  for (int k = H_ENTB + 4; k < H_WORDS; ++k) h[k] = 0;
+}
+
+// Division by a grid extent without a hardware divide: Granlund & Montgomery
+// ("Division by invariant integers using multiplication", 1994):
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> l for every 32-bit n.
+struct FastDiv {
+  uint32_t d, m, l;
+};
+
+inline FastDiv make_fastdiv(uint32_t d) {
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+  return FastDiv{d, (uint32_t)m, l};
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+  return (uint32_t)(((uint64_t)__umulhi(n, f.m) + n) >> f.l);
+}
 
 struct FcGrid {
   const float *x, *s, *beta, *alpha, *gamma;
@@ -192,14 +231,32 @@ struct FcGrid {
   int sy, sx;  // vertex strides: j -> rz + 1, i -> (ry + 1)(rz + 1)
   int nc, nv;
   int training;
+  FastDiv by_rz, by_ry, by_sy, by_ry1;  // rz, ry, rz + 1, ry + 1
 };
+
+// (i, j, k) of cube c and of grid vertex v
+__device__ __forceinline__ void cube_ijk(const FcGrid &G, int c, int &ci, int &cj, int &ck) {
+  const uint32_t t = fdiv((uint32_t)c, G.by_rz);
+  const uint32_t i = fdiv(t, G.by_ry);
+  ck = c - (int)t * G.rz;
+  cj = (int)t - (int)i * G.ry;
+  ci = (int)i;
+}
+
+__device__ __forceinline__ void vertex_ijk(const FcGrid &G, int v, int &vi, int &vj, int &vk) {
+  const uint32_t t = fdiv((uint32_t)v, G.by_sy);
+  const uint32_t i = fdiv(t, G.by_ry1);
+  vk = v - (int)t * G.sy;
+  vj = (int)t - (int)i * (G.ry + 1);
+  vi = (int)i;
+}
 
 struct SurfCube {  // one surface cube, in surface-cube order
   int cube, vd, ent, cs;
 };
 
 struct FcState {
-  uint32_t *hdr;     // H_WORDS
+  uint32_t *hdr;     // [NVAL] totals (scan) then [H_WORDS] derived
   uint32_t *blk;     // [nblk][NVAL]
   int32_t *cube_vd;  // [nc] first dual vertex of a surface cube
   uint8_t *cube_cs;  // [nc] its (re-checked) case
@@ -211,7 +268,7 @@ size_t fc_state_bytes_(int rx, int ry, int rz, FcState *st, char *base) {
   const size_t nc = (size_t)rx * ry * rz, nv = (size_t)(rx + 1) * (ry + 1) * (rz + 1);
   const size_t nblk = (nv + FC_TILE - 1) / FC_TILE;
   size_t o = 0;
-  const size_t hdr = o; o = align_up(o + H_WORDS * 4, 256);
+  const size_t hdr = o; o = align_up(o + (NVAL + H_WORDS) * 4, 256);
   const size_t blk = o; o = align_up(o + nblk * NVAL * 4, 256);
   const size_t cvd = o; o = align_up(o + nc * 4, 256);
   const size_t ccs = o; o = align_up(o + nc, 256);
@@ -236,7 +293,8 @@ __device__ __forceinline__ float gamma_n(const float *gamma, int c) {
 }
 
 __device__ __forceinline__ int corner_vertex(const FcGrid &G, int c, int n) {
-  const int ck = c % G.rz, t = c / G.rz, cj = t % G.ry, ci = t / G.ry;
+  int ci, cj, ck;
+  cube_ijk(G, c, ci, cj, ck);
   return ((ci + (n & 1)) * (G.ry + 1) + cj + ((n >> 1) & 1)) * G.sy + ck + ((n >> 2) & 1);
 }
 
@@ -255,7 +313,8 @@ __device__ __forceinline__ int raw_case(const FcGrid &G, int ci, int cj, int ck)
 // when the case and the neighbour across its ambiguous face are both
 // flagged, the case becomes its complement.
 __device__ __forceinline__ int cube_case(const FcGrid &G, int c) {
-  const int ck = c % G.rz, t = c / G.rz, cj = t % G.ry, ci = t / G.ry;
+  int ci, cj, ck;
+  cube_ijk(G, c, ci, cj, ck);
   int cs = raw_case(G, ci, cj, ck);
   if (c_fc.check[cs][0]) {
     const int ni = ci + c_fc.check[cs][1], nj = cj + c_fc.check[cs][2], nk = ck + c_fc.check[cs][3];
@@ -270,7 +329,8 @@ __device__ __forceinline__ int cube_case(const FcGrid &G, int c) {
 // surface (bits 0-2), which of those have all four cubes inside the grid
 // (a quad, bits 4-6), and whether the vertex is outside (s > 0, flipped).
 __device__ __forceinline__ uint32_t vertex_edges(const FcGrid &G, int v) {
-  const int vk = v % G.sy, t = v / G.sy, vj = t % (G.ry + 1), vi = t / (G.ry + 1);
+  int vi, vj, vk;
+  vertex_ijk(G, v, vi, vj, vk);
   const float sv = __ldg(G.s + v);
   const bool in = sv < 0.f;
   uint32_t m = 0;
@@ -379,40 +439,36 @@ __global__ void __launch_bounds__(FC_THREADS) fc_count_kernel(const FcGrid G, ui
     for (int j = 0; j < NVAL; ++j) blk[(size_t)blockIdx.x * NVAL + j] = tot[j];
 }
 
-// One block: block counters -> exclusive block offsets (in place) and the
-// header (totals, first dual vertex and first L_dev entry of each group).
-__global__ void __launch_bounds__(FC_SCAN_THREADS) fc_scan_kernel(uint32_t *blk, int nblk, uint32_t *hdr) {
-  __shared__ uint32_t sm[FC_SCAN_THREADS / 32 * NVAL];
+// Block counters -> exclusive block offsets, in place: block j of the
+// launch scans counter column j (thread t owns a contiguous run of blocks);
+// the column totals go to tot[j].
+__global__ void __launch_bounds__(FC_SCAN_THREADS) fc_scan_kernel(uint32_t *blk, int nblk, uint32_t *tot) {
+  __shared__ uint32_t wsum[FC_SCAN_THREADS / 32];
+  const int j = blockIdx.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int per = (nblk + FC_SCAN_THREADS - 1) / FC_SCAN_THREADS;
   const int b0 = min(nblk, (int)threadIdx.x * per), b1 = min(nblk, b0 + per);
-  uint32_t v[NVAL] = {}, tot[NVAL];
-  for (int b = b0; b < b1; ++b)
+  uint32_t v = 0;
+  for (int b = b0; b < b1; ++b) v += blk[(size_t)b * NVAL + j];
+  uint32_t x = v;
 #pragma unroll
-    for (int j = 0; j < NVAL; ++j) v[j] += blk[(size_t)b * NVAL + j];
-  block_scan<FC_SCAN_THREADS>(v, tot, sm);
-  for (int b = b0; b < b1; ++b)
-#pragma unroll
-    for (int j = 0; j < NVAL; ++j) {
-      const uint32_t x = blk[(size_t)b * NVAL + j];
-      blk[(size_t)b * NVAL + j] = v[j];
-      v[j] += x;
-    }
-  if (threadIdx.x == 0) {
-    uint32_t vdb = 0, entb = 0;
-#pragma unroll
-    for (int g = 1; g <= 4; ++g) {
-      hdr[H_VDB + g - 1] = vdb;
-      hdr[H_ENTB + g - 1] = entb;
-      vdb += tot[V_CUBES + g - 1] * (uint32_t)g;
-      entb += tot[V_ENTS + g - 1];
-    }
-    hdr[H_SURF] = tot[V_SURF];
-    hdr[H_VD] = vdb;
-    hdr[H_ENT] = entb;
-    hdr[H_EDGES] = tot[V_EDGES];
-    hdr[H_QF] = tot[V_QF];
-    hdr[H_QUADS] = tot[V_QF] + tot[V_QN];
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
+  if (lane == 31) wsum[wid] = x;
+  __syncthreads();
+  uint32_t off = 0, all = 0;
+  for (int w = 0; w < FC_SCAN_THREADS / 32; ++w) {
+    off += w < wid ? wsum[w] : 0u;
+    all += wsum[w];
+  }
+  uint32_t run = off + x - v;
+  for (int b = b0; b < b1; ++b) {
+    const uint32_t c = blk[(size_t)b * NVAL + j];
+    blk[(size_t)b * NVAL + j] = run;
+    run += c;
+  }
+  if (threadIdx.x == 0) tot[j] = all;
 }
 
 // Corner data of one cube.
@@ -473,10 +529,10 @@ __device__ __forceinline__ float dist3(const float (&a)[3], const float (&b)[3])
 
 __global__ void __launch_bounds__(FC_THREADS)
 fc_emit_kernel(const FcGrid G, FcState S, SurfCube *__restrict__ surf, uint32_t *__restrict__ quad_edge,
-               float *__restrict__ vertices, float *__restrict__ L_dev, int64_t *__restrict__ surf_edges) {
+               int64_t *__restrict__ surf_edges) {
   __shared__ uint32_t sm[FC_THREADS / 32 * NVAL];
   __shared__ uint32_t hdr[H_WORDS];
-  if (threadIdx.x < H_WORDS) hdr[threadIdx.x] = S.hdr[threadIdx.x];
+  if (threadIdx.x == 0) derive_header(S.hdr, hdr);
   const int base = blockIdx.x * FC_TILE + threadIdx.x * FC_IPT;
   ItemInfo it[FC_IPT];
   uint32_t v[NVAL] = {}, tot[NVAL];
@@ -496,35 +552,10 @@ fc_emit_kernel(const FcGrid G, FcState S, SurfCube *__restrict__ surf, uint32_t 
     if (itk.cs >= 0) {
       const int cs = itk.cs, g = c_fc.nvd[cs];
       const int vd0 = (int)(hdr[H_VDB + g - 1] + get_at(v, V_CUBES + g - 1) * (uint32_t)g);
-      int ent = (int)(hdr[H_ENTB + g - 1] + get_at(v, V_ENTS + g - 1));
+      const int ent = (int)(hdr[H_ENTB + g - 1] + get_at(v, V_ENTS + g - 1));
       surf[v[V_SURF]] = SurfCube{i, vd0, ent, cs};
       S.cube_vd[i] = vd0;
       S.cube_cs[i] = (uint8_t)cs;
-      CubeCorners C;
-      load_corners(G, i, C);
-      for (int l = 0; l < g; ++l) {
-        const uint32_t m = c_fc.group[cs][l];
-        float vd[3], bsum;
-        dual_vertex(G, C, i, m, vd, bsum);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) vertices[3 * (size_t)(vd0 + l) + d] = vd[d];
-        // L_dev: |dist - mean dist| over the unweighted zero crossings
-        // (geo/flexicubes.py:253-260)
-        float dist[12], sum = 0.f;
-#pragma unroll
-        for (int e = 0; e < 12; ++e) {
-          dist[e] = 0.f;
-          if (!((m >> e) & 1u)) continue;
-          float u[3], w0, w1;
-          crossing(C, e, false, u, w0, w1);
-          dist[e] = dist3(u, vd);
-          sum = __fadd_rn(sum, dist[e]);
-        }
-        const float mean = __fdiv_rn(sum, (float)__popc(m));
-#pragma unroll
-        for (int e = 0; e < 12; ++e)
-          if ((m >> e) & 1u) L_dev[ent++] = fabsf(__fsub_rn(dist[e], mean));
-      }
       v[V_SURF] += 1;
       add_at(v, V_CUBES + g - 1, 1u);
       add_at(v, V_ENTS + g - 1, (uint32_t)__popc(c_fc.cross[cs]));
@@ -548,6 +579,43 @@ fc_emit_kernel(const FcGrid G, FcState S, SurfCube *__restrict__ surf, uint32_t 
   }
 }
 
+// Per surface cube (from the emission's surface-cube list): its dual
+// vertices and their L_dev entries.
+__global__ void __launch_bounds__(128)
+fc_vd_kernel(const FcGrid G, const SurfCube *__restrict__ surf, int n_surf, float *__restrict__ vertices,
+             float *__restrict__ L_dev) {
+  const int i = blockIdx.x * 128 + threadIdx.x;
+  if (i >= n_surf) return;
+  const SurfCube sc = surf[i];
+  const int g = c_fc.nvd[sc.cs];
+  CubeCorners C;
+  load_corners(G, sc.cube, C);
+  int ent = sc.ent;
+  for (int l = 0; l < g; ++l) {
+    const uint32_t m = c_fc.group[sc.cs][l];
+    float vd[3], bsum;
+    dual_vertex(G, C, sc.cube, m, vd, bsum);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) vertices[3 * (size_t)(sc.vd + l) + d] = vd[d];
+    // L_dev: |dist - mean dist| over the unweighted zero crossings
+    // (geo/flexicubes.py:253-260)
+    float dist[12], sum = 0.f;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) {
+      dist[e] = 0.f;
+      if (!((m >> e) & 1u)) continue;
+      float u[3], w0, w1;
+      crossing(C, e, false, u, w0, w1);
+      dist[e] = dist3(u, vd);
+      sum = __fadd_rn(sum, dist[e]);
+    }
+    const float mean = __fdiv_rn(sum, (float)__popc(m));
+#pragma unroll
+    for (int e = 0; e < 12; ++e)
+      if ((m >> e) & 1u) L_dev[ent++] = fabsf(__fsub_rn(dist[e], mean));
+  }
+}
+
 // The four cubes around a quad's edge in ascending index, with the edge's
 // index in each (see the orders above), and their dual vertices.
 struct QuadRing {
@@ -557,7 +625,8 @@ struct QuadRing {
 
 __device__ __forceinline__ QuadRing quad_ring(const FcGrid &G, const FcState &S, uint32_t qe) {
   const int v = (int)(qe >> 2), dir = (int)(qe & 3u);
-  const int vk = v % G.sy, t = v / G.sy, vj = t % (G.ry + 1), vi = t / (G.ry + 1);
+  int vi, vj, vk;
+  vertex_ijk(G, v, vi, vj, vk);
   auto cid = [&](int ci, int cj, int ck) { return (ci * G.ry + cj) * G.rz + ck; };
   QuadRing R;
   int le[4];
@@ -820,6 +889,10 @@ FcGrid make_grid(const DmgsFcGrid *a) {
   G.nc = a->rx * a->ry * a->rz;
   G.nv = (a->rx + 1) * G.sx;
   G.training = a->training;
+  G.by_rz = make_fastdiv((uint32_t)a->rz);
+  G.by_ry = make_fastdiv((uint32_t)a->ry);
+  G.by_sy = make_fastdiv((uint32_t)G.sy);
+  G.by_ry1 = make_fastdiv((uint32_t)(a->ry + 1));
   return G;
 }
 
@@ -879,12 +952,13 @@ int dmgs_fc_count(const DmgsFcGrid *a, void *state, size_t state_bytes, uint32_t
   const int nblk = fc_blocks(G.nv);
   DMGS_TIMED(K_FC_FWD, s, {
     dmgs_host::note_launch(), fc_count_kernel<<<nblk, FC_THREADS, 0, s>>>(G, S.blk);
-    dmgs_host::note_launch(), fc_scan_kernel<<<1, FC_SCAN_THREADS, 0, s>>>(S.blk, nblk, S.hdr);
+    dmgs_host::note_launch(), fc_scan_kernel<<<NVAL, FC_SCAN_THREADS, 0, s>>>(S.blk, nblk, S.hdr);
   });
   DMGS_LAUNCH_CHECK("fc_count");
-  uint32_t h[H_WORDS];
-  DMGS_CUDA(cudaMemcpyAsync(h, S.hdr, sizeof(h), cudaMemcpyDeviceToHost, s));
+  uint32_t tot[NVAL], h[H_WORDS];
+  DMGS_CUDA(cudaMemcpyAsync(tot, S.hdr, sizeof(tot), cudaMemcpyDeviceToHost, s));
   DMGS_CUDA(cudaStreamSynchronize(s));
+  derive_header(tot, h);
   counts[0] = h[H_SURF];
   counts[1] = h[H_VD];
   counts[2] = h[H_ENT];
@@ -921,8 +995,9 @@ int dmgs_fc_emit(const DmgsFcGrid *a, const uint32_t *counts, void *state, size_
   const int nblk = fc_blocks(G.nv);
   const int nq = (int)counts[4];
   DMGS_TIMED(K_FC_FWD, s, {
-    dmgs_host::note_launch(), fc_emit_kernel<<<nblk, FC_THREADS, 0, s>>>(G, S, surf, quad_edge, vertices,
-                                                                         L_dev, surf_edges);
+    dmgs_host::note_launch(), fc_emit_kernel<<<nblk, FC_THREADS, 0, s>>>(G, S, surf, quad_edge, surf_edges);
+    dmgs_host::note_launch(), fc_vd_kernel<<<((int)counts[0] + 127) / 128, 128, 0, s>>>(
+        G, surf, (int)counts[0], vertices, L_dev);
     if (nq > 0)
       dmgs_host::note_launch(), fc_quads_kernel<<<(nq + FC_THREADS - 1) / FC_THREADS, FC_THREADS, 0, s>>>(
           G, S, quad_edge, nq, (int)counts[5], (int)counts[1], vertices, faces);

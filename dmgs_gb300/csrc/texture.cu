@@ -240,9 +240,29 @@ tex_fwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
   }
 }
 
-// Adjoint.  Shared memory: weights, two staging tiles for the outer-product
-// GEMMs (rows = the block's 128 points).
+// Adjoint.  Shared memory per block (rows = the block's 128 points): the
+// weights; R0 [128][SA] (dL/dout, then dh2, then dh1: the left operands of
+// the outer-product GEMMs); R1 [128][SB] (h2, then each thread's dL/denc);
+// H1 and E [128][SB] (h1 and enc, kept from the recomputation: right
+// operands of the layer-2 and layer-1 GEMMs and the ReLU masks).
 constexpr int SA = TEX_MAXC + 1, SB = 33;
+
+// acc[r][c] += sum over the block's points q of a[q][row r] b[q][col c]
+template <int R, int SAx>
+__device__ __forceinline__ void outer_gemm(const float *__restrict__ a, int row0, int nrows,
+                                           const float *__restrict__ b, int col0, float (&acc)[R][4]) {
+  for (int q = 0; q < TEX_THREADS; ++q) {
+    float bv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) bv[c] = b[q * SB + col0 + c];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const float av = row0 + r < nrows ? a[q * SAx + row0 + r] : 0.f;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(av, bv[c], acc[r][c]);
+    }
+  }
+}
 
 template <int C>
 __global__ void __launch_bounds__(TEX_THREADS)
@@ -251,14 +271,18 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
                float *__restrict__ dW1, float *__restrict__ dW2, float *__restrict__ dW3) {
   extern __shared__ __align__(16) float smem[];
   float *sW1 = smem, *sW2 = sW1 + 32 * 32, *sW3 = sW2 + 32 * 32;
-  float *bufA = sW3 + TEX_MAXC * 32;     // [128][SA]
-  float *bufB = bufA + TEX_THREADS * SA;  // [128][SB]
+  float *R0 = sW3 + TEX_MAXC * 32;
+  float *R1 = R0 + TEX_THREADS * SA;
+  float *H1 = R1 + TEX_THREADS * SB;
+  float *E = H1 + TEX_THREADS * SB;
+  __shared__ TexLevels sL;  // the level table, indexed by a rolled loop
+  if (threadIdx.x == 0) sL = L;
   load_weights<C>(A, sW1, sW2, sW3);
   const int tid = threadIdx.x;
-  // owned sub-blocks: dW3 rows 3 (t/8) .. +2 (for C = 48; fewer rows for
-  // smaller C), cols 4 (t%8) .. +3; dW2 / dW1 rows 2 (t/8) .. +1
+  // owned sub-blocks: dW3 rows R3 (t/8) .., cols 4 (t%8) .. +3; dW2 / dW1
+  // rows 2 (t/8) .. +1
   const int cg = (tid & 7) * 4, rg = tid >> 3;
-  constexpr int R3 = (C + 15) / 16;  // rows of dW3 per thread
+  constexpr int R3 = (C + 15) / 16;
   float acc3[R3][4], acc2[2][4], acc1[2][4];
 #pragma unroll
   for (int r = 0; r < R3; ++r)
@@ -268,6 +292,7 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
   for (int r = 0; r < 2; ++r)
 #pragma unroll
     for (int c = 0; c < 4; ++c) acc2[r][c] = acc1[r][c] = 0.f;
+  float *e_row = E + tid * SB, *h1_row = H1 + tid * SB;
 
   const int64_t ntiles = (A.n + TEX_THREADS - 1) / TEX_THREADS;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -275,109 +300,82 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
     const bool valid = p < A.n;
     float t[3] = {0.f, 0.f, 0.f};
     bool pass[3] = {false, false, false};
-    float enc[TEX_FEAT], h1[32], h2[32], dy[C];
+    float h2[32];
+    {
+      float enc[TEX_FEAT], h1[32];
 #pragma unroll
-    for (int k = 0; k < 32; ++k) enc[k] = h1[k] = h2[k] = 0.f;
+      for (int k = 0; k < 32; ++k) enc[k] = h1[k] = h2[k] = 0.f;
+      if (valid) {
+        tex_coord(A, xyz, p, t, pass);
+        encode(A, L, t, enc);
+        matvec<32>(sW1, enc, h1);
 #pragma unroll
-    for (int j = 0; j < C; ++j) dy[j] = 0.f;
-    if (valid) {
-      tex_coord(A, xyz, p, t, pass);
-      encode(A, L, t, enc);
-      matvec<32>(sW1, enc, h1);
+        for (int k = 0; k < 32; ++k) h1[k] = fmaxf(h1[k], 0.f);
+        matvec<32>(sW2, h1, h2);
 #pragma unroll
-      for (int k = 0; k < 32; ++k) h1[k] = fmaxf(h1[k], 0.f);
-      matvec<32>(sW2, h1, h2);
+        for (int k = 0; k < 32; ++k) h2[k] = fmaxf(h2[k], 0.f);
+      }
 #pragma unroll
-      for (int k = 0; k < 32; ++k) h2[k] = fmaxf(h2[k], 0.f);
+      for (int k = 0; k < 32; ++k) {
+        e_row[k] = enc[k];
+        h1_row[k] = h1[k];
+        R1[tid * SB + k] = h2[k];
+      }
     }
-    // dout rows of the block, coalesced through bufA
+    // dL/dout rows of the block into R0 (coalesced); invalid rows zero
     {
       const int64_t p0 = tile * TEX_THREADS;
-      const int64_t nrow = A.n - p0 < TEX_THREADS ? A.n - p0 : TEX_THREADS;
-      for (int i = tid; i < nrow * C; i += TEX_THREADS) bufA[(i / C) * SA + i % C] = dout[p0 * C + i];
-      __syncthreads();
-      if (valid)
+      const int nrow = (int)(A.n - p0 < TEX_THREADS ? A.n - p0 : TEX_THREADS);
+      for (int i = tid; i < nrow * C; i += TEX_THREADS) R0[(i / C) * SA + i % C] = dout[p0 * C + i];
+      if (!valid)
 #pragma unroll
-        for (int j = 0; j < C; ++j) dy[j] = bufA[tid * SA + j];
-      __syncthreads();
-    }
-    // layer 3: dW3 += dy h2^T; dh2 = relu'(h2) (W3^T dy)
-#pragma unroll
-    for (int j = 0; j < C; ++j) bufA[tid * SA + j] = dy[j];
-#pragma unroll
-    for (int k = 0; k < 32; ++k) bufB[tid * SB + k] = h2[k];
-    __syncthreads();
-    for (int q = 0; q < TEX_THREADS; ++q) {
-      float b[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = bufB[q * SB + cg + c];
-#pragma unroll
-      for (int r = 0; r < R3; ++r) {
-        const int row = R3 * rg + r;
-        const float a = row < C ? bufA[q * SA + row] : 0.f;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc3[r][c] = fmaf(a, b[c], acc3[r][c]);
-      }
+        for (int j = 0; j < C; ++j) R0[tid * SA + j] = 0.f;
     }
     __syncthreads();
+    // layer 3: dW3 += dy h2^T;  dh2 = relu'(h2) (W3^T dy)
+    outer_gemm<R3, SA>(R0, R3 * rg, C, R1, cg, acc3);
     float d[32];
-    matvec_t<C>(sW3, dy, d);
+    {
+      float dy[C];
 #pragma unroll
-    for (int k = 0; k < 32; ++k) d[k] = h2[k] > 0.f ? d[k] : 0.f;  // dh2
-    // layer 2: dW2 += dh2 h1^T; dh1 = relu'(h1) (W2^T dh2)
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      bufA[tid * SA + k] = d[k];
-      bufB[tid * SB + k] = h1[k];
+      for (int j = 0; j < C; ++j) dy[j] = R0[tid * SA + j];
+      matvec_t<C>(sW3, dy, d);
     }
+#pragma unroll
+    for (int k = 0; k < 32; ++k) d[k] = h2[k] > 0.f ? d[k] : 0.f;
     __syncthreads();
-    for (int q = 0; q < TEX_THREADS; ++q) {
-      float b[4];
+    // layer 2: dW2 += dh2 h1^T;  dh1 = relu'(h1) (W2^T dh2)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = bufB[q * SB + cg + c];
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const float a = bufA[q * SA + 2 * rg + r];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc2[r][c] = fmaf(a, b[c], acc2[r][c]);
-      }
-    }
+    for (int k = 0; k < 32; ++k) R0[tid * SA + k] = d[k];
     __syncthreads();
-    float e[32];
-    matvec_t<32>(sW2, d, e);
+    outer_gemm<2, SA>(R0, 2 * rg, 32, H1, cg, acc2);
+    float g[32];
+    matvec_t<32>(sW2, d, g);
 #pragma unroll
-    for (int k = 0; k < 32; ++k) e[k] = h1[k] > 0.f ? e[k] : 0.f;  // dh1
-    // layer 1: dW1 += dh1 enc^T; denc = W1^T dh1
-#pragma unroll
-    for (int k = 0; k < 32; ++k) {
-      bufA[tid * SA + k] = e[k];
-      bufB[tid * SB + k] = enc[k];
-    }
+    for (int k = 0; k < 32; ++k) g[k] = h1_row[k] > 0.f ? g[k] : 0.f;
     __syncthreads();
-    for (int q = 0; q < TEX_THREADS; ++q) {
-      float b[4];
+    // layer 1: dW1 += dh1 enc^T;  dL/denc = W1^T dh1
 #pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = bufB[q * SB + cg + c];
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const float a = bufA[q * SA + 2 * rg + r];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc1[r][c] = fmaf(a, b[c], acc1[r][c]);
-      }
-    }
+    for (int k = 0; k < 32; ++k) R0[tid * SA + k] = g[k];
     __syncthreads();
+    outer_gemm<2, SA>(R0, 2 * rg, 32, E, cg, acc1);
+    matvec_t<32>(sW1, g, d);
+    __syncthreads();  // every GEMM read of R1 / E done: R1 now holds dL/denc rows
     if (!valid) continue;
-    matvec_t<32>(sW1, e, d);  // d = dL/denc (true gradient)
-    // table (128 x true gradient) and position gradients
-    float gt[3] = {0.f, 0.f, 0.f};
+    float *sd = R1 + tid * SB;  // own row
 #pragma unroll
+    for (int k = 0; k < 32; ++k) sd[k] = d[k];
+    // table (128 x the true gradient) and position gradients; the level
+    // loop stays rolled (the unrolled form was limited by instruction fetch)
+    float gt[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
     for (int l = 0; l < TEX_LEVELS; ++l) {
-      const LevelPos q = level_pos(L, l, t);
-      const float g0 = d[2 * l], g1 = d[2 * l + 1];
+      const LevelPos q = level_pos(sL, l, t);
+      const float g0 = sd[2 * l], g1 = sd[2 * l + 1];
       float dl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int corner = 0; corner < 8; ++corner) {
-        const uint32_t idx = corner_index(L, l, q.c[0] + (corner & 1), q.c[1] + ((corner >> 1) & 1),
+        const uint32_t idx = corner_index(sL, l, q.c[0] + (corner & 1), q.c[1] + ((corner >> 1) & 1),
                                           q.c[2] + ((corner >> 2) & 1));
         const float w = corner_weight(q, corner);
         if (dtable) atomicAdd(dtable + idx, make_float2(TEX_GRAD_SCALE * w * g0, TEX_GRAD_SCALE * w * g1));
@@ -396,7 +394,7 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
         }
       }
 #pragma unroll
-      for (int dd = 0; dd < 3; ++dd) gt[dd] += dl[dd] * L.scale[l];
+      for (int dd = 0; dd < 3; ++dd) gt[dd] += dl[dd] * sL.scale[l];
     }
     if (dxyz)
 #pragma unroll
@@ -420,7 +418,7 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
 }
 
 constexpr size_t tex_bwd_smem() {
-  return (size_t)(32 * 32 * 2 + TEX_MAXC * 32 + TEX_THREADS * (SA + SB)) * sizeof(float);
+  return (size_t)(32 * 32 * 2 + TEX_MAXC * 32 + TEX_THREADS * (SA + 3 * SB)) * sizeof(float);
 }
 
 bool tex_ok(const DmgsTexture *tx) {
