@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving-loop leg")
     ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-bound training leg")
     ap.add_argument("--no-fc", action="store_true", help="skip the FlexiCubes extraction leg")
+    ap.add_argument("--families", nargs="*", default=None,
+                    help="run each named kernel family once and exit (profiling driver): "
+                         "raster batched bind loss fc tex (all when none is named)")
     ap.add_argument("--no-tex", action="store_true", help="skip the hash-grid texture leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="requests per second")
@@ -436,6 +439,79 @@ def texture_leg(args, dev):
     return out
 
 
+def kernel_families(which, dev):
+    """Run every kernel family of the library once, at small sizes above L2
+    or at the configurations' own sizes (the driver of the per-kernel ncu
+    captures): the drop-in forward + backward (1M Gaussians of the
+    large-scene generator, 1237x822), the batched form on 2 views, the
+    stage-2 / stage-3 binding and the face culling on the configuration-2
+    mesh, the fused loss on 3x800x800, FlexiCubes at 250^3, the hash-grid
+    texture at 271,824 points."""
+    import torch
+    import dmgs_gb300
+    from dmgs_gb300.batched import BatchedRasterizer
+    from dmgs_gb300.binding import barycentric_table, bind_faces, bind_faces_scale_rot, frustum_faces
+    from dmgs_gb300.flexicubes import FlexiCubes
+    from dmgs_gb300.loss import l1_ssim_loss
+    from dmgs_gb300.meshbound import sdf_sphere_torus, sphere_torus_mesh
+    from dmgs_gb300.scenes import large_scene
+    from dmgs_gb300.texture import MLPTexture3D
+    t = lambda a: torch.tensor(a, device=dev)  # noqa: E731
+    if {"raster", "batched", "bind"} & set(which):
+        scene = large_scene(P=1_000_000, seed=0, n_views=2, width=1237, height=822)
+        g = {"means3D": t(scene.means3D), "opacities": t(scene.opacities), "shs": t(scene.shs),
+             "scales": t(scene.scales), "rotations": t(scene.rotations)}
+        sets = [dmgs_gb300.GaussianRasterizationSettings(
+            image_height=v.height, image_width=v.width, tanfovx=v.tanfovx, tanfovy=v.tanfovy,
+            bg=torch.zeros(3, device=dev), scale_modifier=1.0, viewmatrix=t(v.viewmatrix),
+            projmatrix=t(v.projmatrix), sh_degree=3, campos=t(v.campos), prefiltered=False,
+            debug=False) for v in scene.views]
+    if "raster" in which:
+        leaves = {k: v.clone().requires_grad_(True) for k, v in g.items()}
+        m2 = torch.zeros_like(leaves["means3D"], requires_grad=True)
+        img, _ = dmgs_gb300.GaussianRasterizer(sets[0])(
+            means3D=leaves["means3D"], means2D=m2, opacities=leaves["opacities"],
+            shs=leaves["shs"], scales=leaves["scales"], rotations=leaves["rotations"])
+        img.backward(torch.randn_like(img))
+    if "batched" in which:
+        br = BatchedRasterizer(sets, g, means2D_grads=False, densify_stats=True)
+        br.forward()
+        br.backward([torch.randn(3, s.image_height, s.image_width, device=dev) for s in sets])
+    if "bind" in which:
+        v, f = sphere_torus_mesh(64)
+        verts = v.clone().requires_grad_(True)
+        bc, rad = barycentric_table(6)
+        sf = torch.full((1,), 0.55, device=dev, requires_grad=True)
+        xyz, cov, _ = bind_faces(verts, f, bc, sf, rad, 1.0)
+        (xyz.sum() + cov.sum()).backward()
+        s2 = torch.randn(f.shape[0] * 6, 2, device=dev, requires_grad=True)
+        r2 = torch.randn(f.shape[0] * 6, 2, device=dev, requires_grad=True)
+        sum(o.sum() for o in bind_faces_scale_rot(verts, f, bc, s2, r2, 1e-6)).backward()
+        frustum_faces(v, f, t(scene.views[0].projmatrix))
+    if "loss" in which:
+        x = torch.rand(3, 800, 800, device=dev, requires_grad=True)
+        l1_ssim_loss(x, torch.rand(3, 800, 800, device=dev)).backward()
+    if "fc" in which:
+        fc = FlexiCubes(device=dev)
+        for res in (250, 64):
+            grid, cubes = fc.construct_voxel_grid_v2(res, [-1.0] * 3, [1.0] * 3)
+            s = torch.as_tensor(sdf_sphere_torus(grid.double().cpu().numpy()), dtype=torch.float32,
+                                device=dev).requires_grad_(True)
+            w = torch.zeros((cubes.shape[0], 21), device=dev, requires_grad=True)
+            x = grid.clone().requires_grad_(True)
+            vv, ff, L, se = fc(x, s, cubes, res, w[:, :12], w[:, 12:20], w[:, 20], training=True)
+            (vv.square().sum() + L.mean()).backward()
+    if "tex" in which:
+        v, f = sphere_torus_mesh(64)
+        bc = torch.distributions.Dirichlet(torch.ones(3, device=dev)).sample((f.shape[0] * 6,))
+        xyz = (bc.unsqueeze(2) * v[f].repeat_interleave(6, 0)).sum(1).contiguous().requires_grad_(True)
+        aabb = torch.stack([v.min(0).values, v.max(0).values]) * 1.1
+        tex = MLPTexture3D(aabb, channels=48, device=dev)
+        (tex.sample_noact(xyz) * torch.randn(xyz.shape[0], 48, device=dev)).sum().backward()
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"kernel_families": sorted(which), "ok": True}))
+
+
 def bytes_model(name, P, V, K, npix, nviews=1):
     """Algorithmic DRAM bytes per launch (SH3, scale/rotation inputs).  For
     a batched launch V, K, npix are sums over the views."""
@@ -495,6 +571,12 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
     from dmgs_gb300.scenes import large_scene
+    if args.families is not None:
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        kernel_families(args.families or ["raster", "batched", "bind", "loss", "fc", "tex"], dev)
+        return
     if args.impl == "reference":
         if rank != 0:
             return

@@ -31,8 +31,8 @@
 //   lane's column — only pairs the exact test would reject are skipped;
 // * the forward and the adjoint evaluate the exponent with the same
 //   explicitly rounded operations, so their skip/stop decisions agree;
-// * the adjoint sums a Gaussian's nine gradient terms over the thread's two
-//   pixels, then over the warp with a transposed reduce-scatter (16
+// * the adjoint sums a Gaussian's nine gradient terms over the thread's
+//   pixels, then over the warp with a transposed reduce-scatter (12
 //   shuffles); nine lanes then issue one scalar reduction each.
 #include "kernels.cuh"
 
@@ -422,37 +422,42 @@ __device__ __forceinline__ void adjoint_finish(float dx, const float4 &s2, const
   e[4] = suy2;
 }
 
-// Transposed reduce-scatter of 16 slots over the warp: afterwards the lane
-// whose bits (4,3,2,1) equal s holds the warp sum of slot s.
-__device__ __forceinline__ float warp_reduce_scatter16(float v[16], int lane) {
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
+// Transposed reduce-scatter of the 9 gradient slots over the warp, 12
+// shuffles: each level halves the slots a lane keeps (5 | 4, 3 | 2, 2 | 1,
+// 1 | 1) and adds its partner's copy of them; afterwards the even lane 2q
+// holds the warp sum of slot slot9(q) (q = lane bits 4..1), none when that
+// is >= 9.
+__device__ __forceinline__ float warp_reduce_scatter9(const float (&v)[9], int lane) {
+  float a[5], b[3], c[2];
+  {
     const bool hi = lane & 16;
-    const float keep = hi ? v[i + 8] : v[i];
-    const float send = hi ? v[i] : v[i + 8];
-    v[i] = keep + __shfl_xor_sync(FULL, send, 16);
-  }
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const bool hi = lane & 8;
-    const float keep = hi ? v[i + 4] : v[i];
-    const float send = hi ? v[i] : v[i + 4];
-    v[i] = keep + __shfl_xor_sync(FULL, send, 8);
-  }
-#pragma unroll
-  for (int i = 0; i < 2; ++i) {
-    const bool hi = lane & 4;
-    const float keep = hi ? v[i + 2] : v[i];
-    const float send = hi ? v[i] : v[i + 2];
-    v[i] = keep + __shfl_xor_sync(FULL, send, 4);
+    for (int i = 0; i < 5; ++i) {
+      const float up = i < 4 ? v[5 + i] : 0.f;
+      a[i] = (hi ? up : v[i]) + __shfl_xor_sync(FULL, hi ? v[i] : up, 16);
+    }
   }
   {
-    const bool hi = lane & 2;
-    const float keep = hi ? v[1] : v[0];
-    const float send = hi ? v[0] : v[1];
-    v[0] = keep + __shfl_xor_sync(FULL, send, 2);
+    const bool hi = lane & 8;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float up = i < 2 ? a[3 + i] : 0.f;
+      b[i] = (hi ? up : a[i]) + __shfl_xor_sync(FULL, hi ? a[i] : up, 8);
+    }
   }
-  return v[0] + __shfl_xor_sync(FULL, v[0], 1);
+  {
+    const bool hi = lane & 4;
+    c[0] = (hi ? b[2] : b[0]) + __shfl_xor_sync(FULL, hi ? b[0] : b[2], 4);
+    c[1] = (hi ? 0.f : b[1]) + __shfl_xor_sync(FULL, hi ? b[1] : 0.f, 4);
+  }
+  const bool hi = lane & 2;
+  const float d = (hi ? c[1] : c[0]) + __shfl_xor_sync(FULL, hi ? c[0] : c[1], 2);
+  return d + __shfl_xor_sync(FULL, d, 1);
+}
+
+// slot of the even lane 2q after warp_reduce_scatter9 (15: none)
+__device__ __forceinline__ int slot9(int q) {
+  return (int)((0xFFF8F765FF43F210ull >> (4 * q)) & 15u);
 }
 
 
@@ -531,9 +536,9 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
           cand |= ok[k];
         }
         if (!__any_sync(FULL, cand)) continue;  // warp-uniform
-        float e[16];
+        float e[9];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) e[i] = 0.f;
+        for (int i = 0; i < 9; ++i) e[i] = 0.f;
         bool any = false;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
@@ -545,8 +550,8 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
         }
         if (__ballot_sync(FULL, any)) {
           adjoint_finish(dx, s2, s3, e);
-          const float sum = warp_reduce_scatter16(e, lane);
-          const int slot = (lane >> 1) & 15;  // lane bits (4,3,2,1)
+          const float sum = warp_reduce_scatter9(e, lane);
+          const int slot = slot9((lane >> 1) & 15);
           if (!(lane & 1) && slot < 9) {
             const float scale = (slot == 2 || slot == 4) ? -0.5f : (slot == 3 ? -1.f : 1.f);
             atomicAdd(V.gacc + (size_t)__float_as_uint(s3.z) * 12 + slot, sum * scale);
