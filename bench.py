@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-bound training leg")
     ap.add_argument("--no-fc", action="store_true", help="skip the FlexiCubes extraction leg")
     ap.add_argument("--families", nargs="*", default=None,
-                    help="run each named kernel family once and exit (profiling driver): "
+                    help="run each named kernel family once and exit (for per-kernel profiling): "
                          "raster batched bind loss fc tex (all when none is named)")
     ap.add_argument("--no-tex", action="store_true", help="skip the hash-grid texture leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
@@ -289,6 +289,17 @@ def mesh_leg(args, dev):
     e1.record()
     torch.cuda.synchronize(dev)
     ms_torch_loss = e0.elapsed_time(e1) / steps
+    # colour and loss both composed from torch ops (the reference's form)
+    for i in range(3):
+        training_step(scene, views[i], targets[i], bg, window=window, fused_loss=False,
+                      fused_color=False)
+    e0.record()
+    for i in range(steps):
+        training_step(scene, views[i % len(views)], targets[i % len(views)], bg, window=window,
+                      fused_loss=False, fused_color=False)
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms_torch_both = e0.elapsed_time(e1) / steps
     F, P, Vn = int(f.shape[0]), scene.P, int(v.shape[0])
     # binding bytes: fwd reads faces (24 B) + 3 vertices (36 B) + per-Gaussian barycentrics
     # (12 B) and writes xyz + covariance (36 B); bwd reads the same geometry and the 36 B
@@ -297,13 +308,15 @@ def mesh_leg(args, dev):
     bwd_bytes = F * (24 + 36) + P * (12 + 36) + Vn * 12
     out = {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "faces": F, "gaussians": P,
            "resolution": [800, 800], "cameras": len(views), "steps": steps,
-           "loss": "0.8 L1 + 0.2 (1 - SSIM) by the fused loss kernels; SH colour in torch",
-           "steps_per_s_torch_loss": 1e3 / ms_torch_loss}
+           "loss": "0.8 L1 + 0.2 (1 - SSIM) by the fused loss kernels; sigmoid(SH) colour by "
+                   "the fused colour kernel",
+           "steps_per_s_torch_loss": 1e3 / ms_torch_loss,
+           "steps_per_s_torch_loss_and_colour": 1e3 / ms_torch_both}
     for name, nbytes in (("bind_fwd", fwd_bytes), ("bind_bwd", bwd_bytes)):
         if name in kt:
             t = kt[name][0] / kt[name][1]
             out[name] = {"ms": t, "alg_bytes": nbytes, "achieved_gbs": nbytes / (t * 1e-3) / 1e9}
-    for name in ("preprocess", "blend_fwd", "blend_bwd", "preprocess_bwd"):
+    for name in ("preprocess", "blend_fwd", "blend_bwd", "preprocess_bwd", "sh_colors", "l1_ssim"):
         if name in kt:
             out.setdefault("kernels_ms", {})[name] = kt[name][0] / kt[name][1]
     del scene, target, targets
@@ -441,8 +454,8 @@ def texture_leg(args, dev):
 
 def kernel_families(which, dev):
     """Run every kernel family of the library once, at small sizes above L2
-    or at the configurations' own sizes (the driver of the per-kernel ncu
-    captures): the drop-in forward + backward (1M Gaussians of the
+    or at the configurations' own sizes (the program that the per-kernel ncu
+    captures run): the drop-in forward + backward (1M Gaussians of the
     large-scene generator, 1237x822), the batched form on 2 views, the
     stage-2 / stage-3 binding and the face culling on the configuration-2
     mesh, the fused loss on 3x800x800, FlexiCubes at 250^3, the hash-grid
@@ -455,6 +468,7 @@ def kernel_families(which, dev):
     from dmgs_gb300.loss import l1_ssim_loss
     from dmgs_gb300.meshbound import sdf_sphere_torus, sphere_torus_mesh
     from dmgs_gb300.scenes import large_scene
+    from dmgs_gb300.shcolor import sh_colors
     from dmgs_gb300.texture import MLPTexture3D
     t = lambda a: torch.tensor(a, device=dev)  # noqa: E731
     if {"raster", "batched", "bind"} & set(which):
@@ -488,6 +502,8 @@ def kernel_families(which, dev):
         r2 = torch.randn(f.shape[0] * 6, 2, device=dev, requires_grad=True)
         sum(o.sum() for o in bind_faces_scale_rot(verts, f, bc, s2, r2, 1e-6)).backward()
         frustum_faces(v, f, t(scene.views[0].projmatrix))
+        feats = torch.randn(xyz.shape[0], 3, 16, device=dev, requires_grad=True)
+        sh_colors(3, feats, xyz.detach(), t(scene.views[0].campos)).sum().backward()
     if "loss" in which:
         x = torch.rand(3, 800, 800, device=dev, requires_grad=True)
         l1_ssim_loss(x, torch.rand(3, 800, 800, device=dev)).backward()

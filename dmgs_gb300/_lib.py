@@ -114,6 +114,8 @@ SIGNATURES = [
                                vp, vp, vp]),
     ("dmgs_fc_bwd", C.c_int, [C.POINTER(DmgsFcGrid), vp, vp, C.c_size_t, vp, C.c_size_t, vp, vp,
                               vp, vp, vp, vp, vp, vp, vp]),
+    ("dmgs_sh_colors_fwd", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp]),
+    ("dmgs_sh_colors_bwd", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp]),
     ("dmgs_tex_table_entries", C.c_int64, [C.c_float]),
     ("dmgs_tex_fwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp]),
     ("dmgs_tex_bwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]),

@@ -6,9 +6,10 @@ get_covariance_dyn, scene/gaussian_geo_model_mlp_flex.py:258-335,370-385),
 evaluates SH colours in torch (gaussian_renderer/__init__.py:165-170:
 eval_sh then sigmoid), rasterises with precomputed covariance and colours
 (render_dyn, :104-193) and optimises L1 + 0.2 (1 - SSIM)
-(utils/loss_utils.py).  Here the binding and the rasteriser are this
-library's kernels; the SH colour and the loss stay in torch as in the
-reference.
+(utils/loss_utils.py).  Here the binding, the SH colour (sigmoid of
+eval_sh), the rasteriser and the loss are this library's kernels; the torch
+compositions of the colour and the loss remain selectable
+(``fused_color=False``, ``fused_loss=False``) as the reference's form.
 
 The mesh of the workload is built by :func:`sphere_torus_mesh`: this
 library's FlexiCubes extraction (csrc/flexicubes.cu) of the union of a
@@ -26,6 +27,7 @@ import torch.nn.functional as F_
 from .binding import bind_faces
 from .flexicubes import FlexiCubes
 from .loss import l1_ssim_loss
+from .shcolor import sh_colors
 from .rasterizer import GaussianRasterizationSettings, GaussianRasterizer
 
 # Real SH basis constants (degree <= 3), the standard orthonormal basis.
@@ -143,13 +145,17 @@ class MeshBoundScene:
                                  self.rad_base, self.spatial_lr_scale, self.max_scale)
         return xyz, cov
 
-    def render(self, view, bg):
-        """render_dyn: precomputed covariance and sigmoid(SH) colours."""
+    def render(self, view, bg, fused_color=True):
+        """render_dyn: precomputed covariance and sigmoid(SH) colours (the
+        fused colour kernel, or the torch composition with fused_color=False)."""
         xyz, cov = self.gaussians()
         campos = torch.tensor(view.campos, device=self.device)
-        d = xyz - campos
-        d = d / d.norm(dim=1, keepdim=True)
-        colors = torch.sigmoid(eval_sh(self.sh_degree, self.features, d))
+        if fused_color:
+            colors = sh_colors(self.sh_degree, self.features, xyz, campos)
+        else:
+            d = xyz - campos
+            d = d / d.norm(dim=1, keepdim=True)
+            colors = torch.sigmoid(eval_sh(self.sh_degree, self.features, d))
         rs = GaussianRasterizationSettings(
             image_height=view.height, image_width=view.width, tanfovx=view.tanfovx,
             tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0,
@@ -163,13 +169,14 @@ class MeshBoundScene:
 
 
 def training_step(scene: MeshBoundScene, view, target, bg, lambda_dssim=0.2, window=None,
-                  fused_loss=True):
+                  fused_loss=True, fused_color=True):
     """One stage-2 step, forward and backward: bind, colour, rasterise,
-    L1 + lambda (1 - SSIM) (the fused loss kernel, or the torch composition
-    with fused_loss=False), gradients into the scene's parameters."""
+    L1 + lambda (1 - SSIM) (the fused kernels, or the torch compositions with
+    fused_loss=False / fused_color=False), gradients into the scene's
+    parameters."""
     for p in scene.params():
         p.grad = None
-    img, radii, _ = scene.render(view, bg)
+    img, radii, _ = scene.render(view, bg, fused_color=fused_color)
     if fused_loss:
         loss = l1_ssim_loss(img, target, lambda_dssim)
     else:

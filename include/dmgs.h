@@ -327,6 +327,23 @@ int dmgs_tex_bwd(const DmgsTexture *t, int64_t n, const float *xyz, const float 
                  dmgs_stream_t stream);
 
 /* ---------------------------------------------------------------------- *
+ * The renderer's Python colour path (gaussian_renderer/__init__.py:165-170:
+ * eval_sh of utils/sh_utils.py:25-110 on the normalised direction from the
+ * camera centre, then sigmoid) fused:
+ *   colors[p][c] = sigmoid(sum_k b_k(dir_p) sh[p][c][k]),
+ *   dir_p = (xyz[p] - campos) / |xyz[p] - campos|.
+ * sh: [P,3,K] fp32 device (channel-major, K >= (deg+1)^2, deg 0..3); xyz
+ * [P,3]; campos [3] device; colors [P,3].  The adjoint writes dL/dsh
+ * [P,3,K] (zeros above the active degree) and, when dL_dxyz is not NULL,
+ * dL/dxyz [P,3] through the normalisation.
+ * ---------------------------------------------------------------------- */
+int dmgs_sh_colors_fwd(int32_t P, int32_t deg, int32_t K, const float *sh, const float *xyz,
+                       const float *campos, float *colors, dmgs_stream_t stream);
+int dmgs_sh_colors_bwd(int32_t P, int32_t deg, int32_t K, const float *sh, const float *xyz,
+                       const float *campos, const float *dL_dcolors, float *dL_dsh,
+                       float *dL_dxyz, dmgs_stream_t stream);
+
+/* ---------------------------------------------------------------------- *
  * Fused photometric loss (no counterpart kernel in the reference, which
  * composes it from torch ops: l1_loss and ssim of utils/loss_utils.py as
  * used by train_geo_stage2.py:114-116):
