@@ -64,6 +64,7 @@ def parse():
                     help="run each named kernel family once and exit (for per-kernel profiling): "
                          "raster batched bind loss fc tex (all when none is named)")
     ap.add_argument("--no-tex", action="store_true", help="skip the hash-grid texture leg")
+    ap.add_argument("--no-stage2", action="store_true", help="skip the whole stage-2 iteration leg")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="Poisson trace length")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="requests per second")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0, help="HBM budget of in-flight requests")
@@ -392,6 +393,43 @@ def flexicubes_leg(args, dev):
                                "res": 64, "cores": os.cpu_count(), "kind": "port",
                                "sample": "float32 torch oracle on the host, 3 forward+backward"}
     return out
+
+
+def stage2_leg(args, dev):
+    """The reference's whole stage-2 iteration (train_geo_stage2.py:101-135)
+    on the library's kernels: FlexiCubes at 64^3 every step (learnable SDF,
+    deformation, per-cube weights; training mode) -> binding (6 Gaussians per
+    face, shared table) -> hash-grid texture SH features -> sigmoid(SH)
+    colours -> rasteriser (800x800, 100 hemisphere cameras) -> L1 + SSIM +
+    the SDF and FlexiCubes regularisers -> backward into every learnable.
+    Steps/s (forward + backward, no optimiser) and the kernels' share."""
+    import torch
+    from dmgs_gb300 import _lib
+    from dmgs_gb300.meshbound import Stage2Model
+    from dmgs_gb300.scenes import hemisphere_views
+    lib = _lib.load()
+    model = Stage2Model(res=64, device=dev)
+    views = hemisphere_views(100, 800, 800, seed=0)
+    bg = torch.zeros(3, device=dev)
+    with torch.no_grad():
+        saved = model.texture.encoder.params.clone()
+        gen = torch.Generator(device=dev).manual_seed(5)
+        model.texture.encoder.params.add_(0.05 * torch.randn(saved.shape, device=dev, generator=gen))
+        targets = [model.render(w, bg)[0].detach() for w in views[:20]]
+        model.texture.encoder.params.copy_(saved)
+        faces = int(model.mesh()[1].shape[0])
+    steps = max(args.steps, 20)
+    ms = timed(lambda i: model.step(views[i % 20], targets[i % 20], bg), steps, 5, dev) / steps
+    lib.dmgs_timing_enable(1)
+    _lib.timing_collect()
+    for i in range(5):
+        model.step(views[i], targets[i], bg)
+    torch.cuda.synchronize(dev)
+    lib.dmgs_timing_enable(0)
+    kt = _lib.timing_collect()
+    return {"steps_per_s": 1e3 / ms, "ms_per_step": ms, "grid": 64, "faces": faces,
+            "gaussians": faces * 6, "resolution": [800, 800], "steps": steps,
+            "kernel_ms_per_step": {k: v[0] / 5 for k, v in sorted(kt.items())}}
 
 
 def texture_leg(args, dev):
@@ -815,6 +853,9 @@ def main():
     texl = None
     if not args.no_tex:
         texl = texture_leg(args, dev)
+    st2 = None
+    if not args.no_stage2:
+        st2 = stage2_leg(args, dev)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -843,7 +884,7 @@ def main():
             "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
             "serving": serving, "mesh_training": mesh, "flexicubes": fcl,
-            "texture": texl,
+            "texture": texl, "stage2_full": st2,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
         print(json.dumps(line))
     if world > 1:

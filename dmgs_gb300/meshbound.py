@@ -184,3 +184,90 @@ def training_step(scene: MeshBoundScene, view, target, bg, lambda_dssim=0.2, win
             1.0 - ssim(img, target, window))
     loss.backward()
     return loss.detach(), radii
+
+
+def sdf_reg_loss(sdf, edges):
+    """The reference's SDF regulariser (compute_sdf_reg_loss,
+    scene/gaussian_geo_model_mlp_flex.py:233-239): binary cross-entropy of
+    each sign-changing edge's end values against the other end's sign."""
+    s = sdf[edges.reshape(-1)].reshape(-1, 2)
+    s = s[torch.sign(s[:, 0]) != torch.sign(s[:, 1])]
+    return (F_.binary_cross_entropy_with_logits(s[:, 0], (s[:, 1] > 0).float()) +
+            F_.binary_cross_entropy_with_logits(s[:, 1], (s[:, 0] > 0).float()))
+
+
+class Stage2Model:
+    """The reference's stage-2 model and iteration on this library's kernels
+    (scene/gaussian_geo_model_mlp_flex.py with train_geo_stage2.py:101-135):
+    a FlexiCubes grid with learnable SDF, deformation and per-cube weights,
+    extracted every step in training mode (getMesh, :241-255); Gaussians
+    bound to the faces with the shared barycentric table (renew_gaussian,
+    :258-335, opacity 0.9999); SH features from the hash-grid texture (:313);
+    sigmoid(SH) colours; the rasteriser with precomputed covariance and
+    colours (render_dyn); loss (1 - l) L1 + l (1 - SSIM) + lambda_sdf
+    sdf_reg + lambda_flex mean(L_dev) (the defaults of
+    arguments/__init__.py:112-114)."""
+
+    def __init__(self, res=64, gs_per_face=6, device="cuda", sdf=sdf_sphere_torus, sh_degree=3):
+        from .binding import barycentric_table
+        from .texture import MLPTexture3D
+        self.device = torch.device(device)
+        self.res = res
+        self.fc = FlexiCubes(device=device)
+        self.grid, self.cubes = self.fc.construct_voxel_grid_v2(res, [-1.0] * 3, [1.0] * 3)
+        self.sdf = torch.as_tensor(sdf(self.grid.double().cpu().numpy()), dtype=torch.float32,
+                                   device=self.device).requires_grad_(True)
+        self.deform = torch.zeros_like(self.grid, requires_grad=True)
+        self.per_cube_weights = torch.ones((self.cubes.shape[0], 21), device=self.device,
+                                           requires_grad=True)
+        self.max_displacement = (2.0 / res) / 4.0
+        self.bc, self.rad_base = barycentric_table(gs_per_face, device)
+        self.max_scale = 2.0
+        self.scale_factor = torch.full((1,), math.atanh(1.0 / self.max_scale), device=self.device,
+                                       requires_grad=True)
+        self.spatial_lr_scale = 1.0
+        self.sh_degree = sh_degree
+        with torch.no_grad():
+            v = self.mesh()[0]
+            aabb = torch.stack([v.min(0).values, v.max(0).values]) * 1.1
+        self.texture = MLPTexture3D(aabb, channels=3 * (sh_degree + 1) ** 2, device=device)
+
+    def params(self):
+        return [self.sdf, self.deform, self.per_cube_weights, self.scale_factor] + list(
+            self.texture.parameters())
+
+    def mesh(self):
+        v = self.grid + self.max_displacement * torch.tanh(self.deform)
+        w = self.per_cube_weights
+        return self.fc(v, self.sdf, self.cubes, self.res, w[:, :12], w[:, 12:20], w[:, 20],
+                       training=True)
+
+    def render(self, view, bg):
+        verts, faces, L_dev, surf_edges = self.mesh()
+        xyz, cov, _ = bind_faces(verts, faces, self.bc, self.scale_factor, self.rad_base,
+                                 self.spatial_lr_scale, self.max_scale)
+        K = (self.sh_degree + 1) ** 2
+        feats = self.texture.sample_noact(xyz).view(-1, 3, K)
+        campos = torch.tensor(view.campos, device=self.device)
+        colors = sh_colors(self.sh_degree, feats, xyz, campos)
+        rs = GaussianRasterizationSettings(
+            image_height=view.height, image_width=view.width, tanfovx=view.tanfovx,
+            tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0,
+            viewmatrix=torch.tensor(view.viewmatrix, device=self.device),
+            projmatrix=torch.tensor(view.projmatrix, device=self.device),
+            sh_degree=self.sh_degree, campos=campos, prefiltered=False, debug=False)
+        opac = torch.full((xyz.shape[0], 1), 0.9999, device=self.device)
+        img, radii = GaussianRasterizer(rs)(
+            means3D=xyz, means2D=torch.zeros_like(xyz, requires_grad=True), opacities=opac,
+            colors_precomp=colors, cov3D_precomp=cov)
+        return img, radii, L_dev, surf_edges
+
+    def step(self, view, target, bg, lambda_dssim=0.2, lambda_sdf=0.2, lambda_flex=0.25):
+        """One iteration's forward and backward; returns the loss."""
+        for p in self.params():
+            p.grad = None
+        img, radii, L_dev, surf_edges = self.render(view, bg)
+        loss = (l1_ssim_loss(img, target, lambda_dssim) + lambda_sdf * sdf_reg_loss(self.sdf, surf_edges)
+                + lambda_flex * L_dev.mean())
+        loss.backward()
+        return loss.detach()
