@@ -118,7 +118,9 @@ SIGNATURES = [
     ("dmgs_sh_colors_bwd", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp]),
     ("dmgs_tex_table_entries", C.c_int64, [C.c_float]),
     ("dmgs_tex_fwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp]),
-    ("dmgs_tex_bwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("dmgs_tex_bwd_scratch_bytes", C.c_size_t, [C.c_int64]),
+    ("dmgs_tex_bwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp,
+                               C.c_size_t, vp]),
     ("dmgs_l1_ssim_scratch_bytes", C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     ("dmgs_l1_ssim", C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, vp, vp, vp,
                                C.c_size_t, vp]),

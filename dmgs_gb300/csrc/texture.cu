@@ -24,8 +24,9 @@
 //             three weight gradients as 128-point outer-product GEMMs staged
 //             in shared memory (each thread owns a fixed 3x4 / 2x4 sub-block
 //             in registers across all its tiles; one atomic per entry per
-//             block at the end), scatters the table gradient with float2
-//             atomics and forms the position gradient from the
+//             block at the end) and writes each point's dL/denc; then a
+//             light full-occupancy kernel scatters the table gradient with
+//             float2 atomics and forms the position gradient from the
 //             interpolation weights' derivatives.
 // The reference's gradient hooks (geo/texture.py:72-73 with _MLP's
 // loss_scale): the table receives 128x its true gradient, the positions
@@ -267,7 +268,7 @@ __device__ __forceinline__ void outer_gemm(const float *__restrict__ a, int row0
 template <int C>
 __global__ void __launch_bounds__(TEX_THREADS)
 tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz,
-               const float *__restrict__ dout, float *__restrict__ dxyz, float2 *__restrict__ dtable,
+               const float *__restrict__ dout, float *__restrict__ denc,
                float *__restrict__ dW1, float *__restrict__ dW2, float *__restrict__ dW3) {
   extern __shared__ __align__(16) float smem[];
   float *sW1 = smem, *sW2 = sW1 + 32 * 32, *sW3 = sW2 + 32 * 32;
@@ -275,8 +276,6 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
   float *R1 = R0 + TEX_THREADS * SA;
   float *H1 = R1 + TEX_THREADS * SB;
   float *E = H1 + TEX_THREADS * SB;
-  __shared__ TexLevels sL;  // the level table, indexed by a rolled loop
-  if (threadIdx.x == 0) sL = L;
   load_weights<C>(A, sW1, sW2, sW3);
   const int tid = threadIdx.x;
   // owned sub-blocks: dW3 rows R3 (t/8) .., cols 4 (t%8) .. +3; dW2 / dW1
@@ -360,45 +359,11 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
     __syncthreads();
     outer_gemm<2, SA>(R0, 2 * rg, 32, E, cg, acc1);
     matvec_t<32>(sW1, g, d);
-    __syncthreads();  // every GEMM read of R1 / E done: R1 now holds dL/denc rows
+    __syncthreads();  // every GEMM read done before the next tile's staging
     if (!valid) continue;
-    float *sd = R1 + tid * SB;  // own row
+    float4 *row = reinterpret_cast<float4 *>(denc + 32 * p);
 #pragma unroll
-    for (int k = 0; k < 32; ++k) sd[k] = d[k];
-    // table (128 x the true gradient) and position gradients; the level
-    // loop stays rolled (the unrolled form was limited by instruction fetch)
-    float gt[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
-    for (int l = 0; l < TEX_LEVELS; ++l) {
-      const LevelPos q = level_pos(sL, l, t);
-      const float g0 = sd[2 * l], g1 = sd[2 * l + 1];
-      float dl[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-      for (int corner = 0; corner < 8; ++corner) {
-        const uint32_t idx = corner_index(sL, l, q.c[0] + (corner & 1), q.c[1] + ((corner >> 1) & 1),
-                                          q.c[2] + ((corner >> 2) & 1));
-        const float w = corner_weight(q, corner);
-        if (dtable) atomicAdd(dtable + idx, make_float2(TEX_GRAD_SCALE * w * g0, TEX_GRAD_SCALE * w * g1));
-        if (dxyz) {
-          const float2 v = __ldg(A.table + idx);
-          const float gv = g0 * v.x + g1 * v.y;
-#pragma unroll
-          for (int dd = 0; dd < 3; ++dd) {
-            // d w / d f_dd: the other two factors, signed by the corner's bit
-            float o = 1.f;
-#pragma unroll
-            for (int e2 = 0; e2 < 3; ++e2)
-              if (e2 != dd) o *= ((corner >> e2) & 1) ? q.f[e2] : 1.f - q.f[e2];
-            dl[dd] += (((corner >> dd) & 1) ? o : -o) * gv;
-          }
-        }
-      }
-#pragma unroll
-      for (int dd = 0; dd < 3; ++dd) gt[dd] += dl[dd] * sL.scale[l];
-    }
-    if (dxyz)
-#pragma unroll
-      for (int dd = 0; dd < 3; ++dd) dxyz[3 * p + dd] = pass[dd] ? gt[dd] / A.ext[dd] : 0.f;
+    for (int k = 0; k < 8; ++k) row[k] = make_float4(d[4 * k], d[4 * k + 1], d[4 * k + 2], d[4 * k + 3]);
   }
   // block partials of the weight gradients
 #pragma unroll
@@ -415,6 +380,56 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
       atomicAdd(dW2 + (2 * rg + r) * 32 + cg + c, acc2[r][c]);
       atomicAdd(dW1 + (2 * rg + r) * 32 + cg + c, acc1[r][c]);
     }
+}
+
+// Table (128 x the true gradient) and position gradients from each point's
+// dL/denc row: a light kernel (few registers, full occupancy) so that the
+// latency of the gathers and atomics is hidden by many warps.  The level
+// loop stays rolled and reads the level table from shared memory.
+__global__ void __launch_bounds__(256)
+tex_scatter_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz,
+                   const float *__restrict__ denc, float *__restrict__ dxyz, float2 *__restrict__ dtable) {
+  __shared__ TexLevels sL;
+  if (threadIdx.x == 0) sL = L;
+  __syncthreads();
+  const int64_t p = (int64_t)blockIdx.x * 256 + threadIdx.x;
+  if (p >= A.n) return;
+  float t[3];
+  bool pass[3];
+  tex_coord(A, xyz, p, t, pass);
+  const float *dr = denc + 32 * p;
+  float gt[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int l = 0; l < TEX_LEVELS; ++l) {
+    const LevelPos q = level_pos(sL, l, t);
+    const float2 g = *reinterpret_cast<const float2 *>(dr + 2 * l);
+    float dl[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int corner = 0; corner < 8; ++corner) {
+      const uint32_t idx = corner_index(sL, l, q.c[0] + (corner & 1), q.c[1] + ((corner >> 1) & 1),
+                                        q.c[2] + ((corner >> 2) & 1));
+      const float w = corner_weight(q, corner);
+      if (dtable) atomicAdd(dtable + idx, make_float2(TEX_GRAD_SCALE * w * g.x, TEX_GRAD_SCALE * w * g.y));
+      if (dxyz) {
+        const float2 v = __ldg(A.table + idx);
+        const float gv = g.x * v.x + g.y * v.y;
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd) {
+          // d w / d f_dd: the other two factors, signed by the corner's bit
+          float o = 1.f;
+#pragma unroll
+          for (int e2 = 0; e2 < 3; ++e2)
+            if (e2 != dd) o *= ((corner >> e2) & 1) ? q.f[e2] : 1.f - q.f[e2];
+          dl[dd] += (((corner >> dd) & 1) ? o : -o) * gv;
+        }
+      }
+    }
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) gt[dd] += dl[dd] * sL.scale[l];
+  }
+  if (dxyz)
+#pragma unroll
+    for (int dd = 0; dd < 3; ++dd) dxyz[3 * p + dd] = pass[dd] ? gt[dd] / A.ext[dd] : 0.f;
 }
 
 constexpr size_t tex_bwd_smem() {
@@ -471,7 +486,7 @@ int run_fwd(const TexArgs &A, const TexLevels &L, const float *xyz, float *out, 
 
 template <int C>
 int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float *dout, float *dxyz,
-            float *dtable, float *dW1, float *dW2, float *dW3, cudaStream_t s) {
+            float *dtable, float *dW1, float *dW2, float *dW3, float *denc, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     DMGS_CUDA(cudaFuncSetAttribute(tex_bwd_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -481,7 +496,10 @@ int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float 
   int grid;
   if (int r = persistent_grid(tex_bwd_kernel<C>, tex_bwd_smem(), A.n, grid)) return r;
   dmgs_host::note_launch(), tex_bwd_kernel<C><<<grid, TEX_THREADS, tex_bwd_smem(), s>>>(
-      A, L, xyz, dout, dxyz, reinterpret_cast<float2 *>(dtable), dW1, dW2, dW3);
+      A, L, xyz, dout, denc, dW1, dW2, dW3);
+  if (dxyz || dtable)
+    dmgs_host::note_launch(), tex_scatter_kernel<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(
+        A, L, xyz, denc, dxyz, reinterpret_cast<float2 *>(dtable));
   return DMGS_OK;
 }
 
@@ -522,12 +540,21 @@ int dmgs_tex_fwd(const DmgsTexture *tx, int64_t n, const float *xyz, float *out,
   return DMGS_OK;
 }
 
+size_t dmgs_tex_bwd_scratch_bytes(int64_t n) { return n > 0 ? (size_t)n * 32 * sizeof(float) : 0; }
+
 int dmgs_tex_bwd(const DmgsTexture *tx, int64_t n, const float *xyz, const float *dout, float *dxyz,
-                 float *dtable, float *dW1, float *dW2, float *dW3, dmgs_stream_t stream) {
+                 float *dtable, float *dW1, float *dW2, float *dW3, void *scratch,
+                 size_t scratch_bytes, dmgs_stream_t stream) {
   if (!tex_ok(tx) || n < 0 || !dW1 || !dW2 || !dW3 || (n > 0 && (!xyz || !dout))) {
     set_error("tex_bwd: invalid arguments");
     return DMGS_ERR_ARG;
   }
+  if (n > 0 && (!scratch || scratch_bytes < dmgs_tex_bwd_scratch_bytes(n) ||
+                (reinterpret_cast<uintptr_t>(scratch) & 15))) {
+    set_error("tex_bwd: scratch must hold dmgs_tex_bwd_scratch_bytes(n) bytes, 16-byte aligned");
+    return DMGS_ERR_STATE;
+  }
+  float *denc = static_cast<float *>(scratch);
   const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const TexLevels L = make_levels(tx->per_level_scale);
   DMGS_CUDA(cudaMemsetAsync(dW1, 0, 32 * 32 * 4, s));
@@ -539,10 +566,10 @@ int dmgs_tex_bwd(const DmgsTexture *tx, int64_t n, const float *xyz, const float
   int r = DMGS_OK;
   DMGS_TIMED(K_TEX_BWD, s, {
     switch (tx->channels) {
-      case 3: r = run_bwd<3>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, s); break;
-      case 12: r = run_bwd<12>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, s); break;
-      case 27: r = run_bwd<27>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, s); break;
-      default: r = run_bwd<48>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, s); break;
+      case 3: r = run_bwd<3>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+      case 12: r = run_bwd<12>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+      case 27: r = run_bwd<27>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+      default: r = run_bwd<48>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
     }
   });
   if (r != DMGS_OK) return r;

@@ -63,9 +63,11 @@ class _TextureFn(torch.autograd.Function):
         dx = torch.empty_like(x) if ctx.needs_input_grad[0] else None
         dt = torch.empty_like(t) if ctx.needs_input_grad[1] else None
         dw1, dw2, dw3 = torch.empty_like(w1), torch.empty_like(w2), torch.empty_like(w3)
+        scratch = torch.empty(max(1, lib.dmgs_tex_bwd_scratch_bytes(x.shape[0]) // 4),
+                              dtype=torch.float32, device=x.device)
         check(lib.dmgs_tex_bwd(C.byref(d), x.shape[0], ptr(x), ptr(g), ptr(dx), ptr(dt),
-                               dw1.data_ptr(), dw2.data_ptr(), dw3.data_ptr(), stream_of(x.device)),
-              "tex_bwd")
+                               dw1.data_ptr(), dw2.data_ptr(), dw3.data_ptr(), scratch.data_ptr(),
+                               scratch.numel() * 4, stream_of(x.device)), "tex_bwd")
         return dx, dt, dw1, dw2, dw3, None, None
 
 

@@ -322,9 +322,10 @@ typedef struct DmgsTexture {
 int64_t dmgs_tex_table_entries(float per_level_scale);
 int dmgs_tex_fwd(const DmgsTexture *t, int64_t n, const float *xyz, float *out,
                  dmgs_stream_t stream);
+size_t dmgs_tex_bwd_scratch_bytes(int64_t n);  /* 128 B per point, 16-byte aligned */
 int dmgs_tex_bwd(const DmgsTexture *t, int64_t n, const float *xyz, const float *dout,
                  float *dxyz, float *dtable, float *dW1, float *dW2, float *dW3,
-                 dmgs_stream_t stream);
+                 void *scratch, size_t scratch_bytes, dmgs_stream_t stream);
 
 /* ---------------------------------------------------------------------- *
  * The renderer's Python colour path (gaussian_renderer/__init__.py:165-170:
