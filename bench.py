@@ -581,10 +581,12 @@ def bytes_model(name, P, V, K, npix, nviews=1):
         return K * 40 + npix * 20 + P * 36
     if name == "preprocess_bwd":
         return P * (236 + 36 + 236)
-    if name == "segment_sort":
-        return K * 12
-    if name == "scatter":
-        return K * 8 + V * 16
+    if name == "bin_depth_sort":  # 4 LSD passes over (depth bits, index): 4 B read by the
+        return V * 80             # histogram, 8 B read + 8 B written by the scatter, per key
+    if name == "bin_compact":
+        return P * nviews + V * 12
+    if name == "bin_emit":
+        return K * 4 + V * 16
     return None
 
 
@@ -615,6 +617,8 @@ def kernel_table(kt, model_args):
         if b is not None:
             kernels[name]["alg_bytes"] = int(b)
             kernels[name]["achieved_gbs"] = round(b / (avg / 1e3) / 1e9, 1)
+        if name == "bin_depth_sort":
+            kernels[name]["keys_per_s"] = round(model_args[1] / (avg / 1e3), 1)
     return kernels
 
 
