@@ -204,3 +204,39 @@ def test_mark_visible_matches_oracle():
     pts = np.random.default_rng(0).uniform(-8, 8, (5000, 3)).astype(np.float32)
     vis = GaussianRasterizer(rs).markVisible(torch.tensor(pts, device=d)).cpu().numpy()
     np.testing.assert_array_equal(vis, R.mark_visible(pts, view.viewmatrix))
+
+
+def test_full_size_integer_outputs_bit_exact():
+    """Configuration 3 at its full size (3M Gaussians of the large-scene
+    generator, 1237x822): radii, tile rectangles, tiles touched, depth keys,
+    the ~19M sorted (tile, depth) keys and Gaussian indices and the tile
+    ranges all equal the oracle's float32 geometry and its stable sort; the
+    ranges partition the instance list, and every listed Gaussian's rectangle
+    contains its tile (size-independent properties of the same run)."""
+    from dmgs_gb300.scenes import large_scene
+    sc = large_scene(P=3_000_000, seed=0, n_views=1)
+    view = sc.views[0]
+    inp = mode_inputs(sc, ("shs", "sr"))
+    run = AbiRun(view, inp, debug=False).forward()
+    dv = run.debug_views()
+    cam = oracle_camera(view)
+    geom = R.geometry_f32(inp["means3D"], cam, inp["opacities"], inp["scales"], inp["rotations"])
+    vis = geom["visible"]
+    np.testing.assert_array_equal(run.radii.cpu().numpy()[:run.P], geom["radii"])
+    np.testing.assert_array_equal(dv["rect"], np.where(vis[:, None], geom["rect"], 0))
+    np.testing.assert_array_equal(dv["tiles_touched"], geom["tiles_touched"])
+    np.testing.assert_array_equal(dv["depth"][vis].view(np.uint32), geom["depth"][vis].view(np.uint32))
+    keys, vals, ranges = R.binning_fast(geom, cam)
+    assert run.K == len(keys) > 10_000_000
+    np.testing.assert_array_equal(dv["keys"], keys)
+    np.testing.assert_array_equal(dv["values"], vals)
+    np.testing.assert_array_equal(dv["ranges"], ranges)
+    # properties: the non-empty ranges tile [0, K) in tile order; rectangles contain their tiles
+    nz = ranges[:, 1] > ranges[:, 0]
+    r = ranges[nz]
+    assert r[0, 0] == 0 and r[-1, 1] == run.K and np.array_equal(r[1:, 0], r[:-1, 1])
+    gx = (view.width + 15) // 16
+    tiles = (dv["keys"] >> np.uint64(32)).astype(np.int64)
+    rect = geom["rect"][dv["values"]]
+    tx, ty = tiles % gx, tiles // gx
+    assert np.all((rect[:, 0] <= tx) & (tx < rect[:, 2]) & (rect[:, 1] <= ty) & (ty < rect[:, 3]))
