@@ -592,12 +592,12 @@ tile_scan_kernel(const BinViews bv) {
   uint32_t run = 0;
   if (t < T) {
     uint32_t c = c0;
-    for (; c + 8 <= c1; c += 8) {
-      uint32_t x[8];
+    for (; c + 16 <= c1; c += 16) {
+      uint32_t x[16];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) x[u] = col[(size_t)(c + u) * T];
+      for (int u = 0; u < 16; ++u) x[u] = col[(size_t)(c + u) * T];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < 16; ++u) {
         col[(size_t)(c + u) * T] = run;
         run += x[u];
       }
