@@ -77,6 +77,22 @@ __device__ __forceinline__ void sh_basis(float x, float y, float z, int deg, flo
   }
 }
 
+// The first 16 coefficients of one channel row: four 16-byte loads when the
+// row is 16-byte aligned (K a multiple of 4 and an aligned base), else scalar.
+__device__ __forceinline__ void load_row16(const float *s, bool vec, int nb, float (&v)[16]) {
+  if (vec) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(s);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 f = q * 4 < nb ? __ldg(s4 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+      v[4 * q] = f.x; v[4 * q + 1] = f.y; v[4 * q + 2] = f.z; v[4 * q + 3] = f.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = k < nb ? __ldg(s + k) : 0.f;
+  }
+}
+
 __device__ __forceinline__ void unit_dir(const float *xyz, const float *campos, int p, float (&d)[3],
                                          float &len) {
   const float dx = xyz[3 * (size_t)p] - __ldg(campos), dy = xyz[3 * (size_t)p + 1] - __ldg(campos + 1),
@@ -97,13 +113,15 @@ sh_colors_fwd_kernel(int P, int deg, int K, const float *__restrict__ sh, const 
   float b[16], G[16][3];
   sh_basis<false>(d[0], d[1], d[2], deg, b, G);
   const int nb = (deg + 1) * (deg + 1);
+  const bool vec = (K & 3) == 0 && (reinterpret_cast<uintptr_t>(sh) & 15) == 0;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float *s = sh + ((size_t)p * 3 + c) * K;
+    float v[16];
+    load_row16(sh + ((size_t)p * 3 + c) * K, vec, nb, v);
     float r = 0.f;
 #pragma unroll
     for (int k = 0; k < 16; ++k)
-      if (k < nb) r = fmaf(b[k], __ldg(s + k), r);
+      if (k < nb) r = fmaf(b[k], v[k], r);
     colors[3 * (size_t)p + c] = 1.f / (1.f + expf(-r));
   }
 }
@@ -119,28 +137,39 @@ sh_colors_bwd_kernel(int P, int deg, int K, const float *__restrict__ sh, const 
   float b[16], G[16][3];
   sh_basis<true>(d[0], d[1], d[2], deg, b, G);
   const int nb = (deg + 1) * (deg + 1);
+  const bool vec = (K & 3) == 0 && (reinterpret_cast<uintptr_t>(sh) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(dsh) & 15) == 0;
   float gd[3] = {0.f, 0.f, 0.f};
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float *s = sh + ((size_t)p * 3 + c) * K;
-    float r = 0.f, v[16];
+    float v[16];
+    load_row16(sh + ((size_t)p * 3 + c) * K, vec, nb, v);
+    float r = 0.f;
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      v[k] = k < nb ? __ldg(s + k) : 0.f;
+    for (int k = 0; k < 16; ++k)
       if (k < nb) r = fmaf(b[k], v[k], r);
-    }
     const float sg = 1.f / (1.f + expf(-r));
     const float dr = dcolors[3 * (size_t)p + c] * sg * (1.f - sg);
-    float *o = dsh + ((size_t)p * 3 + c) * K;
+    float o[16];
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      if (k < nb) {
-        o[k] = dr * b[k];
+      o[k] = k < nb ? dr * b[k] : 0.f;
+      if (k < nb)
 #pragma unroll
         for (int a = 0; a < 3; ++a) gd[a] = fmaf(dr * v[k], G[k][a], gd[a]);
-      }
     }
-    for (int k = nb; k < K; ++k) o[k] = 0.f;
+    float *out = dsh + ((size_t)p * 3 + c) * K;
+    if (vec) {
+      float4 *o4 = reinterpret_cast<float4 *>(out);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q * 4 < K) o4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        if (k < K) out[k] = o[k];
+    }
+    for (int k = 16; k < K; ++k) out[k] = 0.f;
   }
   if (dxyz) {
     // through dir = D / |D|: dL/dD = (g - dir (dir . g)) / |D|
