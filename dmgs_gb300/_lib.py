@@ -52,7 +52,8 @@ class DmgsFaceBinding3(C.Structure):
 
 class DmgsFcGrid(C.Structure):
     _fields_ = [("x", vp), ("s", vp), ("beta", vp), ("alpha", vp), ("gamma", vp),
-                ("rx", C.c_int32), ("ry", C.c_int32), ("rz", C.c_int32), ("training", C.c_int32)]
+                ("rx", C.c_int32), ("ry", C.c_int32), ("rz", C.c_int32), ("training", C.c_int32),
+                ("beta_stride", C.c_int32), ("alpha_stride", C.c_int32), ("gamma_stride", C.c_int32)]
 
 
 class DmgsTexture(C.Structure):

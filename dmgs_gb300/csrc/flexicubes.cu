@@ -231,6 +231,7 @@ struct FcGrid {
   int sy, sx;  // vertex strides: j -> rz + 1, i -> (ry + 1)(rz + 1)
   int nc, nv;
   int training;
+  int bs, as, gs;  // row strides (floats) of the beta / alpha / gamma arrays and their gradients
   FastDiv by_rz, by_ry, by_sy, by_ry1;  // rz, ry, rz + 1, ry + 1
 };
 
@@ -281,15 +282,17 @@ size_t fc_state_bytes_(int rx, int ry, int rz, FcState *st, char *base) {
   return o;
 }
 
-__device__ __forceinline__ float beta_n(const float *beta, int c, int e) {
-  return beta ? __fadd_rn(__fmul_rn(tanhf(__ldg(beta + (size_t)c * 12 + e)), WEIGHT_SCALE), 1.f) : 1.f;
+__device__ __forceinline__ float beta_n(const FcGrid &G, int c, int e) {
+  return G.beta ? __fadd_rn(__fmul_rn(tanhf(__ldg(G.beta + (size_t)c * G.bs + e)), WEIGHT_SCALE), 1.f) : 1.f;
 }
-__device__ __forceinline__ float alpha_n(const float *alpha, int c, int n) {
-  return alpha ? __fadd_rn(__fmul_rn(tanhf(__ldg(alpha + (size_t)c * 8 + n)), WEIGHT_SCALE), 1.f) : 1.f;
+__device__ __forceinline__ float alpha_n(const FcGrid &G, int c, int n) {
+  return G.alpha ? __fadd_rn(__fmul_rn(tanhf(__ldg(G.alpha + (size_t)c * G.as + n)), WEIGHT_SCALE), 1.f)
+                 : 1.f;
 }
 __device__ __forceinline__ float sigmoid_(float g) { return 1.f / (1.f + expf(-g)); }
-__device__ __forceinline__ float gamma_n(const float *gamma, int c) {
-  return gamma ? __fadd_rn(__fmul_rn(sigmoid_(__ldg(gamma + c)), WEIGHT_SCALE), 0.005f) : 1.f;
+__device__ __forceinline__ float gamma_n(const FcGrid &G, int c) {
+  return G.gamma ? __fadd_rn(__fmul_rn(sigmoid_(__ldg(G.gamma + (size_t)c * G.gs)), WEIGHT_SCALE), 0.005f)
+                 : 1.f;
 }
 
 __device__ __forceinline__ int corner_vertex(const FcGrid &G, int c, int n) {
@@ -484,7 +487,7 @@ __device__ __forceinline__ void load_corners(const FcGrid &G, int c, CubeCorners
     C.x[n][1] = __ldg(G.x + 3 * (size_t)v + 1);
     C.x[n][2] = __ldg(G.x + 3 * (size_t)v + 2);
     C.s[n] = __ldg(G.s + v);
-    C.a[n] = alpha_n(G.alpha, c, n);
+    C.a[n] = alpha_n(G, c, n);
   }
 }
 
@@ -513,7 +516,7 @@ __device__ __forceinline__ void dual_vertex(const FcGrid &G, const CubeCorners &
     if (!((m >> e) & 1u)) continue;
     float u[3], w0, w1;
     crossing(C, e, true, u, w0, w1);
-    const float be = beta_n(G.beta, c, e);
+    const float be = beta_n(G, c, e);
 #pragma unroll
     for (int d = 0; d < 3; ++d) acc[d] = __fadd_rn(acc[d], __fmul_rn(u[d], be));
     bsum = __fadd_rn(bsum, be);
@@ -670,7 +673,7 @@ fc_quads_kernel(const FcGrid G, const FcState S, const uint32_t *__restrict__ qu
   wind(q < n_qf, R.cube, cq);
   float gq[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) gq[k] = gamma_n(G.gamma, cq[k]);
+  for (int k = 0; k < 4; ++k) gq[k] = gamma_n(G, cq[k]);
   const float g02 = __fmul_rn(gq[0], gq[2]), g13 = __fmul_rn(gq[1], gq[3]);
   if (!G.training) {  // split along the diagonal with the larger gamma product
     int64_t *f = faces + 6 * (size_t)q;
@@ -723,7 +726,7 @@ fc_quads_bwd_kernel(const FcGrid G, const FcState S, const uint32_t *__restrict_
   wind(q < n_qf, R.cube, cq);
   float gq[4];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) gq[k] = gamma_n(G.gamma, cq[k]);
+  for (int k = 0; k < 4; ++k) gq[k] = gamma_n(G, cq[k]);
   const float g02 = gq[0] * gq[2], g13 = gq[1] * gq[3];
   const float W = g02 + g13 + 1e-8f, iW = 1.f / W;
   const float *dc = dvert + 3 * (size_t)(n_vd + q);
@@ -743,10 +746,10 @@ fc_quads_bwd_kernel(const FcGrid G, const FcState S, const uint32_t *__restrict_
   atomic_add3(dvert + 3 * (size_t)vq[1], h13[0], h13[1], h13[2]);
   atomic_add3(dvert + 3 * (size_t)vq[3], h13[0], h13[1], h13[2]);
   if (dgamma_n) {
-    atomicAdd(dgamma_n + cq[0], dg02 * gq[2]);
-    atomicAdd(dgamma_n + cq[2], dg02 * gq[0]);
-    atomicAdd(dgamma_n + cq[1], dg13 * gq[3]);
-    atomicAdd(dgamma_n + cq[3], dg13 * gq[1]);
+    atomicAdd(dgamma_n + (size_t)cq[0] * G.gs, dg02 * gq[2]);
+    atomicAdd(dgamma_n + (size_t)cq[2] * G.gs, dg02 * gq[0]);
+    atomicAdd(dgamma_n + (size_t)cq[1] * G.gs, dg13 * gq[3]);
+    atomicAdd(dgamma_n + (size_t)cq[3] * G.gs, dg13 * gq[1]);
   }
 }
 
@@ -832,7 +835,7 @@ fc_cubes_bwd_kernel(const FcGrid G, const SurfCube *__restrict__ surf, int n_sur
       const int a = edge_a(e), b = edge_b(e);
       float u[3], w0, w1;
       crossing(C, e, true, u, w0, w1);
-      const float be = beta_n(G.beta, c, e);
+      const float be = beta_n(G, c, e);
       const float iD = 1.f / (w1 - w0);
       float db = 0.f, p1 = 0.f, p0 = 0.f;
 #pragma unroll
@@ -856,20 +859,21 @@ fc_cubes_bwd_kernel(const FcGrid G, const SurfCube *__restrict__ surf, int n_sur
   if (dbeta) {
 #pragma unroll
     for (int e = 0; e < 12; ++e) {
-      const float t = tanhf(__ldg(G.beta + (size_t)c * 12 + e));
-      dbeta[(size_t)c * 12 + e] = gb[e] * WEIGHT_SCALE * (1.f - t * t);
+      const float t = tanhf(__ldg(G.beta + (size_t)c * G.bs + e));
+      dbeta[(size_t)c * G.bs + e] = gb[e] * WEIGHT_SCALE * (1.f - t * t);
     }
   }
   if (dalpha) {
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-      const float t = tanhf(__ldg(G.alpha + (size_t)c * 8 + n));
-      dalpha[(size_t)c * 8 + n] = ga[n] * WEIGHT_SCALE * (1.f - t * t);
+      const float t = tanhf(__ldg(G.alpha + (size_t)c * G.as + n));
+      dalpha[(size_t)c * G.as + n] = ga[n] * WEIGHT_SCALE * (1.f - t * t);
     }
   }
   if (dgamma) {  // holds the normalised-gamma gradient from the quad kernel
-    const float sg = sigmoid_(__ldg(G.gamma + c));
-    dgamma[c] = dgamma[c] * WEIGHT_SCALE * sg * (1.f - sg);
+    const float sg = sigmoid_(__ldg(G.gamma + (size_t)c * G.gs));
+    float *dg = dgamma + (size_t)c * G.gs;
+    *dg = *dg * WEIGHT_SCALE * sg * (1.f - sg);
   }
 #pragma unroll
   for (int n = 0; n < 8; ++n) {
@@ -889,6 +893,9 @@ FcGrid make_grid(const DmgsFcGrid *a) {
   G.nc = a->rx * a->ry * a->rz;
   G.nv = (a->rx + 1) * G.sx;
   G.training = a->training;
+  G.bs = a->beta_stride > 0 ? a->beta_stride : 12;
+  G.as = a->alpha_stride > 0 ? a->alpha_stride : 8;
+  G.gs = a->gamma_stride > 0 ? a->gamma_stride : 1;
   G.by_rz = make_fastdiv((uint32_t)a->rz);
   G.by_ry = make_fastdiv((uint32_t)a->ry);
   G.by_sy = make_fastdiv((uint32_t)G.sy);
@@ -898,6 +905,9 @@ FcGrid make_grid(const DmgsFcGrid *a) {
 
 bool grid_ok(const DmgsFcGrid *a) {
   if (!a || a->rx <= 0 || a->ry <= 0 || a->rz <= 0 || !a->x || !a->s) return false;
+  if ((a->beta_stride != 0 && a->beta_stride < 12) || (a->alpha_stride != 0 && a->alpha_stride < 8) ||
+      a->gamma_stride < 0)
+    return false;
   const double nv = (double)(a->rx + 1) * (a->ry + 1) * (a->rz + 1);
   return nv * 4 < 2147483647.0;  // int32 vertex indices, quad words v * 4 + dir
 }
@@ -1024,9 +1034,23 @@ int dmgs_fc_bwd(const DmgsFcGrid *a, const uint32_t *counts, const void *state, 
   const FcGrid G = make_grid(a);
   DMGS_CUDA(cudaMemsetAsync(dx, 0, (size_t)G.nv * 12, s));
   DMGS_CUDA(cudaMemsetAsync(ds, 0, (size_t)G.nv * 4, s));
-  if (dbeta) DMGS_CUDA(cudaMemsetAsync(dbeta, 0, (size_t)G.nc * 48, s));
-  if (dalpha) DMGS_CUDA(cudaMemsetAsync(dalpha, 0, (size_t)G.nc * 32, s));
-  if (dgamma) DMGS_CUDA(cudaMemsetAsync(dgamma, 0, (size_t)G.nc * 4, s));
+  // weight gradients share their weights' row strides (rows of 12 / 8 / 1 floats): one
+  // memset when they are the interleaved columns of one [C, 21] block or dense, a
+  // 2D memset otherwise
+  auto zero_rows = [&](float *p, int stride, int width) -> int {
+    if (!p) return DMGS_OK;
+    if (stride == width) DMGS_CUDA(cudaMemsetAsync(p, 0, (size_t)G.nc * width * 4, s));
+    else DMGS_CUDA(cudaMemset2DAsync(p, (size_t)stride * 4, 0, (size_t)width * 4, (size_t)G.nc, s));
+    return DMGS_OK;
+  };
+  if (dbeta && dalpha && dgamma && G.bs == 21 && G.as == 21 && G.gs == 21 && dalpha == dbeta + 12 &&
+      dgamma == dbeta + 20) {
+    DMGS_CUDA(cudaMemsetAsync(dbeta, 0, (size_t)G.nc * 84, s));
+  } else {
+    if (int r = zero_rows(dbeta, G.bs, 12)) return r;
+    if (int r = zero_rows(dalpha, G.as, 8)) return r;
+    if (int r = zero_rows(dgamma, G.gs, 1)) return r;
+  }
   const int n_surf = (int)counts[0];
   if (n_surf == 0) return DMGS_OK;
   if (!vertices || !dL_dvertices || !dL_dL_dev) {

@@ -23,13 +23,38 @@ from ._lib import check, ptr, stream_of
 __all__ = ["FlexiCubes", "flexicubes"]
 
 
-def _grid(x, s, beta, alpha, gamma, res, training):
+def _grid(x, s, beta, alpha, gamma, res, training, fused=False):
+    """Kernel arguments.  fused: ``beta`` is the whole [C, 21] weight tensor
+    (beta, alpha, gamma = its columns 0-11, 12-19, 20), read in place."""
     g = _lib.DmgsFcGrid()
     g.x, g.s = x.data_ptr(), s.data_ptr()
-    g.beta, g.alpha, g.gamma = ptr(beta), ptr(alpha), ptr(gamma)
+    if fused:
+        g.beta, g.alpha, g.gamma = beta.data_ptr(), beta.data_ptr() + 48, beta.data_ptr() + 80
+        g.beta_stride = g.alpha_stride = g.gamma_stride = 21
+    else:
+        g.beta, g.alpha, g.gamma = ptr(beta), ptr(alpha), ptr(gamma)
     g.rx, g.ry, g.rz = (int(r) for r in res)
     g.training = 1 if training else 0
     return g
+
+
+def _fused_weights(beta, alpha, gamma, C):
+    """The [C, 21] tensor whose column slices 0:12, 12:20 and 20 the three
+    weights are (stage 2 slices per_cube_weights this way,
+    scene/gaussian_geo_model_mlp_flex.py:246-247), else None."""
+    if beta is None or alpha is None or gamma is None:
+        return None
+    W = beta._base
+    if W is None or alpha._base is not W or gamma._base is not W:
+        return None
+    if W.dtype != torch.float32 or not W.is_contiguous() or tuple(W.shape) != (C, 21):
+        return None
+    o = W.storage_offset()
+    ok = (tuple(beta.shape) == (C, 12) and tuple(alpha.shape) == (C, 8) and tuple(gamma.shape) == (C,)
+          and beta.stride() == (21, 1) and alpha.stride() == (21, 1) and gamma.stride() == (21,)
+          and beta.storage_offset() == o and alpha.storage_offset() == o + 12
+          and gamma.storage_offset() == o + 20)
+    return W if ok else None
 
 
 def _f32(t):
@@ -38,11 +63,11 @@ def _f32(t):
 
 class _FlexiCubesFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, x, s, beta, alpha, gamma, res, training):
+    def forward(ctx, x, s, beta, alpha, gamma, res, training, fused=False):
         lib = _lib.load()
         dev = x.device
         xs, ss, bs, as_, gs = (_f32(t) for t in (x, s, beta, alpha, gamma))
-        grid = _grid(xs, ss, bs, as_, gs, res, training)
+        grid = _grid(xs, ss, bs, as_, gs, res, training, fused)
         state = torch.empty(lib.dmgs_fc_state_bytes(*grid_res(res)), dtype=torch.uint8, device=dev)
         counts = (C.c_uint32 * 8)()
         stream = stream_of(dev)
@@ -60,7 +85,7 @@ class _FlexiCubesFn(torch.autograd.Function):
             check(lib.dmgs_fc_emit(C.byref(grid), C.addressof(counts), state.data_ptr(), state.numel(),
                                    work.data_ptr(), work.numel(), vertices.data_ptr(), ptr(faces),
                                    ptr(L_dev), ptr(surf_edges), stream), "fc_emit")
-        ctx.res, ctx.training, ctx.counts = tuple(res), training, bytes(counts)
+        ctx.res, ctx.training, ctx.counts, ctx.fused = tuple(res), training, bytes(counts), fused
         ctx.has = (beta is not None, alpha is not None, gamma is not None)
         ctx.save_for_backward(xs, ss, bs, as_, gs, state, work, vertices)
         ctx.mark_non_differentiable(faces, surf_edges)
@@ -72,21 +97,30 @@ class _FlexiCubesFn(torch.autograd.Function):
         xs, ss, bs, as_, gs, state, work, vertices = ctx.saved_tensors
         dev = xs.device
         counts = (C.c_uint32 * 8).from_buffer_copy(ctx.counts)
-        grid = _grid(xs, ss, bs, as_, gs, ctx.res, ctx.training)
+        grid = _grid(xs, ss, bs, as_, gs, ctx.res, ctx.training, ctx.fused)
         dvert = (dvertices.float().contiguous().clone() if dvertices is not None
                  else torch.zeros_like(vertices))
         dL = dL_dev.float().contiguous() if dL_dev is not None else \
             torch.zeros((int(counts[2]),), dtype=torch.float32, device=dev)
         dx = torch.empty_like(xs)
         ds = torch.empty_like(ss)
-        db = torch.empty_like(bs) if ctx.has[0] and ctx.needs_input_grad[2] else None
-        da = torch.empty_like(as_) if ctx.has[1] and ctx.needs_input_grad[3] else None
-        dg = torch.empty_like(gs) if ctx.has[2] and ctx.needs_input_grad[4] else None
+        if ctx.fused:  # one [C, 21] gradient, written in place by column
+            if not ctx.needs_input_grad[2]:
+                db = None
+                pb = pa = pg = None
+            else:
+                db = torch.empty_like(bs)
+                pb, pa, pg = db.data_ptr(), db.data_ptr() + 48, db.data_ptr() + 80
+            da = dg = None
+        else:
+            db = torch.empty_like(bs) if ctx.has[0] and ctx.needs_input_grad[2] else None
+            da = torch.empty_like(as_) if ctx.has[1] and ctx.needs_input_grad[3] else None
+            dg = torch.empty_like(gs) if ctx.has[2] and ctx.needs_input_grad[4] else None
+            pb, pa, pg = ptr(db), ptr(da), ptr(dg)
         check(lib.dmgs_fc_bwd(C.byref(grid), C.addressof(counts), state.data_ptr(), state.numel(),
                               work.data_ptr(), work.numel(), ptr(vertices), ptr(dvert), ptr(dL),
-                              dx.data_ptr(), ds.data_ptr(), ptr(db), ptr(da), ptr(dg),
-                              stream_of(dev)), "fc_bwd")
-        return dx, ds, db, da, dg, None, None
+                              dx.data_ptr(), ds.data_ptr(), pb, pa, pg, stream_of(dev)), "fc_bwd")
+        return dx, ds, db, da, dg, None, None, None
 
 
 def grid_res(res):
@@ -112,8 +146,13 @@ def flexicubes(x_nx3, s_n, res, beta_fx12=None, alpha_fx8=None, gamma_f=None, tr
                          ("gamma_f", gamma_f, (Cn,))):
         if t is not None and tuple(t.shape) != shp:
             raise ValueError(f"flexicubes: {name} must be {list(shp)}, got {list(t.shape)}")
-    v, f, L, se = _FlexiCubesFn.apply(x_nx3, s_n.reshape(-1), beta_fx12, alpha_fx8,
-                                      gamma_f, res, bool(training))
+    W = _fused_weights(beta_fx12, alpha_fx8, gamma_f, Cn)
+    if W is not None:  # the three weights are column slices of one tensor: read it in place
+        v, f, L, se = _FlexiCubesFn.apply(x_nx3, s_n.reshape(-1), W, None, None, res,
+                                          bool(training), True)
+    else:
+        v, f, L, se = _FlexiCubesFn.apply(x_nx3, s_n.reshape(-1), beta_fx12, alpha_fx8,
+                                          gamma_f, res, bool(training), False)
     if v.shape[0] == 0 and f.shape[0] == 0 and se.shape[0] == 0:
         return v, f, L, None   # the reference's result for a grid without surface
     return v, f, L, se

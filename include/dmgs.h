@@ -279,6 +279,10 @@ typedef struct DmgsFcGrid {
   const float *gamma; /* [C] raw quad-split weights or NULL */
   int32_t rx, ry, rz; /* cubes per axis */
   int32_t training;   /* 1: four triangles per quad around a centre vertex */
+  /* row strides in floats of beta / alpha / gamma (0: dense, 12 / 8 / 1);
+   * the gradient arrays of dmgs_fc_bwd use the same strides.  The reference
+   * passes column slices of one [C,21] tensor (strides 21, 21, 21). */
+  int32_t beta_stride, alpha_stride, gamma_stride;
 } DmgsFcGrid;
 
 /* Dual Marching Cubes tables this build derives: groups[256*4] edge masks of

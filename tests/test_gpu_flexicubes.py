@@ -179,3 +179,31 @@ def test_class_interface():
         m(verts, s, cubes.flip(0), [6, 5, 4])
     with pytest.raises(NotImplementedError):
         m(verts, s, cubes, [6, 5, 4], output_tetmesh=True)
+
+
+def test_weight_slices_of_one_tensor_read_in_place():
+    """Stage 2 passes per_cube_weights[:, :12], [:, 12:20], [:, 20] (one
+    [C, 21] tensor): the kernels then read and write it in place.  Same
+    outputs and gradients as separate dense weight tensors."""
+    res = (20, 24, 22)
+    d = synthetic(res, "shape", True, True, seed=9)
+    dev = "cuda"
+    x = torch.tensor(d["x"], device=dev, requires_grad=True)
+    s = torch.tensor(d["s"], device=dev, requires_grad=True)
+    Wd = torch.cat([torch.tensor(d["beta"]), torch.tensor(d["alpha"]),
+                    torch.tensor(d["gamma"])[:, None]], 1).to(dev)
+    W = Wd.clone().requires_grad_(True)
+    sep = [Wd[:, :12].clone().requires_grad_(True), Wd[:, 12:20].clone().requires_grad_(True),
+           Wd[:, 20].clone().requires_grad_(True)]
+    out_w = fc()(x, s, res, W[:, :12], W[:, 12:20], W[:, 20], training=True)
+    out_s = fc()(x.detach().requires_grad_(True), s.detach().requires_grad_(True), res, *sep,
+                 training=True)
+    for a, b in zip(out_w, out_s):
+        assert torch.equal(a, b)
+    rng = np.random.default_rng(1)
+    up_v = torch.tensor(rng.standard_normal(tuple(out_w[0].shape)), dtype=torch.float32, device=dev)
+    up_L = torch.tensor(rng.standard_normal(tuple(out_w[2].shape)), dtype=torch.float32, device=dev)
+    ((out_w[0] * up_v).sum() + (out_w[2] * up_L).sum()).backward()
+    ((out_s[0] * up_v).sum() + (out_s[2] * up_L).sum()).backward()
+    ref = torch.cat([sep[0].grad, sep[1].grad, sep[2].grad[:, None]], 1)
+    assert rel_l2(W.grad.cpu().numpy(), ref.cpu().numpy()) < 1e-6
