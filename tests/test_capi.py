@@ -129,3 +129,24 @@ def test_texture_table_size_matches_oracle(lib):
     from oracle.texture import per_level_scale, table_entries
     assert lib.dmgs_tex_table_entries(per_level_scale()) == table_entries()
     assert lib.dmgs_tex_table_entries(0.5) == -1
+
+
+def test_new_entry_points_reject_bad_arguments(lib):
+    """Host-side validation of the texture, colour and FlexiCubes entry
+    points (each returns before any CUDA call)."""
+    tx = _lib.DmgsTexture(table=8, W1=8, W2=8, W3=8, channels=5,
+                          aabb=(C.c_float * 6)(-1, -1, -1, 1, 1, 1), per_level_scale=1.447)
+    assert lib.dmgs_tex_fwd(C.byref(tx), 10, 8, 8, None) == -1          # channels not 3/12/27/48
+    tx.channels = 48
+    tx.aabb = (C.c_float * 6)(1, -1, -1, -1, 1, 1)
+    assert lib.dmgs_tex_fwd(C.byref(tx), 10, 8, 8, None) == -1          # empty box
+    tx.aabb = (C.c_float * 6)(-1, -1, -1, 1, 1, 1)
+    assert lib.dmgs_tex_bwd(C.byref(tx), 10, 8, 8, None, None, 8, 8, 8, None, 0, None) == -3
+    assert lib.dmgs_tex_bwd(C.byref(tx), 10, 8, 8, None, None, 8, 8, 8, 8, 10 * 128, None) == -3
+    assert lib.dmgs_tex_bwd_scratch_bytes(10) == 10 * 128
+    assert lib.dmgs_sh_colors_fwd(10, 4, 25, 8, 8, 8, 8, None) == -1     # degree above 3
+    assert lib.dmgs_sh_colors_fwd(10, 3, 9, 8, 8, 8, 8, None) == -1      # K < (deg + 1)^2
+    assert lib.dmgs_sh_colors_bwd(10, 2, 9, 8, 8, 8, 8, None, None, None) == -1  # no dL/dsh
+    g = _lib.DmgsFcGrid(x=8, s=8, rx=4, ry=4, rz=4, beta_stride=5)
+    counts = (C.c_uint32 * 8)()
+    assert lib.dmgs_fc_count(C.byref(g), 8, 1 << 20, C.addressof(counts), None) == -1  # stride < 12
