@@ -591,6 +591,24 @@ def bytes_model(name, P, V, K, npix, nviews=1):
 
 
 
+def job_time_ms(ms_local, world, device):
+    """The job's timed-region length: the max over ranks of each rank's own
+    (every rank runs the same steps; the job ends with the slowest).  One
+    all-reduce over the default process group when world > 1."""
+    if world <= 1:
+        return ms_local
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms_job, world, views_per_step, steps):
+    """Whole-job views/s of `world` independent replicas (weak scaling)."""
+    return world * views_per_step * steps / (ms_job / 1e3)
+
+
 def timed(fn, steps, warmup, sync_dev):
     """Run fn(i) warmup times, then time `steps` calls with CUDA events."""
     import torch
@@ -739,11 +757,8 @@ def main():
         torch.distributed.barrier()
     ms_batch = timed(lambda i: br.step(), args.steps, args.warmup, dev)
     br.status()  # raises on a capacity overflow
-    if world > 1:
-        tt = torch.tensor([ms_batch], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms_batch = float(tt.item())
-    value = world * nv * args.steps / (ms_batch / 1e3)
+    ms_batch = job_time_ms(ms_batch, world, dev)
+    value = replica_value(ms_batch, world, nv, args.steps)
 
     # ---------------- mixed resolutions (16 views) ----------------
     mixed = None
@@ -823,16 +838,18 @@ def main():
 
         e2e_run(2)  # warm-up
         torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         e2e_run(n_e2e)
         e1.record()
         torch.cuda.synchronize(dev)
-        ems = e0.elapsed_time(e1)
+        ems = job_time_ms(e0.elapsed_time(e1), world, dev)
         h2d = sum(h.numel() * 4 for h in host_in.values()) + sum(h.numel() * 4 for h in host_dout)
         d2h = (sum(h.numel() * 4 for h in host_img[0]) +
                sum(h.numel() * 4 for h in host_grad[0].values()))
-        e2e = {"value": world * nv * n_e2e / (ems / 1e3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": replica_value(ems, world, nv, n_e2e), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": n_e2e, "views_per_step": nv,
                "api": "dmgs_gb300.batched.HostPipeline (uploads and downloads of neighbouring "
                       "steps overlap the current step), pinned host buffers"}
