@@ -317,6 +317,25 @@ def mesh_leg(args, dev):
         if name in kt:
             t = kt[name][0] / kt[name][1]
             out[name] = {"ms": t, "alg_bytes": nbytes, "achieved_gbs": nbytes / (t * 1e-3) / 1e9}
+    if int(os.environ.get("RANK", "0")) == 0 and not getattr(args, "no_cpu", False):
+        # the binding's CPU baseline: the oracle's torch restatement of the
+        # reference's renew_gaussian / get_covariance_dyn on the same mesh
+        import time as _time
+        from oracle import binding as obind  # CPU baseline only
+        torch.set_num_threads(os.cpu_count())
+        vc = v.detach().cpu().double().requires_grad_(True)
+        sfc = torch.full((1,), 0.5493, dtype=torch.float64, requires_grad=True)
+        bcc = scene.bc.detach().cpu().double()
+        rad = scene.rad_base
+        reps = 3
+        t0 = _time.perf_counter()
+        for _ in range(reps):
+            xyz_c, cov_c, _, _ = obind.bind_stage2(vc, f.cpu(), bcc, rad, 1e-6, sfc)
+            (xyz_c.sum() + cov_c.sum()).backward()
+        out["binding_cpu_baseline"] = {
+            "fwd_bwd_ms": (_time.perf_counter() - t0) / reps * 1e3, "cores": os.cpu_count(),
+            "kind": "port", "sample": "float64 torch restatement of the stage-2 binding on the host, "
+                                      f"{F} faces x 6 Gaussians, 3 forward+backward"}
     for name in ("preprocess", "blend_fwd", "blend_bwd", "preprocess_bwd", "sh_colors", "l1_ssim"):
         if name in kt:
             out.setdefault("kernels_ms", {})[name] = kt[name][0] / kt[name][1]
