@@ -13,6 +13,7 @@ import torch  # noqa: F401  (loads libcudart before the extension)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdmgs_gb300.so")
+ABI_VERSION = 3  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
 
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -163,6 +164,9 @@ def load(path: str | None = None):
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.dmgs_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{p} has ABI version {lib.dmgs_abi_version()}, this package expects "
+                               f"{ABI_VERSION}: rebuild it with `python -m dmgs_gb300.build`")
         _lib = lib
         return lib
 

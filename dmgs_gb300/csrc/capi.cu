@@ -151,7 +151,7 @@ int debug_sync(const DmgsView *v, cudaStream_t s, const char *what) {
 extern "C" {
 
 const char *dmgs_last_error(void) { return dmgs_host::g_err; }
-int32_t dmgs_abi_version(void) { return 2; }
+int32_t dmgs_abi_version(void) { return DMGS_ABI_VERSION; }
 
 size_t dmgs_geom_state_bytes(int32_t P, int32_t width, int32_t height) {
   return geom_layout(P, width, height).total;

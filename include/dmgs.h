@@ -24,6 +24,11 @@
 #include <stddef.h>
 #include <stdint.h>
 
+/* Version of the structs and entry points below; dmgs_abi_version() returns
+ * the value the library was built with.  Raised whenever a struct layout or
+ * a signature changes. */
+#define DMGS_ABI_VERSION 3
+
 #ifdef __cplusplus
 extern "C" {
 #endif

@@ -36,7 +36,9 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_sizes_are_consistent(lib):
-    assert lib.dmgs_abi_version() == 2
+    header = open(os.path.join(ROOT, "include", "dmgs.h")).read()
+    assert f"#define DMGS_ABI_VERSION {_lib.ABI_VERSION}\n" in header
+    assert lib.dmgs_abi_version() == _lib.ABI_VERSION
     g1 = lib.dmgs_geom_state_bytes(1000, 256, 256)
     g2 = lib.dmgs_geom_state_bytes(2000, 256, 256)
     assert g2 > g1 and g1 % 256 == 0
