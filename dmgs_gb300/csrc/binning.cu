@@ -34,6 +34,8 @@
 // its own geometry state and sizes): a batch of views fills the GPU with one
 // launch per stage instead of one small launch per stage and view.
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "kernels.cuh"
 
@@ -685,17 +687,25 @@ int band_plan(int gx, int gy, BandPlan &pl) {
   int dev = 0;
   DMGS_CUDA(cudaGetDevice(&dev));
   thread_local int cached_dev = -1;
-  thread_local size_t cached_smem = 0, attr_smem = 48 * 1024;
+  thread_local size_t cached_smem = 0;
   thread_local int cached_resident = 0;
-  if (dev != cached_dev) attr_smem = 48 * 1024;
   if (dev != cached_dev || pl.smem != cached_smem) {
     const size_t csm = count_grid_bytes(pl.bd);
-    if (std::max(pl.smem, csm) > attr_smem) {  // only ever raised: a launch uses its largest view
-      attr_smem = std::max(pl.smem, csm);
-      DMGS_CUDA(cudaFuncSetAttribute(count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)attr_smem));
-      DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)attr_smem));
+    {
+      // The attribute is per device and shared by every host thread: only
+      // ever raised (a launch uses its largest view), under one lock.
+      static std::mutex mu;
+      static std::map<int, size_t> attr_smem;
+      std::lock_guard<std::mutex> lk(mu);
+      const size_t need = std::max(pl.smem, csm);
+      size_t &cur = attr_smem[dev];
+      if (need > std::max<size_t>(cur, 48 * 1024)) {
+        DMGS_CUDA(cudaFuncSetAttribute(count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)need));
+        DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)need));
+        cur = need;
+      }
     }
     int sms = 0, a = 0, b = 0;
     DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

@@ -584,7 +584,7 @@ int grid_for(K kernel, int threads, int total, bool persistent, int &grid, int &
 
 template <int PPT, int BATCH>
 int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
-  static int cdev = -1, cslots = 0;  // per kernel instantiation
+  thread_local int cdev = -1, cslots = 0;  // per kernel instantiation and host thread
   int grid;
   const int r = grid_for(blend_fwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
                          cdev, cslots);
@@ -595,7 +595,7 @@ int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
 
 template <int PPT, int BATCH>
 int run_bwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
-  static int cdev = -1, cslots = 0;  // per kernel instantiation
+  thread_local int cdev = -1, cslots = 0;  // per kernel instantiation and host thread
   int grid;
   const int r = grid_for(blend_bwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
                          cdev, cslots);

@@ -461,7 +461,7 @@ TexArgs make_args(const DmgsTexture *tx, int64_t n) {
 
 template <typename K>
 int persistent_grid(K kernel, size_t smem, int64_t n, int &grid) {
-  static int cached_dev = -1, cached_slots = 0;  // per kernel instantiation
+  thread_local int cached_dev = -1, cached_slots = 0;  // per kernel instantiation and host thread
   int dev = 0;
   DMGS_CUDA(cudaGetDevice(&dev));
   if (dev != cached_dev) {
@@ -487,11 +487,13 @@ int run_fwd(const TexArgs &A, const TexLevels &L, const float *xyz, float *out, 
 template <int C>
 int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float *dout, float *dxyz,
             float *dtable, float *dW1, float *dW2, float *dW3, float *denc, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
+  thread_local int attr_dev = -1;  // the attribute is per device; setting it again is harmless
+  int dev = 0;
+  DMGS_CUDA(cudaGetDevice(&dev));
+  if (dev != attr_dev) {
     DMGS_CUDA(cudaFuncSetAttribute(tex_bwd_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)tex_bwd_smem()));
-    attr = true;
+    attr_dev = dev;
   }
   int grid;
   if (int r = persistent_grid(tex_bwd_kernel<C>, tex_bwd_smem(), A.n, grid)) return r;
