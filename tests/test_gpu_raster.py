@@ -179,6 +179,35 @@ def test_large_footprints_and_clamped_jacobian():
         assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
 
 
+def test_depth_ties_keep_gaussian_index_order():
+    """Exact depth ties: the second half of the Gaussians repeats the first
+    half's positions, scales and rotations (identical depth keys and tile
+    rectangles) with their own opacities and colours.  Within a tile, tied
+    Gaussians blend in index order (the stable sort of the reference's
+    (tile, depth) keys), so the sorted values, the image and the gradients
+    must match the oracle's order exactly."""
+    sc = small_scene(P=1600, width=128, height=96, seed=13)
+    half = sc.means3D.shape[0] // 2
+    for a in (sc.means3D, sc.scales, sc.rotations):
+        a[half:] = a[:half]
+    view = sc.views[0]
+    inp = mode_inputs(sc, ("shs", "sr"))
+    cam = oracle_camera(view)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], scales=inp["scales"],
+                   rotations=inp["rotations"])
+    vis = ref.geom["visible"]
+    assert vis[:half].any() and np.array_equal(vis[:half], vis[half:])
+    run = AbiRun(view, inp).forward()
+    dv = _check_integer_outputs(run, ref, cam)
+    ok = ~ref.ambiguous
+    assert np.abs(run.color.cpu().numpy() - ref.image)[:, ok].max() <= IMG_TOL
+    np.testing.assert_array_equal(dv["n_contrib"][ok], ref.n_contrib[ok])
+    dimg = np.random.default_rng(13).standard_normal((3, 96, 128)).astype(np.float32)
+    gk, go = run.backward(dimg), ref.backward(dimg)
+    for name, gref in go.items():
+        assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
+
+
 def test_prefiltered_violation_is_an_error():
     sc = small_scene(P=100, width=32, height=32, seed=8)
     view = sc.views[0]
