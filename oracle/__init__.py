@@ -13,6 +13,11 @@ raster   Gaussian rasteriser: FP32 emulation of the integer-determining
          reference adjoint's conventions.
 binding  Mesh -> Gaussian face binding (stage-2 covariance form and the
          stage-3 scale/rotation form), FP64 torch restatement.
+flexicubes  FlexiCubes triangle extraction on a regular grid (both
+         quad-splitting modes) and, by autograd, its adjoint; float64 by
+         default, float32 on request.
+texture  The hash-grid texture (multiresolution hash encoding + bias-free
+         MLP, ``MLPTexture3D.sample_noact``) and its adjoint.
 
 Parity status
 -------------
@@ -30,4 +35,11 @@ Parity status
 * Binding: pinned against the reference's own ``renew_gaussian`` /
   ``get_covariance_dyn`` (``scene/gaussian_geo_model_mlp_flex.py:258-385``)
   run on CPU in the build container (fixtures in ``tests/golden/``).
+* FlexiCubes: pinned against the reference's own class
+  (``geo/flexicubes.py``) run on the CPU (``tests/golden/flexicubes_golden.npz``)
+  and its tables against ``geo/tables.py``.
+* Texture: the code around the encoding is pinned against the reference's
+  ``MLPTexture3D`` (``tests/golden/texture_golden.npz``); the encoding itself
+  lives in the absent third-party tiny-cuda-nn: ENCODING PARITY UNPINNED
+  (restated from the published algorithm).
 """
