@@ -119,7 +119,15 @@ class MLPTexture3D(torch.nn.Module):
         self.net = _MLP(N_LEVELS * N_FEATURES, internal_dims, hidden, channels, device)
 
     def _aabb_host(self):
-        return torch.as_tensor(self.AABB, dtype=torch.float32).detach().cpu().reshape(2, 3)
+        """The AABB as a host float32 [2, 3] tensor for the kernel arguments,
+        copied again only when ``self.AABB`` is replaced or modified in place
+        (a device AABB would otherwise cost a device->host sync per call)."""
+        a = self.AABB
+        version = getattr(a, "_version", None)
+        if getattr(self, "_aabb_src", None) is not a or self._aabb_ver != version:
+            self._aabb_cache = torch.as_tensor(a, dtype=torch.float32).detach().cpu().reshape(2, 3).clone()
+            self._aabb_src, self._aabb_ver = a, version
+        return self._aabb_cache
 
     def sample_noact(self, texc):
         """Features [..., channels] at positions texc [..., 3]
