@@ -14,6 +14,13 @@ whose instance list overflowed its capacity is re-admitted at the head of
 the queue with the exact count the device reported.  Memory is accounted per
 request (its state bytes plus its image), released when its wave completes.
 
+Cancellation and timeouts are host decisions (no kernel is interrupted): a
+request cancelled, or not admitted within its ``admit_timeout`` seconds of
+arriving, leaves the queue unrendered; one cancelled while its wave runs is
+rendered with the wave but its result is dropped (neither delivered nor
+re-admitted after an overflow).  Each request ends with ``status`` "done",
+"cancelled" or "timeout".
+
 The scheduler is independent of the device: :class:`Scheduler` drives a
 backend (``footprint``/``reserve``/``launch``/``ready``/``results``/
 ``release``), so its admission, ordering and retry logic is tested on the CPU
@@ -46,6 +53,9 @@ class Request:
     t_done: float = -1.0
     result: object = None  # the image (host copy when the backend copies out)
     blocks: object = None  # backend placement while admitted
+    admit_timeout: float | None = None  # seconds after arrival to be admitted by, or dropped
+    cancelled: bool = False  # set by the client (any thread); see Scheduler.cancel
+    status: str = ""       # "done", "cancelled" or "timeout" once finished
 
     @property
     def key(self):
@@ -89,6 +99,8 @@ class ServeStats:
     latencies_ms: list = field(default_factory=list)
     waves: int = 0
     retries: int = 0
+    cancelled: int = 0
+    timeouts: int = 0
     peak_bytes: int = 0
     peak_inflight: int = 0
     wall_s: float = 0.0
@@ -103,7 +115,8 @@ class ServeStats:
                 "max_ms": float(lat.max()) if n else None,
                 "views_per_s": n / self.wall_s if self.wall_s > 0 else None,
                 "waves": self.waves, "mean_wave": n / self.waves if self.waves else None,
-                "retries": self.retries, "peak_bytes": self.peak_bytes,
+                "retries": self.retries, "cancelled": self.cancelled,
+                "timeouts": self.timeouts, "peak_bytes": self.peak_bytes,
                 "peak_inflight": self.peak_inflight, "wall_s": self.wall_s}
 
 
@@ -127,24 +140,59 @@ class Scheduler:
         self.estimator = estimator or CapacityEstimator()
         self.clock = clock
         self.idle = idle or (lambda: time.sleep(50e-6))
+        self._cancel_posted = False
+
+    def cancel(self, request):
+        """Cancel a request (callable from another thread or from `deliver`):
+        it is dropped from the queue, or its result is dropped if its wave is
+        already running."""
+        request.cancelled = True
+        self._cancel_posted = True
+
+    @staticmethod
+    def _dropped(r, now, st):
+        """Whether queued request r leaves unrendered now (cancelled, or not
+        admitted within its timeout; a retry after an overflow keeps its
+        place); marks it."""
+        if r.cancelled:
+            r.status, st.cancelled = "cancelled", st.cancelled + 1
+        elif r.admit_timeout is not None and r.attempts == 0 and now - r.arrival > r.admit_timeout:
+            r.status, st.timeouts = "timeout", st.timeouts + 1
+        else:
+            return False
+        r.t_done, r.result = now, None
+        return True
 
     def run(self, requests, deliver=None):
         """Serve `requests` (arrival times in seconds from the start) in real
-        time; returns ServeStats.  Each request gets t_admit, t_done and
-        result; `deliver(request)`, if given, is called as each completes
-        (a client taking the image; it may recycle the buffer)."""
+        time; returns ServeStats.  Each request gets t_admit, t_done, status
+        and result; `deliver(request)`, if given, is called as each completes
+        (a client taking the image; it may recycle the buffer).  Cancelled
+        and timed-out requests are not delivered."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         be, est = self.backend, self.estimator
         pending, inflight = deque(), []
         st = ServeStats()
         used = n_in = done = nxt = 0
         stream = 0
+        # the queue is scanned for drops only when some request can be dropped
+        timeouts = any(r.admit_timeout is not None for r in reqs)
+        self._cancel_posted = self._cancel_posted or any(r.cancelled for r in reqs)
         t0 = self.clock()
         while done < len(reqs):
             now = self.clock() - t0
             while nxt < len(reqs) and reqs[nxt].arrival <= now:
                 pending.append(reqs[nxt])
                 nxt += 1
+            if pending and (timeouts or self._cancel_posted):
+                self._cancel_posted = False
+                keep = deque()
+                for r in pending:
+                    if self._dropped(r, now, st):
+                        done += 1
+                    else:
+                        keep.append(r)
+                pending = keep
             progressed = False
             for w in list(inflight):
                 if not be.ready(w.handle):
@@ -156,13 +204,19 @@ class Scheduler:
                     est.observe(r, K)
                     if status & ST_ERRORS:
                         raise RuntimeError(f"request {r.rid}: device status {status}")
-                    if status & ST_OVERFLOW:
+                    if r.cancelled:  # rendered, but nobody wants it any more
+                        if r.result is not None and hasattr(be, "recycle"):
+                            be.recycle(r)  # its host buffer back to the backend's pool
+                        r.status, r.t_done, r.result = "cancelled", t_obs, None
+                        st.cancelled += 1
+                        done += 1
+                    elif status & ST_OVERFLOW:
                         r.capacity = int(K) + est.slack
                         r.result = None
                         retry.append(r)
                         st.retries += 1
                     else:
-                        r.t_done = t_obs
+                        r.t_done, r.status = t_obs, "done"
                         st.latencies_ms.append(1e3 * r.latency)
                         done += 1
                         if deliver is not None:
@@ -176,6 +230,10 @@ class Scheduler:
             wave, wbytes = [], 0
             while pending and len(wave) < self.max_wave and n_in + len(wave) < self.max_inflight:
                 r = pending[0]
+                if self._dropped(r, now, st):  # cancelled after the last scan
+                    pending.popleft()
+                    done += 1
+                    continue
                 cap = r.capacity or est.capacity(r)
                 fb = be.footprint(r, cap)
                 if fb > self.budget:

@@ -152,3 +152,63 @@ def test_device_arena_first_fit_and_coalescing():
     assert a.free == [(0, 4096)] and a.used == 0
     t = a.tensor(256, 6, torch.float32, (2, 3))
     assert t.shape == (2, 3) and t.data_ptr() == a.base + 256
+
+
+def test_admission_timeout_drops_requests_never_admitted():
+    """One wave at a time (the budget fits one request), 10 ms per wave: of a
+    burst of 6 requests allowed 25 ms to be admitted, the first three are
+    served and the rest time out unrendered."""
+    clk = FakeClock()
+    be = FakeBackend(clk, delay=10e-3)
+    reqs = [Request(i, 0, View(32, 32), 0.0, admit_timeout=25e-3) for i in range(6)]
+    delivered = []
+    est = CapacityEstimator(margin=1.0, slack=0, default=lambda r: 1000)
+    st = _sched(be, clk, budget_bytes=be.footprint(reqs[0], 1000),
+                estimator=est).run(reqs, deliver=delivered.append)
+    launched = [r.rid for h in be.launched for r in h["reqs"]]
+    assert launched == [0, 1, 2]
+    assert [r.status for r in reqs] == ["done"] * 3 + ["timeout"] * 3
+    assert [r.rid for r in delivered] == [0, 1, 2]
+    assert all(r.result is None for r in reqs[3:])
+    s = st.summary()
+    assert s["requests"] == 3 and s["timeouts"] == 3 and s["cancelled"] == 0
+
+
+def test_timeout_does_not_drop_an_overflow_retry():
+    clk = FakeClock()
+    be = FakeBackend(clk, delay=10e-3, K=lambda r: 5000)
+    est = CapacityEstimator(margin=1.0, slack=0, default=lambda r: 100)  # overflows first
+    reqs = [Request(0, 0, View(32, 32), 0.0, admit_timeout=1e-3)]
+    st = _sched(be, clk, budget_bytes=10**9, estimator=est).run(reqs)
+    assert reqs[0].status == "done" and reqs[0].attempts == 2 and st.timeouts == 0
+
+
+def test_cancellation_before_admission_and_while_rendering():
+    """Arrivals every 1 ms, 4 ms per wave.  Request 3 is cancelled before it
+    arrives; when request 0 is delivered (t = 4 ms) the client cancels
+    request 2 (its wave is running: rendered, result dropped), request 1
+    (running and about to overflow: not retried) and request 6 (not yet
+    arrived: never rendered)."""
+    clk = FakeClock()
+    be = FakeBackend(clk, delay=4e-3, K=lambda r: 5000 if r.rid == 1 else 1000)
+    est = CapacityEstimator(margin=1.0, slack=0, default=lambda r: 2000)
+    reqs = [Request(i, 0, View(32, 32), 1e-3 * i) for i in range(10)]
+    reqs[3].cancelled = True
+    sched = _sched(be, clk, budget_bytes=10**9, estimator=est)
+    delivered = []
+
+    def deliver(r):
+        delivered.append(r.rid)
+        if r.rid == 0:
+            for k in (2, 1, 6):
+                sched.cancel(reqs[k])
+
+    st = sched.run(reqs, deliver=deliver)
+    launched = sorted(r.rid for h in be.launched for r in h["reqs"])
+    assert launched == [0, 1, 2, 4, 5, 7, 8, 9]
+    status = {r.rid: r.status for r in reqs}
+    assert [k for k, v in status.items() if v == "cancelled"] == [1, 2, 3, 6]
+    assert all(status[k] == "done" for k in (0, 4, 5, 7, 8, 9))
+    assert delivered == [0, 4, 5, 7, 8, 9]
+    assert all(reqs[k].result is None for k in (1, 2, 3, 6))
+    assert st.cancelled == 4 and st.retries == 0 and st.summary()["requests"] == 6
