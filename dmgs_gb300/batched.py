@@ -24,7 +24,10 @@ import torch
 
 from . import _lib
 from ._lib import DmgsBatch, DmgsError, DmgsGaussians, DmgsGrads, DmgsView, check, ptr
-from .rasterizer import GaussianRasterizationSettings, _f32
+from .rasterizer import GaussianRasterizationSettings, _f32, check_inputs
+
+GAUSSIAN_KEYS = ("means3D", "opacities", "shs", "colors_precomp", "scales", "rotations",
+                 "cov3D_precomp")
 
 MAX_VIEWS = 16
 TUNE_SPACE = [(p, b) for p in (1, 2, 4) for b in (128, 256, 512)]
@@ -64,6 +67,7 @@ class BatchedRasterizer:
                  means2D_grads=True, densify_stats=False):
         if not 1 <= len(settings) <= MAX_VIEWS:
             raise ValueError(f"a batch holds 1..{MAX_VIEWS} views")
+        check_inputs(**{k: gaussians.get(k) for k in GAUSSIAN_KEYS}, settings=settings)
         self.lib = _lib.load()
         self.settings = list(settings)
         self.g = {k: (None if v is None else _f32(v, v.device)) for k, v in gaussians.items()}

@@ -20,6 +20,7 @@ synchronises once (to size the tile-instance buffers), like the reference.
 """
 from __future__ import annotations
 
+import math
 from typing import NamedTuple
 
 import torch
@@ -57,6 +58,39 @@ def _f32(t, device):
     return t
 
 
+def _dims(t):
+    return tuple(t.shape) if hasattr(t, "shape") else tuple(torch.as_tensor(t).shape)
+
+
+def check_inputs(means3D, opacities, shs=None, colors_precomp=None, scales=None, rotations=None,
+                 cov3D_precomp=None, settings=()):
+    """Shapes of the arrays the kernels index, checked on the host before any
+    device work (the reference's extension rejects a means3D that is not
+    [P, 3] with the same message).  Empty arrays count as absent, as in the
+    reference's wrapper; which inputs must be present is the input-mode rule,
+    checked separately."""
+    if means3D is None or len(_dims(means3D)) != 2 or _dims(means3D)[1] != 3:
+        raise RuntimeError("means3D must have dimensions (num_points, 3)")
+    P = _dims(means3D)[0]
+    present = lambda t: t is not None and math.prod(_dims(t)) > 0  # noqa: E731
+    if opacities is None or math.prod(_dims(opacities)) != P:
+        got = None if opacities is None else list(_dims(opacities))
+        raise RuntimeError(f"opacities must hold one value per point ({P}), got {got}")
+    if present(shs):
+        d = _dims(shs)
+        if len(d) != 3 or d[0] != P or d[2] != 3:
+            raise RuntimeError(f"shs must have dimensions (num_points, M, 3), got {list(d)}")
+    for name, t, w in (("colors_precomp", colors_precomp, 3), ("scales", scales, 3),
+                       ("rotations", rotations, 4), ("cov3D_precomp", cov3D_precomp, 6)):
+        if present(t) and _dims(t) != (P, w):
+            raise RuntimeError(f"{name} must have dimensions (num_points, {w}), got {list(_dims(t))}")
+    for rs in settings:
+        for name, n in (("bg", 3), ("viewmatrix", 16), ("projmatrix", 16), ("campos", 3)):
+            t = getattr(rs, name)
+            if t is None or math.prod(_dims(t)) != n:
+                raise RuntimeError(f"raster settings: {name} must hold {n} values")
+
+
 def _aligned16(t):
     if t is not None and t.data_ptr() % 16 != 0:
         t = t.clone()
@@ -88,6 +122,8 @@ class _RasterizeGaussians(torch.autograd.Function):
     @staticmethod
     def forward(ctx, means3D, means2D, sh, colors_precomp, opacities, scales, rotations,
                 cov3Ds_precomp, raster_settings):
+        check_inputs(means3D, opacities, sh, colors_precomp, scales, rotations, cov3Ds_precomp,
+                     (raster_settings,))
         lib = _lib.load()
         device = means3D.device
         if device.type != "cuda":

@@ -357,6 +357,9 @@ class ResidentScene:
 
     def __init__(self, tensors, sh_degree=3):
         from . import _lib
+        from .rasterizer import check_inputs
+        check_inputs(tensors.get("means3D"), tensors.get("opacities"), tensors.get("shs"),
+                     scales=tensors.get("scales"), rotations=tensors.get("rotations"))
         self.t = {k: v.contiguous().float() for k, v in tensors.items()}
         self.P = self.t["means3D"].shape[0]
         self.M = self.t["shs"].shape[1]
