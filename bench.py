@@ -688,9 +688,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": "large-scene fwd+bwd: 3M Gaussians, 1237x822, SH3, one view "
-                                   "(CPU oracle, bounded sample)", "P": args.P,
-                       "width": args.width, "height": args.height},
+            "config": {"workload": WORKLOAD, "P": args.P, "width": args.width,
+                       "height": args.height, "views_per_step": max(1, min(16, args.views)),
+                       "parallelism": "host cores"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                              "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
