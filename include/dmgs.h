@@ -290,7 +290,7 @@ typedef struct DmgsFcGrid {
   int32_t beta_stride, alpha_stride, gamma_stride;
 } DmgsFcGrid;
 
-/* Dual Marching Cubes tables this build derives: groups[256*4] edge masks of
+/* Dual Marching Cubes tables the library derives: groups[256*4] edge masks of
  * the dual vertices, num_vd[256], check[256*5] (flag, di, dj, dk, complement
  * case) — the meaning of geo/tables.py's dmc_table / num_vd_table /
  * check_table.  Host only. */

@@ -1,7 +1,7 @@
 """CPU oracle for the DMGS hot path — TEST INFRASTRUCTURE ONLY.
 
 Nothing in the product path (``dmgs_gb300``) imports this package.  It is
-imported only by ``tests/``, by ``__graft_entry__.smoke()`` (as the checker)
+imported only by ``tests/``, by ``__graft_entry__.smoke()`` (to check the CUDA path's result)
 and by ``bench.py``'s CPU baseline / ``--impl reference`` leg.
 
 Modules
