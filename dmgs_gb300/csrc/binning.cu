@@ -34,8 +34,6 @@
 // its own geometry state and sizes): a batch of views fills the GPU with one
 // launch per stage instead of one small launch per stage and view.
 #include <algorithm>
-#include <map>
-#include <mutex>
 
 #include "kernels.cuh"
 
@@ -691,22 +689,10 @@ int band_plan(int gx, int gy, BandPlan &pl) {
   thread_local int cached_resident = 0;
   if (dev != cached_dev || pl.smem != cached_smem) {
     const size_t csm = count_grid_bytes(pl.bd);
-    {
-      // The attribute is per device and shared by every host thread: only
-      // ever raised (a launch uses its largest view), under one lock.
-      static std::mutex mu;
-      static std::map<int, size_t> attr_smem;
-      std::lock_guard<std::mutex> lk(mu);
-      const size_t need = std::max(pl.smem, csm);
-      size_t &cur = attr_smem[dev];
-      if (need > std::max<size_t>(cur, 48 * 1024)) {
-        DMGS_CUDA(cudaFuncSetAttribute(count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)need));
-        DMGS_CUDA(cudaFuncSetAttribute(emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)need));
-        cur = need;
-      }
-    }
+    // raised only (a launch uses its largest view), shared by every host thread
+    const size_t need = std::max(pl.smem, csm);
+    if (int r = dmgs_host::raise_smem_limit((const void *)count_kernel, need)) return r;
+    if (int r = dmgs_host::raise_smem_limit((const void *)emit_kernel, need)) return r;
     int sms = 0, a = 0, b = 0;
     DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, count_kernel, 32, csm));

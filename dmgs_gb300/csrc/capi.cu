@@ -6,6 +6,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "kernels.cuh"
 
@@ -23,6 +26,21 @@ void set_error(const char *fmt, ...) {
 int cuda_fail(cudaError_t e, const char *what) {
   set_error("CUDA error in %s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
   return DMGS_ERR_CUDA;
+}
+
+int raise_smem_limit(const void *func, size_t bytes) {
+  if (bytes <= 48 * 1024) return DMGS_OK;  // the default limit
+  int dev = 0;
+  DMGS_CUDA(cudaGetDevice(&dev));
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[{dev, func}];
+  if (bytes > cur) {
+    DMGS_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+  }
+  return DMGS_OK;
 }
 
 }  // namespace dmgs_host

@@ -202,6 +202,11 @@ enum KernelId {
 void timing_begin(int kid, cudaStream_t s);
 void timing_end(int kid, cudaStream_t s);
 void note_launch();  // counts every kernel launch (dmgs_kernel_launches)
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes` (never lowers it: the attribute is per device and shared by
+// every host thread, so concurrent callers with different sizes cannot undo
+// each other).  One lock for every kernel of the library.
+int raise_smem_limit(const void *func, size_t bytes);
 }  // namespace dmgs_host
 
 // Bracket one kernel launch with the timing registry (no-op when disabled).

@@ -13,10 +13,12 @@
 // The array's name is only a host-side stand-in in host code, so the first
 // call on each device (with that device current) looks up its device address
 // with cudaGetSymbolAddress and caches it; that first call should come before
-// any stream capture begins.  All calls share the one array and it keeps the
-// previous call's contents: the adjoint clears the accumulators it needs at
-// the start of every call, and calls whose work overlaps on the GPU (two
-// streams, or two host threads) race on the array.
+// any stream capture begins.  The cached address outlives a cudaDeviceReset
+// (after which the array may live elsewhere), so the entry point must not be
+// used on a device after that device was reset.  All calls share the one
+// array and it keeps the previous call's contents: the adjoint clears the
+// accumulators it needs at the start of every call, and calls whose work
+// overlaps on the GPU (two streams, or two host threads) race on the array.
 #include <mutex>
 
 #include "kernels.cuh"

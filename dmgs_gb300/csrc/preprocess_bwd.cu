@@ -487,9 +487,7 @@ int launch_preprocess_bwd(const ViewParams &vp, const float *viewm, const float 
     dmgs_host::set_error("preprocess_bwd: %d SH coefficients per Gaussian exceed shared memory", g.M);
     return DMGS_ERR_ARG;
   }
-  if (smem > 48 * 1024)
-    DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_kernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (int r = dmgs_host::raise_smem_limit((const void *)preprocess_bwd_kernel, smem)) return r;
   DMGS_TIMED(K_PREPROCESS_BWD, s, dmgs_host::note_launch(), preprocess_bwd_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
       vp, viewm, projm, campos, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D,
       reinterpret_cast<const uint8_t *>(geom + L.flags), gacc, out));
@@ -511,9 +509,8 @@ int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, c
   }
   int want_xy = densify_accum != nullptr;
   for (int v = 0; v < bv.nviews; ++v) want_xy |= bv.v[v].dL_dmeans2D != nullptr;
-  if (smem > 48 * 1024)
-    DMGS_CUDA(cudaFuncSetAttribute(preprocess_bwd_batched_kernel,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (int r = dmgs_host::raise_smem_limit((const void *)preprocess_bwd_batched_kernel, smem))
+    return r;
   DMGS_TIMED(K_BATCH_PREPROCESS_BWD, s,
              dmgs_host::note_launch(), preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
                  bv, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D, out, want_xy,

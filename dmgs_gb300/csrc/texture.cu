@@ -487,14 +487,7 @@ int run_fwd(const TexArgs &A, const TexLevels &L, const float *xyz, float *out, 
 template <int C>
 int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float *dout, float *dxyz,
             float *dtable, float *dW1, float *dW2, float *dW3, float *denc, cudaStream_t s) {
-  thread_local int attr_dev = -1;  // the attribute is per device; setting it again is harmless
-  int dev = 0;
-  DMGS_CUDA(cudaGetDevice(&dev));
-  if (dev != attr_dev) {
-    DMGS_CUDA(cudaFuncSetAttribute(tex_bwd_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)tex_bwd_smem()));
-    attr_dev = dev;
-  }
+  if (int r = dmgs_host::raise_smem_limit((const void *)tex_bwd_kernel<C>, tex_bwd_smem())) return r;
   int grid;
   if (int r = persistent_grid(tex_bwd_kernel<C>, tex_bwd_smem(), A.n, grid)) return r;
   dmgs_host::note_launch(), tex_bwd_kernel<C><<<grid, TEX_THREADS, tex_bwd_smem(), s>>>(

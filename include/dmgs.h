@@ -153,7 +153,9 @@ int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g,
  * scratch pair; g->P above the limit returns DMGS_ERR_ARG.  The first call on
  * a device looks up the array's address (cudaGetSymbolAddress), so make it
  * before any stream capture begins.  All calls share the array: calls whose
- * work overlaps on the GPU race. */
+ * work overlaps on the GPU race.  The looked-up address is kept for the life
+ * of the process: after a cudaDeviceReset on a device, do not call this entry
+ * point on that device again (the array may then live at another address). */
 #define DMGS_NOALLOC_MAX_GAUSSIANS 262144
 int dmgs_raster_bwd_noalloc(const DmgsView *view, const DmgsGaussians *g,
                             const float *dL_dout_color, const void *geom_state,

@@ -84,4 +84,8 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_tree = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DMGS_REFERENCE_TREE")
+    if not ref_tree:
+        sys.exit(f"usage: python {os.path.basename(__file__)} <reference tree> "
+                 "(or set DMGS_REFERENCE_TREE)")
+    main(ref_tree)

@@ -14,7 +14,10 @@ import torch
 from oracle import flexicubes as ofc
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "flexicubes_golden.npz")
-REF_TABLES = "/root/reference/geo/tables.py"
+# the reference tree (read-only), located through the environment; the tests
+# that run the reference's own code skip without it
+REF_ROOT = os.environ.get("DMGS_REFERENCE_TREE", "")
+REF_TABLES = os.path.join(REF_ROOT, "geo", "tables.py") if REF_ROOT else ""
 CASES = ("shape", "noise", "plain")
 
 
@@ -38,8 +41,8 @@ def rel_l2(a, b):
 
 
 def test_tables_match_reference():
-    if not os.path.exists(REF_TABLES):
-        pytest.skip("reference tree not present")
+    if not REF_TABLES or not os.path.exists(REF_TABLES):
+        pytest.skip("reference tree not present (set DMGS_REFERENCE_TREE)")
     ns = {}
     exec(compile(open(REF_TABLES).read(), REF_TABLES, "exec"), ns)
     dmc, num_vd, check = ofc.derive_tables()
@@ -92,9 +95,9 @@ def test_oracle_matches_reference_class(res, training):
     quad-splitting mode), the sphere-union-torus field, deformed vertices and
     random weights; both in float32."""
     import sys
-    ref_root = os.path.dirname(os.path.dirname(REF_TABLES))
-    if not os.path.exists(os.path.join(ref_root, "geo", "flexicubes.py")):
-        pytest.skip("reference tree not present")
+    ref_root = REF_ROOT
+    if not ref_root or not os.path.exists(os.path.join(ref_root, "geo", "flexicubes.py")):
+        pytest.skip("reference tree not present (set DMGS_REFERENCE_TREE)")
     sys.path.insert(0, ref_root)
     try:
         from geo.flexicubes import FlexiCubes
