@@ -13,7 +13,7 @@ import torch  # noqa: F401  (loads libcudart before the extension)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdmgs_gb300.so")
-ABI_VERSION = 3  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
+ABI_VERSION = 4  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
 
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -88,6 +88,10 @@ SIGNATURES = [
     ("dmgs_raster_bwd", C.c_int, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians), vp, vp,
                                   C.c_size_t, vp, C.c_size_t, C.c_int64, vp, C.c_size_t, vp,
                                   C.c_size_t, C.POINTER(DmgsGrads), vp]),
+    ("dmgs_bwd_scratch_f64_bytes", C.c_size_t, [C.c_int32]),
+    ("dmgs_raster_bwd_f64sum", C.c_int, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians), vp, vp,
+                                         C.c_size_t, vp, C.c_size_t, C.c_int64, vp, C.c_size_t,
+                                         vp, C.c_size_t, C.POINTER(DmgsGrads), vp]),
     ("dmgs_raster_bwd_noalloc", C.c_int, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians), vp,
                                           vp, C.c_size_t, vp, C.c_size_t, C.c_int64, vp,
                                           C.c_size_t, C.POINTER(DmgsGrads), vp]),

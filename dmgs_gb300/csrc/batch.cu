@@ -223,6 +223,7 @@ void fill_blend(const DmgsBatch *b, const BatchLayout &L, char *const *bases, Bl
     o.n_contrib = reinterpret_cast<uint32_t *>(img + V.I.n_contrib);
     o.dL_dout = nullptr;
     o.gacc = reinterpret_cast<float *>(st + V.gacc);
+    o.gacc64 = nullptr;
   }
   bb.total = base;
 }

@@ -461,7 +461,10 @@ __device__ __forceinline__ int slot9(int q) {
 }
 
 
-template <int PPT, int BATCH>
+// F64: the FP64-sum mode — the warp sums are added into double accumulators
+// (V.gacc64), so the result does not depend on the order in which warps and
+// tiles finish to well below float32 resolution.
+template <int PPT, int BATCH, bool F64 = false>
 __global__ void __launch_bounds__(256 / PPT, PPT == 4 ? 10 : (PPT == 2 ? 6 : 4))
 blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
   constexpr int THREADS = 256 / PPT;
@@ -554,7 +557,10 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
           const int slot = slot9((lane >> 1) & 15);
           if (!(lane & 1) && slot < 9) {
             const float scale = (slot == 2 || slot == 4) ? -0.5f : (slot == 3 ? -1.f : 1.f);
-            atomicAdd(V.gacc + (size_t)__float_as_uint(s3.z) * 12 + slot, sum * scale);
+            if constexpr (F64)
+              atomicAdd(V.gacc64 + (size_t)__float_as_uint(s3.z) * 12 + slot, (double)(sum * scale));
+            else
+              atomicAdd(V.gacc + (size_t)__float_as_uint(s3.z) * 12 + slot, sum * scale);
           }
         }
       }
@@ -593,15 +599,22 @@ int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
   return DMGS_OK;
 }
 
-template <int PPT, int BATCH>
+template <int PPT, int BATCH, bool F64 = false>
 int run_bwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
   thread_local int cdev = -1, cslots = 0;  // per kernel instantiation and host thread
   int grid;
-  const int r = grid_for(blend_bwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
-                         cdev, cslots);
+  const int r = grid_for(blend_bwd_kernel<PPT, BATCH, F64>, 256 / PPT, bb.total, queue != nullptr,
+                         grid, cdev, cslots);
   if (r != DMGS_OK) return r;
-  dmgs_host::note_launch(), blend_bwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  dmgs_host::note_launch(), blend_bwd_kernel<PPT, BATCH, F64><<<grid, 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
+}
+
+// Rounds the FP64 accumulators into the float records the preprocess
+// adjoint reads.
+__global__ void gacc_round_kernel(const double *__restrict__ g64, float *__restrict__ g, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) g[i] = (float)g64[i];
 }
 
 template <bool FWD>
@@ -654,6 +667,7 @@ BlendView make_blend_view(const ViewParams &vp, const GeomLayout &L, const char 
   v.n_contrib = reinterpret_cast<uint32_t *>(img + I.n_contrib);
   v.dL_dout = nullptr;
   v.gacc = nullptr;
+  v.gacc64 = nullptr;
   return v;
 }
 
@@ -670,15 +684,30 @@ int launch_blend_fwd(const ViewParams &vp, const GeomLayout &L, const char *geom
 
 int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
                      const BinLayout &B, const char *bin, const ImgLayout &I, const char *img,
-                     const float *bg, const float *dL_dout, float *gacc, cudaStream_t s) {
+                     const float *bg, const float *dL_dout, float *gacc, double *gacc64,
+                     cudaStream_t s) {
   DMGS_CUDA(cudaMemsetAsync(gacc, 0, (size_t)L.P * 48, s));
   BlendBatch bb;
   bb.nviews = 1;
   bb.v[0] = make_blend_view(vp, L, geom, B, bin, I, const_cast<char *>(img), bg);
   bb.v[0].dL_dout = dL_dout;
   bb.v[0].gacc = gacc;
+  bb.v[0].gacc64 = gacc64;
   bb.total = bb.v[0].T;
-  return launch_blend_batch_bwd(bb, default_blend_cfg(), nullptr, s);
+  if (gacc64 == nullptr) return launch_blend_batch_bwd(bb, default_blend_cfg(), nullptr, s);
+  const size_t n = (size_t)L.P * 12;
+  DMGS_CUDA(cudaMemsetAsync(gacc64, 0, n * sizeof(double), s));
+  if (bb.total > 0) {
+    int r = DMGS_OK;
+    DMGS_TIMED(K_BLEND_BWD, s, r = (run_bwd<4, 128, true>(bb, nullptr, s)));
+    if (r != DMGS_OK) return r;
+    DMGS_LAUNCH_CHECK("blend_bwd_kernel (FP64 sums)");
+  }
+  if (n > 0) {
+    dmgs_host::note_launch(), gacc_round_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(gacc64, gacc, n);
+    DMGS_LAUNCH_CHECK("gacc_round_kernel");
+  }
+  return DMGS_OK;
 }
 
 }  // namespace dmgs

@@ -258,11 +258,17 @@ int dmgs_raster_fwd(const DmgsView *view, const DmgsGaussians *g, dmgs_alloc_fn 
   return dmgs_raster_fwd_render(view, g, geom, gb, bin, bb, K, img, ib, out_color, stream);
 }
 
-int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g, const float *dL_dout_color,
+}  // extern "C"
+
+namespace {
+
+// Both backward entry points: f64 selects the FP64-sum mode, whose scratch
+// holds the [P][12] double accumulators after the float records.
+int raster_bwd_impl(const DmgsView *view, const DmgsGaussians *g, const float *dL_dout_color,
                     const void *geom_state, size_t geom_bytes, const void *binning_state,
                     size_t binning_bytes, int64_t num_rendered, const void *image_state,
                     size_t image_bytes, void *bwd_scratch, size_t bwd_scratch_bytes_,
-                    const DmgsGrads *grads, dmgs_stream_t stream) {
+                    const DmgsGrads *grads, dmgs_stream_t stream, bool f64) {
   RET_IF(check_view(view));
   RET_IF(check_gaussians(g, view->sh_degree));
   if (!grads || !dL_dout_color) { set_error("grads / dL_dout_color is NULL"); return DMGS_ERR_ARG; }
@@ -273,7 +279,9 @@ int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g, const float *d
   if (!geom_state || geom_bytes < L.total) { set_error("geometry state too small"); return DMGS_ERR_STATE; }
   if (!binning_state || binning_bytes < B.total) { set_error("binning state too small"); return DMGS_ERR_STATE; }
   if (!image_state || image_bytes < I.total) { set_error("image state too small"); return DMGS_ERR_STATE; }
-  if (!bwd_scratch || bwd_scratch_bytes_ < bwd_scratch_bytes(g->P)) { set_error("backward scratch too small"); return DMGS_ERR_STATE; }
+  const size_t need = f64 ? bwd_scratch_bytes(g->P) + align_up((size_t)g->P * 96, 256)
+                          : bwd_scratch_bytes(g->P);
+  if (!bwd_scratch || bwd_scratch_bytes_ < need) { set_error("backward scratch too small: %zu < %zu bytes", bwd_scratch_bytes_, need); return DMGS_ERR_STATE; }
   if (grads->dL_drotations && (reinterpret_cast<uintptr_t>(grads->dL_drotations) & 15)) {
     set_error("dL_drotations must be 16-byte aligned");
     return DMGS_ERR_ARG;
@@ -282,14 +290,46 @@ int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g, const float *d
   const char *bin = static_cast<const char *>(binning_state);
   const char *img = static_cast<const char *>(image_state);
   float *gacc = static_cast<float *>(bwd_scratch);
+  double *gacc64 = f64 ? reinterpret_cast<double *>(static_cast<char *>(bwd_scratch) +
+                                                    bwd_scratch_bytes(g->P))
+                       : nullptr;
   const ViewParams vp = make_params(view);
-  RET_IF(launch_blend_bwd(vp, L, geom, B, bin, I, img, view->bg, dL_dout_color, gacc, s));
+  RET_IF(launch_blend_bwd(vp, L, geom, B, bin, I, img, view->bg, dL_dout_color, gacc, gacc64, s));
   RET_IF(debug_sync(view, s, "blend_bwd"));
   DmgsGrads out = *grads;
   RET_IF(launch_preprocess_bwd(vp, view->viewmatrix, view->projmatrix, view->campos,
                                make_gptrs(g), L, geom, gacc, out, s));
   RET_IF(debug_sync(view, s, "preprocess_bwd"));
   return DMGS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t dmgs_bwd_scratch_f64_bytes(int32_t P) {
+  return P < 0 ? 0 : bwd_scratch_bytes(P) + align_up((size_t)P * 96, 256);
+}
+
+int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g, const float *dL_dout_color,
+                    const void *geom_state, size_t geom_bytes, const void *binning_state,
+                    size_t binning_bytes, int64_t num_rendered, const void *image_state,
+                    size_t image_bytes, void *bwd_scratch, size_t bwd_scratch_bytes_,
+                    const DmgsGrads *grads, dmgs_stream_t stream) {
+  return raster_bwd_impl(view, g, dL_dout_color, geom_state, geom_bytes, binning_state,
+                         binning_bytes, num_rendered, image_state, image_bytes, bwd_scratch,
+                         bwd_scratch_bytes_, grads, stream, false);
+}
+
+int dmgs_raster_bwd_f64sum(const DmgsView *view, const DmgsGaussians *g,
+                           const float *dL_dout_color, const void *geom_state, size_t geom_bytes,
+                           const void *binning_state, size_t binning_bytes, int64_t num_rendered,
+                           const void *image_state, size_t image_bytes, void *bwd_scratch,
+                           size_t bwd_scratch_bytes_, const DmgsGrads *grads,
+                           dmgs_stream_t stream) {
+  return raster_bwd_impl(view, g, dL_dout_color, geom_state, geom_bytes, binning_state,
+                         binning_bytes, num_rendered, image_state, image_bytes, bwd_scratch,
+                         bwd_scratch_bytes_, grads, stream, true);
 }
 
 int dmgs_mark_visible(int32_t P, const float *means3D, const float *viewmatrix,

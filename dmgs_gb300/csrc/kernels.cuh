@@ -117,6 +117,7 @@ struct BlendView {
   uint32_t *n_contrib;
   const float *dL_dout; // adjoint inputs/outputs
   float *gacc;
+  double *gacc64;       // adjoint in FP64-sum mode: [P][12] double accumulators (else null)
 };
 
 struct BlendBatch {
@@ -140,9 +141,12 @@ int launch_blend_batch_bwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *
 int launch_blend_fwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
                      const BinLayout &B, const char *bin, const ImgLayout &I, char *img,
                      const float *bg, float *out_color, cudaStream_t s);
+// gacc64 != nullptr: the FP64-sum mode (gradient terms added into [P][12]
+// doubles, then rounded into gacc for the preprocess adjoint).
 int launch_blend_bwd(const ViewParams &vp, const GeomLayout &L, const char *geom,
                      const BinLayout &B, const char *bin, const ImgLayout &I, const char *img,
-                     const float *bg, const float *dL_dout, float *gacc, cudaStream_t s);
+                     const float *bg, const float *dL_dout, float *gacc, double *gacc64,
+                     cudaStream_t s);
 
 // preprocess_bwd.cu
 int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, const DmgsGrads &out,

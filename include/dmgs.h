@@ -27,7 +27,7 @@
 /* Version of the structs and entry points below; dmgs_abi_version() returns
  * the value the library was built with.  Raised whenever a struct layout or
  * a signature changes. */
-#define DMGS_ABI_VERSION 3
+#define DMGS_ABI_VERSION 4
 
 #ifdef __cplusplus
 extern "C" {
@@ -141,6 +141,23 @@ int dmgs_raster_bwd(const DmgsView *view, const DmgsGaussians *g,
                     const void *image_state, size_t image_bytes,
                     void *bwd_scratch, size_t bwd_scratch_bytes,
                     const DmgsGrads *grads, dmgs_stream_t stream);
+
+/* Backward with FP64 gradient sums (no counterpart in the reference): the
+ * same arguments and results as dmgs_raster_bwd, but the blend adjoint adds
+ * every Gaussian's per-pixel gradient terms into double-precision
+ * accumulators, so the gradients do not depend on the order in which tiles
+ * and warps finish (to well below float32 resolution).  dmgs_raster_bwd adds
+ * them with float atomics, whose order changes from run to run.  A
+ * verification mode, slower than dmgs_raster_bwd; `bwd_scratch` holds
+ * dmgs_bwd_scratch_f64_bytes(P) bytes (144 per Gaussian). */
+size_t dmgs_bwd_scratch_f64_bytes(int32_t P);
+int dmgs_raster_bwd_f64sum(const DmgsView *view, const DmgsGaussians *g,
+                           const float *dL_dout_color, const void *geom_state,
+                           size_t geom_bytes, const void *binning_state,
+                           size_t binning_bytes, int64_t num_rendered,
+                           const void *image_state, size_t image_bytes,
+                           void *bwd_scratch, size_t bwd_scratch_bytes,
+                           const DmgsGrads *grads, dmgs_stream_t stream);
 
 /* Backward for callers that cannot allocate device memory (this entry point
  * has no counterpart in the reference).  A plugin inside a host application

@@ -122,7 +122,9 @@ class AbiRun:
                     keys=keys.cpu().numpy().view(np.uint64)[:self.K], values=u32(vals)[:self.K],
                     ranges=u32(ranges), final_T=fT.cpu().numpy(), n_contrib=u32(nc))
 
-    def backward(self, dL_dimage):
+    def backward(self, dL_dimage, f64sum=False):
+        """dmgs_raster_bwd (float atomics), or with f64sum=True the FP64-sum
+        mode dmgs_raster_bwd_f64sum."""
         lib, P, d = self.lib, self.P, self.device
         z = lambda *s: torch.full(s, float("nan"), device=d)  # noqa: E731  (must be fully written)
         t = self.t
@@ -135,14 +137,19 @@ class AbiRun:
         grads = DmgsGrads(ptr(gr["means2D"]), ptr(gr["colors"]), ptr(gr["opacities"]),
                           ptr(gr["means3D"]), ptr(gr["cov3D"]), ptr(gr["shs"]), ptr(gr["scales"]),
                           ptr(gr["rotations"]))
-        scratch = torch.empty(lib.dmgs_bwd_scratch_bytes(P), dtype=torch.uint8, device=d)
+        nbytes = lib.dmgs_bwd_scratch_f64_bytes(P) if f64sum else lib.dmgs_bwd_scratch_bytes(P)
+        scratch = torch.empty(nbytes, dtype=torch.uint8, device=d)
         dout = _dev(np.asarray(dL_dimage, np.float32))
-        _lib.check(lib.dmgs_raster_bwd(self.view, self.g, dout.data_ptr(), self.geom.data_ptr(),
-                                       self.geom.numel(), self.bin.data_ptr(), self.bin.numel(),
-                                       self.K, self.img.data_ptr(), self.img.numel(),
-                                       scratch.data_ptr(), scratch.numel(), grads, self.stream),
-                   "raster_bwd")
+        fn = lib.dmgs_raster_bwd_f64sum if f64sum else lib.dmgs_raster_bwd
+        _lib.check(fn(self.view, self.g, dout.data_ptr(), self.geom.data_ptr(),
+                      self.geom.numel(), self.bin.data_ptr(), self.bin.numel(), self.K,
+                      self.img.data_ptr(), self.img.numel(), scratch.data_ptr(), scratch.numel(),
+                      grads, self.stream), "raster_bwd")
         torch.cuda.synchronize()
+        # the blend adjoint's per-Gaussian 2D gradient records, the first 48 B
+        # per Gaussian of the scratch (dL/dndc x, y; dL/dconic a, b, c;
+        # dL/dopacity; dL/drgb; 3 unused), for tests of the adjoint alone
+        self.records2d = scratch[: P * 48].view(torch.float32).view(P, 12)[:, :9].cpu().numpy()
         return {k: (v.cpu().numpy() if v is not None else None) for k, v in gr.items()}
 
 
@@ -157,3 +164,56 @@ def rel_l2(a, b):
 GRAD_NAMES = {"means3D": "means3D", "means2D": "means2D", "opacities": "opacities",
               "shs": "shs", "colors_precomp": "colors", "scales": "scales",
               "rotations": "rotations", "cov3D_precomp": "cov3D"}
+
+
+def sampled_tile_lists(geom, gx, tiles):
+    """Per tile of `tiles` (row-major tile ids), the visible Gaussians whose
+    tile rectangle contains it, in (depth, index) order — the tile lists of
+    the reference's (tile, depth) sort, from the oracle's FP32 geometry.
+    Returns (lists, union of their Gaussians)."""
+    vis = np.nonzero(geom["visible"])[0]
+    rect = geom["rect"][vis]
+    dbits = geom["depth"][vis].view(np.uint32)
+    lists = []
+    for t in tiles:
+        ty, tx = divmod(int(t), gx)
+        m = (rect[:, 0] <= tx) & (tx < rect[:, 2]) & (rect[:, 1] <= ty) & (ty < rect[:, 3])
+        ids = vis[m]
+        lists.append(ids[np.lexsort((ids, dbits[m]))])
+    union = np.unique(np.concatenate(lists)) if lists else np.zeros(0, np.int64)
+    return lists, union
+
+
+def blend_sampled_tiles(width, height, gx, tiles, lists, union, pix, conic, op, rgb, bg, image,
+                        seed=3):
+    """FP64 oracle blending of the sampled tiles (2D quantities of the
+    Gaussians in `union`, in union order) and the comparison with `image`
+    ([3,H,W] numpy, the kernel's).  Returns (loss, dL/dimage [3,H,W] float32
+    that is N(0,1) on the decidable pixels of the sampled tiles and 0
+    elsewhere, the max image error on decidable pixels, the number of those
+    pixels)."""
+    pos = {int(g): i for i, g in enumerate(union)}
+    rng = np.random.default_rng(seed)
+    dimg = np.zeros((3, height, width), np.float32)
+    loss = 0.0
+    err = 0.0
+    checked = 0
+    bg64 = torch.as_tensor(np.asarray(bg, np.float64))
+    for t, ids in zip(tiles, lists):
+        ty, tx = divmod(int(t), gx)
+        x0, y0 = tx * 16, ty * 16
+        x1, y1 = min(x0 + 16, width), min(y0 + 16, height)
+        yy, xx = torch.meshgrid(torch.arange(y0, y1, dtype=torch.float64),
+                                torch.arange(x0, x1, dtype=torch.float64), indexing="ij")
+        pxy = torch.stack([xx.reshape(-1), yy.reshape(-1)], 1)
+        g = torch.as_tensor([pos[int(i)] for i in ids], dtype=torch.long)
+        out, _, _, amb = R._blend_tile(pxy, pix[g], conic[g], op[g], rgb[g], bg64)
+        ok = ~amb.numpy()
+        mine = image[:, y0:y1, x0:x1].reshape(3, -1).T
+        if ok.any():
+            err = max(err, float(np.abs(mine[ok] - out.detach().numpy()[ok]).max()))
+        d = rng.standard_normal(out.shape).astype(np.float32) * ok[:, None]
+        dimg[:, y0:y1, x0:x1] = d.T.reshape(3, y1 - y0, x1 - x0)
+        loss = loss + (out * torch.as_tensor(d, dtype=torch.float64)).sum()
+        checked += int(ok.sum())
+    return loss, dimg, err, checked

@@ -271,17 +271,59 @@ def test_full_size_integer_outputs_bit_exact():
     assert np.all((rect[:, 0] <= tx) & (tx < rect[:, 2]) & (rect[:, 1] <= ty) & (ty < rect[:, 3]))
 
 
+def _chain_magnitudes(inter, leaves, names):
+    """Per Gaussian and input x, S(x) = sum over the nine 2D gradient
+    components y_k (dL/dndc x, y; dL/dconic a, b, c; dL/dopacity; dL/drgb)
+    of |d x / d y_k . dL/dy_k|: the first-order bound on the error of dL/dx
+    when every 2D gradient carries a relative error of at most 1 (so e S(x)
+    bounds it for a relative error e).  Computed on the oracle's FP64 graph."""
+    import torch
+    n = leaves[names[0]].shape[0]
+    S = {k: torch.zeros(n, dtype=torch.float64) for k in names}
+    comps = [(inter["ndc"], 0), (inter["ndc"], 1), (inter["conic"], 0), (inter["conic"], 1),
+             (inter["conic"], 2), (inter["op"], None), (inter["rgb"], 0), (inter["rgb"], 1),
+             (inter["rgb"], 2)]
+    for y, c in comps:
+        go = torch.zeros_like(y.grad)
+        if c is None:
+            go.copy_(y.grad)
+        else:
+            go[:, c] = y.grad[:, c]
+        gs = torch.autograd.grad(y, [leaves[k] for k in names], grad_outputs=go,
+                                 retain_graph=True, allow_unused=True)
+        for k, g in zip(names, gs):
+            if g is not None:
+                S[k] += g.reshape(n, -1).norm(dim=1)
+    return {k: v.numpy() for k, v in S.items()}
+
+
 def test_full_size_sampled_tiles_image_and_gradients():
-    """Configuration 3 at full size: on 24 tiles spread over the view, the
-    image matches the FP64 oracle blending of the same tile lists (pixels
-    FP32 can decide), and with dL/dimage non-zero only on those tiles the
-    gradients w.r.t. every input match the oracle's autograd (1e-3 relative
-    L2); Gaussians that touch no sampled tile get zero.  n_contrib (the
-    position of the last blended Gaussian) may differ on a few pixels here:
-    after hundreds of factors the FP32 transmittance drifts by more than the
-    oracle's 1e-5 relative ambiguity band around the 1e-4 stop, so the stop
-    can move by one Gaussian whose contribution is below 1e-4 (the images
-    still agree to 2e-4); the small-scene tests check n_contrib exactly."""
+    """Configuration 3 at full size (3M Gaussians, 1237x822), 24 tiles spread
+    over the view: the image matches the FP64 oracle blending of the same
+    tile lists (pixels FP32 can decide); with dL/dimage non-zero only on those
+    tiles:
+
+    * the blend adjoint's per-Gaussian 2D gradients (NDC mean, conic,
+      opacity, colour) match the oracle's intermediate gradients (1e-3
+      relative L2);
+    * the gradients of all five inputs match the oracle's autograd to 1e-3
+      relative L2 over the Gaussians whose 3D gradient is well conditioned
+      w.r.t. the 2D ones (the terms it sums cancel by less than 10x); for
+      the rest — a handful of near-plane needles thousands of pixels long
+      whose position gradient is the difference of chain terms 1000x larger
+      than itself, so float32 cannot carry it to 1e-3 — the error stays
+      within 1e-3 of the magnitude of the terms summed;
+    * the FP64-sum mode (dmgs_raster_bwd_f64sum) is run to run identical and
+      meets the bars above; the default float-atomic adjoint meets them up
+      to its own measured run-to-run spread (its summation order varies);
+    * Gaussians that touch no sampled tile get zero.
+
+    n_contrib (the position of the last blended Gaussian) may differ on a few
+    pixels: after hundreds of factors the FP32 transmittance drifts by more
+    than the oracle's 1e-5 relative ambiguity band around the 1e-4 stop, so
+    the stop can move by one Gaussian whose contribution is below 1e-4 (the
+    images still agree to 2e-4); the small-scene tests check it exactly."""
+    import json
     import torch
     from dmgs_gb300.scenes import large_scene
     sc = large_scene(P=3_000_000, seed=0, n_views=1)
@@ -311,6 +353,9 @@ def test_full_size_sampled_tiles_image_and_gradients():
                                               shs=leaves["shs"], scales=leaves["scales"],
                                               rotations=leaves["rotations"],
                                               sel=torch.arange(len(union)))
+    inter = {"ndc": ndc, "conic": conic, "op": op, "rgb": rgb}
+    for v in inter.values():
+        v.retain_grad()
     pos = {int(g): i for i, g in enumerate(union)}
     rng = np.random.default_rng(3)
     dimg = np.zeros((3, view.height, view.width), np.float32)
@@ -337,20 +382,43 @@ def test_full_size_sampled_tiles_image_and_gradients():
         checked += int(ok.sum())
     assert checked > 5000
     assert nc_diff <= 0.02 * checked, (nc_diff, checked)
-    loss.backward()
-    gk = run.backward(dimg)
+    loss.backward(retain_graph=True)
+    S = _chain_magnitudes(inter, leaves, names)
+
+    g64 = run.backward(dimg, f64sum=True)
+    rec = run.records2d[union].astype(np.float64)
+    g64b = run.backward(dimg, f64sum=True)
+    gfa = [run.backward(dimg) for _ in range(2)]  # float atomics
     rest = np.ones(run.P, bool)
     rest[union] = False
-    errs = {}
+    # 2D records of the blend adjoint against the oracle's intermediate gradients
+    e2d = {"ndc": rel_l2(rec[:, 0:2], ndc.grad.numpy()),
+           "conic": rel_l2(rec[:, 2:5], conic.grad.numpy()),
+           "opacity": rel_l2(rec[:, 5], op.grad.numpy()),
+           "rgb": rel_l2(rec[:, 6:9], rgb.grad.numpy())}
+    report = {"records_2d": e2d, "inputs": {}}
     for k in names:
-        ref = leaves[k].grad.numpy()
-        errs[k] = rel_l2(gk[GRAD_NAMES[k]][union].reshape(ref.shape), ref)
-        assert np.abs(gk[GRAD_NAMES[k]][rest]).max() == 0.0, k
-    # opacity and SH gradients are sums of same-signed terms: the 1e-3 bar;
-    # position, scale and rotation gradients are sums over hundreds of
-    # pixels of terms of both signs that nearly cancel, so float atomics'
-    # summation order alone moves them by ~1e-3..5e-3 relative at this size
-    # (two runs of the same kernel differ that much): a 1e-2 bar
-    tol = {"opacities": GRAD_TOL, "shs": GRAD_TOL, "means3D": 1e-2, "scales": 1e-2,
-           "rotations": 1e-2}
-    assert all(errs[k] <= tol[k] for k in names), errs
+        ref = leaves[k].grad.numpy().reshape(len(union), -1)
+        mine = g64[GRAD_NAMES[k]][union].reshape(ref.shape).astype(np.float64)
+        fa = [x[GRAD_NAMES[k]][union].reshape(ref.shape).astype(np.float64) for x in gfa]
+        assert np.array_equal(g64[GRAD_NAMES[k]], g64b[GRAD_NAMES[k]]), k  # reproducible
+        for x in (g64, *gfa):
+            assert np.abs(x[GRAD_NAMES[k]][rest]).max() == 0.0, k
+        gn = np.linalg.norm(ref, axis=1)
+        well = S[k] <= 10.0 * np.maximum(gn, 1e-300)
+        err = np.linalg.norm(mine - ref, axis=1)
+        r = {"ill_conditioned": int((~well).sum()),
+             "f64sum_vs_oracle_well": rel_l2(mine[well], ref[well]),
+             "f64sum_vs_oracle_all": rel_l2(mine, ref),
+             "atomics_vs_oracle_well": rel_l2(fa[0][well], ref[well]),
+             "atomics_run_to_run_well": rel_l2(fa[1][well], fa[0][well]),
+             "atomics_run_to_run_all": rel_l2(fa[1], fa[0]),
+             "worst_err_over_S_ill": float((err[~well] / S[k][~well]).max()) if (~well).any() else 0.0}
+        report["inputs"][k] = r
+    print("FULL_SIZE_GRADIENTS", json.dumps(report))
+    assert all(v <= GRAD_TOL for v in e2d.values()), e2d
+    for k, r in report["inputs"].items():
+        assert r["ill_conditioned"] <= 1e-3 * len(union), (k, r)
+        assert r["f64sum_vs_oracle_well"] <= GRAD_TOL, (k, r)
+        assert r["worst_err_over_S_ill"] <= GRAD_TOL, (k, r)
+        assert r["atomics_vs_oracle_well"] <= GRAD_TOL + 2 * r["atomics_run_to_run_well"], (k, r)
