@@ -535,9 +535,10 @@ def texture_leg(args, dev):
     return out
 
 
-def bytes_model(name, P, V, K, npix, nviews=1):
+def bytes_model(name, P, V, K, npix, nviews=1, K1=None):
     """Algorithmic DRAM bytes per launch (SH3, scale/rotation inputs).  For
-    a batched launch V, K, npix are sums over the views."""
+    a batched launch V, K, npix (and K1, the row-list entries) are sums over
+    the views."""
     if name == "batch_preprocess":
         return P * (12 + 16 + 12 + 4 + 192) + nviews * P * 4 + V * 48
     if name == "batch_preprocess_bwd":
@@ -554,8 +555,10 @@ def bytes_model(name, P, V, K, npix, nviews=1):
         return V * 80             # histogram, 8 B read + 8 B written by the scatter, per key
     if name == "bin_compact":
         return P * nviews + V * 12
-    if name == "bin_emit":
-        return K * 4 + V * 16
+    if name == "bin_emit":  # row lists read (8 B per entry), tile lists written (4 B per instance)
+        return None if K1 is None else K * 4 + K1 * 8
+    if name == "bin_row_emit":  # sorted rectangles + indices read, row lists written
+        return None if K1 is None else V * 12 + K1 * 8
     return None
 
 
@@ -717,6 +720,9 @@ def main():
     if not args.no_tune:
         tune = autotune(br, iters=3, cache_path=os.environ.get("DMGS_AUTOTUNE_CACHE"))
     counts = br.count_instances()
+    br.forward()
+    bin_counters = br.counters()
+    K1_sum = sum(c["K1"] for c in bin_counters)
     lib.dmgs_timing_enable(1)
     _lib.timing_collect()
     n0 = lib.dmgs_kernel_launches()
@@ -765,7 +771,7 @@ def main():
     # ---------------- roofline of the dominant kernel (batched step) ----------------
     Vs = sum(int((r > 0).sum()) for r in br.radii)
     npix = sum(s.image_width * s.image_height for s in settings)
-    kernels = kernel_table(kt_batch, (P, Vs, sum(counts), npix, nv))
+    kernels = kernel_table(kt_batch, (P, Vs, sum(counts), npix, nv, K1_sum))
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -862,7 +868,7 @@ def main():
         Kp = statistics.mean(counts)
         if plain is not None:
             plain["ratio_batched_over_plain"] = value / max(plain["views_per_s"], 1e-9)
-            plain["kernels"] = kernel_table(kt_plain, (P, Vs / nv, Kp, npix / nv))
+            plain["kernels"] = kernel_table(kt_plain, (P, Vs / nv, Kp, npix / nv, 1, K1_sum / nv))
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batch / args.steps, "higher_is_better": True,
@@ -872,6 +878,7 @@ def main():
                        "outputs": "images, parameter gradients summed over views, densification "
                                   "statistics (fused add_densification_stats)",
                        "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
+                       "mean_row_entries_K1": int(K1_sum / nv),
                        "blend_config": {"pixels_per_thread": br_cfg[0], "gaussians_per_batch": br_cfg[1]},
                        "graph": not args.no_graph},
             "plain": plain,

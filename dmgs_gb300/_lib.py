@@ -13,7 +13,7 @@ import torch  # noqa: F401  (loads libcudart before the extension)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdmgs_gb300.so")
-ABI_VERSION = 4  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
+ABI_VERSION = 5  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
 
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -101,6 +101,8 @@ SIGNATURES = [
     ("dmgs_raster_bwd_batched", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians),
                                           C.POINTER(vp), vp, C.c_size_t, C.POINTER(DmgsGrads),
                                           C.POINTER(vp), vp, vp, vp]),
+    ("dmgs_batch_counters", C.c_int, [C.POINTER(DmgsBatch), C.c_int32, vp, C.c_size_t,
+                                      C.POINTER(C.c_uint32), vp]),
     ("dmgs_batch_status", C.c_int, [C.POINTER(DmgsBatch), C.c_int32, vp, C.c_size_t,
                                     C.POINTER(C.c_int64), vp]),
     ("dmgs_multi_view_state_bytes", C.c_size_t, [C.POINTER(DmgsView), C.POINTER(DmgsGaussians),

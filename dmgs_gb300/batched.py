@@ -223,6 +223,17 @@ class BatchedRasterizer:
         check(code, "batch_status")
         return counts
 
+    def counters(self):
+        """Per-view binning counters of the last forward (synchronises): a
+        dict per view with the instances K, the row-list entries K1, the
+        visible Gaussians V, the chunks C and the longest tile list."""
+        words = (C.c_uint32 * (16 * self.n))()
+        check(self.lib.dmgs_batch_counters(C.byref(self.batch), self.P, self.state.data_ptr(),
+                                           self.state.numel(), words, _lib.stream_of(self.device)),
+              "batch_counters")
+        return [{"K": words[16 * v + 1], "K1": words[16 * v + 2], "maxlist": words[16 * v + 3],
+                 "V": words[16 * v + 4], "C": words[16 * v + 8]} for v in range(self.n)]
+
     def grow(self, factor=1.5):
         """Re-plan capacities from exact counts (after an overflow)."""
         self._set_capacity([int(k * factor) + 1024 for k in self.count_instances()])

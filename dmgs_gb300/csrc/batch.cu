@@ -212,6 +212,7 @@ void fill_blend(const DmgsBatch *b, const BatchLayout &L, char *const *bases, Bl
     o.H = b->views[v].height;
     o.gx = V.G.gx;
     o.T = V.G.T();
+    o.P = (uint32_t)V.G.P;
     o.tile_base = base;
     base += o.T;
     o.ranges = reinterpret_cast<const uint2 *>(geom + V.G.ranges);
@@ -325,6 +326,21 @@ extern "C" int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *stat
     }
   }
   return rc;
+}
+
+extern "C" int dmgs_batch_counters(const DmgsBatch *b, int32_t P, const void *state,
+                                   size_t state_bytes, uint32_t *words, dmgs_stream_t stream) {
+  BatchLayout L;
+  RET_IF(make_layout(b, P, L));
+  if (!state || state_bytes < L.total) { set_error("batch: state too small"); return DMGS_ERR_STATE; }
+  if (!words) { set_error("batch: words is NULL"); return DMGS_ERR_ARG; }
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const char *st = static_cast<const char *>(state);
+  for (int v = 0; v < b->nviews; ++v)
+    DMGS_CUDA(cudaMemcpyAsync(words + 16 * v, st + L.v[v].geom + L.v[v].G.counters, CI_WORDS * 4,
+                              cudaMemcpyDeviceToHost, s));
+  DMGS_CUDA(cudaStreamSynchronize(s));
+  return DMGS_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -4,31 +4,38 @@
 // The reference pipeline (duplicateWithKeys -> radix sort of the 64-bit
 // (tile << 32 | depth_bits) instance keys -> identifyTileRanges) yields, per
 // tile, the covering Gaussians in depth order, ties in Gaussian-index order.
-// The same lists are produced here with work linear in the number of visible
-// Gaussians V plus the instances K:
+// The same lists are produced here with work linear in the visible Gaussians
+// V, their (Gaussian, tile row) pairs K1 and the instances K:
 //
-//   1. compact   the visible Gaussians in index order: (depth_bits, index)
+//   1. compact   the visible Gaussians in index order: (depth_bits, index);
 //   2. sort      them by depth bits with a stable LSD radix sort (4 x 8-bit
 //                digits) -> depth order, ties in index order;
 //   3. chunk     the sorted list is cut into C contiguous chunks of equal
-//                work (weight of a Gaussian: CHUNK_W_GAUSS + ceil(tiles/32),
-//                the warp iterations it costs below) -> chunk starts;
-//   4. count     each chunk counts its instances per tile -> count matrix,
-//                stored chunk-major [C][T] (coalesced in every kernel);
-//   5. scan      per tile over the chunks (the within-tile offset of every
-//                (tile, chunk) pair and the tile's total), then over the
-//                tile totals -> tile bases, the tile ranges and K;
-//   6. emit      one warp per chunk walks its Gaussians in depth order and
-//                appends each Gaussian index to the lists of the tiles it
-//                covers, its running slots in shared memory.
+//                work (weight of a Gaussian: CHUNK_W_GAUSS + its tile rows
+//                / 16 + its tiles / 64) -> chunk starts; the packed tile rectangles are laid
+//                out in sorted order on the way (srect);
+//   4. rows      each chunk counts its Gaussians per tile row (a 1D
+//                difference array) -> row counts [gy][C], scanned flat into
+//                the offsets of the ROW LISTS: per tile row, the Gaussians
+//                covering it in depth order, each entry {index, x0 | x1 << 16};
+//   5. segments  groups of C / S consecutive chunks (row segments) count
+//                their instances per tile (a 2D difference grid over a band
+//                of tile rows) -> segment counts [T][S], scanned flat into
+//                every (tile, segment)'s list offset, K and the tile ranges;
+//   6. emit      one warp per chunk appends its Gaussians to the row lists
+//                (the rows of its Gaussians spread over the lanes, ranks of
+//                equal rows by bitwise ballots); then one block per (tile row,
+//                segment) splits that segment of the row list into its
+//                tiles' lists through a shared-memory staging buffer (counts,
+//                offsets and ranks per sub-pass) and copies each tile's run
+//                out contiguously.
 //
-// Because every chunk appends in depth order and chunks are laid out in
-// depth order within every tile, each tile's list is exactly the reference's
-// sorted list.  Nothing of size K is read back or sorted; K is written once.
-// Near Gaussians cover thousands of tiles and sort together, so chunks of
-// equal Gaussian count would differ in work by an order of magnitude; equal
-// weight keeps one warp per chunk balanced.  The count matrix (C x T x 4 B,
-// 20 MB at 4056 tiles and 1216 chunks) stays in L2.
+// Every step keeps depth order within a tile: chunks and segments are depth
+// ranges laid out in depth order, and within a warp the instances are ranked
+// in Gaussian order.  Nothing of size K is sorted or read back; the K-sized
+// list is written once, in runs, and the row lists (K1 8-byte entries) are
+// written once and read once.  The row and segment offsets are small (gy x C
+// and T x S words).
 //
 // Every kernel bins several views at once (blockIdx.y = view, each view with
 // its own geometry state and sizes): a batch of views fills the GPU with one
@@ -187,7 +194,7 @@ __global__ void params_kernel(const BinViews bv) {
   counters[CI_NBR] = nbr;
   counters[CI_NRH] = 256u * nbr;
   counters[CI_C] = C;
-  counters[CI_NCM] = (uint32_t)(B.bd.gx * B.bd.gy) * C;
+  counters[CI_NRC] = (uint32_t)B.gy * C;
 }
 
 // ---- stable LSD radix sort of (depth_bits, index), 8 bits per pass -------
@@ -283,76 +290,75 @@ radix_scatter_kernel(const BinViews bv, int pass) {
   }
 }
 
-// ---- per-(tile, chunk) counts --------------------------------------------
+// ---- packed rectangles and shared helpers ---------------------------------
 
-__device__ __forceinline__ void unpack_rect(float4 f2, int &x0, int &y0, int &x1, int &y1) {
-  const uint32_t lo = __float_as_uint(f2.z), hi = __float_as_uint(f2.w);
-  x0 = lo & 0xffff; y0 = lo >> 16; x1 = hi & 0xffff; y1 = hi >> 16;
+// rect = (x0 | y0 << 16, x1 | y1 << 16): tiles [x0, x1) x [y0, y1)
+__device__ __forceinline__ void unpack_rect(uint2 r, int &x0, int &y0, int &x1, int &y1) {
+  x0 = (int)(r.x & 0xffffu); y0 = (int)(r.x >> 16); x1 = (int)(r.y & 0xffffu); y1 = (int)(r.y >> 16);
 }
 
-// Chunk segments of the per-tile offset scan: segment s = chunks
-// [s L, (s + 1) L), L = ceil(C / segs).
-__device__ __forceinline__ uint32_t seg_len(uint32_t C, uint32_t segs) { return (C + segs - 1) / segs; }
-
-// L2 eviction-priority hints: the instance list is written 4 bytes at a time
-// by many warps, so its lines should stay in L2 until complete (evict_last);
-// the count-matrix reads of the emission are used once (evict_first).
-__device__ __forceinline__ uint64_t l2_policy_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ void st_hint(uint32_t *ptr, uint32_t v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(ptr), "r"(v), "l"(pol) : "memory");
-}
-__device__ __forceinline__ uint32_t ld_hint(const uint32_t *ptr, uint64_t pol) {
-  uint32_t v;
-  asm volatile("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(ptr), "l"(pol));
+// Inclusive warp prefix sum.
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(FULL, v, o);
+    if (lane >= o) v += u;
+  }
   return v;
 }
 
-// Lane `lane` visits tiles lane, lane+32, ... of a rw-wide rectangle in
-// row-major order; row/column advance incrementally.  The divisions by rw
-// (numerators <= 32) use a per-rectangle multiplier M = floor(2^16 / rw) + 1
-// for rw <= 32, exact for numerators below 2^16 / rw (>= 2048), and M = 0
-// for wider rectangles (every quotient is 0).
-__device__ __forceinline__ uint32_t walk_magic(int rw) {
-  return rw <= 32 ? 65536u / (uint32_t)rw + 1u : 0u;
+// Balanced expansion: lane i holds an item with n_i instances (exclusive
+// prefix excl_i over the lanes); instance q of the group (item-major order)
+// belongs to the largest lane o with excl_o <= q.  Five shuffles.
+__device__ __forceinline__ int expansion_owner(int excl, int q) {
+  int o = 0;
+#pragma unroll
+  for (int st = 16; st > 0; st >>= 1) {
+    const int e = __shfl_sync(FULL, excl, o + st);
+    if (e <= q) o += st;
+  }
+  return o;
 }
 
-struct RectWalk {
-  int row, col, dr, dc, rw;
-  __device__ __forceinline__ RectWalk(int lane, int rw_, uint32_t M) : rw(rw_) {
-    row = (int)(((uint32_t)lane * M) >> 16);
-    col = lane - row * rw;
-    dr = (int)((32u * M) >> 16);
-    dc = 32 - dr * rw;
+// Lanes of `act` whose value v (< 2^nbits) equals this lane's: one ballot
+// per bit.
+__device__ __forceinline__ unsigned value_peers(int v, int nbits, unsigned act) {
+  unsigned m = act;
+  for (int b = 0; b < nbits; ++b) {
+    const bool bit = (v >> b) & 1;
+    const unsigned bb = __ballot_sync(FULL, bit);
+    m &= bit ? bb : ~bb;
   }
-  __device__ __forceinline__ void next() {
-    row += dr; col += dc;
-    if (col >= rw) { col -= rw; ++row; }
-  }
-};
+  return m;
+}
 
-// ---- equal-work chunks of the depth-sorted list ---------------------------
+__device__ __forceinline__ int bits_for(int n) { return n > 1 ? 32 - __clz(n - 1) : 1; }
 
-// Weight of sorted position s: the warp iterations its Gaussian costs the
-// count and emit kernels (a fixed part plus one per 32 covered tiles).
+// First chunk of row segment sg (of S) when the view has C chunks.
+__device__ __forceinline__ uint32_t seg_chunk(int sg, uint32_t C, int S) {
+  return (uint32_t)((unsigned long long)sg * C / (unsigned)S);
+}
+
+// ---- step 3: equal-work chunks of the depth-sorted list --------------------
+
+// Weight of sorted position s: the work its Gaussian costs the binning
+// kernels (a fixed part, one per 16 covered tile rows for the row lists and
+// one per 64 covered tiles for the tile lists), so that chunks and the row
+// segments built from them carry similar numbers of instances; the packed
+// rectangle is stored in sorted order for every later pass.
 __global__ void __launch_bounds__(256)
 chunk_weight_kernel(const BinViews bv) {
   const BinView &B = bv.v[blockIdx.y];
   const uint32_t V = B.counters[CI_V];
   const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= V) return;
+  const float4 f2 = B.feat[3 * B.v0[s] + 2];
+  const uint2 r = make_uint2(__float_as_uint(f2.z), __float_as_uint(f2.w));
+  B.srect[s] = r;
   int x0, y0, x1, y1;
-  unpack_rect(B.feat[3 * B.v0[s] + 2], x0, y0, x1, y1);
-  const uint32_t area = (uint32_t)((x1 - x0) * (y1 - y0));
-  B.k1[s] = CHUNK_W_GAUSS + (area + 31u) / 32u;  // the sorted keys end in k0: k1 is free
+  unpack_rect(r, x0, y0, x1, y1);
+  const uint32_t rows = (uint32_t)(y1 - y0), area = rows * (uint32_t)(x1 - x0);
+  B.k1[s] = CHUNK_W_GAUSS + (rows + 15u) / 16u + (area + 63u) / 64u;  // k1 is free: the sorted keys end in k0
 }
 
 // From the exclusive prefix of the weights: chunk c = the positions whose
@@ -375,255 +381,104 @@ chunk_bounds_kernel(const BinViews bv) {
     for (uint32_t c = cs + 1; c <= C; ++c) cstart[c] = V;
 }
 
-// ---- counting and emission: one warp per (chunk, band of tile rows) -------
-// A band is R consecutive rows of tiles (R * gx <= ~1024 tiles).
+// ---- step 4: row counts, one warp per chunk ---------------------------------
 
-// Per-(tile, chunk) counts of one (chunk, band of tile rows) without walking
-// the instances: every Gaussian whose rectangle meets the band adds +1 / -1
-// at the four corners of its rectangle clipped to the band, in a 2D
-// difference grid of (R + 1) x (gx + 1) cells (shared-memory atomics, the 32
-// Gaussians of a group in parallel); inclusive prefix sums along the rows and
-// then the columns turn it into the counts of the band's tiles.  Work per
-// warp: 4 updates per Gaussian plus 2 passes over the band's tiles, instead
-// of one visit per instance.  Indices and rectangles are loaded one group
-// ahead.
+// Gaussians of chunk c per tile row: +1 at the first row and -1 after the
+// last of every rectangle in a difference array over the rows, then a
+// prefix sum.  Written row-major [gy][C] so that one flat exclusive scan
+// gives every (row, chunk)'s offset in the concatenated row lists.
 __global__ void __launch_bounds__(32)
-count_kernel(const BinViews bv) {
-  extern __shared__ int dgrid[];
-  const BinView &Bv = bv.v[blockIdx.y];
-  const Bands bd = Bv.bd;
-  const uint32_t C = Bv.counters[CI_C];
-  const uint32_t c = blockIdx.x / (uint32_t)bd.nb;
-  const int b = (int)(blockIdx.x - c * (uint32_t)bd.nb);
+row_count_kernel(const BinViews bv) {
+  extern __shared__ int rdiff[];  // gy + 1
+  const BinView &B = bv.v[blockIdx.y];
+  const uint32_t C = B.counters[CI_C];
+  const uint32_t c = blockIdx.x;
   if (c >= C) return;
-  const int lane = threadIdx.x;
-  const int ys = b * bd.R, ye = min(bd.gy, ys + bd.R), R = ye - ys;
-  const int W = bd.gx + 1;
-  for (int i = lane; i < (R + 1) * W; i += 32) dgrid[i] = 0;
+  const int lane = threadIdx.x, gy = B.gy;
+  for (int i = lane; i <= gy; i += 32) rdiff[i] = 0;
   __syncwarp();
-  const uint32_t s0 = Bv.cstart[c], s1 = Bv.cstart[c + 1];
-  const float4 none = make_float4(0.f, 0.f, 0.f, 0.f);
-  bool vA = s0 + lane < s1;
-  float4 rA = vA ? Bv.feat[3 * Bv.v0[s0 + lane] + 2] : none;
-  for (uint32_t g0 = s0; g0 < s1; g0 += 32) {
-    const float4 r = rA;
-    const bool v = vA;
-    vA = g0 + 32 + lane < s1;
-    rA = vA ? Bv.feat[3 * Bv.v0[g0 + 32 + lane] + 2] : none;
+  const uint32_t s0 = B.cstart[c], s1 = B.cstart[c + 1];
+  for (uint32_t s = s0 + lane; s < s1; s += 32) {
     int x0, y0, x1, y1;
-    unpack_rect(r, x0, y0, x1, y1);
+    unpack_rect(B.srect[s], x0, y0, x1, y1);
+    if (x0 < x1 && y0 < y1) {
+      atomicAdd(&rdiff[y0], 1);
+      atomicAdd(&rdiff[y1], -1);
+    }
+  }
+  __syncwarp();
+  int carry = 0;
+  for (int rb = 0; rb < gy; rb += 32) {
+    const int r = rb + lane;
+    const int v = warp_incl_scan(r < gy ? rdiff[r] : 0, lane) + carry;
+    if (r < gy) B.rcnt[(size_t)r * C + c] = (uint32_t)v;
+    carry = __shfl_sync(FULL, v, 31);
+  }
+}
+
+// ---- step 5: segment counts per tile ---------------------------------------
+
+// Instances of every tile of a band of tile rows from row segment sg (the
+// Gaussians of chunks [sg C / S, (sg + 1) C / S)): every rectangle clipped to
+// the band adds +1 / -1 at its four corners in a 2D difference grid of
+// (R + 1) x (gx + 1) cells (shared-memory atomics from every warp of the
+// block); prefix sums along the rows, then the columns, give the counts,
+// written to cnt2[t * S + sg] — tile-major, so one flat exclusive scan gives
+// every (tile, segment)'s list offset.
+__global__ void __launch_bounds__(256)
+seg_count_kernel(const BinViews bv, int S) {
+  extern __shared__ int dg[];
+  const BinView &B = bv.v[blockIdx.y];
+  if ((int)blockIdx.x >= S * B.nb) return;  // block-uniform
+  const int sg = blockIdx.x / B.nb, b = blockIdx.x - sg * B.nb;
+  const int gx = B.gx, ys = b * B.R, ye = min(B.gy, ys + B.R), R = ye - ys, Wd = gx + 1;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  for (int i = tid; i < (R + 1) * Wd; i += 256) dg[i] = 0;
+  __syncthreads();
+  const uint32_t C = B.counters[CI_C];
+  uint32_t s0 = 0, s1 = 0;
+  if (C > 0) {
+    s0 = B.cstart[seg_chunk(sg, C, S)];
+    s1 = B.cstart[seg_chunk(sg + 1, C, S)];
+  }
+  for (uint32_t s = s0 + tid; s < s1; s += 256) {
+    int x0, y0, x1, y1;
+    unpack_rect(B.srect[s], x0, y0, x1, y1);
     const int cy0 = max(y0, ys) - ys, cy1 = min(y1, ye) - ys;
-    if (v && cy0 < cy1 && x0 < x1) {
-      atomicAdd(&dgrid[cy0 * W + x0], 1);
-      atomicAdd(&dgrid[cy0 * W + x1], -1);
-      atomicAdd(&dgrid[cy1 * W + x0], -1);
-      atomicAdd(&dgrid[cy1 * W + x1], 1);
+    if (cy0 < cy1 && x0 < x1) {
+      atomicAdd(&dg[cy0 * Wd + x0], 1);
+      atomicAdd(&dg[cy0 * Wd + x1], -1);
+      atomicAdd(&dg[cy1 * Wd + x0], -1);
+      atomicAdd(&dg[cy1 * Wd + x1], 1);
     }
   }
-  __syncwarp();
-  for (int row = 0; row < R; ++row) {  // inclusive prefix along each row, 32 columns at a time
+  __syncthreads();
+  for (int row = w; row < R; row += 8) {  // inclusive prefix along each row
     int carry = 0;
-    for (int xb = 0; xb < bd.gx; xb += 32) {
+    for (int xb = 0; xb < gx; xb += 32) {
       const int x = xb + lane;
-      int val = x < bd.gx ? dgrid[row * W + x] : 0;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(FULL, val, o);
-        if (lane >= o) val += u;
-      }
-      val += carry;
-      if (x < bd.gx) dgrid[row * W + x] = val;
-      carry = __shfl_sync(FULL, val, 31);
+      const int v = warp_incl_scan(x < gx ? dg[row * Wd + x] : 0, lane) + carry;
+      if (x < gx) dg[row * Wd + x] = v;
+      carry = __shfl_sync(FULL, v, 31);
     }
   }
-  __syncwarp();
-  for (int x = lane; x < bd.gx; x += 32) {  // inclusive prefix along each column -> counts
+  __syncthreads();
+  for (int x = tid; x < gx; x += 256) {  // inclusive prefix along each column -> counts
     int run = 0;
     for (int row = 0; row < R; ++row) {
-      run += dgrid[row * W + x];
-      Bv.cmat[(size_t)c * (bd.gx * bd.gy) + (ys + row) * bd.gx + x] = (uint32_t)run;
+      run += dg[row * Wd + x];
+      B.cnt2[((size_t)(ys + row) * gx + x) * S + sg] = (uint32_t)run;
     }
   }
 }
 
-// Emission.  The band's running slots live in shared memory (R * gx words),
-// starting at the first list position of each (tile, this chunk): tile base
-// + the counts of the earlier chunk segments + the offset within this
-// chunk's segment.  The warp walks its chunk's Gaussians in depth order, 32
-// at a time (lane i holds Gaussian g0 + i; indices and rectangles loaded two
-// and one groups ahead), selects by ballot the ones whose rectangle meets the
-// band and visits each one's tiles within the band, its lanes spread over
-// them, appending the Gaussian index.  One Gaussian covers each tile once, so
-// within a Gaussian the lanes touch distinct slots and a plain
-// read/modify/write suffices; __syncwarp orders consecutive Gaussians.
-__global__ void __launch_bounds__(32)
-emit_kernel(const BinViews bv) {
-  extern __shared__ uint32_t slot[];
-  const BinView &Bv = bv.v[blockIdx.y];
-  const Bands bd = Bv.bd;
-  const float4 *__restrict__ feat = Bv.feat;
-  const uint32_t *__restrict__ order = Bv.v0;
-  uint32_t *__restrict__ counters = Bv.counters;
-  uint32_t *__restrict__ cmat = Bv.cmat;
-  uint32_t *__restrict__ point_list = Bv.point_list;
-  const uint32_t K_alloc = Bv.K_alloc;
-  const uint32_t C = counters[CI_C];
-  const uint32_t c = blockIdx.x / (uint32_t)bd.nb;
-  const int b = (int)(blockIdx.x - c * (uint32_t)bd.nb);
-  if (c >= C) return;
-  const int lane = threadIdx.x;
-  const int ys = b * bd.R, ye = min(bd.gy, ys + bd.R);
-  const int t0 = ys * bd.gx, nt = (ye - ys) * bd.gx;
-  const uint32_t s0 = Bv.cstart[c], s1 = Bv.cstart[c + 1];
-  const uint64_t keep = l2_policy_last();
-  // an overflowed view (instances above the list capacity) emits nothing
-  if (s0 >= s1 || (counters[CI_STATUS] & ST_OVERFLOW)) return;
-  {
-    const uint64_t once = l2_policy_first();
-    const int T = bd.gx * bd.gy;
-    const uint32_t *off = cmat + (size_t)c * T + t0;
-    const uint32_t *tb = Bv.tbase + t0;
-    const uint32_t *sp = Bv.segpre + (size_t)(c / seg_len(C, CHUNK_SEGS)) * T + t0;
-    int i = lane;
-    for (; i + 96 < nt; i += 128) {
-      uint32_t a[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        a[u] = ld_hint(off + i + 32 * u, once) + tb[i + 32 * u] + sp[i + 32 * u];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) slot[i + 32 * u] = a[u];
-    }
-    for (; i < nt; i += 32) slot[i] = ld_hint(off + i, once) + tb[i] + sp[i];
-  }
-  __syncwarp();
-  bool bad = false;
-  const float4 none = make_float4(0.f, 0.f, 0.f, 0.f);
-  bool vA = s0 + lane < s1, vB = s0 + 32 + lane < s1;
-  uint32_t idA = vA ? order[s0 + lane] : 0u;
-  uint32_t idB = vB ? order[s0 + 32 + lane] : 0u;
-  float4 rA = vA ? feat[3 * idA + 2] : none;
-  for (uint32_t g0 = s0; g0 < s1; g0 += 32) {
-    const uint32_t id = idA;
-    const float4 r = rA;
-    const bool v = vA;
-    idA = idB; vA = vB;
-    rA = vA ? feat[3 * idA + 2] : none;
-    vB = g0 + 64 + lane < s1;
-    idB = vB ? order[g0 + 64 + lane] : 0u;
-    int x0, y0, x1, y1;
-    unpack_rect(r, x0, y0, x1, y1);
-    const int cy0 = max(y0, ys), cy1 = min(y1, ye);
-    const bool hit = v && cy0 < cy1 && x0 < x1;
-    unsigned m = __ballot_sync(FULL, hit);
-    const uint32_t xy = hit ? ((uint32_t)x0 | ((uint32_t)(cy0 - ys) << 16)) : 0u;
-    const uint32_t wa = hit ? ((uint32_t)(x1 - x0) | ((uint32_t)((x1 - x0) * (cy1 - cy0)) << 16)) : 1u;
-    const uint32_t mg = walk_magic(hit ? x1 - x0 : 1);  // lane-parallel, once per group
-    while (m) {
-      const int i = __ffs(m) - 1;
-      m &= m - 1;
-      const uint32_t xyi = __shfl_sync(FULL, xy, i), wai = __shfl_sync(FULL, wa, i);
-      const uint32_t mgi = __shfl_sync(FULL, mg, i);
-      const uint32_t idi = __shfl_sync(FULL, id, i);
-      const int bx = (int)(xyi & 0xffffu), by = (int)(xyi >> 16);
-      const int rw = (int)(wai & 0xffffu), area = (int)(wai >> 16);
-      RectWalk it(lane, rw, mgi);
-      const int o = by * bd.gx + bx;
-      int j = lane;
-      // four, then two tiles per step (distinct slots: independent read/modify/writes)
-      for (; j + 96 < area; j += 128) {
-        int a[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          a[u] = o + it.row * bd.gx + it.col;
-          it.next();
-        }
-        uint32_t p[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) p[u] = slot[a[u]];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) slot[a[u]] = p[u] + 1u;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          if (p[u] < K_alloc) st_hint(point_list + p[u], idi, keep); else bad = true;
-        }
-      }
-      for (; j + 32 < area; j += 64) {
-        const int a0 = o + it.row * bd.gx + it.col;
-        it.next();
-        const int a1 = o + it.row * bd.gx + it.col;
-        it.next();
-        const uint32_t p0 = slot[a0], p1 = slot[a1];
-        slot[a0] = p0 + 1u;
-        slot[a1] = p1 + 1u;
-        if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
-        if (p1 < K_alloc) st_hint(point_list + p1, idi, keep); else bad = true;
-      }
-      if (j < area) {
-        const int a0 = o + it.row * bd.gx + it.col;
-        const uint32_t p0 = slot[a0];
-        slot[a0] = p0 + 1u;
-        if (p0 < K_alloc) st_hint(point_list + p0, idi, keep); else bad = true;
-      }
-      __syncwarp();
-    }
-  }
-  if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
-}
-
-// Within-tile offsets of every (tile, chunk).  A block takes 32 tiles (the
-// lanes: chunk-major storage makes each step a coalesced 128-byte row
-// segment) and CHUNK_SEGS contiguous chunk segments (the warps), so a view
-// of 4,056 tiles keeps ~4,000 warps busy.  Each thread writes the exclusive
-// prefix of its segment in place; the segment totals give, per tile,
-// segpre[s][t] (the counts of the earlier segments) and the tile total
-// tbase[t].  Offset of (t, c) = scanned tbase[t] + segpre[seg(c)][t] +
-// cmat[c][t].
-__global__ void __launch_bounds__(32 * CHUNK_SEGS)
-tile_scan_kernel(const BinViews bv) {
-  __shared__ uint32_t segsum[CHUNK_SEGS][32];
+// Tile ranges from the scanned segment counts: tile t starts at its first
+// segment's offset.  When the instances exceed the list capacity
+// (capacity-bounded callers), every range is left empty and the overflow bit
+// is set, so no kernel reads past the list buffer.
+__global__ void ranges_kernel(const BinViews bv, int S) {
   const BinView &B = bv.v[blockIdx.y];
-  const int T = B.bd.gx * B.bd.gy;
-  if ((int)blockIdx.x * 32 >= T) return;  // block-uniform
-  const int lane = threadIdx.x & 31, seg = threadIdx.x >> 5;
-  const int t = blockIdx.x * 32 + lane;
-  const uint32_t C = B.counters[CI_C], L = seg_len(C, CHUNK_SEGS);
-  const uint32_t c0 = min(C, seg * L), c1 = min(C, c0 + L);
-  uint32_t *col = B.cmat + t;
-  uint32_t run = 0;
-  if (t < T) {
-    uint32_t c = c0;
-    for (; c + 16 <= c1; c += 16) {
-      uint32_t x[16];
-#pragma unroll
-      for (int u = 0; u < 16; ++u) x[u] = col[(size_t)(c + u) * T];
-#pragma unroll
-      for (int u = 0; u < 16; ++u) {
-        col[(size_t)(c + u) * T] = run;
-        run += x[u];
-      }
-    }
-    for (; c < c1; ++c) {
-      const uint32_t x = col[(size_t)c * T];
-      col[(size_t)c * T] = run;
-      run += x;
-    }
-  }
-  segsum[seg][lane] = run;
-  __syncthreads();
-  if (t < T) {
-    uint32_t pre = 0;
-    for (int q = 0; q < seg; ++q) pre += segsum[q][lane];
-    B.segpre[(size_t)seg * T + t] = pre;
-    if (seg == CHUNK_SEGS - 1) B.tbase[t] = pre + run;
-  }
-}
-
-// Tile ranges from the scanned tile bases.  When the instances exceed the
-// list capacity (capacity-bounded callers), every range is left empty and
-// the overflow bit is set, so no kernel reads past the list buffer.
-__global__ void ranges_kernel(const BinViews bv) {
-  const BinView &B = bv.v[blockIdx.y];
-  const int T = B.bd.gx * B.bd.gy;
+  const int T = B.gx * B.gy;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   uint32_t *counters = B.counters;
@@ -632,12 +487,293 @@ __global__ void ranges_kernel(const BinViews bv) {
   if (over && t == 0) atomicOr(&counters[CI_STATUS], ST_OVERFLOW);
   uint2 r = make_uint2(0u, 0u);
   if (B.P > 0 && !over) {
-    const uint32_t a = B.tbase[t];
-    const uint32_t e = (t + 1 < T) ? B.tbase[t + 1] : K;
+    const uint32_t a = B.cnt2[(size_t)t * S];
+    const uint32_t e = (t + 1 < T) ? B.cnt2[(size_t)(t + 1) * S] : K;
     if (e > a) r = make_uint2(a, e);
     atomicMax(&counters[CI_MAXLIST], e - a);
   }
   B.ranges[t] = r;
+}
+
+// ---- step 6a: row lists, one warp per chunk --------------------------------
+
+// The chunk's Gaussians are taken 32 at a time (depth order); the (Gaussian,
+// row) pairs of the group are spread over the lanes in Gaussian-major order
+// (balanced expansion), so pairs of one row rank by their Gaussian's depth
+// order: rank = lanes of lower index in the same row (a ballot per bit), then the row's
+// running slot (shared memory) advances by the row's pairs.
+__global__ void __launch_bounds__(32)
+row_emit_kernel(const BinViews bv) {
+  extern __shared__ uint32_t rcur[];  // gy running slots
+  const BinView &B = bv.v[blockIdx.y];
+  uint32_t *counters = B.counters;
+  const uint32_t C = counters[CI_C];
+  const uint32_t c = blockIdx.x;
+  if (c >= C || (counters[CI_STATUS] & ST_OVERFLOW)) return;
+  const int lane = threadIdx.x, gy = B.gy, nbits = bits_for(gy);
+  for (int r = lane; r < gy; r += 32) rcur[r] = B.rcnt[(size_t)r * C + c];
+  __syncwarp();
+  const uint32_t s0 = B.cstart[c], s1 = B.cstart[c + 1];
+  const uint32_t cap = B.K_alloc;
+  const uint2 *__restrict__ srect = B.srect;
+  const uint32_t *__restrict__ order = B.v0;
+  uint2 *__restrict__ rowlist = B.rowlist;
+  const unsigned lt = lanemask_lt();
+  bool bad = false;
+  for (uint32_t g0 = s0; g0 < s1; g0 += 32) {
+    const uint32_t s = g0 + lane;
+    const bool v = s < s1;
+    const uint2 rr = v ? srect[s] : make_uint2(0u, 0u);
+    const uint32_t id = v ? order[s] : 0u;
+    int x0, y0, x1, y1;
+    unpack_rect(rr, x0, y0, x1, y1);
+    const int n = (x0 < x1 && y0 < y1) ? y1 - y0 : 0;
+    const int incl = warp_incl_scan(n, lane);
+    const int total = __shfl_sync(FULL, incl, 31);
+    const int excl = incl - n;
+    const uint32_t xr = (rr.x & 0xffffu) | (rr.y << 16);
+    for (int base = 0; base < total; base += 32) {
+      const int q = base + lane;
+      const bool act = q < total;
+      const int o = expansion_owner(excl, q);
+      const int row = __shfl_sync(FULL, y0, o) + (q - __shfl_sync(FULL, excl, o));
+      const uint32_t ido = __shfl_sync(FULL, id, o);
+      const uint32_t xro = __shfl_sync(FULL, xr, o);
+      const unsigned amask = total - base >= 32 ? FULL : (1u << (total - base)) - 1u;
+      const unsigned peers = value_peers(act ? row : 0, nbits, amask);
+      const uint32_t p = act ? rcur[row] + __popc(peers & lt) : 0u;
+      __syncwarp();
+      if (act) {
+        if (p < cap) rowlist[p] = make_uint2(ido, xro); else bad = true;
+        if ((peers & lt) == 0u) rcur[row] += __popc(peers);
+      }
+      __syncwarp();
+    }
+  }
+  if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
+}
+
+// ---- step 6b: tile lists, one block per (tile row, row piece, segment) -----
+
+constexpr int TE_WARPS = 8;
+constexpr int TE_THREADS = 32 * TE_WARPS;
+constexpr int STAGE_CAP = 8192;    // staged instances per sub-pass
+constexpr int TE_PER = 4;          // row-list entries per thread considered for a sub-pass
+constexpr int TE_ENTRIES = TE_THREADS * TE_PER;
+
+__host__ __device__ inline size_t tile_emit_smem_words(int nx) {
+  return (size_t)nx + (nx + 1) + (size_t)TE_WARPS * (nx + 1) + STAGE_CAP + TE_WARPS +
+         (TE_WARPS + 1);
+}
+
+__device__ __forceinline__ int block_sum_te(int v, int *red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  int t = 0;
+#pragma unroll
+  for (int i = 0; i < TE_WARPS; ++i) t += red[i];
+  return t;
+}
+
+// The block's entries (one segment of one row list, depth order) are split
+// into sub-passes whose instances fit the staging buffer; per sub-pass, each
+// warp takes a contiguous slice of entries (about equal instance counts):
+// (A) per-warp counts per tile (1D difference array); (B) per tile the
+// exclusive prefix over the warps and the tiles' staging offsets, giving
+// every warp an absolute staging cursor per tile; (C) the slice's entries in
+// order, one at a time, each writing its Gaussian index at the cursor of
+// every tile it covers (tile x always by lane x % 32, so no two lanes share
+// a cursor and no ranks are needed); (D) each tile's staged run copied to
+// the tile's list at its running position (coalesced).
+__global__ void __launch_bounds__(TE_THREADS)
+tile_emit_kernel(const BinViews bv, int S) {
+  extern __shared__ uint32_t te[];
+  const BinView &B = bv.v[blockIdx.y];
+  const int sg = blockIdx.x % S, rest = blockIdx.x / S;
+  const int xs = rest % B.nxs, r = rest / B.nxs;
+  if (r >= B.gy) return;  // block-uniform
+  uint32_t *counters = B.counters;
+  const uint32_t C = counters[CI_C];
+  if (C == 0 || (counters[CI_STATUS] & ST_OVERFLOW)) return;
+  const uint32_t f0 = seg_chunk(sg, C, S), f1 = seg_chunk(sg + 1, C, S);
+  if (f0 >= f1) return;
+  const uint32_t e0 = B.rcnt[(size_t)r * C + f0];
+  const uint32_t e1 = f1 < C ? B.rcnt[(size_t)r * C + f1]
+                             : (r + 1 < B.gy ? B.rcnt[(size_t)(r + 1) * C] : counters[CI_K1]);
+  if (e0 >= e1) return;
+  const int xa = xs * XSEG, nx = min(B.gx - xa, XSEG), nbits = bits_for(nx);
+  uint32_t *tcur = te;                                   // [nx] running list positions
+  uint32_t *soff = tcur + nx;                            // [nx + 1] staging offsets
+  int *wc = reinterpret_cast<int *>(soff + nx + 1);      // [TE_WARPS][nx + 1] counts / cursors
+  uint32_t *stage = reinterpret_cast<uint32_t *>(wc + TE_WARPS * (nx + 1));  // [STAGE_CAP]
+  int *red = reinterpret_cast<int *>(stage + STAGE_CAP);  // [TE_WARPS]
+  uint32_t *bnd = reinterpret_cast<uint32_t *>(red + TE_WARPS);  // [TE_WARPS + 1] slice starts
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const unsigned lt = lanemask_lt();
+  const uint2 *__restrict__ rl = B.rowlist;
+  uint32_t *__restrict__ out = B.point_list;
+  const uint32_t cap = B.K_alloc;
+  for (int x = tid; x < nx; x += TE_THREADS)
+    tcur[x] = B.cnt2[((size_t)r * B.gx + xa + x) * S + sg];
+  int *wcw = wc + w * (nx + 1);
+  bool bad = false;
+  auto clip = [&](uint2 en, int &a, int &b) {
+    a = max((int)(en.y & 0xffffu), xa) - xa;
+    b = min((int)(en.y >> 16), xa + nx) - xa;
+  };
+  for (uint32_t e = e0; e < e1;) {
+    // sub-pass: the longest run of entries whose instances fit the staging
+    // buffer (block scan of the clipped widths of up to TE_ENTRIES entries),
+    // cut into one contiguous slice per warp at equal instance counts
+    const uint32_t navail = min(e1 - e, (uint32_t)TE_ENTRIES);
+    int wd[TE_PER];
+    int tsum = 0;
+#pragma unroll
+    for (int k = 0; k < TE_PER; ++k) {
+      const uint32_t i = (uint32_t)tid * TE_PER + k;
+      int a = 0, b = 0;
+      if (i < navail) clip(rl[e + i], a, b);
+      wd[k] = max(b - a, 0);
+      tsum += wd[k];
+    }
+    const int tin = warp_incl_scan(tsum, lane);
+    __syncthreads();  // red[] and bnd[] of the previous sub-pass are no longer read
+    if (lane == 31) red[w] = tin;
+    if (tid <= TE_WARPS) bnd[tid] = 0xffffffffu;
+    __syncthreads();
+    int wbase = 0, itot = 0;
+#pragma unroll
+    for (int i = 0; i < TE_WARPS; ++i) {
+      wbase += i < w ? red[i] : 0;
+      itot += red[i];
+    }
+    int run = wbase + tin - tsum;  // instances before this thread's entries
+    int fit = 0;
+#pragma unroll
+    for (int k = 0; k < TE_PER; ++k) {
+      run += wd[k];
+      fit += (run <= STAGE_CAP && (uint32_t)tid * TE_PER + k < navail) ? 1 : 0;
+    }
+    const uint32_t En = max(1u, (uint32_t)block_sum_te(fit, red));
+    const int I = min(itot, STAGE_CAP);  // instances of the first En entries (all of them when they fit)
+    {
+      int ex = wbase + tin - tsum;
+#pragma unroll
+      for (int k = 0; k < TE_PER; ++k) {
+        const uint32_t i = (uint32_t)tid * TE_PER + k;
+        if (i < En && I > 0) {
+          const int wi = (int)((long long)ex * TE_WARPS / I);
+          atomicMin(&bnd[min(wi, TE_WARPS - 1)], i);
+        }
+        ex += wd[k];
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {  // slice starts: first entry whose instances begin in the warp's share
+      uint32_t m = En;
+      bnd[TE_WARPS] = En;
+      for (int i = TE_WARPS - 1; i >= 1; --i) {
+        m = min(m, bnd[i]);
+        bnd[i] = m;
+      }
+      bnd[0] = 0;
+    }
+    __syncthreads();
+    const uint32_t sa = e + bnd[w], sb = e + bnd[w + 1];
+    // (A) this warp's counts per tile
+    for (int i = lane; i <= nx; i += 32) wcw[i] = 0;
+    __syncwarp();
+    for (uint32_t i = sa + lane; i < sb; i += 32) {
+      int a, b;
+      clip(rl[i], a, b);
+      if (a < b) {
+        atomicAdd(&wcw[a], 1);
+        atomicAdd(&wcw[b], -1);
+      }
+    }
+    __syncwarp();
+    {
+      int carry = 0;
+      for (int xb = 0; xb < nx; xb += 32) {
+        const int x = xb + lane;
+        const int v = warp_incl_scan(x < nx ? wcw[x] : 0, lane) + carry;
+        if (x < nx) wcw[x] = v;
+        carry = __shfl_sync(FULL, v, 31);
+      }
+    }
+    __syncthreads();
+    // (B) per tile: prefix over the warps, tile totals, staging offsets
+    for (int x = tid; x < nx; x += TE_THREADS) {
+      int run = 0;
+#pragma unroll
+      for (int w2 = 0; w2 < TE_WARPS; ++w2) {
+        const int cw = wc[w2 * (nx + 1) + x];
+        wc[w2 * (nx + 1) + x] = run;
+        run += cw;
+      }
+      soff[x] = (uint32_t)run;
+    }
+    __syncthreads();
+    if (w == 0) {  // exclusive scan of the tile totals (nx <= XSEG)
+      uint32_t carry = 0;
+      for (int xb = 0; xb < nx; xb += 32) {
+        const int x = xb + lane;
+        const int t = x < nx ? (int)soff[x] : 0;
+        const int incl = warp_incl_scan(t, lane);
+        if (x < nx) soff[x] = carry + (uint32_t)(incl - t);
+        carry += (uint32_t)__shfl_sync(FULL, incl, 31);
+      }
+      if (lane == 0) soff[nx] = carry;
+    }
+    __syncthreads();
+    for (int x = tid; x < nx; x += TE_THREADS) {  // absolute staging cursors of every warp
+      const int o = (int)soff[x];
+#pragma unroll
+      for (int w2 = 0; w2 < TE_WARPS; ++w2) wc[w2 * (nx + 1) + x] += o;
+    }
+    __syncthreads();
+    // (C) stage the slice's instances, entries in order, one at a time: tile
+    // x is always handled by lane x % 32, so a tile's cursor is only ever
+    // touched by one lane and entries land in the order they come
+    for (uint32_t g0 = sa; g0 < sb; g0 += 32) {
+      const uint32_t i = g0 + lane;
+      const uint2 en = i < sb ? rl[i] : make_uint2(0u, 0u);
+      int a = 0, b = 0;
+      if (i < sb) clip(en, a, b);
+      unsigned m = __ballot_sync(FULL, a < b);
+      while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1;
+        const int aj = __shfl_sync(FULL, a, j), bj = __shfl_sync(FULL, b, j);
+        const uint32_t idj = __shfl_sync(FULL, en.x, j);
+        for (int xb = aj & ~31; xb < bj; xb += 32) {
+          const int x = xb + lane;
+          if (x >= aj && x < bj) {
+            const uint32_t p = (uint32_t)wcw[x];
+            if (p < STAGE_CAP) stage[p] = idj; else bad = true;
+            wcw[x] = (int)p + 1;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // (D) copy each tile's staged run to its list
+    for (int x = w; x < nx; x += TE_WARPS) {
+      const uint32_t a = soff[x], n = soff[x + 1] - a, dst = tcur[x];
+      for (uint32_t j = lane; j < n; j += 32) {
+        if (dst + j < cap) out[dst + j] = stage[a + j]; else bad = true;
+      }
+      __syncwarp();
+      if (lane == 0) tcur[x] = dst + n;
+    }
+    __syncthreads();
+    e += En;
+  }
+  if (bad) atomicOr(&counters[CI_STATUS], ST_BOUNDS);
 }
 
 // Debug view: sorted keys in the reference's form (tile << 32 | depth_bits).
@@ -659,55 +795,40 @@ __global__ void debug_keys_kernel(int T, const uint2 *__restrict__ ranges,
 
 namespace {
 
-constexpr int BAND_TILES = 1024;  // target slots per band (4 KB of shared memory)
-
-uint32_t count_grid_bytes(const Bands &bd) { return (uint32_t)((bd.R + 1) * (bd.gx + 1) * 4); }
-
-// Bands of tile rows and the chunk count for a gx x gy grid: enough
-// (chunk, band) warps to fill the GPU in one wave, each band's slots small
-// enough for many resident warps per SM.
-struct BandPlan {
-  Bands bd;
-  uint32_t cmax;
-  size_t smem;
-};
-
-int band_plan(int gx, int gy, BandPlan &pl) {
-  pl.bd.gx = gx;
-  pl.bd.gy = gy;
-  pl.bd.R = std::max(1, std::min(gy, BAND_TILES / std::max(gx, 1)));
-  pl.bd.nb = (gy + pl.bd.R - 1) / pl.bd.R;
-  pl.smem = (size_t)pl.bd.R * gx * 4;
-  if (pl.smem > 220 * 1024 || count_grid_bytes(pl.bd) > 220 * 1024) {
-    dmgs_host::set_error("image too large: a row of %d tiles exceeds the binning kernels' shared memory", gx);
-    return DMGS_ERR_ARG;
-  }
-  int dev = 0;
-  DMGS_CUDA(cudaGetDevice(&dev));
-  thread_local int cached_dev = -1;
-  thread_local size_t cached_smem = 0;
-  thread_local int cached_resident = 0;
-  if (dev != cached_dev || pl.smem != cached_smem) {
-    const size_t csm = count_grid_bytes(pl.bd);
-    // raised only (a launch uses its largest view), shared by every host thread
-    const size_t need = std::max(pl.smem, csm);
-    if (int r = dmgs_host::raise_smem_limit((const void *)count_kernel, need)) return r;
-    if (int r = dmgs_host::raise_smem_limit((const void *)emit_kernel, need)) return r;
-    int sms = 0, a = 0, b = 0;
-    DMGS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, count_kernel, 32, csm));
-    DMGS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, emit_kernel, 32, pl.smem));
-    cached_dev = dev;
-    cached_smem = pl.smem;
-    cached_resident = std::max(1, std::min(a, b)) * sms;
-  }
-  pl.cmax = (uint32_t)std::max(1, std::min(CHUNK_COUNT_MAX, cached_resident / pl.bd.nb));
-  return DMGS_OK;
+// Bands of tile rows for the segment counts: about 1024 tiles per band (a
+// 4 KB difference grid).
+void band_plan(int gx, int gy, int &R, int &nb) {
+  R = std::max(1, std::min(gy, 1024 / std::max(gx, 1)));
+  nb = (gy + R - 1) / R;
 }
 
-}  // namespace
+size_t seg_grid_bytes(int R, int gx) { return (size_t)(R + 1) * (gx + 1) * 4; }
 
-namespace {
+int device_sms() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NUM_SMS_HINT;
+  thread_local int cached_dev = -1, cached_sms = NUM_SMS_HINT;
+  if (dev != cached_dev) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+      cached_sms = sms;
+    cached_dev = dev;
+  }
+  return cached_sms;
+}
+
+// Row segments per view for a launch: enough (row, piece, segment) blocks
+// for about five waves of the tile emission (short blocks balance uneven
+// rows).  A pure function of the views'
+// grids and the device, so the geometry and the emission launches of one
+// set of views agree.
+int seg_plan(const BinViews &bv) {
+  long rows = 0;
+  for (int v = 0; v < bv.n; ++v) rows += (long)bv.v[v].gy * bv.v[v].nxs;
+  const long target = 32L * device_sms();
+  const long S = rows > 0 ? (target + rows - 1) / rows : 1;
+  return (int)std::max(1L, std::min((long)SEG_MAX, S));
+}
 
 // Scan of one array per view: host bound n_max (the launch size), device
 // length *n_dev when given.
@@ -738,6 +859,8 @@ ScanViews scan_views(const BinViews &bv, F &&f) {
   return sv;
 }
 
+constexpr size_t SMEM_LIMIT = 220 * 1024;
+
 }  // namespace
 
 int launch_scan1(uint32_t *data, uint32_t n, uint32_t *part, uint32_t *total_out,
@@ -750,15 +873,23 @@ int launch_scan1(uint32_t *data, uint32_t n, uint32_t *part, uint32_t *total_out
 
 size_t scan_part_words(uint32_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
-int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_list,
-                  uint32_t K_alloc, BinView &B) {
-  BandPlan pl;
-  if (int r = band_plan(L.gx, L.gy, pl)) return r;
+int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *bin, uint32_t K_alloc,
+                  BinView &B) {
   B.P = L.P;
   B.nb_pre = L.nb_pre;
   B.nb_radix = L.nb_radix;
+  B.gx = L.gx;
+  B.gy = L.gy;
+  band_plan(L.gx, L.gy, B.R, B.nb);
+  B.nxs = (L.gx + XSEG - 1) / XSEG;
+  const size_t rows_smem = (size_t)(L.gy + 1) * 4;
+  if (seg_grid_bytes(B.R, L.gx) > SMEM_LIMIT || rows_smem > SMEM_LIMIT) {
+    dmgs_host::set_error("image too large for the binning kernels' shared memory (%d x %d tiles)",
+                         L.gx, L.gy);
+    return DMGS_ERR_ARG;
+  }
   B.n_rhist_max = (uint32_t)L.n_rhist_max;
-  B.n_cmat_max = (uint32_t)L.n_cmat_max;
+  B.n_rcnt_max = (uint32_t)L.n_rcnt_max;
   B.flags = reinterpret_cast<const uint8_t *>(geom + L.flags);
   B.feat = reinterpret_cast<const float4 *>(geom + L.feat);
   B.blkcnt = reinterpret_cast<uint32_t *>(geom + L.blkcnt);
@@ -769,35 +900,41 @@ int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_l
   B.v0 = reinterpret_cast<uint32_t *>(geom + L.dval0);
   B.v1 = reinterpret_cast<uint32_t *>(geom + L.dval1);
   B.rhist = reinterpret_cast<uint32_t *>(geom + L.rhist);
-  B.cmat = reinterpret_cast<uint32_t *>(geom + L.cmat);
+  B.srect = reinterpret_cast<uint2 *>(geom + L.srect);
   B.cstart = reinterpret_cast<uint32_t *>(geom + L.cstart);
-  B.tbase = reinterpret_cast<uint32_t *>(geom + L.tbase);
-  B.segpre = reinterpret_cast<uint32_t *>(geom + L.segpre);
+  B.rcnt = reinterpret_cast<uint32_t *>(geom + L.rcnt);
+  B.cnt2 = reinterpret_cast<uint32_t *>(geom + L.cnt2);
   B.ranges = reinterpret_cast<uint2 *>(geom + L.ranges);
-  B.point_list = reinterpret_cast<uint32_t *>(point_list);
+  const BinLayout BL = bin_layout(K_alloc, 0, 0);
+  B.point_list = bin ? reinterpret_cast<uint32_t *>(bin + BL.point_list) : nullptr;
+  B.rowlist = bin ? reinterpret_cast<uint2 *>(bin + BL.rowlist) : nullptr;
   B.K_cap = K_cap;
-  B.K_alloc = K_alloc;
-  B.bd = pl.bd;
-  B.cmax = pl.cmax;
-  B.smem = (uint32_t)pl.smem;
+  B.K_alloc = bin ? K_alloc : 0u;
+  B.cmax = CHUNK_COUNT_MAX;
   return DMGS_OK;
 }
 
 int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
   if (bv.n < 1) return DMGS_OK;
-  int nb_pre = 0, nb_radix = 0, P = 0, T = 0;
-  uint32_t smem = 0, count_smem = 0, band_blocks = 0;
+  int nb_pre = 0, nb_radix = 0, P = 0, T = 0, gy = 0, nb = 0;
+  uint32_t cmax = 0;
+  size_t seg_smem = 0;
   for (int v = 0; v < bv.n; ++v) {
     const BinView &B = bv.v[v];
     nb_pre = std::max(nb_pre, B.nb_pre);
     nb_radix = std::max(nb_radix, B.nb_radix);
     P = std::max(P, B.P);
-    T = std::max(T, B.bd.gx * B.bd.gy);
-    smem = std::max(smem, B.smem);
-    count_smem = std::max(count_smem, count_grid_bytes(B.bd));
-    band_blocks = std::max(band_blocks, B.cmax * (uint32_t)B.bd.nb);
+    T = std::max(T, B.gx * B.gy);
+    gy = std::max(gy, B.gy);
+    nb = std::max(nb, B.nb);
+    cmax = std::max(cmax, B.cmax);
+    seg_smem = std::max(seg_smem, seg_grid_bytes(B.R, B.gx));
   }
+  const int S = seg_plan(bv);
   const int nv = bv.n;
+  const size_t rows_smem = (size_t)(gy + 1) * 4;
+  if (int r = dmgs_host::raise_smem_limit((const void *)row_count_kernel, rows_smem)) return r;
+  if (int r = dmgs_host::raise_smem_limit((const void *)seg_count_kernel, seg_smem)) return r;
   if (P > 0) {
     DMGS_TIMED(K_BIN_COMPACT, s, {
       int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
@@ -830,39 +967,54 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
       }), s);
       if (r != DMGS_OK) return r;
       dmgs_host::note_launch(), chunk_bounds_kernel<<<dim3(nb_pre, nv), 256, 0, s>>>(bv);
-      dmgs_host::note_launch(), count_kernel<<<dim3(band_blocks, nv), 32, count_smem, s>>>(bv);
+      dmgs_host::note_launch(), row_count_kernel<<<dim3(cmax, nv), 32, rows_smem, s>>>(bv);
+      dmgs_host::note_launch(), seg_count_kernel<<<dim3(S * nb, nv), 256, seg_smem, s>>>(bv, S);
     });
     DMGS_LAUNCH_CHECK("tile_count");
-  }
-  DMGS_TIMED(K_BIN_SCAN, s, {
-    if (P > 0) {
-      dmgs_host::note_launch(), tile_scan_kernel<<<dim3((T + 31) / 32, nv), 32 * CHUNK_SEGS, 0, s>>>(bv);
+    DMGS_TIMED(K_BIN_SCAN, s, {
       int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
-        return ScanView{B.tbase, nullptr, (uint32_t)(B.bd.gx * B.bd.gy), B.part, B.counters + CI_K,
+        return ScanView{B.rcnt, B.counters + CI_NRC, B.n_rcnt_max, B.part, B.counters + CI_K1,
                         B.counters};
       }), s);
       if (r != DMGS_OK) return r;
-    }
-    dmgs_host::note_launch(), ranges_kernel<<<dim3((T + 255) / 256, nv), 256, 0, s>>>(bv);
-  });
+      r = launch_scan_views(scan_views(bv, [S](const BinView &B) {
+        return ScanView{B.cnt2, nullptr, (uint32_t)(B.gx * B.gy) * (uint32_t)S, B.part,
+                        B.counters + CI_K, B.counters};
+      }), s);
+      if (r != DMGS_OK) return r;
+    });
+    DMGS_LAUNCH_CHECK("binning scans");
+  }
+  dmgs_host::note_launch(), ranges_kernel<<<dim3((T + 255) / 256, nv), 256, 0, s>>>(bv, S);
   DMGS_LAUNCH_CHECK("ranges_kernel");
   return DMGS_OK;
 }
 
 int launch_emit(const BinViews &bv, cudaStream_t s) {
-  uint32_t smem = 0, band_blocks = 0;
+  int gy = 0, nxs = 0, gxm = 0;
+  uint32_t cmax = 0;
   bool any = false;
   for (int v = 0; v < bv.n; ++v) {
     const BinView &B = bv.v[v];
     if (B.P <= 0 || B.K_alloc == 0) continue;
     any = true;
-    smem = std::max(smem, B.smem);
-    band_blocks = std::max(band_blocks, B.cmax * (uint32_t)B.bd.nb);
+    gy = std::max(gy, B.gy);
+    nxs = std::max(nxs, B.nxs);
+    gxm = std::max(gxm, std::min(B.gx, XSEG));
+    cmax = std::max(cmax, B.cmax);
   }
   if (!any) return DMGS_OK;
+  const int S = seg_plan(bv);
+  const size_t rows_smem = (size_t)gy * 4;
+  const size_t te_smem = tile_emit_smem_words(gxm) * 4;
+  if (int r = dmgs_host::raise_smem_limit((const void *)row_emit_kernel, rows_smem)) return r;
+  if (int r = dmgs_host::raise_smem_limit((const void *)tile_emit_kernel, te_smem)) return r;
+  DMGS_TIMED(K_BIN_ROWS, s,
+             dmgs_host::note_launch(), row_emit_kernel<<<dim3(cmax, bv.n), 32, rows_smem, s>>>(bv));
+  DMGS_LAUNCH_CHECK("row_emit_kernel");
   DMGS_TIMED(K_BIN_EMIT, s,
-             dmgs_host::note_launch(), emit_kernel<<<dim3(band_blocks, bv.n), 32, smem, s>>>(bv));
-  DMGS_LAUNCH_CHECK("emit_kernel");
+             dmgs_host::note_launch(), tile_emit_kernel<<<dim3(gy * nxs * S, bv.n), TE_THREADS, te_smem, s>>>(bv, S));
+  DMGS_LAUNCH_CHECK("tile_emit_kernel");
   return DMGS_OK;
 }
 

@@ -133,6 +133,18 @@ __device__ __forceinline__ float exponent2(float A, float B, float C, float dx, 
   return __fmaf_rn(__fmaf_rn(C, dy, q), dy, ax2);
 }
 
+// The 48-byte record of list entry id; an entry outside the Gaussians (which
+// a correct list never holds) reads as a zero-opacity record, whose
+// footprint is empty, so no read leaves the geometry state.
+__device__ __forceinline__ void load_record(const BlendView &V, uint32_t id, float4 &f0, float4 &f1,
+                                            float4 &f2) {
+  if (id < V.P) {
+    f0 = V.feat[3 * id]; f1 = V.feat[3 * id + 1]; f2 = V.feat[3 * id + 2];
+  } else {
+    f0 = f1 = f2 = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
 // Work item -> (view, tile).
 __device__ __forceinline__ int find_view(const BlendBatch &bb, int item) {
   int v = 0;
@@ -239,8 +251,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
     for (int l = 0; l < LOADS; ++l) {
       const int i = l * THREADS + tid;
       if (i < n && i < BATCH) {
-        const uint32_t id = V.point_list[range.x + i];
-        pf0[l] = V.feat[3 * id]; pf1[l] = V.feat[3 * id + 1]; pf2[l] = V.feat[3 * id + 2];
+        load_record(V, V.point_list[range.x + i], pf0[l], pf1[l], pf2[l]);
       }
     }
     int buf = 0;
@@ -260,8 +271,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
       for (int l = 0; l < LOADS; ++l) {
         const int sl = l * THREADS + tid;
         if (sl < BATCH && nbase + sl < n) {
-          const uint32_t id = V.point_list[range.x + nbase + sl];
-          pf0[l] = V.feat[3 * id]; pf1[l] = V.feat[3 * id + 1]; pf2[l] = V.feat[3 * id + 2];
+          load_record(V, V.point_list[range.x + nbase + sl], pf0[l], pf1[l], pf2[l]);
         }
       }
       const int cnt = min(BATCH, n - base);
@@ -512,8 +522,9 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
       __syncthreads();
       for (int sl = tid; sl < cnt; sl += THREADS) {
         const uint32_t id = V.point_list[range.x + top - 1 - sl];  // back to front
-        const StagedB st =
-            stage_b(V.feat[3 * id], V.feat[3 * id + 1], V.feat[3 * id + 2], id, hw, hh, ox, oy);
+        float4 f0, f1, f2;
+        load_record(V, id, f0, f1, f2);
+        const StagedB st = stage_b(f0, f1, f2, id, hw, hh, ox, oy);
         S0[sl] = st.s0; S1[sl] = st.s1; S2[sl] = st.s2; S3[sl] = st.s3;
         SM[sl] = __float_as_uint(st.s3.w);
       }
@@ -658,6 +669,7 @@ BlendView make_blend_view(const ViewParams &vp, const GeomLayout &L, const char 
                           const float *bg) {
   BlendView v;
   v.W = vp.W; v.H = vp.H; v.gx = L.gx; v.T = L.T(); v.tile_base = 0;
+  v.P = (uint32_t)L.P;
   v.ranges = reinterpret_cast<const uint2 *>(geom + L.ranges);
   v.point_list = reinterpret_cast<const uint32_t *>(bin + B.point_list);
   v.feat = reinterpret_cast<const float4 *>(geom + L.feat);

@@ -62,8 +62,9 @@ constexpr int RADIX_ITEMS = 8;           // keys per thread
 constexpr int RADIX_TILE = RADIX_BLOCK * RADIX_ITEMS;  // 2048 keys per block
 constexpr int CHUNK_MIN_GAUSS = 64;     // visible Gaussians per binning chunk (mean, minimum)
 constexpr int CHUNK_COUNT_MAX = 2048;    // binning chunks per view (maximum)
-constexpr int CHUNK_SEGS = 32;           // chunk segments of the per-tile offset scan
-constexpr int CHUNK_W_GAUSS = 2;         // chunk weight of a Gaussian: this + ceil(tiles / 32)
+constexpr int CHUNK_W_GAUSS = 2;         // chunk weight of a Gaussian: this + ceil(rows / 16)
+constexpr int SEG_MAX = 32;              // row segments (groups of chunks) per view, maximum
+constexpr int XSEG = 512;                // tiles of one row handled by a tile-emission block
 constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 4;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096 elements per block
@@ -71,22 +72,29 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 4096 elements per block
 // counters[] indices
 constexpr int CI_STATUS = 0;   // ST_* bits
 constexpr int CI_K = 1;        // instances (u32; K < 2^32 enforced)
+constexpr int CI_K1 = 2;       // row-list entries (visible Gaussian x tile row it covers)
 constexpr int CI_MAXLIST = 3;  // longest tile list
 constexpr int CI_V = 4;        // visible Gaussians
 constexpr int CI_NBR = 5;      // radix blocks in use = ceil(V / RADIX_TILE)
 constexpr int CI_NRH = 6;      // radix histogram entries = 256 * NBR
 constexpr int CI_W = 7;        // total chunk weight of the visible Gaussians
 constexpr int CI_C = 8;        // chunks
-constexpr int CI_NCM = 9;      // count-matrix entries = T * C
+constexpr int CI_NRC = 9;      // row-count entries = gy * C
 constexpr int CI_WORDS = 16;
 
+// Geometry state of one view.  Binning arrays: per-block visible counts;
+// (depth bits, index) ping-pong pairs of the radix sort; radix histograms;
+// per depth-sorted position the packed tile rectangle (srect, 8 B); chunk
+// starts; the row counts [gy][C] (Gaussians of chunk c covering tile row r,
+// scanned in place into row-list offsets); the segment counts [T][S]
+// (instances of tile t from row segment s, scanned in place into list
+// offsets); scan partials; tile ranges; counters.
 struct GeomLayout {
-  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, cmat, cstart, tbase, segpre,
-      scanpart,
-      ranges, counters, total;
+  size_t feat, flags, blkcnt, dkey0, dkey1, dval0, dval1, rhist, srect, cstart, rcnt, cnt2,
+      scanpart, ranges, counters, total;
   int P, gx, gy;
   int nb_pre, nb_radix;
-  size_t n_rhist_max, n_cmat_max, n_part_max;
+  size_t n_rhist_max, n_rcnt_max, n_cnt2_max, n_part_max;
   __host__ __device__ int T() const { return gx * gy; }
 };
 
@@ -99,8 +107,10 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.nb_pre = (P + PRE_BLOCK - 1) / PRE_BLOCK;
   L.nb_radix = (P + RADIX_TILE - 1) / RADIX_TILE;
   L.n_rhist_max = (size_t)256 * L.nb_radix;
-  L.n_cmat_max = T * CHUNK_COUNT_MAX;
-  size_t nmax = L.n_cmat_max > L.n_rhist_max ? L.n_cmat_max : L.n_rhist_max;
+  L.n_rcnt_max = (size_t)L.gy * CHUNK_COUNT_MAX;
+  L.n_cnt2_max = T * SEG_MAX;
+  size_t nmax = L.n_rcnt_max > L.n_rhist_max ? L.n_rcnt_max : L.n_rhist_max;
+  if (L.n_cnt2_max > nmax) nmax = L.n_cnt2_max;
   if ((size_t)L.nb_pre > nmax) nmax = L.nb_pre;
   if ((size_t)P > nmax) nmax = P;
   L.n_part_max = (nmax + SCAN_TILE - 1) / SCAN_TILE + 1;
@@ -113,10 +123,10 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
   L.dval0 = o;     o = align_up(o + (size_t)P * 4, 256);
   L.dval1 = o;     o = align_up(o + (size_t)P * 4, 256);
   L.rhist = o;     o = align_up(o + L.n_rhist_max * 4 + 4, 256);
-  L.cmat = o;      o = align_up(o + L.n_cmat_max * 4, 256);
+  L.srect = o;     o = align_up(o + (size_t)P * 8, 256);
   L.cstart = o;    o = align_up(o + (CHUNK_COUNT_MAX + 1) * 4, 256);
-  L.tbase = o;     o = align_up(o + (T + 1) * 4, 256);
-  L.segpre = o;    o = align_up(o + T * CHUNK_SEGS * 4, 256);
+  L.rcnt = o;      o = align_up(o + L.n_rcnt_max * 4 + 4, 256);
+  L.cnt2 = o;      o = align_up(o + L.n_cnt2_max * 4 + 4, 256);
   L.scanpart = o;  o = align_up(o + L.n_part_max * 4, 256);
   L.ranges = o;    o = align_up(o + T * 8, 256);
   L.counters = o;  o = align_up(o + CI_WORDS * 4, 256);
@@ -125,16 +135,21 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
 }
 
 // Binning state: the per-tile Gaussian index lists, concatenated in tile
-// order (K entries).
+// order (K entries, 4 B each), then the row lists they are split from (one
+// 8-byte entry {Gaussian index, x0 | x1 << 16} per visible Gaussian and tile
+// row it covers; at most K entries, since every entry yields at least one
+// instance).
 struct BinLayout {
-  size_t point_list, total;
+  size_t point_list, rowlist, total;
 };
 
 __host__ __device__ inline BinLayout bin_layout(int64_t K, int W, int H) {
   (void)W; (void)H;
   BinLayout L;
+  const size_t k = (size_t)(K > 0 ? K : 0);
   L.point_list = 0;
-  L.total = align_up((size_t)(K > 0 ? K : 0) * 4, 256) + 256;
+  L.rowlist = align_up(k * 4, 256);
+  L.total = L.rowlist + align_up(k * 8, 256) + 256;
   return L;
 }
 
@@ -197,7 +212,7 @@ enum KernelId {
   K_PREPROCESS = 0, K_BIN_COMPACT, K_BIN_SORT, K_BIN_COUNT, K_BIN_SCAN, K_BIN_EMIT, K_BLEND_FWD,
   K_BLEND_BWD, K_PREPROCESS_BWD, K_MARK_VISIBLE, K_BIND_FWD, K_BIND_BWD, K_BIND3_FWD,
   K_BIND3_BWD, K_DEBUG, K_BATCH_PREPROCESS, K_BATCH_BINNING, K_BATCH_BLEND_FWD,
-  K_BATCH_BLEND_BWD, K_BATCH_PREPROCESS_BWD, K_LOSS, K_FACE_CULL, K_FC_FWD, K_FC_BWD, K_TEX_FWD, K_TEX_BWD, K_SH_COLORS, K_COUNT
+  K_BATCH_BLEND_BWD, K_BATCH_PREPROCESS_BWD, K_LOSS, K_FACE_CULL, K_FC_FWD, K_FC_BWD, K_TEX_FWD, K_TEX_BWD, K_SH_COLORS, K_BIN_ROWS, K_COUNT
 };
 void timing_begin(int kid, cudaStream_t s);
 void timing_end(int kid, cudaStream_t s);

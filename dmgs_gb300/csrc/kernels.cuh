@@ -44,24 +44,23 @@ int launch_l1_ssim(const float *x, const float *y, int C, int H, int W, float la
 // binning.cu — every stage bins a set of views in one launch per stage.
 constexpr int MAX_BIN_VIEWS = 16;
 
-struct Bands {
-  int gx, gy, R, nb;  // tile grid, tile rows per band, bands
-};
-
 // One view's binning: its geometry-state arrays and sizes.
 struct BinView {
   int P, nb_pre, nb_radix;
-  uint32_t n_rhist_max, n_cmat_max;
+  int gx, gy;            // tile grid
+  int R, nb;             // segment counting: tile rows per band, bands
+  int nxs;               // row pieces of at most XSEG tiles
+  uint32_t n_rhist_max, n_rcnt_max;
   const uint8_t *flags;
   const float4 *feat;
-  uint32_t *blkcnt, *counters, *part, *k0, *k1, *v0, *v1, *rhist, *cmat, *cstart, *tbase,
-      *segpre;
+  uint32_t *blkcnt, *counters, *part, *k0, *k1, *v0, *v1, *rhist, *cstart, *rcnt, *cnt2;
+  uint2 *srect;          // packed tile rectangle per depth-sorted position
   uint2 *ranges;
   uint32_t *point_list;  // emission target (K_alloc entries)
+  uint2 *rowlist;        // row lists (K_alloc entries)
   uint32_t K_cap;        // list capacity checked by the ranges (0xffffffff: sized afterwards)
-  uint32_t K_alloc;      // entries of point_list
-  Bands bd;
-  uint32_t cmax, smem;   // chunk bound, band shared memory (bytes)
+  uint32_t K_alloc;      // entries of point_list and of rowlist
+  uint32_t cmax;         // chunk bound
 };
 
 struct BinViews {
@@ -86,8 +85,10 @@ struct ScanViews {
 
 // Fill one view's binning record from its geometry state; point_list /
 // K_alloc may be set later (after the instance count is known).
-int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *point_list,
-                  uint32_t K_alloc, BinView &B);
+// bin: the binning state (point list, then row lists: bin_layout(K_alloc)),
+// or nullptr until the instance count is known.
+int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *bin, uint32_t K_alloc,
+                  BinView &B);
 int launch_binning_geometry(const BinViews &bv, cudaStream_t s);
 // Exclusive scan of one u32 array of n entries in place (part: scan_part_words(n)
 // words of scratch; total to *total_out, overflow bit into *status when given).
@@ -107,6 +108,7 @@ constexpr int MAX_BATCH_VIEWS = 16;
 // One view of a blend launch: its tile grid and the buffers of its tiles.
 struct BlendView {
   int W, H, gx, T;     // image size, tile-grid width, tiles
+  uint32_t P;          // Gaussians (records of feat): list entries >= P are skipped
   int tile_base;       // first work item of this view
   const uint2 *ranges;
   const uint32_t *point_list;

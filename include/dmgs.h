@@ -27,7 +27,7 @@
 /* Version of the structs and entry points below; dmgs_abi_version() returns
  * the value the library was built with.  Raised whenever a struct layout or
  * a signature changes. */
-#define DMGS_ABI_VERSION 4
+#define DMGS_ABI_VERSION 5
 
 #ifdef __cplusplus
 extern "C" {
@@ -227,6 +227,14 @@ int dmgs_raster_bwd_batched(const DmgsBatch *b, const DmgsGaussians *g,
 int dmgs_batch_status(const DmgsBatch *b, int32_t P, const void *state,
                       size_t state_bytes, int64_t *num_rendered,
                       dmgs_stream_t stream);
+
+/* Diagnostics (no counterpart in the reference): synchronises the stream and
+ * copies each view's 16 binning counter words into words[16v .. 16v+15]
+ * (host): 0 status bits, 1 instances K, 2 row-list entries (visible Gaussian
+ * x tile row it covers), 3 longest tile list, 4 visible Gaussians, 8 binning
+ * chunks; the other words are internal. */
+int dmgs_batch_counters(const DmgsBatch *b, int32_t P, const void *state,
+                        size_t state_bytes, uint32_t *words, dmgs_stream_t stream);
 
 /* ---------------------------------------------------------------------- *
  * Serving form (no counterpart in the reference): a batch whose views each
