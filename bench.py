@@ -516,7 +516,10 @@ def texture_leg(args, dev):
     kt = _lib.timing_collect()
     out = {"points": int(xyz.shape[0]), "channels": 48, "fwd_ms": ms_fwd, "fwd_bwd_ms": ms_step,
            "own_kernels_per_fwd_bwd": launches,
-           "kernel_ms_per_step": {k: kt[k][0] / 5 for k in ("tex_fwd", "tex_bwd") if k in kt},
+           "kernel_ms_per_step": {k: kt[k][0] / 5 for k in ("tex_fwd", "tex_bwd", "tex_scatter")
+                                  if k in kt},
+           "adjoint_split": "tex_bwd = MLP adjoint incl. the weight-gradient GEMMs; tex_scatter = "
+                            "table and position gradients (float2 atomics)",
            "table_mb": tex.encoder.params.numel() * 4 / 1e6,
            "encoding": "float32 hash grid (the reference's tiny-cuda-nn default is half)"}
     if int(os.environ.get("RANK", "0")) == 0 and not args.no_cpu:

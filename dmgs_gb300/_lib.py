@@ -13,7 +13,7 @@ import torch  # noqa: F401  (loads libcudart before the extension)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdmgs_gb300.so")
-ABI_VERSION = 5  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
+ABI_VERSION = 6  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
 
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -54,7 +54,8 @@ class DmgsFaceBinding3(C.Structure):
 class DmgsFcGrid(C.Structure):
     _fields_ = [("x", vp), ("s", vp), ("beta", vp), ("alpha", vp), ("gamma", vp),
                 ("rx", C.c_int32), ("ry", C.c_int32), ("rz", C.c_int32), ("training", C.c_int32),
-                ("beta_stride", C.c_int32), ("alpha_stride", C.c_int32), ("gamma_stride", C.c_int32)]
+                ("beta_stride", C.c_int32), ("alpha_stride", C.c_int32), ("gamma_stride", C.c_int32),
+                ("vert_mask", vp), ("no_ambiguity_check", C.c_int32)]
 
 
 class DmgsTexture(C.Structure):
@@ -111,6 +112,8 @@ SIGNATURES = [
                                     C.POINTER(C.c_size_t), vp, vp]),
     ("dmgs_multi_status_async", C.c_int, [C.POINTER(DmgsBatch), C.POINTER(DmgsGaussians),
                                           C.POINTER(vp), C.POINTER(C.c_size_t), vp, vp]),
+    ("dmgs_vertex_frustum_mask", C.c_int, [vp, C.c_int32, vp, C.c_float, C.c_int32, C.c_int32, vp, vp,
+                                           vp]),
     ("dmgs_face_cull_scratch_bytes", C.c_size_t, [C.c_int32]),
     ("dmgs_face_cull", C.c_int, [vp, C.c_int32, vp, C.c_int32, vp, vp, vp, vp, vp, C.c_size_t,
                                  vp]),

@@ -52,7 +52,7 @@ class _Bind2(torch.autograd.Function):
         v = _prep(verts)
         f = faces.detach().to(torch.int64).contiguous()
         b = _prep(bc)
-        sf = _prep(scale_factor).reshape(1)
+        sf = None if scale_factor is None else _prep(scale_factor).reshape(1)
         F = f.shape[0]
         desc = DmgsFaceBinding(F, v.shape[0], G, int(bool(per_g)), int(bool(adaptive)), float(rad_base), float(z_scale), float(max_scale),
                                ptr(v), ptr(f), ptr(b), ptr(sf))
@@ -63,7 +63,7 @@ class _Bind2(torch.autograd.Function):
               "bind_fwd")
         ctx.save_for_backward(v, f, b, sf)
         ctx.meta = (G, rad_base, z_scale, max_scale, adaptive, desc.bc_per_gaussian)
-        ctx.sf_shape = tuple(scale_factor.shape)
+        ctx.sf_shape = None if scale_factor is None else tuple(scale_factor.shape)
         ctx.mark_non_differentiable(covL)
         return xyz, cov, covL
 
@@ -78,17 +78,21 @@ class _Bind2(torch.autograd.Function):
         dxyz = None if dxyz is None else _prep(dxyz)
         dcov = None if dcov is None else _prep(dcov)
         dverts = torch.empty_like(v)
-        dsf = torch.empty(1, device=v.device)
+        dsf = torch.empty(1, device=v.device) if sf is not None else None
         check(lib.dmgs_bind_bwd(desc, ptr(dxyz), ptr(dcov), ptr(dverts), ptr(dsf),
                                 stream_of(v.device)), "bind_bwd")
-        return dverts, dsf.view(ctx.sf_shape), None, None, None, None, None, None, None, None
+        return (dverts, None if dsf is None else dsf.view(ctx.sf_shape), None, None, None, None,
+                None, None, None, None)
 
 
 def bind_faces(verts, faces, bc, scale_factor, rad_base, spatial_lr_scale, max_scale=2.0,
                adaptive_cov=True):
     """Stage-2 binding.  ``bc``: [G,3] shared table, or [F,G,3] per-Gaussian
-    barycentric coordinates.  Returns (xyz [F*G,3], covariance [F*G,6],
-    cov3D_L [F,3,3])."""
+    barycentric coordinates.  ``scale_factor``: the learnable scale of the
+    synthetic-scene model (covariance factor tanh(scale_factor) * max_scale),
+    or None for the real-scene model, whose covariance has no such factor
+    (scene/gaussian_geo_model_mlp_flex_colmap.py:494-512).  Returns (xyz
+    [F*G,3], covariance [F*G,6], cov3D_L [F,3,3])."""
     per_g = bc.dim() == 3
     G = bc.shape[1] if per_g else bc.shape[0]
     z_scale = float(spatial_lr_scale) * 1e-6
@@ -161,3 +165,23 @@ def frustum_faces(verts, faces, full_proj):
                              ptr(scratch), scratch.numel(), stream_of(dev)), "face_cull")
     idx = kept[:int(num.item())].long()
     return mask.bool(), f[idx], idx
+
+
+def vertex_frustum_mask(verts, full_proj, cube_len, piece_id=-1, n_piece=0, and_mask=None):
+    """The real-scene stage 2's vertex frustum mask (in_frustum,
+    scene/gaussian_geo_model_mlp_flex_colmap.py:31-76): grid vertices moved
+    by half a cube edge, taken through the camera's full_proj_transform
+    (stored [4,4]) and kept inside the whole screen (piece_id < 0), one half
+    (n_piece 2) or one quarter (n_piece 4) of it, widened by 0.05; and_mask
+    (bool [N], the background grid's vertex mask) is ANDed in.  Returns a
+    bool [N] mask for FlexiCubesNoAdjacent.construct_cubes."""
+    lib = _lib.load()
+    v = _prep(verts)
+    M = _prep(full_proj)
+    N = v.shape[0]
+    out = torch.empty(N, dtype=torch.uint8, device=v.device)
+    am = None if and_mask is None else and_mask.reshape(-1).to(torch.uint8).contiguous()
+    check(lib.dmgs_vertex_frustum_mask(ptr(v), N, ptr(M), float(cube_len), int(piece_id),
+                                       int(n_piece), ptr(am), ptr(out), stream_of(v.device)),
+          "vertex_frustum_mask")
+    return out.bool()

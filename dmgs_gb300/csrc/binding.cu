@@ -116,7 +116,9 @@ __global__ void bind_fwd_kernel(DmgsFaceBinding b, float *__restrict__ xyz,
   const Frame F = face_frame(v0, v1, v2);
   float L[9];
   tri_L(F, b.rad_base, b.z_scale, b.adaptive_cov, L);
-  const float k = tanhf(b.scale_factor[0]) * b.max_scale;
+  // no scale factor: the real-scene variant's covariance, L unscaled
+  // (scene/gaussian_geo_model_mlp_flex_colmap.py:494-512)
+  const float k = b.scale_factor ? tanhf(b.scale_factor[0]) * b.max_scale : 1.f;
   const float R[9] = {F.x.x, F.y.x, F.n.x, F.x.y, F.y.y, F.n.y, F.x.z, F.y.z, F.n.z};
   float Mf[9];
 #pragma unroll
@@ -172,8 +174,8 @@ __global__ void bind_bwd_kernel(DmgsFaceBinding b, const float *__restrict__ dxy
       const Frame F = face_frame(v0, v1, v2);
       float L[9];
       tri_L(F, b.rad_base, b.z_scale, b.adaptive_cov, L);
-      const float th = tanhf(b.scale_factor[0]);
-      const float k = th * b.max_scale;
+      const float th = b.scale_factor ? tanhf(b.scale_factor[0]) : 0.f;
+      const float k = b.scale_factor ? th * b.max_scale : 1.f;
       const float R[9] = {F.x.x, F.y.x, F.n.x, F.x.y, F.y.y, F.n.y, F.x.z, F.y.z, F.n.z};
       float RL[9];
 #pragma unroll
@@ -194,7 +196,7 @@ __global__ void bind_bwd_kernel(DmgsFaceBinding b, const float *__restrict__ dxy
       float dk = 0.f;
 #pragma unroll
       for (int i = 0; i < 9; ++i) dk += dMf[i] * RL[i];
-      dk_local = dk * b.max_scale * (1.f - th * th);
+      if (b.scale_factor) dk_local = dk * b.max_scale * (1.f - th * th);
       // dR = dMf (k L)^T
       float dR[9];
 #pragma unroll
@@ -530,7 +532,62 @@ face_cull_compact_kernel(const float *__restrict__ verts, int V, const int64_t *
   }
 }
 
+// Vertex frustum mask of the real-scene stage 2 (in_frustum,
+// scene/gaussian_geo_model_mlp_flex_colmap.py:31-76): the grid vertex
+// shifted by half a cube edge (the shift folded into the matrix's last row,
+// as the reference does) taken through full_proj (row-vector convention,
+// stored [4,4]); kept when w = p.w + 1e-6 > 0 and p.xyz / w lies inside the
+// view's screen piece widened by 0.05 (the whole screen, a half or a
+// quarter).  Optional and_mask ([N] bytes) is ANDed in.
+__global__ void __launch_bounds__(256)
+vertex_frustum_kernel(const float *__restrict__ verts, int N, const float *__restrict__ M, float half,
+                      int piece_id, int n_piece, const uint8_t *__restrict__ and_mask,
+                      uint8_t *__restrict__ out) {
+  const int i = blockIdx.x * 256 + threadIdx.x;
+  if (i >= N) return;
+  const float x = verts[3 * (size_t)i], y = verts[3 * (size_t)i + 1], z = verts[3 * (size_t)i + 2];
+  float p[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float m0 = __ldg(M + j), m1 = __ldg(M + 4 + j), m2 = __ldg(M + 8 + j);
+    const float c = __fadd_rn(__ldg(M + 12 + j),
+                              __fadd_rn(__fadd_rn(__fmul_rn(m0, half), __fmul_rn(m1, half)),
+                                        __fmul_rn(m2, half)));
+    p[j] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, m0), __fmul_rn(y, m1)), __fmul_rn(z, m2)), c);
+  }
+  const float w = __fadd_rn(p[3], 1e-6f);
+  const float q[3] = {__fdiv_rn(p[0], w), __fdiv_rn(p[1], w), __fdiv_rn(p[2], w)};
+  bool keep;
+  if (piece_id < 0) {
+    keep = fabsf(q[0]) < 1.05f && fabsf(q[1]) < 1.05f && fabsf(q[2]) < 1.05f;
+  } else {
+    // screen piece [lo, hi] in x and y (z spans [-1, 1]), widened by 0.05
+    float lx = -1.f, hx = 1.f, ly = -1.f, hy = 1.f;
+    if (n_piece == 2) {
+      if (piece_id == 0) hx = 0.f; else lx = 0.f;
+    } else {
+      if (piece_id & 1) lx = 0.f; else hx = 0.f;
+      if (piece_id & 2) ly = 0.f; else hy = 0.f;
+    }
+    keep = q[0] > __fsub_rn(lx, 0.05f) && q[1] > __fsub_rn(ly, 0.05f) && q[2] > -1.05f &&
+           q[0] < __fadd_rn(hx, 0.05f) && q[1] < __fadd_rn(hy, 0.05f) && q[2] < 1.05f;
+  }
+  keep = keep && w > 0.f;
+  if (and_mask) keep = keep && and_mask[i] != 0;
+  out[i] = keep ? 1 : 0;
+}
+
 }  // namespace
+
+int launch_vertex_frustum(const float *verts, int N, const float *full_proj, float cube_len,
+                          int piece_id, int n_piece, const uint8_t *and_mask, uint8_t *out,
+                          cudaStream_t s) {
+  if (N <= 0) return DMGS_OK;
+  DMGS_TIMED(K_FACE_CULL, s, dmgs_host::note_launch(), vertex_frustum_kernel<<<(N + 255) / 256, 256, 0, s>>>(
+      verts, N, full_proj, 0.5f * cube_len, piece_id, n_piece, and_mask, out));
+  DMGS_LAUNCH_CHECK("vertex_frustum_kernel");
+  return DMGS_OK;
+}
 
 size_t face_cull_scratch_bytes(int F) {
   const uint32_t nb = (uint32_t)((F + CULL_BLOCK - 1) / CULL_BLOCK);

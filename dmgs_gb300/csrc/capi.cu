@@ -381,7 +381,7 @@ int dmgs_debug_image(int32_t width, int32_t height, const void *image_state, siz
 
 int dmgs_bind_fwd(const DmgsFaceBinding *b, float *xyz, float *cov, float *rot_t2w,
                   float *cov3D_L, dmgs_stream_t stream) {
-  if (!b || b->F < 0 || b->G <= 0 || (b->F > 0 && (!b->verts || !b->faces || !b->bc || !b->scale_factor))) {
+  if (!b || b->F < 0 || b->G <= 0 || (b->F > 0 && (!b->verts || !b->faces || !b->bc))) {
     set_error("bind_fwd: invalid arguments");
     return DMGS_ERR_ARG;
   }
@@ -391,7 +391,7 @@ int dmgs_bind_fwd(const DmgsFaceBinding *b, float *xyz, float *cov, float *rot_t
 int dmgs_bind_bwd(const DmgsFaceBinding *b, const float *dL_dxyz, const float *dL_dcov,
                   float *dL_dverts, float *dL_dscale_factor, dmgs_stream_t stream) {
   if (!b || b->F < 0 || b->G <= 0 || !dL_dverts ||
-      (b->F > 0 && (!b->verts || !b->faces || !b->bc || !b->scale_factor))) {
+      (b->F > 0 && (!b->verts || !b->faces || !b->bc))) {
     set_error("bind_bwd: invalid arguments");
     return DMGS_ERR_ARG;
   }
@@ -419,6 +419,22 @@ int dmgs_bind3_bwd(const DmgsFaceBinding3 *b, const float *dL_dxyz, const float 
   }
   return launch_bind3_bwd(*b, dL_dxyz, dL_dscales, dL_drotations, dL_dverts, dL_dscaling2d,
                           dL_drotation2d, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int dmgs_vertex_frustum_mask(const float *verts, int32_t N, const float *full_proj,
+                             float cube_len, int32_t piece_id, int32_t n_piece,
+                             const uint8_t *and_mask, uint8_t *mask, dmgs_stream_t stream) {
+  if (N < 0 || (N > 0 && (!verts || !full_proj || !mask))) {
+    set_error("vertex_frustum_mask: invalid arguments");
+    return DMGS_ERR_ARG;
+  }
+  const bool ok = piece_id < 0 || (n_piece == 2 && piece_id < 2) || (n_piece == 4 && piece_id < 4);
+  if (!ok) {
+    set_error("vertex_frustum_mask: piece %d of %d is not a screen half or quarter", piece_id, n_piece);
+    return DMGS_ERR_ARG;
+  }
+  return launch_vertex_frustum(verts, N, full_proj, cube_len, piece_id, n_piece, and_mask, mask,
+                               reinterpret_cast<cudaStream_t>(stream));
 }
 
 size_t dmgs_face_cull_scratch_bytes(int32_t F) { return F < 0 ? 0 : face_cull_scratch_bytes(F); }

@@ -212,7 +212,7 @@ enum KernelId {
   K_PREPROCESS = 0, K_BIN_COMPACT, K_BIN_SORT, K_BIN_COUNT, K_BIN_SCAN, K_BIN_EMIT, K_BLEND_FWD,
   K_BLEND_BWD, K_PREPROCESS_BWD, K_MARK_VISIBLE, K_BIND_FWD, K_BIND_BWD, K_BIND3_FWD,
   K_BIND3_BWD, K_DEBUG, K_BATCH_PREPROCESS, K_BATCH_BINNING, K_BATCH_BLEND_FWD,
-  K_BATCH_BLEND_BWD, K_BATCH_PREPROCESS_BWD, K_LOSS, K_FACE_CULL, K_FC_FWD, K_FC_BWD, K_TEX_FWD, K_TEX_BWD, K_SH_COLORS, K_BIN_ROWS, K_COUNT
+  K_BATCH_BLEND_BWD, K_BATCH_PREPROCESS_BWD, K_LOSS, K_FACE_CULL, K_FC_FWD, K_FC_BWD, K_TEX_FWD, K_TEX_BWD, K_SH_COLORS, K_BIN_ROWS, K_TEX_SCATTER, K_COUNT
 };
 void timing_begin(int kid, cudaStream_t s);
 void timing_end(int kid, cudaStream_t s);

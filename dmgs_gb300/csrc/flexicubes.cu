@@ -233,6 +233,8 @@ struct FcGrid {
   int training;
   int bs, as, gs;  // row strides (floats) of the beta / alpha / gamma arrays and their gradients
   FastDiv by_rz, by_ry, by_sy, by_ry1;  // rz, ry, rz + 1, ry + 1
+  const uint8_t *vmask;  // cube subset by corner-0 vertex (nullptr: every cube)
+  int nocheck;           // no C16/C19 re-check
 };
 
 // (i, j, k) of cube c and of grid vertex v
@@ -312,14 +314,22 @@ __device__ __forceinline__ int raw_case(const FcGrid &G, int ci, int cj, int ck)
   return cs;
 }
 
+// Whether cube (ci, cj, ck) takes part: inside the grid and, with a cube
+// subset, marked at its corner-0 vertex.
+__device__ __forceinline__ bool cube_on(const FcGrid &G, int ci, int cj, int ck) {
+  if (ci < 0 || ci >= G.rx || cj < 0 || cj >= G.ry || ck < 0 || ck >= G.rz) return false;
+  return G.vmask == nullptr || __ldg(G.vmask + (ci * (G.ry + 1) + cj) * G.sy + ck) != 0;
+}
+
 // Case of cube c after the C16/C19 re-check (geo/flexicubes.py:282-322):
 // when the case and the neighbour across its ambiguous face are both
-// flagged, the case becomes its complement.
+// flagged, the case becomes its complement.  No re-check with G.nocheck
+// (the no-adjacency variant's default).
 __device__ __forceinline__ int cube_case(const FcGrid &G, int c) {
   int ci, cj, ck;
   cube_ijk(G, c, ci, cj, ck);
   int cs = raw_case(G, ci, cj, ck);
-  if (c_fc.check[cs][0]) {
+  if (!G.nocheck && c_fc.check[cs][0]) {
     const int ni = ci + c_fc.check[cs][1], nj = cj + c_fc.check[cs][2], nk = ck + c_fc.check[cs][3];
     if (ni >= 0 && ni < G.rx && nj >= 0 && nj < G.ry && nk >= 0 && nk < G.rz &&
         c_fc.check[raw_case(G, ni, nj, nk)][0])
@@ -328,15 +338,48 @@ __device__ __forceinline__ int cube_case(const FcGrid &G, int c) {
   return cs;
 }
 
+// Cubes around the edge that leaves vertex (vi, vj, vk) along axis dir
+// (0: y down, 1: z up, 2: x up) that take part: bit 0 any, bit 1 all four.
+__device__ __forceinline__ uint32_t edge_ring(const FcGrid &G, int dir, int vi, int vj, int vk) {
+  int n = 0;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const bool on = dir == 0 ? cube_on(G, vi - a, vj - 1, vk - b)
+                               : (dir == 1 ? cube_on(G, vi - a, vj - b, vk) : cube_on(G, vi, vj - a, vk - b));
+      n += on ? 1 : 0;
+    }
+  return (n > 0 ? 1u : 0u) | (n == 4 ? 2u : 0u);
+}
+
 // The three grid edges a vertex stores (y down, z up, x up): which cross the
 // surface (bits 0-2), which of those have all four cubes inside the grid
 // (a quad, bits 4-6), and whether the vertex is outside (s > 0, flipped).
+// With a cube subset an edge counts only when a participating cube holds
+// it, and is a quad only when all four cubes around it take part.
 __device__ __forceinline__ uint32_t vertex_edges(const FcGrid &G, int v) {
   int vi, vj, vk;
   vertex_ijk(G, v, vi, vj, vk);
   const float sv = __ldg(G.s + v);
   const bool in = sv < 0.f;
   uint32_t m = 0;
+  if (G.vmask != nullptr) {
+    if (vj >= 1 && ((__ldg(G.s + v - G.sy) < 0.f) != in)) {
+      const uint32_t r = edge_ring(G, 0, vi, vj, vk);
+      m |= (r & 1u) | ((r >> 1) << 4);
+    }
+    if (vk < G.rz && ((__ldg(G.s + v + 1) < 0.f) != in)) {
+      const uint32_t r = edge_ring(G, 1, vi, vj, vk);
+      m |= ((r & 1u) << 1) | ((r >> 1) << 5);
+    }
+    if (vi < G.rx && ((__ldg(G.s + v + G.sx) < 0.f) != in)) {
+      const uint32_t r = edge_ring(G, 2, vi, vj, vk);
+      m |= ((r & 1u) << 2) | ((r >> 1) << 6);
+    }
+    if (sv > 0.f) m |= 128u;
+    return m;
+  }
   if (vj >= 1 && ((__ldg(G.s + v - G.sy) < 0.f) != in)) {
     m |= 1u;
     if (vi >= 1 && vi < G.rx && vk >= 1 && vk < G.rz) m |= 16u;
@@ -363,7 +406,13 @@ struct ItemInfo {
 __device__ __forceinline__ ItemInfo item_info(const FcGrid &G, int i) {
   ItemInfo it{-1, 0u};
   if (i < G.nc) {
-    const int cs = cube_case(G, i);
+    bool on = true;
+    if (G.vmask != nullptr) {
+      int ci, cj, ck;
+      cube_ijk(G, i, ci, cj, ck);
+      on = cube_on(G, ci, cj, ck);
+    }
+    const int cs = on ? cube_case(G, i) : 0;
     if (cs != 0 && cs != 255) it.cs = cs;
   }
   if (i < G.nv) it.ve = vertex_edges(G, i);
@@ -900,11 +949,16 @@ FcGrid make_grid(const DmgsFcGrid *a) {
   G.by_ry = make_fastdiv((uint32_t)a->ry);
   G.by_sy = make_fastdiv((uint32_t)G.sy);
   G.by_ry1 = make_fastdiv((uint32_t)(a->ry + 1));
+  G.vmask = a->vert_mask;
+  G.nocheck = a->no_ambiguity_check ? 1 : 0;
   return G;
 }
 
 bool grid_ok(const DmgsFcGrid *a) {
   if (!a || a->rx <= 0 || a->ry <= 0 || a->rz <= 0 || !a->x || !a->s) return false;
+  // a cube subset: no per-cube weights (they would be rows of the subset),
+  // no C16/C19 re-check (the reference's re-check assumes the whole grid)
+  if (a->vert_mask && (a->beta || a->alpha || a->gamma || !a->no_ambiguity_check)) return false;
   if ((a->beta_stride != 0 && a->beta_stride < 12) || (a->alpha_stride != 0 && a->alpha_stride < 8) ||
       a->gamma_stride < 0)
     return false;

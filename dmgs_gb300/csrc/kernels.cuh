@@ -168,6 +168,10 @@ size_t face_cull_scratch_bytes(int F);
 int launch_face_cull(const float *verts, int V, const int64_t *faces, int F,
                      const float *full_proj, uint8_t *face_mask, int32_t *kept, int32_t *num_kept,
                      char *scratch, cudaStream_t s);
+// Vertex frustum mask of the real-scene stage 2 (binding.cu).
+int launch_vertex_frustum(const float *verts, int N, const float *full_proj, float cube_len,
+                          int piece_id, int n_piece, const uint8_t *and_mask, uint8_t *out,
+                          cudaStream_t s);
 int launch_bind3_fwd(const DmgsFaceBinding3 &b, float *xyz, float *scales, float *rots,
                      cudaStream_t s);
 int launch_bind3_bwd(const DmgsFaceBinding3 &b, const float *dxyz, const float *dscales,

@@ -490,11 +490,13 @@ int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float 
   if (int r = dmgs_host::raise_smem_limit((const void *)tex_bwd_kernel<C>, tex_bwd_smem())) return r;
   int grid;
   if (int r = persistent_grid(tex_bwd_kernel<C>, tex_bwd_smem(), A.n, grid)) return r;
-  dmgs_host::note_launch(), tex_bwd_kernel<C><<<grid, TEX_THREADS, tex_bwd_smem(), s>>>(
-      A, L, xyz, dout, denc, dW1, dW2, dW3);
+  // timed apart: the MLP adjoint (weight-gradient GEMMs) and the scatter of
+  // the encoding gradients into the table and the positions
+  DMGS_TIMED(K_TEX_BWD, s, dmgs_host::note_launch(), tex_bwd_kernel<C><<<grid, TEX_THREADS, tex_bwd_smem(), s>>>(
+      A, L, xyz, dout, denc, dW1, dW2, dW3));
   if (dxyz || dtable)
-    dmgs_host::note_launch(), tex_scatter_kernel<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(
-        A, L, xyz, denc, dxyz, reinterpret_cast<float2 *>(dtable));
+    DMGS_TIMED(K_TEX_SCATTER, s, dmgs_host::note_launch(), tex_scatter_kernel<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(
+        A, L, xyz, denc, dxyz, reinterpret_cast<float2 *>(dtable)));
   return DMGS_OK;
 }
 
@@ -559,14 +561,12 @@ int dmgs_tex_bwd(const DmgsTexture *tx, int64_t n, const float *xyz, const float
   if (n == 0) return DMGS_OK;
   const TexArgs A = make_args(tx, n);
   int r = DMGS_OK;
-  DMGS_TIMED(K_TEX_BWD, s, {
-    switch (tx->channels) {
-      case 3: r = run_bwd<3>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-      case 12: r = run_bwd<12>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-      case 27: r = run_bwd<27>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-      default: r = run_bwd<48>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-    }
-  });
+  switch (tx->channels) {
+    case 3: r = run_bwd<3>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+    case 12: r = run_bwd<12>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+    case 27: r = run_bwd<27>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+    default: r = run_bwd<48>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+  }
   if (r != DMGS_OK) return r;
   DMGS_LAUNCH_CHECK("tex_bwd");
   return DMGS_OK;

@@ -17,7 +17,7 @@ static const char *kKernelNames[K_COUNT] = {
     "blend_fwd",
     "blend_bwd", "preprocess_bwd", "mark_visible", "bind_fwd", "bind_bwd", "bind3_fwd",
     "bind3_bwd", "debug", "batch_preprocess", "batch_binning", "batch_blend_fwd",
-    "batch_blend_bwd", "batch_preprocess_bwd", "l1_ssim", "face_cull", "fc_fwd", "fc_bwd", "tex_fwd", "tex_bwd", "sh_colors", "bin_row_emit"};
+    "batch_blend_bwd", "batch_preprocess_bwd", "l1_ssim", "face_cull", "fc_fwd", "fc_bwd", "tex_fwd", "tex_bwd", "sh_colors", "bin_row_emit", "tex_scatter"};
 
 namespace {
 struct Pending { int kid; cudaEvent_t a, b; };

@@ -27,7 +27,7 @@
 /* Version of the structs and entry points below; dmgs_abi_version() returns
  * the value the library was built with.  Raised whenever a struct layout or
  * a signature changes. */
-#define DMGS_ABI_VERSION 5
+#define DMGS_ABI_VERSION 6
 
 #ifdef __cplusplus
 extern "C" {
@@ -272,6 +272,19 @@ int dmgs_multi_status_async(const DmgsBatch *b, const DmgsGaussians *g,
  * *num_kept (device int32) their number.  verts: [V,3], faces: [F,3] int64
  * (device); a face with a vertex index outside [0, V) is not kept. */
 size_t dmgs_face_cull_scratch_bytes(int32_t F);
+/* Vertex frustum mask of the real-scene stage 2 (replaces in_frustum,
+ * scene/gaussian_geo_model_mlp_flex_colmap.py:31-76, as getMesh_in_frustum
+ * calls it at :299-302 and :319-322): vertex i of verts [N,3] (device) is
+ * moved by cube_len / 2 on every axis, taken through full_proj (16 floats,
+ * device, stored row-vector convention) and kept (mask[i] = 1) when
+ * w = p.w + 1e-6 > 0 and p.xyz / w lies in the screen piece widened by
+ * 0.05: the whole screen for piece_id < 0, else half piece_id of n_piece = 2
+ * (left, right) or quarter piece_id of n_piece = 4 (bit 0: right, bit 1:
+ * top); z always within +-1.05.  and_mask ([N] bytes, may be NULL) is
+ * ANDed in (the background grid's vertex mask). */
+int dmgs_vertex_frustum_mask(const float *verts, int32_t N, const float *full_proj,
+                             float cube_len, int32_t piece_id, int32_t n_piece,
+                             const uint8_t *and_mask, uint8_t *mask, dmgs_stream_t stream);
 int dmgs_face_cull(const float *verts, int32_t V, const int64_t *faces, int32_t F,
                    const float *full_proj, uint8_t *face_mask, int32_t *kept_faces,
                    int32_t *num_kept, void *scratch, size_t scratch_bytes,
@@ -315,6 +328,19 @@ typedef struct DmgsFcGrid {
    * the gradient arrays of dmgs_fc_bwd use the same strides.  The reference
    * passes column slices of one [C,21] tensor (strides 21, 21, 21). */
   int32_t beta_stride, alpha_stride, gamma_stride;
+  /* Cube subset of the per-view extraction of the real-scene stage 2
+   * (construct_cubes of geo/flexicubes_no_adjacent.py:129-145, fed by the
+   * vertex frustum mask of scene/gaussian_geo_model_mlp_flex_colmap.py:
+   * 299-303): [N] bytes, cube (i,j,k) takes part iff the mask of its corner
+   * (i,j,k) is non-zero; NULL: every cube.  With a subset, a surface edge is
+   * listed when a participating cube holds it and becomes a quad only when
+   * all four cubes around it participate (the reference's edge counts), and
+   * the weights must be NULL. */
+  const uint8_t *vert_mask;
+  /* 1: no C16/C19 re-check (geo/flexicubes_no_adjacent.py:300-340 with
+   * de_ambiguity=False, as that variant is called); 0: the re-check of
+   * geo/flexicubes.py (required to be 1 with a cube subset). */
+  int32_t no_ambiguity_check;
 } DmgsFcGrid;
 
 /* Dual Marching Cubes tables the library derives: groups[256*4] edge masks of
@@ -431,8 +457,10 @@ int dmgs_debug_image(int32_t width, int32_t height, const void *image_state,
  * floats with L = [[s, m01 s, 0], [0, m11 s, 0], [0, 0, z_scale]],
  * s = |v1-v0| rad_base, (m01, m11) the affine map of the equilateral
  * triangle onto the face (identity when adaptive_cov = 0), and
- * k = tanh(scale_factor) * max_scale.  Gradients flow to the vertices through
- * the means and through R only (L is a constant, as in the reference).
+ * k = tanh(scale_factor) * max_scale, or k = 1 when scale_factor is NULL
+ * (the real-scene variant, scene/gaussian_geo_model_mlp_flex_colmap.py:
+ * 494-512, which has no learnable scale).  Gradients flow to the vertices
+ * through the means and through R only (L is a constant, as in the reference).
  * ---------------------------------------------------------------------- */
 typedef struct DmgsFaceBinding {
   int32_t F;             /* faces */
@@ -446,7 +474,7 @@ typedef struct DmgsFaceBinding {
   const float *verts;    /* [V,3] device */
   const int64_t *faces;  /* [F,3] device */
   const float *bc;       /* barycentric weights, device */
-  const float *scale_factor; /* [1] device (pre-tanh) */
+  const float *scale_factor; /* [1] device (pre-tanh), or NULL: k = 1 */
 } DmgsFaceBinding;
 
 /* Forward: xyz [F*G,3], cov [F*G,6] (device); rot_t2w [F,9] (row-major 3x3,

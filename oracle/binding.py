@@ -56,7 +56,8 @@ def face_frames(verts, faces):
 def bind_stage2(verts, faces, bc, rad_base, z_scale, scale_factor, max_scale=2.0,
                 adaptive=True):
     """Returns xyz [F*G,3], cov [F*G,6], R [F,3,3], covL [F,3,3].  `bc` is
-    [G,3] (shared) or [F,G,3] (per Gaussian)."""
+    [G,3] (shared) or [F,G,3] (per Gaussian); scale_factor None: no
+    covariance factor (the real-scene model)."""
     tri, e01, e02, x, y, n, R = face_frames(verts, faces)
     F = faces.shape[0]
     if bc.dim() == 2:
@@ -82,7 +83,8 @@ def bind_stage2(verts, faces, bc, rad_base, z_scale, scale_factor, max_scale=2.0
         L[:, 0, 1] = m01 * s
         L[:, 1, 1] = m11 * s
         L[:, 2, 2] = z_scale
-    k = torch.tanh(scale_factor) * max_scale
+    # no scale factor: the real-scene model (scene/gaussian_geo_model_mlp_flex_colmap.py:494-512)
+    k = torch.tanh(scale_factor) * max_scale if scale_factor is not None else 1.0
     M = R @ (L * k)
     S = M @ M.transpose(1, 2)
     c6 = torch.stack([S[:, 0, 0], S[:, 0, 1], S[:, 0, 2], S[:, 1, 1], S[:, 1, 2], S[:, 2, 2]], 1)
@@ -135,3 +137,33 @@ def bind_stage3(verts, faces, bc, scaling2d, rotation2d, thin_z):
     Rt[:, 2, 2] = 1.0
     R = (Rw.view(-1, 1, 3, 3) @ Rt.view(-1, G, 3, 3)).view(-1, 3, 3)
     return xyz, scales, R, quat_from_matrix(R)
+
+
+def vertex_frustum_mask(verts, full_proj, cube_len, piece_id=-1, n_piece=0):
+    """The real-scene stage 2's vertex frustum test (``in_frustum``,
+    scene/gaussian_geo_model_mlp_flex_colmap.py:31-76) in float64: vertices
+    moved by half a cube edge through full_proj (row-vector convention,
+    stored [4,4]); kept when w = p.w + 1e-6 > 0 and p.xyz / w lies in the
+    screen piece widened by 0.05 (whole screen, halves left / right,
+    quarters bit 0 right, bit 1 top).  Returns (mask bool [N], margin [N]:
+    the distance of the deciding coordinate to its bound, for the tests'
+    float32 ambiguity band)."""
+    v = torch.as_tensor(verts, dtype=torch.float64) + cube_len / 2.0
+    M = torch.as_tensor(full_proj, dtype=torch.float64).reshape(4, 4)
+    p = v @ M[:3] + M[3]
+    w = p[:, 3] + 1e-6
+    q = p[:, :3] / w.unsqueeze(1)
+    lo = torch.tensor([-1.0, -1.0, -1.0], dtype=torch.float64)
+    hi = torch.tensor([1.0, 1.0, 1.0], dtype=torch.float64)
+    if piece_id >= 0:
+        if n_piece == 2:
+            (hi if piece_id == 0 else lo)[0] = 0.0
+        elif n_piece == 4:
+            (lo if piece_id & 1 else hi)[0] = 0.0
+            (lo if piece_id & 2 else hi)[1] = 0.0
+        else:
+            raise NotImplementedError(n_piece)
+    d = torch.minimum(q - (lo - 0.05), (hi + 0.05) - q)
+    mask = (d > 0).all(1) & (w > 0)
+    margin = torch.minimum(d.abs().min(1).values, w.abs())
+    return mask, margin

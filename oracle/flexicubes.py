@@ -121,12 +121,26 @@ def _interp(w0, w1, x0, x1):
     return (x0 * w1 - x1 * w0) / (w1 - w0)
 
 
-def extract(x, s, cubes, res, beta=None, alpha=None, gamma=None, training=False, tables=None):
+def construct_cubes(vert_mask, res):
+    """Cubes [n,8] whose corner-0 vertex is marked and inside the grid, in
+    grid order (``construct_cubes`` of geo/flexicubes_no_adjacent.py:129-145)."""
+    if isinstance(res, int):
+        res = (res, res, res)
+    rx, ry, rz = res
+    m = torch.as_tensor(vert_mask).reshape(rx + 1, ry + 1, rz + 1).bool()[:rx, :ry, :rz]
+    _, cubes = voxel_grid(res)
+    return cubes[m.reshape(-1)]
+
+
+def extract(x, s, cubes, res, beta=None, alpha=None, gamma=None, training=False, tables=None,
+            de_ambiguity=True):
     """FlexiCubes triangle extraction (geo/flexicubes.py:180-260).
 
-    x [N,3], s [N], cubes [C,8] (regular-grid order), raw weights beta [C,12],
-    alpha [C,8], gamma [C] or None.  Returns (vertices, faces [F,3] int64,
-    L_dev [E], surf_edges [Ne,2] int64)."""
+    x [N,3], s [N], cubes [C,8] (regular-grid order, or a subset of the grid's
+    cubes in grid order), raw weights beta [C,12], alpha [C,8], gamma [C] or
+    None.  de_ambiguity: the C16/C19 re-check (whole grid only); False is the
+    no-adjacency variant's default (geo/flexicubes_no_adjacent.py:300-340).
+    Returns (vertices, faces [F,3] int64, L_dev [E], surf_edges [Ne,2] int64)."""
     dmc, num_vd_t, check_t = tables or derive_tables()
     dmc = torch.tensor(dmc)
     num_vd_t = torch.tensor(num_vd_t)
@@ -154,6 +168,8 @@ def extract(x, s, cubes, res, beta=None, alpha=None, gamma=None, training=False,
     # case ids with the C16/C19 fix (geo/flexicubes.py:282-322)
     sc = torch.nonzero(surf).squeeze(1)
     case = (occ8[surf].long() << torch.arange(8)).sum(1)
+    if not de_ambiguity:
+        return _extract_rest(x, s, cubes, occ, surf, sc, case, b, a, g, dmc, num_vd_t, training, dt)
     ijk = torch.stack([sc // (res[1] * res[2]), (sc // res[2]) % res[1], sc % res[2]], 1)
     flagged = torch.zeros(res, dtype=torch.bool)
     chk = check_t[case]
@@ -164,7 +180,12 @@ def extract(x, s, cubes, res, beta=None, alpha=None, gamma=None, training=False,
     invert = torch.zeros_like(inside)
     invert[inside] = flagged[tuple(nb[inside].T)]
     case = torch.where(invert, chk[:, 4], case)
+    return _extract_rest(x, s, cubes, occ, surf, sc, case, b, a, g, dmc, num_vd_t, training, dt)
 
+
+def _extract_rest(x, s, cubes, occ, surf, sc, case, b, a, g, dmc, num_vd_t, training, dt):
+    """Surface edges, dual vertices, L_dev and triangles from the surface
+    cubes and their cases."""
     # surface edges: unique grid edges of the surface cubes with a sign
     # change, lexicographic in (first vertex, second vertex)
     # (geo/flexicubes.py:286-304)
