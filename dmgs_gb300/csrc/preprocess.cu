@@ -156,7 +156,7 @@ __device__ __forceinline__ void color_one(int idx, const ViewParams &vp,
     cr = __ldg(colors + 3 * idx); cg = __ldg(colors + 3 * idx + 1); cbl = __ldg(colors + 3 * idx + 2);
   } else {
     const float *sh = shs + (size_t)idx * M * 3;
-    float dx = x - __ldg(campos_g), dy = y - __ldg(campos_g + 1), dz = z - __ldg(campos_g + 2);
+    float dx = x - campos_g[0], dy = y - campos_g[1], dz = z - campos_g[2];  // global or shared
     const float inv = rsqrtf(dx * dx + dy * dy + dz * dz);
     dx *= inv; dy *= inv; dz *= inv;
     float b[16];
@@ -268,7 +268,21 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
   __shared__ uint32_t wcnt[NW][MAX_BATCH_VIEWS];
   __shared__ uint32_t wsum[NW];
   __shared__ uint16_t pairs[PRE_BLOCK * MAX_BATCH_VIEWS];
+  // per-view constants of the colour pass (a different view per lane: from
+  // the kernel parameters those would be serialised constant-bank loads)
+  __shared__ ViewParams s_vp[MAX_BATCH_VIEWS];
+  __shared__ float s_cam[MAX_BATCH_VIEWS][3];
+  __shared__ float4 *s_feat[MAX_BATCH_VIEWS];
+  __shared__ uint8_t *s_flags[MAX_BATCH_VIEWS];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  if (t < bv.nviews) {
+    s_vp[t] = bv.v[t].vp;
+    s_cam[t][0] = __ldg(bv.v[t].campos);
+    s_cam[t][1] = __ldg(bv.v[t].campos + 1);
+    s_cam[t][2] = __ldg(bv.v[t].campos + 2);
+    s_feat[t] = bv.v[t].feat;
+    s_flags[t] = bv.v[t].flags;
+  }
   const int idx = blockIdx.x * PRE_BLOCK + t;
   uint32_t vm = 0u;
   if (idx < P) {
@@ -319,9 +333,10 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
   for (uint32_t i = t; i < total; i += PRE_BLOCK) {
     const uint32_t pr = pairs[i];
     const int g = base + (int)(pr >> 4);
-    const BatchView &V = bv.v[pr & 15u];
-    color_one(g, V.vp, V.campos, M, __ldg(means + 3 * g), __ldg(means + 3 * g + 1),
-              __ldg(means + 3 * g + 2), shs, colors, V.feat, V.flags);
+    const int v = (int)(pr & 15u);
+    const ViewParams vp = s_vp[v];
+    color_one(g, vp, s_cam[v], M, __ldg(means + 3 * g), __ldg(means + 3 * g + 1),
+              __ldg(means + 3 * g + 2), shs, colors, s_feat[v], s_flags[v]);
   }
 }
 

@@ -81,7 +81,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
 
   float V[16], Pm[16];
 #pragma unroll
-  for (int i = 0; i < 16; ++i) { V[i] = __ldg(viewm_g + i); Pm[i] = __ldg(projm_g + i); }
+  for (int i = 0; i < 16; ++i) { V[i] = viewm_g[i]; Pm[i] = projm_g[i]; }  // global or shared
   const float mx = means[3 * idx], my = means[3 * idx + 1], mz = means[3 * idx + 2];
 
   // --- recompute the forward quantities ---------------------------------
@@ -406,6 +406,23 @@ preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__
   const Slots S_ = make_slots(sm);
   const int nslot = (int)slot_floats(M);
   for (int i = t; i < nslot; i += B) sm[i] = 0.f;
+  // per-view constants in shared memory: the pair loop below reads them
+  // with a different view per lane, which from the kernel parameters would
+  // be serialised constant-bank loads
+  __shared__ ViewParams s_vp[MAX_BATCH_VIEWS];
+  __shared__ float s_mat[MAX_BATCH_VIEWS][36];  // view matrix, projection matrix, camera centre
+  __shared__ const float *s_gacc[MAX_BATCH_VIEWS];
+  __shared__ const uint8_t *s_flags[MAX_BATCH_VIEWS];
+  if (t < bv.nviews) {
+    s_vp[t] = bv.v[t].vp;
+    s_gacc[t] = bv.v[t].gacc;
+    s_flags[t] = bv.v[t].flags;
+  }
+  for (int i = t; i < bv.nviews * 35; i += B) {
+    const int v = i / 35, k = i - v * 35;
+    const BatchView &W = bv.v[v];
+    s_mat[v][k] = k < 16 ? __ldg(W.viewm + k) : (k < 32 ? __ldg(W.projm + k - 16) : __ldg(W.campos + k - 32));
+  }
   uint32_t vm = 0u;
   if (idx < P) {
     uint32_t f[MAX_BATCH_VIEWS];
@@ -460,9 +477,9 @@ preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__
   for (uint32_t i = t; i < total; i += B) {
     const uint32_t pr = pairs[i];
     const int gl = (int)(pr >> 4), v = (int)(pr & 15u);
-    const BatchView &V = bv.v[v];
-    preprocess_bwd_one<true>(start + gl, gl, V.vp, V.viewm, V.projm, V.campos, M, means, shs,
-                             scales, rots, cov3D, V.flags, V.gacc, out, S_);
+    const ViewParams vp = s_vp[v];
+    preprocess_bwd_one<true>(start + gl, gl, vp, s_mat[v], s_mat[v] + 16, s_mat[v] + 32, M, means,
+                             shs, scales, rots, cov3D, s_flags[v], s_gacc[v], out, S_);
   }
   __syncthreads();
   const int nvalid = min(B, P - start);
