@@ -33,7 +33,7 @@ struct BatchLayout {
 size_t view_layout(const DmgsView &view, int P, int64_t cap, bool with_adjoint, size_t o,
                    ViewLayout &V) {
   V.G = geom_layout(P, view.width, view.height);
-  V.B = bin_layout(cap, view.width, view.height);
+  V.B = bin_layout(cap, view.width, view.height, P);
   V.I = img_layout(view.width, view.height);
   V.geom = o;  o = align_up(o + V.G.total, 256);
   V.bin = o;   o = align_up(o + V.B.total, 256);

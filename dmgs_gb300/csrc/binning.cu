@@ -514,7 +514,7 @@ row_emit_kernel(const BinViews bv) {
   for (int r = lane; r < gy; r += 32) rcur[r] = B.rcnt[(size_t)r * C + c];
   __syncwarp();
   const uint32_t s0 = B.cstart[c], s1 = B.cstart[c + 1];
-  const uint32_t cap = B.K_alloc;
+  const uint32_t cap = B.rows_alloc;
   const uint2 *__restrict__ srect = B.srect;
   const uint32_t *__restrict__ order = B.v0;
   uint2 *__restrict__ rowlist = B.rowlist;
@@ -905,11 +905,15 @@ int make_bin_view(const GeomLayout &L, char *geom, uint32_t K_cap, char *bin, ui
   B.rcnt = reinterpret_cast<uint32_t *>(geom + L.rcnt);
   B.cnt2 = reinterpret_cast<uint32_t *>(geom + L.cnt2);
   B.ranges = reinterpret_cast<uint2 *>(geom + L.ranges);
-  const BinLayout BL = bin_layout(K_alloc, 0, 0);
+  // the caller sized the state with bin_layout(K_alloc, ...) (plain form: K
+  // row entries) or bin_layout(K_alloc, ..., P) (capacity-bounded forms:
+  // fewer); the smaller bound is always inside the buffer
+  const BinLayout BL = bin_layout(K_alloc, L.gx * TILE, L.gy * TILE, L.P);
   B.point_list = bin ? reinterpret_cast<uint32_t *>(bin + BL.point_list) : nullptr;
   B.rowlist = bin ? reinterpret_cast<uint2 *>(bin + BL.rowlist) : nullptr;
   B.K_cap = K_cap;
   B.K_alloc = bin ? K_alloc : 0u;
+  B.rows_alloc = bin ? (uint32_t)BL.rows : 0u;
   B.cmax = CHUNK_COUNT_MAX;
   return DMGS_OK;
 }

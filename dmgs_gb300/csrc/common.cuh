@@ -137,19 +137,27 @@ __host__ __device__ inline GeomLayout geom_layout(int P, int W, int H) {
 // Binning state: the per-tile Gaussian index lists, concatenated in tile
 // order (K entries, 4 B each), then the row lists they are split from (one
 // 8-byte entry {Gaussian index, x0 | x1 << 16} per visible Gaussian and tile
-// row it covers; at most K entries, since every entry yields at least one
-// instance).
+// row it covers).  Row entries are at most K (every entry yields at least
+// one instance) and at most P x (tile rows); P < 0: bound by K alone.
 struct BinLayout {
-  size_t point_list, rowlist, total;
+  size_t point_list, rowlist, rows, total;
 };
 
-__host__ __device__ inline BinLayout bin_layout(int64_t K, int W, int H) {
-  (void)W; (void)H;
+__host__ __device__ inline size_t row_entries_max(int64_t K, int H, int64_t P) {
+  const size_t k = (size_t)(K > 0 ? K : 0);
+  if (P < 0) return k;
+  const size_t pr = (size_t)P * (size_t)((H + TILE - 1) / TILE);
+  return pr < k ? pr : k;
+}
+
+__host__ __device__ inline BinLayout bin_layout(int64_t K, int W, int H, int64_t P = -1) {
+  (void)W;
   BinLayout L;
   const size_t k = (size_t)(K > 0 ? K : 0);
   L.point_list = 0;
   L.rowlist = align_up(k * 4, 256);
-  L.total = L.rowlist + align_up(k * 8, 256) + 256;
+  L.rows = row_entries_max(K, H, P);
+  L.total = L.rowlist + align_up(L.rows * 8, 256) + 256;
   return L;
 }
 

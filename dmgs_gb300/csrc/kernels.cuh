@@ -59,7 +59,8 @@ struct BinView {
   uint32_t *point_list;  // emission target (K_alloc entries)
   uint2 *rowlist;        // row lists (K_alloc entries)
   uint32_t K_cap;        // list capacity checked by the ranges (0xffffffff: sized afterwards)
-  uint32_t K_alloc;      // entries of point_list and of rowlist
+  uint32_t K_alloc;      // entries of point_list
+  uint32_t rows_alloc;   // entries of rowlist
   uint32_t cmax;         // chunk bound
 };
 
