@@ -261,7 +261,12 @@ class HostPipeline:
         self.up = torch.cuda.Stream(device=dev)
         self.comp = torch.cuda.Stream(device=dev)
         self.down = torch.cuda.Stream(device=dev)
-        self.free = [None, None]  # per slot: its last download done
+        # Per slot: its last compute done (its inputs may be overwritten) and
+        # its last download done (its outputs may be overwritten).  An upload
+        # waits only for the former, a compute for the latter, so neither
+        # copy direction waits for the other.
+        self.inputs_free = [None, None]
+        self.outputs_free = [None, None]
         self.last = None
         self.i = 0
 
@@ -285,8 +290,8 @@ class HostPipeline:
         k = self.i % 2
         self.i += 1
         br = self.slots[k]
-        if self.free[k] is not None:
-            self.up.wait_event(self.free[k])
+        if self.inputs_free[k] is not None:
+            self.up.wait_event(self.inputs_free[k])
         with torch.cuda.stream(self.up):
             for n in self.names:
                 br.g[n].copy_(host_gaussians[n], non_blocking=True)
@@ -295,6 +300,8 @@ class HostPipeline:
             uploaded = torch.cuda.Event()
             uploaded.record(self.up)
         self.comp.wait_event(uploaded)
+        if self.outputs_free[k] is not None:
+            self.comp.wait_event(self.outputs_free[k])
         with torch.cuda.stream(self.comp):
             br.graph.replay()
             computed = torch.cuda.Event()
@@ -307,7 +314,8 @@ class HostPipeline:
                 host_grads[n].copy_(br.grads[n], non_blocking=True)
             done = torch.cuda.Event()
             done.record(self.down)
-        self.free[k] = done
+        self.inputs_free[k] = computed
+        self.outputs_free[k] = done
         self.last = done
         return done
 

@@ -11,9 +11,10 @@
 //
 // Design (both kernels are instruction-issue bound: the visible Gaussians'
 // records and the tile lists are L2-resident):
-// * a CTA blends one 16x16 tile at a time with 256/PPT threads; thread t
-//   owns the PPT pixels (t%16, t/16 + k*16/PPT), which share dx and every
-//   shared-memory load (PPT = 1, 2 or 4, a tuning parameter);
+// * a CTA blends one 16x16 tile at a time with 256/PPT threads; warp w owns
+//   the 2 PPT consecutive rows from 2 PPT w, lane l the PPT pixels of column
+//   l%16 in rows band + l/16 + 2k, which share dx and every shared-memory
+//   load (PPT = 1, 2 or 4, a tuning parameter);
 // * work items are the (view, tile) pairs of one or several views (the
 //   multi-view batched form renders many views in one launch); CTAs either
 //   take one item each or, persistent, pull items from an atomic counter;
@@ -25,10 +26,10 @@
 //   log2(1/(255 o)) is precomputed: a pair below it cannot reach alpha 1/255
 //   and is rejected before the exponential (the alpha test itself is still
 //   applied afterwards);
-// * each staged Gaussian carries row/column masks of the tile pixels its
-//   alpha >= 1/255 ellipse can reach (a superset): a warp skips it with one
-//   uniform test when it misses the warp's rows, a lane when it misses the
-//   lane's column — only pairs the exact test would reject are skipped;
+// * each staged Gaussian carries a mask of the tile rows its alpha >= 1/255
+//   ellipse can reach (a superset): a warp whose band it misses never
+//   visits it (per-warp visit lists, one ballot per 32 staged Gaussians) —
+//   only pairs the exact test would reject are skipped;
 // * the forward and the adjoint evaluate the exponent with the same
 //   explicitly rounded operations, so their skip/stop decisions agree;
 // * the adjoint sums a Gaussian's nine gradient terms over the thread's
@@ -54,13 +55,12 @@ __device__ __forceinline__ float ex2_approx(float x) {
 }
 
 // Staged Gaussian (forward): s0 = (x, y, A, B), s1 = (C, o, thr, r),
-// s2 = (g, b, footprint masks, 0) with exponent2 = A dx^2 + B dx dy + C dy^2
+// s2 = (g, b, footprint rows, 0) with exponent2 = A dx^2 + B dx dy + C dy^2
 // (A = -a log2e / 2, B = -b log2e, C = -c log2e / 2) and thr = log2(1 / (255 o)).
-// The footprint masks (bits 0-15: tile rows, 16-31: tile columns) cover the
-// pixels of this tile where alpha can reach 1/255: the ellipse
-// (a dx^2 + 2 b dx dy + c dy^2) <= 2 ln(255 o), whose half-extents are
-// sqrt(R^2 c / det) and sqrt(R^2 a / det), inflated by 0.1% + 0.01 px so that
-// the masks are a superset of the pixels the exact test accepts.
+// The footprint rows (bits 0-15) cover the tile rows where alpha can reach
+// 1/255: the ellipse (a dx^2 + 2 b dx dy + c dy^2) <= 2 ln(255 o), whose
+// vertical half-extent is sqrt(R^2 a / det), inflated by 0.1% + 0.01 px so
+// that the mask is a superset of the rows the exact test accepts.
 struct Staged {
   float4 s0, s1, s2;
 };
@@ -76,37 +76,38 @@ __device__ __forceinline__ uint32_t span_mask(float centre, float ext) {
 __device__ __forceinline__ uint32_t footprint(float a, float b, float c, float o, float cx, float cy) {
   if (!(o >= ALPHA_MIN)) return 0u;                  // alpha <= o < 1/255 everywhere
   const float det = a * c - b * b;
-  if (!(det > 0.f) || !(a > 0.f) || !(c > 0.f)) return 0xffffffffu;  // not an ellipse
+  if (!(det > 0.f) || !(a > 0.f) || !(c > 0.f)) return 0xffffu;  // not an ellipse
   const float R2 = 2.f * (__logf(o) + 5.541263545158426f);  // 2 ln(255 o)
   if (!(R2 >= 0.f)) return 0u;
-  const float ex = sqrtf(R2 * c / det) * 1.001f + 0.01f;
   const float ey = sqrtf(R2 * a / det) * 1.001f + 0.01f;
-  return span_mask(cy, ey) | (span_mask(cx, ex) << 16);
+  return span_mask(cy, ey);
 }
 
 // Row mask refined per row: for pixel row r (dy = cy - r fixed) the exponent
 // A dx^2 + B dx dy + C dy^2 (A < 0) is largest at dx = -B dy / (2A), clamped
 // to the tile's columns (dx in [cx - 15, cx], widened by 0.01); the row is kept
-// when that maximum reaches thr less a margin of 0.01 + 1e-5 x the sum of the
-// terms' magnitudes (far above the rounding of either evaluation).  Rows the
+// when that maximum reaches thr less a margin of 0.01 + 1e-5 x a bound on the
+// terms' magnitudes over the tile (|A| X^2 + |B| X Y + |C| Y^2 with X, Y the
+// largest |dx|, |dy|), far above the rounding of either evaluation.  Rows the
 // bounding-box mask keeps but no pixel of which reaches alpha 1/255 — the
 // ellipse passing the tile's corner — are dropped, so warps skip them.
 __device__ __forceinline__ uint32_t exact_rows(uint32_t m, float A, float B, float C, float thr,
                                                float cx, float cy) {
-  if (!(A < 0.f) || (m & 0xffffu) == 0u) return m;
+  if (!(A < 0.f) || m == 0u) return m;
   const float k = -B / (2.f * A);
   const float lo = cx - 15.01f, hi = cx + 0.01f;
+  const float X = fmaxf(fabsf(lo), fabsf(hi)), Y = fmaxf(fabsf(cy), fabsf(cy - 15.f));
+  const float mag = fabsf(A) * X * X + fabsf(B) * X * Y + fabsf(C) * Y * Y;
+  const float lim = thr - (0.01f + 1e-5f * mag);
   uint32_t rows = 0u;
 #pragma unroll
   for (int r = 0; r < 16; ++r) {
     const float dy = cy - (float)r;
     const float dxs = fminf(fmaxf(k * dy, lo), hi);
-    const float t1 = A * dxs * dxs, t2 = B * dxs * dy, t3 = C * dy * dy;
-    const float e = t1 + t2 + t3;
-    const float mag = fabsf(t1) + fabsf(t2) + fabsf(t3);
-    if (e >= thr - (0.01f + 1e-5f * mag)) rows |= 1u << r;
+    const float e = fmaf(fmaf(C, dy, B * dxs), dy, A * dxs * dxs);
+    if (e >= lim) rows |= 1u << r;
   }
-  return (m & 0xffff0000u) | (m & rows);
+  return m & rows;
 }
 
 // (ox, oy): pixel origin of the tile being blended.
@@ -184,24 +185,22 @@ __device__ __forceinline__ int visit_list(const uint32_t *masks, int cnt, uint32
   return nv;
 }
 
+// Warp w owns the band of 2 PPT consecutive tile rows starting at 2 PPT w;
+// lane l the column l % 16 and the rows band + l / 16 + 2k (k < PPT).  A
+// Gaussian whose footprint misses a band is never visited by its warp.
 template <int PPT>
 struct PixelLayout {
   static constexpr int THREADS = 256 / PPT;
-  static constexpr int RSTEP = 16 / PPT;  // rows between one thread's pixels
   int col, r0;
-  uint32_t colbit, warp_rows;
+  uint32_t warp_rows;
   __device__ __forceinline__ PixelLayout() {
     const int tid = threadIdx.x;
-    col = tid & 15;
-    r0 = tid >> 4;
-    colbit = 1u << (16 + col);
     const int w = tid >> 5;
-    uint32_t m = 0;
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) m |= 3u << (2 * w + k * RSTEP);
-    warp_rows = m;
+    col = tid & 15;
+    r0 = 2 * PPT * w + ((tid >> 4) & 1);
+    warp_rows = ((1u << (2 * PPT)) - 1u) << (2 * PPT * w);
   }
-  __device__ __forceinline__ int row(int k) const { return r0 + k * RSTEP; }
+  __device__ __forceinline__ int row(int k) const { return r0 + 2 * k; }
 };
 
 template <int PPT, int BATCH>
@@ -212,7 +211,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
   __shared__ float4 S0[2][BATCH];
   __shared__ float4 S1[2][BATCH];
   __shared__ float4 S2[2][BATCH];
-  __shared__ uint32_t SM[2][BATCH];              // footprint masks
+  __shared__ uint32_t SM[2][BATCH];              // footprint rows
   __shared__ uint16_t VL[THREADS / 32][BATCH];   // per-warp visit lists
   __shared__ int s_item;
   const int tid = threadIdx.x;
@@ -280,21 +279,20 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
       const int nvis = warp_done ? 0 : visit_list(SM[buf], cnt, lay.warp_rows, vl, lane);
       for (int i = 0; i < nvis && !warp_done; ++i) {
         const int j = vl[i];
-        const float4 s2 = S2[buf][j];
-        const uint32_t m = __float_as_uint(s2.z);
         const float4 s0 = S0[buf][j];
         const float4 s1 = S1[buf][j];
+        const float4 s2 = S2[buf][j];
         const float dx = __fsub_rn(s0.x, pxf);
-        const bool col_ok = (m & lay.colbit) != 0u;
-        // pass 1: exponent and range test of every pixel (no branches)
+        // pass 1: exponent and range test of every pixel (no branches); the
+        // footprint rows, a superset of what this test accepts, only
+        // select the warps that visit
         float e2[PPT];
         bool ok[PPT];
         bool any = false;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
           e2[k] = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, pyf[k]));
-          ok[k] = col_ok && !done[k] && ((m >> lay.row(k)) & 1u) && !(e2[k] > 0.f) &&
-                  !(e2[k] < s1.z);
+          ok[k] = !done[k] && !(e2[k] > 0.f) && !(e2[k] < s1.z);
           any |= ok[k];
         }
         if (!__any_sync(FULL, any)) continue;  // warp-uniform
@@ -336,7 +334,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
 // ------------------------------- adjoint -----------------------------------
 
 // Staged Gaussian (adjoint): s0 = (x, y, A, B), s1 = (C, o, thr, r),
-// s2 = (g, b, ka, kb), s3 = (kc, kd, id bits, footprint masks) with ka = -a W/2,
+// s2 = (g, b, ka, kb), s3 = (kc, kd, id bits, footprint rows) with ka = -a W/2,
 // kb = -b W/2, kc = -c H/2, kd = -b H/2 (the NDC-mean gradient factors).
 struct StagedB {
   float4 s0, s1, s2, s3;
@@ -357,9 +355,11 @@ __device__ __forceinline__ StagedB stage_b(const float4 f0, const float4 f1, con
 // being visited (excluding it); after a blended Gaussian with alpha a and
 // colour c it becomes acc + a (c - acc), the reference's one-step-delayed
 // update (last_alpha * last_color + (1 - last_alpha) * accum) done at once.
+// acc enters the gradients only through (c - acc) . dL/dpixel, so the state
+// keeps the scalar ag = acc . dL/dpixel, updated by ag + a (c . dL/dpixel - ag).
 struct PixelState {
   float T, Tfb, g0, g1, g2;  // transmittance, T_final * (bg . dL/dpixel), dL/dpixel
-  float acc_r, acc_g, acc_b;
+  float ag;
   uint32_t last_contrib;
 };
 
@@ -381,49 +381,48 @@ __device__ __forceinline__ void init_pixel(PixelState &ps, bool inside, int pix,
   ps.g2 = inside ? dL_dout[2 * HW + pix] : 0.f;
   ps.T = T_final;
   ps.Tfb = T_final * (bg0 * ps.g0 + bg1 * ps.g1 + bg2 * ps.g2);
-  ps.acc_r = ps.acc_g = ps.acc_b = 0.f;
+  ps.ag = 0.f;
 }
 
-// One (pixel, Gaussian) term of the adjoint, accumulated into e[0..8] when
-// `take` (the pair was blended in the forward); otherwise the state and e[]
-// are left as they are.  Evaluated without branches: the state updates are
-// selects or scaled by a factor selected to 0, so a warp whose lanes differ
-// in `take` runs one straight-line path.  T is recovered by dividing by
-// (1 - alpha) with the hardware reciprocal (alpha <= 0.99).
+// One (pixel, Gaussian) term of the adjoint, accumulated into e[0..2] and
+// e[6..8] when `take` (the pair was blended in the forward); otherwise the
+// state and e[] are left as they are.  Evaluated without branches: the state
+// updates are selects or scaled by a factor selected to 0, so a warp whose
+// lanes differ in `take` runs one straight-line path.  T is recovered by
+// dividing by (1 - alpha) with the hardware reciprocal (alpha <= 0.99).
 __device__ __forceinline__ void adjoint_pair(PixelState &ps, bool take, float alpha, float G,
                                              const float4 &s1, const float4 &s2, float dy,
                                              float *e) {
   const float inv = rcp_approx(1.f - alpha);
   const float Tn = ps.T * inv;
-  const float dr = s1.w - ps.acc_r, dg = s2.x - ps.acc_g, db = s2.y - ps.acc_b;
-  const float dL_dalpha = (dr * ps.g0 + dg * ps.g1 + db * ps.g2) * Tn - ps.Tfb * inv;
+  const float cg = fmaf(s2.y, ps.g2, fmaf(s2.x, ps.g1, s1.w * ps.g0));  // c . dL/dpixel
+  const float S = cg - ps.ag;                    // (c - acc) . dL/dpixel
+  const float dL_dalpha = S * Tn - ps.Tfb * inv;
   const float Gd = take ? G * dL_dalpha : 0.f;  // dL/dopacity term
   const float at = take ? alpha : 0.f;
   const float wt = at * Tn;                      // dL/drgb weight
-  const float u = s1.y * Gd;                     // dL/dpower = o G dL/dalpha
-  const float uy = u * dy;
-  // the thread's pixels share dx: the mean and conic terms need only
-  // sum u, sum u dy and sum u dy^2 (combined with dx once per Gaussian)
-  e[0] += u;
-  e[1] += uy;
-  e[2] += uy * dy;
-  e[5] += Gd;                     // dL/dopacity
+  const float gy = Gd * dy;
+  // dL/dpower = o G dL/dalpha and the thread's pixels share dx: the mean and
+  // conic terms need only sum Gd, sum Gd dy and sum Gd dy^2 (combined with
+  // o and dx once per Gaussian)
+  e[0] += Gd;
+  e[1] += gy;
+  e[2] += gy * dy;
   e[6] += wt * ps.g0;             // dL/drgb
   e[7] += wt * ps.g1;
   e[8] += wt * ps.g2;
   ps.T = take ? Tn : ps.T;
-  ps.acc_r = fmaf(at, dr, ps.acc_r);
-  ps.acc_g = fmaf(at, dg, ps.acc_g);
-  ps.acc_b = fmaf(at, db, ps.acc_b);
+  ps.ag = fmaf(at, S, ps.ag);
 }
 
-// From the thread's sums (e[0] = sum u, e[1] = sum u dy, e[2] = sum u dy^2
-// over its pixels, u = dL/dpower) to the mean and conic gradient terms:
-// e0 = dL/dndc_x, e1 = dL/dndc_y, e2..e4 = (sum u dx^2, sum u dx dy,
-// sum u dy^2) for the conic (scaled by -1/2, -1, -1/2 at the atomics).
-__device__ __forceinline__ void adjoint_finish(float dx, const float4 &s2, const float4 &s3,
-                                               float *e) {
-  const float su = e[0], suy = e[1], suy2 = e[2];
+// From the thread's sums (e[0] = sum Gd, e[1] = sum Gd dy, e[2] = sum Gd dy^2
+// over its pixels; u = o Gd = dL/dpower) to the gradient terms: e0 =
+// dL/dndc_x, e1 = dL/dndc_y, e2..e4 = (sum u dx^2, sum u dx dy, sum u dy^2)
+// for the conic (scaled by -1/2, -1, -1/2 at the atomics), e5 = dL/dopacity.
+__device__ __forceinline__ void adjoint_finish(float dx, float o, const float4 &s2,
+                                               const float4 &s3, float *e) {
+  e[5] = e[0];
+  const float su = o * e[0], suy = o * e[1], suy2 = o * e[2];
   const float sux = dx * su;
   e[0] = sux * s2.z + suy * s2.w;
   e[1] = suy * s3.x + sux * s3.y;
@@ -479,7 +478,7 @@ __global__ void __launch_bounds__(256 / PPT, PPT == 4 ? 10 : (PPT == 2 ? 6 : 4))
 blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
   constexpr int THREADS = 256 / PPT;
   __shared__ float4 S0[BATCH], S1[BATCH], S2[BATCH], S3[BATCH];
-  __shared__ uint32_t SM[BATCH];                // footprint masks
+  __shared__ uint32_t SM[BATCH];                // footprint rows
   __shared__ uint16_t VL[THREADS / 32][BATCH];  // per-warp visit lists
   __shared__ uint32_t sMaxLast;
   __shared__ int s_item;
@@ -534,25 +533,22 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
       for (int i = 0; i < nvis; ++i) {
         const int j = vl[i];
         const int li = top - 1 - j;
-        const float4 s3 = S3[j];
-        const uint32_t m = __float_as_uint(s3.w);
-        const float4 s0 = S0[j], s1 = S1[j], s2 = S2[j];
+        const float4 s0 = S0[j], s1 = S1[j];
         const float dx = __fsub_rn(s0.x, pxf);
-        const bool col_ok = (m & lay.colbit) != 0u;
         float e2[PPT];
         bool ok[PPT];
         bool cand = false;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
           e2[k] = exponent2(s0.z, s0.w, s1.x, dx, __fsub_rn(s0.y, pyf[k]));
-          ok[k] = col_ok && ((m >> lay.row(k)) & 1u) && li < (int)ps[k].last_contrib &&
-                  !(e2[k] > 0.f) && !(e2[k] < s1.z);
+          ok[k] = li < (int)ps[k].last_contrib && !(e2[k] > 0.f) && !(e2[k] < s1.z);
           cand |= ok[k];
         }
         if (!__any_sync(FULL, cand)) continue;  // warp-uniform
+        const float4 s2 = S2[j], s3 = S3[j];
         float e[9];
 #pragma unroll
-        for (int i = 0; i < 9; ++i) e[i] = 0.f;
+        for (int i = 0; i < 9; ++i) e[i] = 0.f;  // e[3..5] are set by adjoint_finish
         bool any = false;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
@@ -563,7 +559,7 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
           any |= take;
         }
         if (__ballot_sync(FULL, any)) {
-          adjoint_finish(dx, s2, s3, e);
+          adjoint_finish(dx, s1.y, s2, s3, e);
           const float sum = warp_reduce_scatter9(e, lane);
           const int slot = slot9((lane >> 1) & 15);
           if (!(lane & 1) && slot < 9) {
