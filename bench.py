@@ -615,6 +615,41 @@ def kernel_table(kt, model_args):
     return kernels
 
 
+def summary_of(line):
+    """The headline figure of every leg in a few hundred bytes, printed as the
+    line's last key so that a reader of only the line's end still sees them."""
+    r = lambda x, n=1: None if x is None else round(x, n)  # noqa: E731
+    s = {"views_per_s": r(line["value"]), "ms_per_step": r(line["ms_per_step"], 3)}
+    pl, mx, sv = line.get("plain"), line.get("mixed"), line.get("serving")
+    if pl:
+        s["plain_views_per_s"] = r(pl["views_per_s"])
+        s["batched_over_plain"] = r(pl.get("ratio_batched_over_plain"), 3)
+    if mx:
+        s["mixed_views_per_s"] = r(mx["batched_views_per_s"])
+        s["mixed_plain_views_per_s"] = r(mx.get("plain_views_per_s"))
+    if line.get("e2e"):
+        s["e2e_views_per_s"] = r(line["e2e"]["value"])
+    if line.get("roofline"):
+        s["roofline"] = f'{line["roofline"]["kernel"]} {line["roofline"]["frac"]}'
+    if line.get("kernels"):
+        s["kernel_ms"] = {k: r(v["avg_ms"], 3) for k, v in line["kernels"].items()}
+    if sv:
+        s["serving_p50_p99_ms"] = [r(sv["batched"]["p50_ms"], 3), r(sv["batched"]["p99_ms"], 3)]
+        s["serving_plain_p50_p99_ms"] = [r(sv["plain"]["p50_ms"], 3), r(sv["plain"]["p99_ms"], 3)]
+        s["serving_saturated_views_per_s"] = [r(sv["batched_saturated"]["views_per_s"]),
+                                              r(sv["plain_saturated"]["views_per_s"])]
+    if line.get("mesh_training"):
+        s["mesh_steps_per_s"] = r(line["mesh_training"]["steps_per_s"])
+    if line.get("stage2_full"):
+        s["stage2_steps_per_s"] = r(line["stage2_full"]["steps_per_s"])
+    if line.get("texture"):
+        s["texture_fwd_bwd_ms"] = r(line["texture"]["fwd_bwd_ms"], 3)
+    if line.get("flexicubes"):
+        s["flexicubes_fwd_bwd_ms"] = {k: r(v["fwd_bwd_ms"], 3) for k, v in line["flexicubes"].items()
+                                      if k.startswith("res")}
+    return s
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -891,6 +926,7 @@ def main():
             "serving": serving, "mesh_training": mesh, "flexicubes": fcl,
             "texture": texl, "stage2_full": st2,
             "gpu_launches": int(launches_per_step * args.steps), "clocks": clk}
+        line["summary"] = summary_of(line)  # last key: the headline figures of every leg
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
