@@ -110,7 +110,47 @@ __device__ __forceinline__ uint32_t exact_rows(uint32_t m, float A, float B, flo
   return m & rows;
 }
 
-// (ox, oy): pixel origin of the tile being blended.
+// Row mask at the granularity of the warps' bands of RB consecutive tile
+// rows (RB >= 4): a band's RB bits are set when the exponent can reach thr
+// somewhere in the rectangle dx in [cx - 15, cx], dy in [cy - r1, cy - r0]
+// (rows r0..r1 of the band, both ranges widened by 0.01): a continuous
+// superset of the band's pixels.  The exponent is concave (A < 0, the conic
+// positive definite), so its maximum over the rectangle is 0 when the
+// centre lies inside, else the largest of the four edges' maxima, each the
+// 1D maximum clamped to its edge (dx = kx dy on a horizontal edge, dy = ky dx
+// on a vertical one).  The margin is that of exact_rows.  Half the cost of
+// the per-row refinement at RB = 8, and the masks only select which warps
+// visit a staged Gaussian.
+template <int RB>
+__device__ __forceinline__ uint32_t band_rows(float a, float b, float c, float o, float A, float B,
+                                              float C, float thr, float cx, float cy) {
+  if (!(o >= ALPHA_MIN)) return 0u;  // alpha <= o < 1/255 everywhere
+  if (!(a * c - b * b > 0.f) || !(a > 0.f) || !(c > 0.f) || !(A < 0.f) || !(C < 0.f))
+    return 0xffffu;  // not an ellipse: every band
+  const float lo = cx - 15.01f, hi = cx + 0.01f;
+  const float X = fmaxf(fabsf(lo), fabsf(hi)), Y = fmaxf(fabsf(cy), fabsf(cy - 15.f));
+  const float mag = fabsf(A) * X * X + fabsf(B) * X * Y + fabsf(C) * Y * Y;
+  const float lim = thr - (0.01f + 1e-5f * mag);
+  const float kx = -B / (2.f * A), ky = -B / (2.f * C);
+  const float yl = ky * lo, yh = ky * hi;  // unclamped optimum dy on the two vertical edges
+  const bool x_in = lo <= 0.f && hi >= 0.f;
+  auto ev = [&](float dx, float dy) { return fmaf(fmaf(C, dy, B * dx), dy, A * dx * dx); };
+  uint32_t rows = 0u;
+#pragma unroll
+  for (int r0 = 0; r0 < 16; r0 += RB) {
+    const float ylo = cy - (float)(r0 + RB - 1) - 0.01f, yhi = cy - (float)r0 + 0.01f;
+    float e = fmaxf(ev(fminf(fmaxf(kx * ylo, lo), hi), ylo), ev(fminf(fmaxf(kx * yhi, lo), hi), yhi));
+    e = fmaxf(e, ev(lo, fminf(fmaxf(yl, ylo), yhi)));
+    e = fmaxf(e, ev(hi, fminf(fmaxf(yh, ylo), yhi)));
+    const bool keep = e >= lim || (x_in && ylo <= 0.f && yhi >= 0.f);
+    if (keep) rows |= ((1u << RB) - 1u) << r0;
+  }
+  return rows;
+}
+
+// (ox, oy): pixel origin of the tile being blended; RB: rows per warp band
+// (the mask's granularity: per row below 4).
+template <int RB>
 __device__ __forceinline__ Staged stage(const float4 f0, const float4 f1, const float4 f2,
                                         float ox, float oy) {
   Staged S;
@@ -119,7 +159,9 @@ __device__ __forceinline__ Staged stage(const float4 f0, const float4 f1, const 
   const float C = __fmul_rn(-0.5f * LOG2E, f1.x);
   const float thr = -LOG2_255 - __log2f(f1.y);
   const float cx = f0.x - ox, cy = f0.y - oy;
-  const uint32_t m = exact_rows(footprint(f0.z, f0.w, f1.x, f1.y, cx, cy), A, B, C, thr, cx, cy);
+  const uint32_t m =
+      RB >= 4 ? band_rows<RB>(f0.z, f0.w, f1.x, f1.y, A, B, C, thr, cx, cy)
+              : exact_rows(footprint(f0.z, f0.w, f1.x, f1.y, cx, cy), A, B, C, thr, cx, cy);
   S.s0 = make_float4(f0.x, f0.y, A, B);
   S.s1 = make_float4(C, f1.y, thr, f1.z);
   S.s2 = make_float4(f1.w, f2.x, __uint_as_float(m), 0.f);
@@ -259,7 +301,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
       for (int l = 0; l < LOADS; ++l) {
         const int sl = l * THREADS + tid;
         if (sl < BATCH && base + sl < n) {
-          const Staged st = stage(pf0[l], pf1[l], pf2[l], ox, oy);
+          const Staged st = stage<2 * PPT>(pf0[l], pf1[l], pf2[l], ox, oy);
           S0[buf][sl] = st.s0; S1[buf][sl] = st.s1; S2[buf][sl] = st.s2;
           SM[buf][sl] = __float_as_uint(st.s2.z);
         }
@@ -340,9 +382,10 @@ struct StagedB {
   float4 s0, s1, s2, s3;
 };
 
+template <int RB>
 __device__ __forceinline__ StagedB stage_b(const float4 f0, const float4 f1, const float4 f2,
                                            uint32_t id, float hw, float hh, float ox, float oy) {
-  const Staged s = stage(f0, f1, f2, ox, oy);
+  const Staged s = stage<RB>(f0, f1, f2, ox, oy);
   StagedB S;
   S.s0 = s.s0;
   S.s1 = s.s1;
@@ -523,7 +566,7 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
         const uint32_t id = V.point_list[range.x + top - 1 - sl];  // back to front
         float4 f0, f1, f2;
         load_record(V, id, f0, f1, f2);
-        const StagedB st = stage_b(f0, f1, f2, id, hw, hh, ox, oy);
+        const StagedB st = stage_b<2 * PPT>(f0, f1, f2, id, hw, hh, ox, oy);
         S0[sl] = st.s0; S1[sl] = st.s1; S2[sl] = st.s2; S3[sl] = st.s3;
         SM[sl] = __float_as_uint(st.s3.w);
       }
