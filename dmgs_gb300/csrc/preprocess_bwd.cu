@@ -50,6 +50,41 @@ __device__ __forceinline__ Slots make_slots(float *sm) {
   return S;
 }
 
+// Calls term(k, b_k, db_k/dx, db_k/dy, db_k/dz) for every SH basis function
+// of degree <= D at the unit direction (x, y, z) (the real SH basis with the
+// PlenOctree constants of utils/sh_utils.py:25-110), k in coefficient order.
+template <typename F>
+__device__ __forceinline__ void for_each_sh_term(int D, float x, float y, float z, F &&term) {
+  term(0, kSH_C0, 0.f, 0.f, 0.f);
+  if (D > 0) {
+    term(1, -kSH_C1 * y, 0.f, -kSH_C1, 0.f);
+    term(2, kSH_C1 * z, 0.f, 0.f, kSH_C1);
+    term(3, -kSH_C1 * x, -kSH_C1, 0.f, 0.f);
+    if (D > 1) {
+      const float xx = x * x, yy = y * y, zz = z * z;
+      term(4, kSH_C2[0] * x * y, kSH_C2[0] * y, kSH_C2[0] * x, 0.f);
+      term(5, kSH_C2[1] * y * z, 0.f, kSH_C2[1] * z, kSH_C2[1] * y);
+      term(6, kSH_C2[2] * (2.f * zz - xx - yy), -2.f * kSH_C2[2] * x, -2.f * kSH_C2[2] * y, 4.f * kSH_C2[2] * z);
+      term(7, kSH_C2[3] * x * z, kSH_C2[3] * z, 0.f, kSH_C2[3] * x);
+      term(8, kSH_C2[4] * (xx - yy), 2.f * kSH_C2[4] * x, -2.f * kSH_C2[4] * y, 0.f);
+      if (D > 2) {
+        term(9, kSH_C3[0] * y * (3.f * xx - yy), 6.f * kSH_C3[0] * x * y, kSH_C3[0] * (3.f * xx - 3.f * yy), 0.f);
+        term(10, kSH_C3[1] * x * y * z, kSH_C3[1] * y * z, kSH_C3[1] * x * z, kSH_C3[1] * x * y);
+        term(11, kSH_C3[2] * y * (4.f * zz - xx - yy), -2.f * kSH_C3[2] * x * y,
+             kSH_C3[2] * (4.f * zz - xx - 3.f * yy), 8.f * kSH_C3[2] * y * z);
+        term(12, kSH_C3[3] * z * (2.f * zz - 3.f * xx - 3.f * yy), -6.f * kSH_C3[3] * x * z,
+             -6.f * kSH_C3[3] * y * z, kSH_C3[3] * (6.f * zz - 3.f * xx - 3.f * yy));
+        term(13, kSH_C3[4] * x * (4.f * zz - xx - yy), kSH_C3[4] * (4.f * zz - 3.f * xx - yy),
+             -2.f * kSH_C3[4] * x * y, 8.f * kSH_C3[4] * x * z);
+        term(14, kSH_C3[5] * z * (xx - yy), 2.f * kSH_C3[5] * x * z, -2.f * kSH_C3[5] * y * z,
+             kSH_C3[5] * (xx - yy));
+        term(15, kSH_C3[6] * x * (xx - 3.f * yy), kSH_C3[6] * (3.f * xx - 3.f * yy),
+             -6.f * kSH_C3[6] * x * y, 0.f);
+      }
+    }
+  }
+}
+
 // ACC: add into the slots (several views of one Gaussian, possibly from
 // several threads at once: a shared-memory atomic add); else assign.
 template <bool ACC>
@@ -58,7 +93,9 @@ __device__ __forceinline__ void put(float &slot, float v) {
   else slot = v;
 }
 
-template <bool ACC>
+// SH: also the SH adjoint (dL/dsh and the direction term of dL/dmean);
+// without it the caller handles the SH colour's adjoint.
+template <bool ACC, bool SH = true>
 __device__ __forceinline__ void
 preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict__ viewm_g,
                    const float *__restrict__ projm_g, const float *__restrict__ campos_g, int M,
@@ -214,7 +251,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
   }
 
   // --- SH colour ---------------------------------------------------------
-  if (shs != nullptr) {
+  if (SH && shs != nullptr) {
     const uint8_t cl = flags[idx];
     if (cl & 1) drgb[0] = 0.f;
     if (cl & 2) drgb[1] = 0.f;
@@ -234,34 +271,7 @@ preprocess_bwd_one(int idx, int t, const ViewParams &vp, const float *__restrict
       const float dot = s0 * drgb[0] + s1 * drgb[1] + s2 * drgb[2];
       gdx += bx * dot; gdy += by * dot; gdz += bz * dot;
     };
-    term(0, kSH_C0, 0.f, 0.f, 0.f);
-    if (vp.D > 0) {
-      term(1, -kSH_C1 * y, 0.f, -kSH_C1, 0.f);
-      term(2, kSH_C1 * z, 0.f, 0.f, kSH_C1);
-      term(3, -kSH_C1 * x, -kSH_C1, 0.f, 0.f);
-      if (vp.D > 1) {
-        const float xx = x * x, yy = y * y, zz = z * z;
-        term(4, kSH_C2[0] * x * y, kSH_C2[0] * y, kSH_C2[0] * x, 0.f);
-        term(5, kSH_C2[1] * y * z, 0.f, kSH_C2[1] * z, kSH_C2[1] * y);
-        term(6, kSH_C2[2] * (2.f * zz - xx - yy), -2.f * kSH_C2[2] * x, -2.f * kSH_C2[2] * y, 4.f * kSH_C2[2] * z);
-        term(7, kSH_C2[3] * x * z, kSH_C2[3] * z, 0.f, kSH_C2[3] * x);
-        term(8, kSH_C2[4] * (xx - yy), 2.f * kSH_C2[4] * x, -2.f * kSH_C2[4] * y, 0.f);
-        if (vp.D > 2) {
-          term(9, kSH_C3[0] * y * (3.f * xx - yy), 6.f * kSH_C3[0] * x * y, kSH_C3[0] * (3.f * xx - 3.f * yy), 0.f);
-          term(10, kSH_C3[1] * x * y * z, kSH_C3[1] * y * z, kSH_C3[1] * x * z, kSH_C3[1] * x * y);
-          term(11, kSH_C3[2] * y * (4.f * zz - xx - yy), -2.f * kSH_C3[2] * x * y,
-               kSH_C3[2] * (4.f * zz - xx - 3.f * yy), 8.f * kSH_C3[2] * y * z);
-          term(12, kSH_C3[3] * z * (2.f * zz - 3.f * xx - 3.f * yy), -6.f * kSH_C3[3] * x * z,
-               -6.f * kSH_C3[3] * y * z, kSH_C3[3] * (6.f * zz - 3.f * xx - 3.f * yy));
-          term(13, kSH_C3[4] * x * (4.f * zz - xx - yy), kSH_C3[4] * (4.f * zz - 3.f * xx - yy),
-               -2.f * kSH_C3[4] * x * y, 8.f * kSH_C3[4] * x * z);
-          term(14, kSH_C3[5] * z * (xx - yy), 2.f * kSH_C3[5] * x * z, -2.f * kSH_C3[5] * y * z,
-               kSH_C3[5] * (xx - yy));
-          term(15, kSH_C3[6] * x * (xx - 3.f * yy), kSH_C3[6] * (3.f * xx - 3.f * yy),
-               -6.f * kSH_C3[6] * x * y, 0.f);
-        }
-      }
-    }
+    for_each_sh_term(vp.D, x, y, z, term);
     if (dsh)
       if (!ACC) for (int i = 3 * nsh; i < 3 * M; ++i) dsh[i * SP] = 0.f;
     // d unit(v)/dv . g = (g - u (u . g)) / |v|
@@ -380,32 +390,46 @@ preprocess_bwd_kernel(ViewParams vp, const float *__restrict__ viewm_g,
 
 // Multi-view adjoint: the gradients of all views of a batch, summed.  A
 // Gaussian is visible in few of the views, so a thread per Gaussian looping
-// over the views would leave most lanes idle.  Instead the block lists its
-// (Gaussian, view) pairs — thread t's Gaussian contributes one pair per view
-// it is visible in, placed by a block-wide scan — and the threads take the
-// pairs in turn, adding each view's gradients into the Gaussian's shared-
-// memory slots with atomic adds; the block then stores its slices once.  The
-// per-view screen-space gradient and the densification statistics (optional
-// outputs) are handled by each Gaussian's own thread: all views' visibility
-// bytes and 2D gradients are loaded at once (independent loads), then
-// written out, zero where the Gaussian is not visible.
+// over the views would leave most lanes idle for the geometric part (the
+// longest).  Instead the block lists its (Gaussian, view) pairs — thread t's
+// Gaussian contributes one pair per view it is visible in, placed by a
+// block-wide scan — and the threads take the pairs in turn, adding each
+// view's geometric gradients (mean through the projection and the EWA
+// Jacobian, scale and rotation or covariance, opacity, colour: 14 values)
+// into the Gaussian's shared-memory sums with atomic adds.  The SH part is
+// linear in each view's colour gradient: the Gaussian's own thread then runs
+// it over its views with the 3M SH-gradient sums in registers, adds each
+// view's direction term to the mean gradient and writes every output of its
+// Gaussian (zeros when it is culled in every view).  The per-view
+// screen-space gradient and the densification statistics (optional
+// outputs) are handled by the same thread: all views' visibility bytes and
+// 2D gradients are loaded at once (independent loads), then written out,
+// zero where the Gaussian is not visible.
+constexpr int ACC_SLOTS = 14;  // colour 3, opacity 1, mean 3, scale 3 + rotation 4 (or covariance 6)
+
 __global__ void __launch_bounds__(BWD_BLOCK)
 preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__restrict__ means,
                               const float *__restrict__ shs, const float *__restrict__ scales,
                               const float *__restrict__ rots, const float *__restrict__ cov3D,
                               DmgsGrads out, int want_xy, float *__restrict__ densify_accum,
                               float *__restrict__ densify_count) {
-  extern __shared__ float sm[];
-  __shared__ uint32_t vmask[BWD_BLOCK / 32];
+  __shared__ float acc[ACC_SLOTS * SP];
   __shared__ uint32_t wsum[BWD_BLOCK / 32];
   __shared__ uint16_t pairs[BWD_BLOCK * MAX_BATCH_VIEWS];
   const int B = BWD_BLOCK;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const int start = blockIdx.x * B;
   const int idx = start + t;
-  const Slots S_ = make_slots(sm);
-  const int nslot = (int)slot_floats(M);
-  for (int i = t; i < nslot; i += B) sm[i] = 0.f;
+  Slots S_;
+  S_.m2 = nullptr;
+  S_.col = acc;
+  S_.op = acc + 3 * SP;
+  S_.m3 = acc + 4 * SP;
+  S_.sc = acc + 7 * SP;
+  S_.rot = acc + 10 * SP;
+  S_.cov = acc + 7 * SP;  // covariance mode has no scale/rotation
+  S_.sh = nullptr;
+  for (int i = t; i < ACC_SLOTS * SP; i += B) acc[i] = 0.f;
   // per-view constants in shared memory: the pair loop below reads them
   // with a different view per lane, which from the kernel parameters would
   // be serialised constant-bank loads
@@ -424,12 +448,12 @@ preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__
     s_mat[v][k] = k < 16 ? __ldg(W.viewm + k) : (k < 32 ? __ldg(W.projm + k - 16) : __ldg(W.campos + k - 32));
   }
   uint32_t vm = 0u;
+  uint8_t fl[MAX_BATCH_VIEWS];
   if (idx < P) {
-    uint32_t f[MAX_BATCH_VIEWS];
 #pragma unroll
-    for (int v = 0; v < MAX_BATCH_VIEWS; ++v) f[v] = v < bv.nviews ? bv.v[v].flags[idx] : 0u;
+    for (int v = 0; v < MAX_BATCH_VIEWS; ++v) fl[v] = v < bv.nviews ? bv.v[v].flags[idx] : 0u;
 #pragma unroll
-    for (int v = 0; v < MAX_BATCH_VIEWS; ++v) vm |= ((f[v] & FLAG_VISIBLE) ? 1u : 0u) << v;
+    for (int v = 0; v < MAX_BATCH_VIEWS; ++v) vm |= ((fl[v] & FLAG_VISIBLE) ? 1u : 0u) << v;
     if (want_xy) {
       float2 g2[MAX_BATCH_VIEWS];
 #pragma unroll
@@ -463,8 +487,6 @@ preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__
     if (lane >= o) inc += u;
   }
   if (lane == 31) wsum[wid] = inc;
-  const uint32_t bal = __ballot_sync(0xffffffffu, vm != 0u);
-  if (lane == 0) vmask[wid] = bal;
   __syncthreads();
   uint32_t off = inc - cnt, total = 0;
 #pragma unroll
@@ -478,18 +500,84 @@ preprocess_bwd_batched_kernel(const BatchViews bv, int P, int M, const float *__
     const uint32_t pr = pairs[i];
     const int gl = (int)(pr >> 4), v = (int)(pr & 15u);
     const ViewParams vp = s_vp[v];
-    preprocess_bwd_one<true>(start + gl, gl, vp, s_mat[v], s_mat[v] + 16, s_mat[v] + 32, M, means,
-                             shs, scales, rots, cov3D, s_flags[v], s_gacc[v], out, S_);
+    preprocess_bwd_one<true, false>(start + gl, gl, vp, s_mat[v], s_mat[v] + 16, s_mat[v] + 32, M,
+                                    means, shs, scales, rots, cov3D, s_flags[v], s_gacc[v], out, S_);
   }
   __syncthreads();
-  const int nvalid = min(B, P - start);
-  store_slice(out.dL_dcolors, S_.col, 3, start, nvalid, vmask);
-  store_slice(out.dL_dopacity, S_.op, 1, start, nvalid, vmask);
-  store_slice(out.dL_dmeans3D, S_.m3, 3, start, nvalid, vmask);
-  store_slice(out.dL_dcov3D, S_.cov, 6, start, nvalid, vmask);
-  store_slice(out.dL_dscales, S_.sc, 3, start, nvalid, vmask);
-  store_slice(out.dL_drotations, S_.rot, 4, start, nvalid, vmask);
-  store_slice(out.dL_dsh, S_.sh, 3 * M, start, nvalid, vmask);
+  if (idx >= P) return;
+
+  // --- the Gaussian's own thread: SH over its views, then every output ---
+  float dm[3] = {S_.m3[t], S_.m3[SP + t], S_.m3[2 * SP + t]};
+  const bool want_sh = shs != nullptr && (out.dL_dsh != nullptr || out.dL_dmeans3D != nullptr);
+  float dsh[48];
+#pragma unroll
+  for (int i = 0; i < 48; ++i) dsh[i] = 0.f;
+  if (want_sh && vm) {
+    const float mx = means[3 * (size_t)idx], my = means[3 * (size_t)idx + 1],
+                mz = means[3 * (size_t)idx + 2];
+    const float *sh = shs + (size_t)idx * M * 3;
+    for (uint32_t m = vm; m; m &= m - 1) {
+      const int v = __ffs(m) - 1;
+      const float *gv = s_gacc[v] + 12 * (size_t)idx;
+      float drgb[3] = {gv[6], gv[7], gv[8]};
+      const uint32_t clamp = s_flags[v][idx];
+      if (clamp & 1) drgb[0] = 0.f;
+      if (clamp & 2) drgb[1] = 0.f;
+      if (clamp & 4) drgb[2] = 0.f;
+      const float *cp = s_mat[v] + 32;
+      const float vx_ = mx - cp[0], vy_ = my - cp[1], vz_ = mz - cp[2];
+      const float len = sqrtf(vx_ * vx_ + vy_ * vy_ + vz_ * vz_);
+      const float il = 1.f / len;
+      const float x = vx_ * il, y = vy_ * il, z = vz_ * il;
+      float gdx = 0.f, gdy = 0.f, gdz = 0.f;
+      for_each_sh_term(s_vp[v].D, x, y, z, [&](int k, float b, float bx, float by, float bz) {
+        dsh[3 * k] += b * drgb[0];
+        dsh[3 * k + 1] += b * drgb[1];
+        dsh[3 * k + 2] += b * drgb[2];
+        const float dot = sh[3 * k] * drgb[0] + sh[3 * k + 1] * drgb[1] + sh[3 * k + 2] * drgb[2];
+        gdx += bx * dot; gdy += by * dot; gdz += bz * dot;
+      });
+      const float ug = x * gdx + y * gdy + z * gdz;
+      dm[0] += (gdx - x * ug) * il;
+      dm[1] += (gdy - y * ug) * il;
+      dm[2] += (gdz - z * ug) * il;
+    }
+  }
+  const size_t i3 = 3 * (size_t)idx;
+  if (out.dL_dcolors) {
+    out.dL_dcolors[i3] = S_.col[t]; out.dL_dcolors[i3 + 1] = S_.col[SP + t]; out.dL_dcolors[i3 + 2] = S_.col[2 * SP + t];
+  }
+  if (out.dL_dopacity) out.dL_dopacity[idx] = S_.op[t];
+  if (out.dL_dmeans3D) {
+    out.dL_dmeans3D[i3] = dm[0]; out.dL_dmeans3D[i3 + 1] = dm[1]; out.dL_dmeans3D[i3 + 2] = dm[2];
+  }
+  if (out.dL_dcov3D) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) out.dL_dcov3D[6 * (size_t)idx + k] = S_.cov[k * SP + t];
+  }
+  if (out.dL_dscales) {
+    out.dL_dscales[i3] = S_.sc[t]; out.dL_dscales[i3 + 1] = S_.sc[SP + t]; out.dL_dscales[i3 + 2] = S_.sc[2 * SP + t];
+  }
+  if (out.dL_drotations)
+    reinterpret_cast<float4 *>(out.dL_drotations)[idx] =
+        make_float4(S_.rot[t], S_.rot[SP + t], S_.rot[2 * SP + t], S_.rot[3 * SP + t]);
+  if (out.dL_dsh) {
+    // the Gaussian's 3M contiguous floats: coefficients above degree 3 (or
+    // the active degree) stay zero
+    float *d = out.dL_dsh + (size_t)idx * M * 3;
+    const int n = 3 * M;
+    if (n >= 48 && (n & 3) == 0 && (reinterpret_cast<uintptr_t>(d) & 15) == 0) {
+      float4 *d4 = reinterpret_cast<float4 *>(d);
+#pragma unroll
+      for (int i = 0; i < 12; ++i) d4[i] = make_float4(dsh[4 * i], dsh[4 * i + 1], dsh[4 * i + 2], dsh[4 * i + 3]);
+      for (int i = 12; i < (n >> 2); ++i) d4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 48; ++i)
+        if (i < n) d[i] = dsh[i];
+      for (int i = 48; i < n; ++i) d[i] = 0.f;
+    }
+  }
 }
 
 }  // namespace
@@ -519,17 +607,10 @@ namespace dmgs {
 int launch_preprocess_bwd_batched(const BatchViews &bv, const GaussianPtrs &g, const DmgsGrads &out,
                                   float *densify_accum, float *densify_count, cudaStream_t s) {
   if (g.P <= 0) return DMGS_OK;
-  const size_t smem = slot_floats(g.M) * 4;
-  if (smem > 200 * 1024) {
-    dmgs_host::set_error("preprocess_bwd: %d SH coefficients per Gaussian exceed shared memory", g.M);
-    return DMGS_ERR_ARG;
-  }
   int want_xy = densify_accum != nullptr;
   for (int v = 0; v < bv.nviews; ++v) want_xy |= bv.v[v].dL_dmeans2D != nullptr;
-  if (int r = dmgs_host::raise_smem_limit((const void *)preprocess_bwd_batched_kernel, smem))
-    return r;
   DMGS_TIMED(K_BATCH_PREPROCESS_BWD, s,
-             dmgs_host::note_launch(), preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, smem, s>>>(
+             dmgs_host::note_launch(), preprocess_bwd_batched_kernel<<<(g.P + BWD_BLOCK - 1) / BWD_BLOCK, BWD_BLOCK, 0, s>>>(
                  bv, g.P, g.M, g.means3D, g.shs, g.scales, g.rotations, g.cov3D, out, want_xy,
                  densify_accum, densify_count));
   DMGS_LAUNCH_CHECK("preprocess_bwd_batched_kernel");
