@@ -615,6 +615,12 @@ def kernel_table(kt, model_args):
     return kernels
 
 
+def blend_config(cfg):
+    from dmgs_gb300.batched import TILE_SHAPES
+    return {"pixels_per_thread": cfg[0], "gaussians_per_batch": cfg[1],
+            "cta_shape": TILE_SHAPES[cfg[2] if len(cfg) > 2 else 0]}
+
+
 def summary_of(line):
     """The headline figure of every leg in a few hundred bytes, printed as the
     line's last key so that a reader of only the line's end still sees them."""
@@ -798,8 +804,9 @@ def main():
         bm.status()
         mixed = {"views": nv, "resolutions": MIXED,
                  "batched_views_per_s": nv * args.steps / (ms_mb / 1e3),
-                 "blend_config": {"pixels_per_thread": bm.cfg[0], "gaussians_per_batch": bm.cfg[1]},
-                 "autotune": mtune and {"best": mtune["best"], "ms": mtune["ms"]}}
+                 "blend_config": blend_config(bm.cfg),
+                 "autotune": mtune and {"best": mtune["best"], "axes": mtune.get("axes"),
+                                        "ms": mtune["ms"]}}
         if ms_mplain is not None:
             mixed["plain_views_per_s"] = nv / (ms_mplain / 1e3)
             mixed["ratio_batched_over_plain"] = (nv * args.steps / ms_mb) / (nv / ms_mplain)
@@ -917,11 +924,11 @@ def main():
                                   "statistics (fused add_densification_stats)",
                        "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
                        "mean_row_entries_K1": int(K1_sum / nv),
-                       "blend_config": {"pixels_per_thread": br_cfg[0], "gaussians_per_batch": br_cfg[1]},
+                       "blend_config": blend_config(br_cfg),
                        "graph": not args.no_graph},
             "plain": plain,
             "mixed": mixed,
-            "autotune": tune and {"best": tune["best"], "ms": tune["ms"]},
+            "autotune": tune and {"best": tune["best"], "axes": tune.get("axes"), "ms": tune["ms"]},
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
             "serving": serving, "mesh_training": mesh, "flexicubes": fcl,
             "texture": texl, "stage2_full": st2,

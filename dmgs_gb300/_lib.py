@@ -13,7 +13,7 @@ import torch  # noqa: F401  (loads libcudart before the extension)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdmgs_gb300.so")
-ABI_VERSION = 6  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
+ABI_VERSION = 7  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
 
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -67,7 +67,7 @@ class DmgsBatch(C.Structure):
     _fields_ = [("nviews", C.c_int32), ("views", C.POINTER(DmgsView)),
                 ("out_color", C.POINTER(vp)), ("radii", C.POINTER(vp)),
                 ("capacity", C.POINTER(C.c_int64)), ("pixels_per_thread", C.c_int32),
-                ("gaussians_per_batch", C.c_int32)]
+                ("gaussians_per_batch", C.c_int32), ("tile_shape", C.c_int32)]
 
 
 DMGS_ERRORS = {-1: "DMGS_ERR_ARG", -2: "DMGS_ERR_CUDA", -3: "DMGS_ERR_STATE",

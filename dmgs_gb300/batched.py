@@ -30,7 +30,12 @@ GAUSSIAN_KEYS = ("means3D", "opacities", "shs", "colors_precomp", "scales", "rot
                  "cov3D_precomp")
 
 MAX_VIEWS = 16
-TUNE_SPACE = [(p, b) for p in (1, 2, 4) for b in (128, 256, 512)]
+# Blend tuning: (pixels per thread, Gaussians per staged batch, CTA shape);
+# shape 0 = one 16x16 binning tile per CTA, 1 = 32x16 and 2 = 16x32 pixels
+# (two adjacent binning tiles, each blended from its own list).
+TILE_SHAPES = {0: "16x16", 1: "32x16", 2: "16x32"}
+TUNE_SPACE = ([(p, b, 0) for p in (1, 2, 4) for b in (128, 256, 512)] +
+              [(p, b, sh) for sh in (1, 2) for p in (2, 4) for b in (128, 256)])
 
 
 def _view_struct(rs: GaussianRasterizationSettings, device, keep):
@@ -63,7 +68,7 @@ class BatchedRasterizer:
     gradients for training, without writing [P, 3] per view.
     """
 
-    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(4, 128),
+    def __init__(self, settings, gaussians, capacity=None, margin=1.25, cfg=(4, 128, 0),
                  means2D_grads=True, densify_stats=False):
         if not 1 <= len(settings) <= MAX_VIEWS:
             raise ValueError(f"a batch holds 1..{MAX_VIEWS} views")
@@ -93,7 +98,7 @@ class BatchedRasterizer:
                               if means2D_grads else None)
         self.densify_accum = torch.zeros(self.P, device=d) if densify_stats else None
         self.densify_count = torch.zeros(self.P, device=d) if densify_stats else None
-        self.cfg = tuple(cfg)
+        self.cfg = _cfg3(cfg)
         self.graph = None
         if capacity is None:
             capacity = [int(k * margin) + 1024 for k in self.count_instances()]
@@ -135,8 +140,7 @@ class BatchedRasterizer:
         self._dout = (C.c_void_p * self.n)(*[t.data_ptr() for t in self.dL_dout])
         self._m2 = ((C.c_void_p * self.n)(*[t.data_ptr() for t in self.means2D_grads])
                     if self.means2D_grads is not None else None)
-        self.batch = DmgsBatch(self.n, self.views, self._out, self._rad, self._cap, self.cfg[0],
-                               self.cfg[1])
+        self.batch = DmgsBatch(self.n, self.views, self._out, self._rad, self._cap, *self.cfg)
         nbytes = self.lib.dmgs_batch_state_bytes(C.byref(self.batch), self.P)
         if nbytes == 0:
             raise DmgsError(-1, "batch", self.lib.dmgs_last_error().decode())
@@ -147,10 +151,13 @@ class BatchedRasterizer:
                                 ptr(g["rotations"]))
         self.graph = None
 
-    def set_config(self, ppt, batch):
-        self.cfg = (int(ppt), int(batch))
+    def set_config(self, ppt, batch, shape=0):
+        """Blend tuning: pixels per thread, Gaussians per batch, CTA shape
+        (see ``TILE_SHAPES``)."""
+        self.cfg = _cfg3((ppt, batch, shape))
         self.batch.pixels_per_thread = self.cfg[0]
         self.batch.gaussians_per_batch = self.cfg[1]
+        self.batch.tile_shape = self.cfg[2]
         self.graph = None
 
     # -- work ---------------------------------------------------------------
@@ -270,9 +277,9 @@ class HostPipeline:
         self.last = None
         self.i = 0
 
-    def set_config(self, ppt, batch):
+    def set_config(self, ppt, batch, shape=0):
         for br in self.slots:
-            br.set_config(ppt, batch)
+            br.set_config(ppt, batch, shape)
             br.capture()
 
     def start(self):
@@ -326,10 +333,22 @@ class HostPipeline:
             cur.wait_stream(st)
 
 
+def _cfg3(cfg):
+    """(pixels per thread, batch[, shape]) -> a 3-tuple of ints (shape 0 if absent)."""
+    c = tuple(int(x) for x in cfg)
+    return c if len(c) == 3 else (c[0], c[1], 0)
+
+
+def config_name(cfg):
+    ppt, b, sh = _cfg3(cfg)
+    return f"{ppt}x{b}@{TILE_SHAPES[sh]}"
+
+
 def autotune(br: BatchedRasterizer, space=TUNE_SPACE, iters=5, cache_path=None):
-    """Time forward + backward for every (pixels/thread, batch) pair and
-    keep the fastest; the choice is cached in JSON at ``cache_path`` (default
-    ``$DMGS_AUTOTUNE_CACHE`` if set) keyed by device, P and resolutions."""
+    """Time forward + backward for every (pixels/thread, batch, CTA shape)
+    in ``space`` and keep the fastest; the choice is cached in JSON at
+    ``cache_path`` (default ``$DMGS_AUTOTUNE_CACHE`` if set) keyed by device,
+    P and resolutions."""
     key = json.dumps([torch.cuda.get_device_name(br.device), br.P,
                       [(s.image_width, s.image_height) for s in br.settings]])
     cache_path = cache_path or os.environ.get("DMGS_AUTOTUNE_CACHE")
@@ -342,9 +361,9 @@ def autotune(br: BatchedRasterizer, space=TUNE_SPACE, iters=5, cache_path=None):
     if key in cache:
         br.set_config(*cache[key]["best"])
         return cache[key]
-    times = {}
-    for ppt, b in space:
-        br.set_config(ppt, b)
+    times, names = {}, {}
+    for cfg in space:
+        br.set_config(*cfg)
         br.step()
         torch.cuda.synchronize(br.device)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -353,11 +372,15 @@ def autotune(br: BatchedRasterizer, space=TUNE_SPACE, iters=5, cache_path=None):
             br.step()
         e1.record()
         torch.cuda.synchronize(br.device)
-        times[f"{ppt}x{b}"] = e0.elapsed_time(e1) / iters
+        name = config_name(cfg)
+        times[name] = e0.elapsed_time(e1) / iters
+        names[name] = _cfg3(cfg)
     best = min(times, key=times.get)
-    ppt, b = (int(x) for x in best.split("x"))
-    br.set_config(ppt, b)
-    result = {"best": [ppt, b], "ms": times, "when": time.time()}
+    br.set_config(*names[best])
+    result = {"best": list(names[best]), "ms": times, "when": time.time(),
+              "axes": {"pixels_per_thread": sorted({c[0] for c in names.values()}),
+                       "gaussians_per_batch": sorted({c[1] for c in names.values()}),
+                       "cta_shape": [TILE_SHAPES[k] for k in sorted({c[2] for c in names.values()})]}}
     if cache_path:
         cache[key] = result
         os.makedirs(os.path.dirname(os.path.abspath(cache_path)), exist_ok=True)

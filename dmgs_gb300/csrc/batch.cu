@@ -158,6 +158,15 @@ int check_common(const DmgsBatch *b, const DmgsGaussians *g, void *state, size_t
   }
   for (int v = 0; v < b->nviews; ++v) RET_IF(check_view(b->views[v], v));
   for (int v = 0; v < b->nviews; ++v) RET_IF(check_gaussians(g, b->views[v], v));
+  const int ppt = b->pixels_per_thread ? b->pixels_per_thread : 4;
+  const int gpb = b->gaussians_per_batch ? b->gaussians_per_batch : 128;
+  const bool pair = b->tile_shape == 1 || b->tile_shape == 2;
+  if ((ppt != 1 && ppt != 2 && ppt != 4) || (gpb != 128 && gpb != 256 && gpb != 512) ||
+      b->tile_shape < 0 || b->tile_shape > 2 || (pair && (ppt == 1 || gpb == 512))) {
+    set_error("batch: unsupported blend tuning: %d pixels/thread, batch %d, tile shape %d", ppt,
+              gpb, b->tile_shape);
+    return DMGS_ERR_ARG;
+  }
   return DMGS_OK;
 }
 
@@ -165,6 +174,8 @@ BlendCfg cfg_of(const DmgsBatch *b) {
   BlendCfg c = default_blend_cfg();
   if (b->pixels_per_thread) c.ppt = b->pixels_per_thread;
   if (b->gaussians_per_batch) c.batch = b->gaussians_per_batch;
+  if (b->tile_shape == 1) c.sx = 2;
+  if (b->tile_shape == 2) c.sy = 2;
   return c;
 }
 

@@ -162,23 +162,47 @@ scan_down_kernel(const ScanViews sv) {
 
 // ---- compaction of visible Gaussians (index order) ----------------------
 
+// Each block compacts CPT preprocess blocks (PRE_BLOCK x CPT Gaussians, CPT
+// consecutive per thread, their flag bytes read as one word); the scanned
+// per-preprocess-block counts give the block's first output position.
+constexpr int CPT = 4;
+
 __global__ void __launch_bounds__(PRE_BLOCK)
 compact_kernel(const BinViews bv) {
   const BinView &B = bv.v[blockIdx.y];
-  if ((int)blockIdx.x >= B.nb_pre) return;
-  const int idx = blockIdx.x * PRE_BLOCK + threadIdx.x;
-  const bool v = idx < B.P && (B.flags[idx] & FLAG_VISIBLE);
-  __shared__ uint32_t wcount[PRE_BLOCK / 32];
+  const int base = blockIdx.x * PRE_BLOCK * CPT;
+  if (base >= B.P) return;  // block-uniform
+  const int i0 = base + threadIdx.x * CPT;
+  uint32_t f4 = 0u;
+  if (i0 + CPT <= B.P) {
+    f4 = *reinterpret_cast<const uint32_t *>(B.flags + i0);  // i0 % 4 == 0, the array 256-B aligned
+  } else {
+#pragma unroll
+    for (int k = 0; k < CPT; ++k)
+      if (i0 + k < B.P) f4 |= (uint32_t)B.flags[i0 + k] << (8 * k);
+  }
+  uint32_t vis = 0u;
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) vis |= ((f4 >> (8 * k)) & FLAG_VISIBLE) ? 1u << k : 0u;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned b = __ballot_sync(FULL, v);
-  if (lane == 0) wcount[wid] = __popc(b);
+  const int c = __popc(vis);
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(FULL, incl, o);
+    if (lane >= o) incl += u;
+  }
+  __shared__ int wsum[PRE_BLOCK / 32];
+  if (lane == 31) wsum[wid] = incl;
   __syncthreads();
-  uint32_t before = 0;
-  for (int w = 0; w < wid; ++w) before += wcount[w];
-  if (v) {
-    const uint32_t pos = B.blkcnt[blockIdx.x] + before + __popc(b & lanemask_lt());
-    B.k0[pos] = __float_as_uint(B.feat[3 * idx + 2].y);
+  uint32_t pos = B.blkcnt[blockIdx.x * CPT] + (uint32_t)(incl - c);
+  for (int w = 0; w < wid; ++w) pos += (uint32_t)wsum[w];
+  const float *feat = reinterpret_cast<const float *>(B.feat);
+  for (uint32_t m = vis; m; m &= m - 1) {
+    const int idx = i0 + __ffs(m) - 1;
+    B.k0[pos] = __float_as_uint(feat[12 * (size_t)idx + 9]);  // depth: record float 9
     B.v0[pos] = (uint32_t)idx;
+    ++pos;
   }
 }
 
@@ -945,7 +969,7 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
         return ScanView{B.blkcnt, nullptr, (uint32_t)B.nb_pre, B.part, B.counters + CI_V, B.counters};
       }), s);
       if (r != DMGS_OK) return r;
-      dmgs_host::note_launch(), compact_kernel<<<dim3(nb_pre, nv), PRE_BLOCK, 0, s>>>(bv);
+      dmgs_host::note_launch(), compact_kernel<<<dim3((nb_pre + CPT - 1) / CPT, nv), PRE_BLOCK, 0, s>>>(bv);
     });
     DMGS_LAUNCH_CHECK("compact_kernel");
   }

@@ -15,6 +15,12 @@
 //   the 2 PPT consecutive rows from 2 PPT w, lane l the PPT pixels of column
 //   l%16 in rows band + l/16 + 2k, which share dx and every shared-memory
 //   load (PPT = 1, 2 or 4, a tuning parameter);
+// * CTA shape (a tuning parameter): 16x16 (one binning tile), or 32x16 /
+//   16x32 pixels — a union of two adjacent 16x16 binning tiles, each half of
+//   the CTA blending one of them from its own list (so every pixel still sees
+//   exactly its tile's Gaussians in the same order); the halves synchronise
+//   on their own named barriers and meet only between work items, and the
+//   pair's records, mostly the same Gaussians, share the SM's L1;
 // * work items are the (view, tile) pairs of one or several views (the
 //   multi-view batched form renders many views in one launch); CTAs either
 //   take one item each or, persistent, pull items from an atomic counter;
@@ -195,6 +201,51 @@ __device__ __forceinline__ int find_view(const BlendBatch &bb, int item) {
   return v;
 }
 
+// Tile of half h of a CTA covering NT tiles for the view-local work item q:
+// NT = 1, one tile per item; NT = 2, the item is a cell of the grid of
+// (sx x sy)-tile cells, sx * sy = 2.  Returns false when that tile lies
+// outside the grid (an odd tile count along the pair's axis).
+template <int NT>
+__device__ __forceinline__ bool item_tile(const BlendBatch &bb, const BlendView &V, int q, int h,
+                                          int &tx, int &ty) {
+  if constexpr (NT == 1) {
+    tx = q % V.gx;
+    ty = q / V.gx;
+    return true;
+  } else {
+    const int gxs = (V.gx + bb.sx - 1) / bb.sx;
+    const int qx = q % gxs, qy = q / gxs;
+    tx = qx * bb.sx + (bb.sx == 2 ? h : 0);
+    ty = qy * bb.sy + (bb.sy == 2 ? h : 0);
+    return tx < V.gx && ty < V.T / V.gx;
+  }
+}
+
+// Barrier of the ht threads of half h (NT = 2: named barrier 1 + h; barrier
+// 0 stays the whole CTA's), and its popc-reduction form.
+template <int NT>
+__device__ __forceinline__ void half_sync(int h, int ht) {
+  if constexpr (NT == 1) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + h), "r"(ht) : "memory");
+  }
+}
+
+template <int NT>
+__device__ __forceinline__ int half_count(int h, int ht, bool p) {
+  if constexpr (NT == 1) {
+    return __syncthreads_count(p);
+  } else {
+    int r;
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.popc.u32 %0, %2, %3, q;\n\t}"
+                 : "=r"(r)
+                 : "r"((int)p), "r"(1 + h), "r"(ht)
+                 : "memory");
+    return r;
+  }
+}
+
 // Next work item of this CTA (all threads receive the same value).
 __device__ __forceinline__ int next_item(uint32_t *queue, int &slot, int *s_item) {
   if (queue == nullptr) return slot++ == 0 ? (int)blockIdx.x : INT_MAX;
@@ -235,8 +286,7 @@ struct PixelLayout {
   static constexpr int THREADS = 256 / PPT;
   int col, r0;
   uint32_t warp_rows;
-  __device__ __forceinline__ PixelLayout() {
-    const int tid = threadIdx.x;
+  __device__ __forceinline__ explicit PixelLayout(int tid) {  // tid: thread index in the tile's half
     const int w = tid >> 5;
     col = tid & 15;
     r0 = 2 * PPT * w + ((tid >> 4) & 1);
@@ -245,30 +295,33 @@ struct PixelLayout {
   __device__ __forceinline__ int row(int k) const { return r0 + 2 * k; }
 };
 
-template <int PPT, int BATCH>
-__global__ void __launch_bounds__(256 / PPT)
+// NT: tiles per CTA (1, or 2 for the 32x16 / 16x32 shapes); THREADS per tile.
+template <int PPT, int BATCH, int NT = 1>
+__global__ void __launch_bounds__(NT * 256 / PPT)
 blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
   constexpr int THREADS = 256 / PPT;
   constexpr int LOADS = (BATCH + THREADS - 1) / THREADS;
-  __shared__ float4 S0[2][BATCH];
-  __shared__ float4 S1[2][BATCH];
-  __shared__ float4 S2[2][BATCH];
-  __shared__ uint32_t SM[2][BATCH];              // footprint rows
-  __shared__ uint16_t VL[THREADS / 32][BATCH];   // per-warp visit lists
+  __shared__ float4 S0[NT][2][BATCH];
+  __shared__ float4 S1[NT][2][BATCH];
+  __shared__ float4 S2[NT][2][BATCH];
+  __shared__ uint32_t SM[NT][2][BATCH];               // footprint rows
+  __shared__ uint16_t VL[NT * THREADS / 32][BATCH];   // per-warp visit lists
   __shared__ int s_item;
-  const int tid = threadIdx.x;
+  const int h = NT == 1 ? 0 : (int)threadIdx.x / THREADS;  // the CTA half (tile) of this thread
+  const int tid = (int)threadIdx.x - h * THREADS;
   const int lane = tid & 31;
-  const PixelLayout<PPT> lay;
+  const PixelLayout<PPT> lay(tid);
   int slot = 0;
   for (int item = next_item(queue, slot, &s_item); item < bb.total;
        item = next_item(queue, slot, &s_item)) {
     const BlendView &V = bb.v[find_view(bb, item)];
-    const int tile = item - V.tile_base;
-    const int tx = tile % V.gx, ty = tile / V.gx;
+    int tx, ty;
+    const bool tv = item_tile<NT>(bb, V, item - V.tile_base, h, tx, ty);
+    const int tile = ty * V.gx + tx;
     const int px = tx * TILE + lay.col;
     const float pxf = (float)px;
     const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
-    const uint2 range = V.ranges[tile];
+    const uint2 range = tv ? V.ranges[tile] : make_uint2(0u, 0u);
     const int n = (int)(range.y - range.x);
     bool done[PPT], inside[PPT];
     float T[PPT], cr[PPT], cg[PPT], cb[PPT], pyf[PPT];
@@ -276,7 +329,7 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
 #pragma unroll
     for (int k = 0; k < PPT; ++k) {
       const int py = ty * TILE + lay.row(k);
-      inside[k] = px < V.W && py < V.H;
+      inside[k] = tv && px < V.W && py < V.H;
       done[k] = !inside[k];
       pyf[k] = (float)py;
       T[k] = 1.f; cr[k] = cg[k] = cb[k] = 0.f; last[k] = 0;
@@ -302,11 +355,11 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
         const int sl = l * THREADS + tid;
         if (sl < BATCH && base + sl < n) {
           const Staged st = stage<2 * PPT>(pf0[l], pf1[l], pf2[l], ox, oy);
-          S0[buf][sl] = st.s0; S1[buf][sl] = st.s1; S2[buf][sl] = st.s2;
-          SM[buf][sl] = __float_as_uint(st.s2.z);
+          S0[h][buf][sl] = st.s0; S1[h][buf][sl] = st.s1; S2[h][buf][sl] = st.s2;
+          SM[h][buf][sl] = __float_as_uint(st.s2.z);
         }
       }
-      if (__syncthreads_count(all_done()) == THREADS) break;
+      if (half_count<NT>(h, THREADS, all_done()) == THREADS) break;
       const int nbase = base + BATCH;
 #pragma unroll
       for (int l = 0; l < LOADS; ++l) {
@@ -317,13 +370,13 @@ blend_fwd_kernel(const BlendBatch bb, uint32_t *queue) {
       }
       const int cnt = min(BATCH, n - base);
       bool warp_done = __all_sync(FULL, all_done());
-      uint16_t *vl = VL[tid >> 5];
-      const int nvis = warp_done ? 0 : visit_list(SM[buf], cnt, lay.warp_rows, vl, lane);
+      uint16_t *vl = VL[threadIdx.x >> 5];
+      const int nvis = warp_done ? 0 : visit_list(SM[h][buf], cnt, lay.warp_rows, vl, lane);
       for (int i = 0; i < nvis && !warp_done; ++i) {
         const int j = vl[i];
-        const float4 s0 = S0[buf][j];
-        const float4 s1 = S1[buf][j];
-        const float4 s2 = S2[buf][j];
+        const float4 s0 = S0[h][buf][j];
+        const float4 s1 = S1[h][buf][j];
+        const float4 s2 = S2[h][buf][j];
         const float dx = __fsub_rn(s0.x, pxf);
         // pass 1: exponent and range test of every pixel (no branches); the
         // footprint rows, a superset of what this test accepts, only
@@ -516,30 +569,32 @@ __device__ __forceinline__ int slot9(int q) {
 // F64: the FP64-sum mode — the warp sums are added into double accumulators
 // (V.gacc64), so the result does not depend on the order in which warps and
 // tiles finish to well below float32 resolution.
-template <int PPT, int BATCH, bool F64 = false>
-__global__ void __launch_bounds__(256 / PPT, PPT == 4 ? 10 : (PPT == 2 ? 6 : 4))
+template <int PPT, int BATCH, bool F64 = false, int NT = 1>
+__global__ void __launch_bounds__(NT * 256 / PPT, (PPT == 4 ? 10 : (PPT == 2 ? 6 : 4)) / NT)
 blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
   constexpr int THREADS = 256 / PPT;
-  __shared__ float4 S0[BATCH], S1[BATCH], S2[BATCH], S3[BATCH];
-  __shared__ uint32_t SM[BATCH];                // footprint rows
-  __shared__ uint16_t VL[THREADS / 32][BATCH];  // per-warp visit lists
-  __shared__ uint32_t sMaxLast;
+  __shared__ float4 S0[NT][BATCH], S1[NT][BATCH], S2[NT][BATCH], S3[NT][BATCH];
+  __shared__ uint32_t SM[NT][BATCH];                 // footprint rows
+  __shared__ uint16_t VL[NT * THREADS / 32][BATCH];  // per-warp visit lists
+  __shared__ uint32_t sMaxLast[NT];
   __shared__ int s_item;
-  const int tid = threadIdx.x;
+  const int h = NT == 1 ? 0 : (int)threadIdx.x / THREADS;  // the CTA half (tile) of this thread
+  const int tid = (int)threadIdx.x - h * THREADS;
   const int lane = tid & 31;
-  const PixelLayout<PPT> lay;
+  const PixelLayout<PPT> lay(tid);
   int slot_ = 0;
   for (int item = next_item(queue, slot_, &s_item); item < bb.total;
        item = next_item(queue, slot_, &s_item)) {
     const BlendView &V = bb.v[find_view(bb, item)];
-    const int tile = item - V.tile_base;
-    const int tx = tile % V.gx, ty = tile / V.gx;
+    int tx, ty;
+    const bool tv = item_tile<NT>(bb, V, item - V.tile_base, h, tx, ty);
+    const int tile = ty * V.gx + tx;
     const int px = tx * TILE + lay.col;
     const float pxf = (float)px;
     const float ox = (float)(tx * TILE), oy = (float)(ty * TILE);
-    const uint2 range = V.ranges[tile];
+    const uint2 range = tv ? V.ranges[tile] : make_uint2(0u, 0u);
     const int n = (int)(range.y - range.x);
-    if (n == 0) continue;  // block-uniform
+    if (n == 0) continue;  // uniform over the tile's half
     const size_t HW = (size_t)V.H * V.W;
     const float bg0 = __ldg(V.bg), bg1 = __ldg(V.bg + 1), bg2 = __ldg(V.bg + 2);
     PixelState ps[PPT];
@@ -549,34 +604,34 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
     for (int k = 0; k < PPT; ++k) {
       const int py = ty * TILE + lay.row(k);
       pyf[k] = (float)py;
-      const bool in = px < V.W && py < V.H;
+      const bool in = tv && px < V.W && py < V.H;
       init_pixel(ps[k], in, py * V.W + px, HW, V.final_T, V.n_contrib, V.dL_dout, bg0, bg1, bg2);
       mylast = max(mylast, ps[k].last_contrib);
     }
-    if (tid == 0) sMaxLast = 0;
-    __syncthreads();
-    atomicMax(&sMaxLast, mylast);
-    __syncthreads();
-    const int max_last = (int)sMaxLast;  // list positions >= max_last are never blended
+    if (tid == 0) sMaxLast[h] = 0;
+    half_sync<NT>(h, THREADS);
+    atomicMax(&sMaxLast[h], mylast);
+    half_sync<NT>(h, THREADS);
+    const int max_last = (int)sMaxLast[h];  // list positions >= max_last are never blended
     const float hw = 0.5f * (float)V.W, hh = 0.5f * (float)V.H;
     for (int top = max_last; top > 0; top -= BATCH) {
       const int cnt = min(BATCH, top);
-      __syncthreads();
+      half_sync<NT>(h, THREADS);
       for (int sl = tid; sl < cnt; sl += THREADS) {
         const uint32_t id = V.point_list[range.x + top - 1 - sl];  // back to front
         float4 f0, f1, f2;
         load_record(V, id, f0, f1, f2);
         const StagedB st = stage_b<2 * PPT>(f0, f1, f2, id, hw, hh, ox, oy);
-        S0[sl] = st.s0; S1[sl] = st.s1; S2[sl] = st.s2; S3[sl] = st.s3;
-        SM[sl] = __float_as_uint(st.s3.w);
+        S0[h][sl] = st.s0; S1[h][sl] = st.s1; S2[h][sl] = st.s2; S3[h][sl] = st.s3;
+        SM[h][sl] = __float_as_uint(st.s3.w);
       }
-      __syncthreads();
-      uint16_t *vl = VL[tid >> 5];
-      const int nvis = visit_list(SM, cnt, lay.warp_rows, vl, lane);
+      half_sync<NT>(h, THREADS);
+      uint16_t *vl = VL[threadIdx.x >> 5];
+      const int nvis = visit_list(SM[h], cnt, lay.warp_rows, vl, lane);
       for (int i = 0; i < nvis; ++i) {
         const int j = vl[i];
         const int li = top - 1 - j;
-        const float4 s0 = S0[j], s1 = S1[j];
+        const float4 s0 = S0[h][j], s1 = S1[h][j];
         const float dx = __fsub_rn(s0.x, pxf);
         float e2[PPT];
         bool ok[PPT];
@@ -588,7 +643,7 @@ blend_bwd_kernel(const BlendBatch bb, uint32_t *queue) {
           cand |= ok[k];
         }
         if (!__any_sync(FULL, cand)) continue;  // warp-uniform
-        const float4 s2 = S2[j], s3 = S3[j];
+        const float4 s2 = S2[h][j], s3 = S3[h][j];
         float e[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) e[i] = 0.f;  // e[3..5] are set by adjoint_finish
@@ -638,25 +693,25 @@ int grid_for(K kernel, int threads, int total, bool persistent, int &grid, int &
   return DMGS_OK;
 }
 
-template <int PPT, int BATCH>
+template <int PPT, int BATCH, int NT = 1>
 int run_fwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
   thread_local int cdev = -1, cslots = 0;  // per kernel instantiation and host thread
   int grid;
-  const int r = grid_for(blend_fwd_kernel<PPT, BATCH>, 256 / PPT, bb.total, queue != nullptr, grid,
-                         cdev, cslots);
+  const int r = grid_for(blend_fwd_kernel<PPT, BATCH, NT>, NT * 256 / PPT, bb.total,
+                         queue != nullptr, grid, cdev, cslots);
   if (r != DMGS_OK) return r;
-  dmgs_host::note_launch(), blend_fwd_kernel<PPT, BATCH><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  dmgs_host::note_launch(), blend_fwd_kernel<PPT, BATCH, NT><<<grid, NT * 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
 }
 
-template <int PPT, int BATCH, bool F64 = false>
+template <int PPT, int BATCH, bool F64 = false, int NT = 1>
 int run_bwd(const BlendBatch &bb, uint32_t *queue, cudaStream_t s) {
   thread_local int cdev = -1, cslots = 0;  // per kernel instantiation and host thread
   int grid;
-  const int r = grid_for(blend_bwd_kernel<PPT, BATCH, F64>, 256 / PPT, bb.total, queue != nullptr,
-                         grid, cdev, cslots);
+  const int r = grid_for(blend_bwd_kernel<PPT, BATCH, F64, NT>, NT * 256 / PPT, bb.total,
+                         queue != nullptr, grid, cdev, cslots);
   if (r != DMGS_OK) return r;
-  dmgs_host::note_launch(), blend_bwd_kernel<PPT, BATCH, F64><<<grid, 256 / PPT, 0, s>>>(bb, queue);
+  dmgs_host::note_launch(), blend_bwd_kernel<PPT, BATCH, F64, NT><<<grid, NT * 256 / PPT, 0, s>>>(bb, queue);
   return DMGS_OK;
 }
 
@@ -669,16 +724,44 @@ __global__ void gacc_round_kernel(const double *__restrict__ g64, float *__restr
 
 template <bool FWD>
 int dispatch(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *queue, cudaStream_t s) {
+  const bool pair = cfg.sx * cfg.sy == 2;
+  if (cfg.sx * cfg.sy > 2 || cfg.sx < 1 || cfg.sy < 1) {
+    dmgs_host::set_error("unsupported blend CTA shape: %d x %d tiles", cfg.sx, cfg.sy);
+    return DMGS_ERR_ARG;
+  }
 #define DMGS_BLEND_CASE(P_, B_)                                                     \
-  if (cfg.ppt == P_ && cfg.batch == B_)                                             \
+  if (!pair && cfg.ppt == P_ && cfg.batch == B_)                                    \
     return FWD ? run_fwd<P_, B_>(bb, queue, s) : run_bwd<P_, B_>(bb, queue, s);
   DMGS_BLEND_CASE(1, 128) DMGS_BLEND_CASE(1, 256) DMGS_BLEND_CASE(1, 512)
   DMGS_BLEND_CASE(2, 128) DMGS_BLEND_CASE(2, 256) DMGS_BLEND_CASE(2, 512)
   DMGS_BLEND_CASE(4, 128) DMGS_BLEND_CASE(4, 256) DMGS_BLEND_CASE(4, 512)
 #undef DMGS_BLEND_CASE
-  dmgs_host::set_error("unsupported blend configuration: %d pixels/thread, batch %d", cfg.ppt,
-                       cfg.batch);
+#define DMGS_BLEND_PAIR(P_, B_)                                                     \
+  if (pair && cfg.ppt == P_ && cfg.batch == B_)                                     \
+    return FWD ? run_fwd<P_, B_, 2>(bb, queue, s) : run_bwd<P_, B_, false, 2>(bb, queue, s);
+  DMGS_BLEND_PAIR(2, 128) DMGS_BLEND_PAIR(2, 256)
+  DMGS_BLEND_PAIR(4, 128) DMGS_BLEND_PAIR(4, 256)
+#undef DMGS_BLEND_PAIR
+  dmgs_host::set_error("unsupported blend configuration: %d pixels/thread, batch %d, %dx%d tiles",
+                       cfg.ppt, cfg.batch, cfg.sx, cfg.sy);
   return DMGS_ERR_ARG;
+}
+
+// The batch with its work items counted in CTA cells of sx x sy tiles.
+BlendBatch with_shape(const BlendBatch &bb, const BlendCfg &cfg) {
+  BlendBatch b = bb;
+  b.sx = cfg.sx;
+  b.sy = cfg.sy;
+  if (cfg.sx * cfg.sy == 1) return b;
+  int base = 0;
+  for (int v = 0; v < b.nviews; ++v) {
+    BlendView &o = b.v[v];
+    const int gy = o.gx > 0 ? o.T / o.gx : 0;
+    o.tile_base = base;
+    base += ((o.gx + cfg.sx - 1) / cfg.sx) * ((gy + cfg.sy - 1) / cfg.sy);
+  }
+  b.total = base;
+  return b;
 }
 
 }  // namespace
@@ -687,7 +770,8 @@ int launch_blend_batch_fwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *
                            cudaStream_t s) {
   if (bb.total <= 0) return DMGS_OK;
   int r = DMGS_OK;
-  DMGS_TIMED(K_BLEND_FWD, s, r = dispatch<true>(bb, cfg, queue, s));
+  const BlendBatch b = with_shape(bb, cfg);
+  DMGS_TIMED(K_BLEND_FWD, s, r = dispatch<true>(b, cfg, queue, s));
   if (r != DMGS_OK) return r;
   DMGS_LAUNCH_CHECK("blend_fwd_kernel");
   return DMGS_OK;
@@ -697,7 +781,8 @@ int launch_blend_batch_bwd(const BlendBatch &bb, const BlendCfg &cfg, uint32_t *
                            cudaStream_t s) {
   if (bb.total <= 0) return DMGS_OK;
   int r = DMGS_OK;
-  DMGS_TIMED(K_BLEND_BWD, s, r = dispatch<false>(bb, cfg, queue, s));
+  const BlendBatch b = with_shape(bb, cfg);
+  DMGS_TIMED(K_BLEND_BWD, s, r = dispatch<false>(b, cfg, queue, s));
   if (r != DMGS_OK) return r;
   DMGS_LAUNCH_CHECK("blend_bwd_kernel");
   return DMGS_OK;

@@ -124,16 +124,20 @@ struct BlendView {
 };
 
 struct BlendBatch {
-  int nviews, total;    // views, work items (sum of tiles)
+  int nviews, total;    // views, work items (sum of tiles, or of CTA cells)
+  int sx = 1, sy = 1;   // tiles per CTA along x and y (set by the launchers)
   BlendView v[MAX_BATCH_VIEWS];
 };
 
-// Tuning parameters of the blend kernels: pixels per thread (1, 2, 4) and
-// Gaussians staged per batch (128, 256, 512).
+// Tuning parameters of the blend kernels: pixels per thread (1, 2, 4),
+// Gaussians staged per batch (128, 256, 512) and the CTA shape in 16x16
+// tiles, sx x sy: 1x1, or 2x1 / 1x2 (32x16 / 16x32 pixels: two binning
+// tiles per CTA; pixels per thread 2 or 4, batch 128 or 256).
 struct BlendCfg {
   int ppt, batch;
+  int sx = 1, sy = 1;
 };
-inline BlendCfg default_blend_cfg() { return BlendCfg{4, 128}; }  // autotuned on GB300
+inline BlendCfg default_blend_cfg() { return BlendCfg{4, 128, 1, 1}; }  // autotuned on GB300
 
 // queue == nullptr: one CTA per work item; else a persistent grid pulling
 // items from *queue (which must be zero at launch).

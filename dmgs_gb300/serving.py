@@ -461,7 +461,7 @@ class GpuBackend:
             sizes = (C.c_size_t * n)(*[r.blocks[1] for r in reqs])
             capa = (C.c_int64 * n)(*caps)
             gauss = (L.DmgsGaussians * n)(*[self.scenes[r.scene].gauss for r in reqs])
-            b = L.DmgsBatch(n, views, out, None, capa, self.cfg[0], self.cfg[1])
+            b = L.DmgsBatch(n, views, out, None, capa, *self.cfg)
             queue = self.queues.data_ptr() + 256 * q
             L.check(self.lib.dmgs_render_multi(C.byref(b), gauss, states, sizes, queue,
                                                s.cuda_stream), "render_multi")

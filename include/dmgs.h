@@ -27,7 +27,7 @@
 /* Version of the structs and entry points below; dmgs_abi_version() returns
  * the value the library was built with.  Raised whenever a struct layout or
  * a signature changes. */
-#define DMGS_ABI_VERSION 6
+#define DMGS_ABI_VERSION 7
 
 #ifdef __cplusplus
 extern "C" {
@@ -200,6 +200,10 @@ typedef struct DmgsBatch {
   const int64_t *capacity;         /* [nviews] instance-list capacity per view */
   int32_t pixels_per_thread;       /* blend tuning: 1, 2 or 4 (0: 4) */
   int32_t gaussians_per_batch;     /* blend tuning: 128, 256 or 512 (0: 128) */
+  int32_t tile_shape;              /* blend tuning, pixels per CTA: 0 = 16x16 (one binning
+                                      tile), 1 = 32x16, 2 = 16x32 (two adjacent tiles, each
+                                      blended from its own list; pixels per thread 2 or 4,
+                                      batch 128 or 256) */
 } DmgsBatch;
 
 size_t dmgs_batch_state_bytes(const DmgsBatch *b, int32_t P);

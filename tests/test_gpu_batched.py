@@ -66,20 +66,20 @@ def test_batched_matches_per_view_path_for_every_config():
     plain = [_plain(g, rs, d) for rs, d in zip(settings, dimgs)]
     gsum = {k: sum(p[1][k] for p in plain) for k in g}
     br = BatchedRasterizer(settings, g)
-    for ppt, b in TUNE_SPACE:
-        br.set_config(ppt, b)
+    for ppt, b, shape in TUNE_SPACE:
+        br.set_config(ppt, b, shape)
         br.forward()
         br.backward(dimgs)
         torch.cuda.synchronize()
         br.status()
         for v in range(len(views)):
-            assert torch.equal(br.images[v], plain[v][0]), (ppt, b, v)
+            assert torch.equal(br.images[v], plain[v][0]), (ppt, b, shape, v)
             assert torch.equal(br.radii[v], dmgs_gb300.GaussianRasterizer(settings[v])(
                 means3D=g["means3D"], means2D=torch.zeros_like(g["means3D"]), opacities=g["opacities"],
                 shs=g["shs"], scales=g["scales"], rotations=g["rotations"])[1])
             assert rel_l2(br.means2D_grads[v].cpu().numpy(), plain[v][2].cpu().numpy()) <= 1e-5
         for k in g:
-            assert rel_l2(br.grads[k].cpu().numpy(), gsum[k].cpu().numpy()) <= 1e-5, (ppt, b, k)
+            assert rel_l2(br.grads[k].cpu().numpy(), gsum[k].cpu().numpy()) <= 1e-5, (ppt, b, shape, k)
 
 
 def test_batched_against_oracle():
