@@ -96,17 +96,18 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 scan_reduce_kernel(const ScanViews sv) {
   const ScanView &v = sv.v[blockIdx.y];
   const uint32_t n = scan_len(v);
-  const uint32_t base = blockIdx.x * SCAN_TILE;
-  if (base >= n) return;
-  unsigned long long s = 0;
+  for (uint32_t tile = blockIdx.x; tile * (uint32_t)SCAN_TILE < n; tile += gridDim.x) {
+    const uint32_t base = tile * SCAN_TILE;
+    unsigned long long s = 0;
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; ++i) {
-    const uint32_t k = base + i * SCAN_THREADS + threadIdx.x;
-    if (k < n) s += v.data[k];
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      const uint32_t k = base + i * SCAN_THREADS + threadIdx.x;
+      if (k < n) s += v.data[k];
+    }
+    unsigned long long tot;
+    block_exclusive_scan<SCAN_THREADS>(s, &tot);
+    if (threadIdx.x == 0) v.part[tile] = (uint32_t)tot;
   }
-  unsigned long long tot;
-  block_exclusive_scan<SCAN_THREADS>(s, &tot);
-  if (threadIdx.x == 0) v.part[blockIdx.x] = (uint32_t)tot;
 }
 
 // One block per view: exclusive scan of the per-block partials (or of the
@@ -141,22 +142,22 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 scan_down_kernel(const ScanViews sv) {
   const ScanView &v = sv.v[blockIdx.y];
   const uint32_t n = scan_len(v);
-  const uint32_t base = blockIdx.x * SCAN_TILE;
-  if (base >= n) return;
-  // blocked: thread i owns elements base + i*ITEMS .. +ITEMS-1
-  uint32_t x[SCAN_ITEMS];
-  unsigned long long s = 0;
-  const uint32_t k0 = base + threadIdx.x * SCAN_ITEMS;
+  for (uint32_t tile = blockIdx.x; tile * (uint32_t)SCAN_TILE < n; tile += gridDim.x) {
+    // blocked: thread i owns elements base + i*ITEMS .. +ITEMS-1
+    uint32_t x[SCAN_ITEMS];
+    unsigned long long s = 0;
+    const uint32_t k0 = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; ++i) {
-    x[i] = (k0 + i < n) ? v.data[k0 + i] : 0u;
-    s += x[i];
-  }
-  unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, nullptr) + v.part[blockIdx.x];
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      x[i] = (k0 + i < n) ? v.data[k0 + i] : 0u;
+      s += x[i];
+    }
+    unsigned long long run = block_exclusive_scan<SCAN_THREADS>(s, nullptr) + v.part[tile];
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; ++i) {
-    if (k0 + i < n) v.data[k0 + i] = (uint32_t)run;
-    run += x[i];
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+      if (k0 + i < n) v.data[k0 + i] = (uint32_t)run;
+      run += x[i];
+    }
   }
 }
 
@@ -229,18 +230,19 @@ radix_hist_kernel(const BinViews bv, int pass) {
   const uint32_t *keys = (pass & 1) ? B.k1 : B.k0;
   const int shift = 8 * pass;
   const uint32_t V = B.counters[CI_V], nbr = B.counters[CI_NBR];
-  const uint32_t b = blockIdx.x;
-  if (b >= nbr) return;
   __shared__ uint32_t h[256];
-  h[threadIdx.x] = 0;
-  __syncthreads();
+  for (uint32_t b = blockIdx.x; b < nbr; b += gridDim.x) {  // key tiles of RADIX_TILE
+    h[threadIdx.x] = 0;
+    __syncthreads();
 #pragma unroll
-  for (int i = 0; i < RADIX_ITEMS; ++i) {
-    const uint32_t k = b * RADIX_TILE + i * RADIX_BLOCK + threadIdx.x;
-    if (k < V) atomicAdd(&h[(keys[k] >> shift) & 255u], 1u);
+    for (int i = 0; i < RADIX_ITEMS; ++i) {
+      const uint32_t k = b * RADIX_TILE + i * RADIX_BLOCK + threadIdx.x;
+      if (k < V) atomicAdd(&h[(keys[k] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    B.rhist[threadIdx.x * nbr + b] = h[threadIdx.x];  // digit-major
+    __syncthreads();
   }
-  __syncthreads();
-  B.rhist[threadIdx.x * nbr + b] = h[threadIdx.x];  // digit-major
 }
 
 // Lanes whose 8-bit digit equals this lane's (invalid lanes, digit 256, group
@@ -267,50 +269,51 @@ radix_scatter_kernel(const BinViews bv, int pass) {
   const int shift = 8 * pass;
   const uint32_t *rhist_scanned = B.rhist;
   const uint32_t V = B.counters[CI_V], nbr = B.counters[CI_NBR];
-  const uint32_t b = blockIdx.x;
-  if (b >= nbr) return;
   __shared__ uint32_t wh[RADIX_BLOCK / 32][256];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < (RADIX_BLOCK / 32) * 256; i += RADIX_BLOCK) (&wh[0][0])[i] = 0u;
-  __syncthreads();
-  uint32_t key[RADIX_ITEMS], val[RADIX_ITEMS];
-  int dig[RADIX_ITEMS];
-  const uint32_t base = b * RADIX_TILE + w * (32 * RADIX_ITEMS);
+  for (uint32_t b = blockIdx.x; b < nbr; b += gridDim.x) {  // key tiles of RADIX_TILE
+    for (int i = threadIdx.x; i < (RADIX_BLOCK / 32) * 256; i += RADIX_BLOCK) (&wh[0][0])[i] = 0u;
+    __syncthreads();
+    uint32_t key[RADIX_ITEMS], val[RADIX_ITEMS];
+    int dig[RADIX_ITEMS];
+    unsigned peers[RADIX_ITEMS];
+    const uint32_t base = b * RADIX_TILE + w * (32 * RADIX_ITEMS);
 #pragma unroll
-  for (int r = 0; r < RADIX_ITEMS; ++r) {
-    const uint32_t k = base + r * 32 + lane;
-    const bool ok = k < V;
-    key[r] = ok ? kin[k] : 0u;
-    val[r] = ok ? vin[k] : 0u;
-    dig[r] = ok ? (int)((key[r] >> shift) & 255u) : 256;
-    const unsigned peers = digit_peers(dig[r]);
-    if (dig[r] < 256 && lane == __ffs(peers) - 1) wh[w][dig[r]] += __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  {
-    const int d = threadIdx.x;  // RADIX_BLOCK == 256 digits
-    uint32_t run = rhist_scanned[d * nbr + b];
-#pragma unroll
-    for (int w2 = 0; w2 < RADIX_BLOCK / 32; ++w2) {
-      const uint32_t c = wh[w2][d];
-      wh[w2][d] = run;
-      run += c;
+    for (int r = 0; r < RADIX_ITEMS; ++r) {
+      const uint32_t k = base + r * 32 + lane;
+      const bool ok = k < V;
+      key[r] = ok ? kin[k] : 0u;
+      val[r] = ok ? vin[k] : 0u;
+      dig[r] = ok ? (int)((key[r] >> shift) & 255u) : 256;
+      peers[r] = digit_peers(dig[r]);
+      if (dig[r] < 256 && lane == __ffs(peers[r]) - 1) wh[w][dig[r]] += __popc(peers[r]);
+      __syncwarp();
     }
-  }
-  __syncthreads();
+    __syncthreads();
+    {
+      const int d = threadIdx.x;  // RADIX_BLOCK == 256 digits
+      uint32_t run = rhist_scanned[d * nbr + b];
 #pragma unroll
-  for (int r = 0; r < RADIX_ITEMS; ++r) {
-    const unsigned peers = digit_peers(dig[r]);
-    uint32_t pos = 0;
-    if (dig[r] < 256) pos = wh[w][dig[r]] + __popc(peers & lanemask_lt());
-    __syncwarp();
-    if (dig[r] < 256) {
-      kout[pos] = key[r];
-      vout[pos] = val[r];
-      if (lane == __ffs(peers) - 1) wh[w][dig[r]] += __popc(peers);
+      for (int w2 = 0; w2 < RADIX_BLOCK / 32; ++w2) {
+        const uint32_t c = wh[w2][d];
+        wh[w2][d] = run;
+        run += c;
+      }
     }
-    __syncwarp();
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RADIX_ITEMS; ++r) {
+      uint32_t pos = 0;
+      if (dig[r] < 256) pos = wh[w][dig[r]] + __popc(peers[r] & lanemask_lt());
+      __syncwarp();
+      if (dig[r] < 256) {
+        kout[pos] = key[r];
+        vout[pos] = val[r];
+        if (lane == __ffs(peers[r]) - 1) wh[w][dig[r]] += __popc(peers[r]);
+      }
+      __syncwarp();
+    }
+    __syncthreads();  // wh is cleared for the next tile
   }
 }
 
@@ -374,15 +377,15 @@ __global__ void __launch_bounds__(256)
 chunk_weight_kernel(const BinViews bv) {
   const BinView &B = bv.v[blockIdx.y];
   const uint32_t V = B.counters[CI_V];
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= V) return;
-  const float4 f2 = B.feat[3 * B.v0[s] + 2];
-  const uint2 r = make_uint2(__float_as_uint(f2.z), __float_as_uint(f2.w));
-  B.srect[s] = r;
-  int x0, y0, x1, y1;
-  unpack_rect(r, x0, y0, x1, y1);
-  const uint32_t rows = (uint32_t)(y1 - y0), area = rows * (uint32_t)(x1 - x0);
-  B.k1[s] = CHUNK_W_GAUSS + (rows + 15u) / 16u + (area + 63u) / 64u;  // k1 is free: the sorted keys end in k0
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < V; s += gridDim.x * blockDim.x) {
+    const float4 f2 = B.feat[3 * B.v0[s] + 2];
+    const uint2 r = make_uint2(__float_as_uint(f2.z), __float_as_uint(f2.w));
+    B.srect[s] = r;
+    int x0, y0, x1, y1;
+    unpack_rect(r, x0, y0, x1, y1);
+    const uint32_t rows = (uint32_t)(y1 - y0), area = rows * (uint32_t)(x1 - x0);
+    B.k1[s] = CHUNK_W_GAUSS + (rows + 15u) / 16u + (area + 63u) / 64u;  // k1 is free: the sorted keys end in k0
+  }
 }
 
 // From the exclusive prefix of the weights: chunk c = the positions whose
@@ -396,13 +399,14 @@ chunk_bounds_kernel(const BinViews bv) {
   uint32_t *cstart = B.cstart;
   const uint32_t V = B.counters[CI_V], C = B.counters[CI_C];
   const unsigned long long W = B.counters[CI_W];
-  const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= V || W == 0) return;
-  const uint32_t cs = (uint32_t)((unsigned long long)prefix[s] * C / W);
-  const uint32_t cp = s > 0 ? (uint32_t)((unsigned long long)prefix[s - 1] * C / W) : 0u;
-  for (uint32_t c = (s > 0 ? cp + 1 : 0u); c <= cs; ++c) cstart[c] = s;
-  if (s == V - 1)
-    for (uint32_t c = cs + 1; c <= C; ++c) cstart[c] = V;
+  if (W == 0) return;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < V; s += gridDim.x * blockDim.x) {
+    const uint32_t cs = (uint32_t)((unsigned long long)prefix[s] * C / W);
+    const uint32_t cp = s > 0 ? (uint32_t)((unsigned long long)prefix[s - 1] * C / W) : 0u;
+    for (uint32_t c = (s > 0 ? cp + 1 : 0u); c <= cs; ++c) cstart[c] = s;
+    if (s == V - 1)
+      for (uint32_t c = cs + 1; c <= C; ++c) cstart[c] = V;
+  }
 }
 
 // ---- step 4: row counts, one warp per chunk ---------------------------------
@@ -587,7 +591,7 @@ constexpr int TE_ENTRIES = TE_THREADS * TE_PER;
 
 __host__ __device__ inline size_t tile_emit_smem_words(int nx) {
   return (size_t)nx + (nx + 1) + (size_t)TE_WARPS * (nx + 1) + STAGE_CAP + TE_WARPS +
-         (TE_WARPS + 1);
+         (TE_WARPS + 1) + (size_t)TE_WARPS * (2 * (size_t)nx + 32);
 }
 
 __device__ __forceinline__ int block_sum_te(int v, int *red) {
@@ -636,7 +640,12 @@ tile_emit_kernel(const BinViews bv, int S) {
   uint32_t *stage = reinterpret_cast<uint32_t *>(wc + TE_WARPS * (nx + 1));  // [STAGE_CAP]
   int *red = reinterpret_cast<int *>(stage + STAGE_CAP);  // [TE_WARPS]
   uint32_t *bnd = reinterpret_cast<uint32_t *>(red + TE_WARPS);  // [TE_WARPS + 1] slice starts
+  // per warp: start / end bit masks per tile [nx] each (zero between
+  // groups) and the Gaussian indices of the current group of 32 entries
+  uint32_t *smask = bnd + TE_WARPS + 1;
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  uint32_t *sbeg = smask + (size_t)w * (2 * nx + 32), *send = sbeg + nx, *gids = send + nx;
+  for (int i = tid; i < TE_WARPS * (2 * nx + 32); i += TE_THREADS) smask[i] = 0u;
   const unsigned lt = lanemask_lt();
   const uint2 *__restrict__ rl = B.rowlist;
   uint32_t *__restrict__ out = B.point_list;
@@ -760,29 +769,59 @@ tile_emit_kernel(const BinViews bv, int S) {
       for (int w2 = 0; w2 < TE_WARPS; ++w2) wc[w2 * (nx + 1) + x] += o;
     }
     __syncthreads();
-    // (C) stage the slice's instances, entries in order, one at a time: tile
-    // x is always handled by lane x % 32, so a tile's cursor is only ever
-    // touched by one lane and entries land in the order they come
+    // (C) stage the slice's instances, 32 entries (depth order) at a time:
+    // lane j sets bit j at its entry's first tile a_j in sbeg and at its end
+    // b_j in send; inclusive OR-prefixes over the tiles give the entries
+    // begun at or before tile x and those ended at or before it, so tile x
+    // is covered by M_x = begun & ~ended, which the lane owning x (x % 32)
+    // appends in bit (entry) order at its cursor — so a tile's cursor is
+    // only ever touched by one lane and entries land in the order they come.
     for (uint32_t g0 = sa; g0 < sb; g0 += 32) {
       const uint32_t i = g0 + lane;
       const uint2 en = i < sb ? rl[i] : make_uint2(0u, 0u);
       int a = 0, b = 0;
       if (i < sb) clip(en, a, b);
-      unsigned m = __ballot_sync(FULL, a < b);
-      while (m) {
-        const int j = __ffs(m) - 1;
-        m &= m - 1;
-        const int aj = __shfl_sync(FULL, a, j), bj = __shfl_sync(FULL, b, j);
-        const uint32_t idj = __shfl_sync(FULL, en.x, j);
-        for (int xb = aj & ~31; xb < bj; xb += 32) {
+      const bool has = a < b;
+      gids[lane] = en.x;
+      if (has) {
+        atomicOr(&sbeg[a], 1u << lane);
+        if (b < nx) atomicOr(&send[b], 1u << lane);  // an end at nx is never read
+      }
+      const int lo = (int)__reduce_min_sync(FULL, has ? (unsigned)a : 0xffffffffu);
+      const int hi = (int)__reduce_max_sync(FULL, has ? (unsigned)b : 0u);
+      __syncwarp();
+      if (lo < hi) {  // warp-uniform; chunks up to the one holding hi (clears send[hi])
+        uint32_t cb = 0u, ce = 0u;  // carries of the two OR-prefixes
+        for (int xb = lo & ~31; xb <= hi && xb < nx; xb += 32) {
           const int x = xb + lane;
-          if (x >= aj && x < bj) {
-            const uint32_t p = (uint32_t)wcw[x];
-            if (p < STAGE_CAP) stage[p] = idj; else bad = true;
-            wcw[x] = (int)p + 1;
+          uint32_t vb = x < nx ? sbeg[x] : 0u, ve = x < nx ? send[x] : 0u;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t ub = __shfl_up_sync(FULL, vb, o), ue = __shfl_up_sync(FULL, ve, o);
+            if (lane >= o) { vb |= ub; ve |= ue; }
+          }
+          vb |= cb;
+          ve |= ce;
+          cb = __shfl_sync(FULL, vb, 31);
+          ce = __shfl_sync(FULL, ve, 31);
+          if (x < nx) {
+            sbeg[x] = 0u;
+            send[x] = 0u;
+            uint32_t mm = vb & ~ve;
+            if (mm) {
+              uint32_t p = (uint32_t)wcw[x];
+              do {
+                const int j = __ffs(mm) - 1;
+                mm &= mm - 1;
+                if (p < STAGE_CAP) stage[p] = gids[j]; else bad = true;
+                ++p;
+              } while (mm);
+              wcw[x] = (int)p;
+            }
           }
         }
       }
+      __syncwarp();
     }
     __syncthreads();
     // (D) copy each tile's staged run to its list
@@ -856,6 +895,15 @@ int seg_plan(const BinViews &bv) {
 
 // Scan of one array per view: host bound n_max (the launch size), device
 // length *n_dev when given.
+// Blocks per view for a grid-stride launch over at most `units` work units
+// whose actual count is only known on the device: about two resident waves
+// of `per_sm` blocks per SM shared by the views, so that a launch sized for
+// the worst case does not schedule thousands of blocks that find no work.
+int bounded_blocks(size_t units, int nviews, int per_sm) {
+  const size_t cap = std::max<size_t>(1, (size_t)2 * device_sms() * per_sm / std::max(nviews, 1));
+  return (int)std::max<size_t>(1, std::min(units, cap));
+}
+
 int launch_scan_views(const ScanViews &sv, cudaStream_t s) {
   uint32_t n_max = 0;
   for (int v = 0; v < sv.n; ++v) n_max = std::max(n_max, sv.v[v].n_max);
@@ -865,7 +913,7 @@ int launch_scan_views(const ScanViews &sv, cudaStream_t s) {
     DMGS_LAUNCH_CHECK("scan_single_kernel");
     return DMGS_OK;
   }
-  const dim3 grid((n_max + SCAN_TILE - 1) / SCAN_TILE, sv.n);
+  const dim3 grid(bounded_blocks((n_max + SCAN_TILE - 1) / SCAN_TILE, sv.n, 2), sv.n);
   dmgs_host::note_launch(), scan_reduce_kernel<<<grid, SCAN_THREADS, 0, s>>>(sv);
   DMGS_LAUNCH_CHECK("scan_reduce_kernel");
   dmgs_host::note_launch(), scan_single_kernel<<<one, SCAN_THREADS, 0, s>>>(sv, 1);
@@ -960,6 +1008,9 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
   }
   const int S = seg_plan(bv);
   const int nv = bv.n;
+  // grid-stride kernels over the visible Gaussians (counted on the device)
+  const int rgrid = bounded_blocks((size_t)nb_radix, nv, 8);  // key tiles
+  const int pgrid = bounded_blocks((size_t)nb_pre, nv, 8);    // blocks of 256 positions
   const size_t rows_smem = (size_t)(gy + 1) * 4;
   if (int r = dmgs_host::raise_smem_limit((const void *)row_count_kernel, rows_smem)) return r;
   if (int r = dmgs_host::raise_smem_limit((const void *)seg_count_kernel, seg_smem)) return r;
@@ -981,20 +1032,20 @@ int launch_binning_geometry(const BinViews &bv, cudaStream_t s) {
         return ScanView{B.rhist, B.counters + CI_NRH, B.n_rhist_max, B.part, nullptr, nullptr};
       });
       for (int pass = 0; pass < 4; ++pass) {
-        dmgs_host::note_launch(), radix_hist_kernel<<<dim3(nb_radix, nv), RADIX_BLOCK, 0, s>>>(bv, pass);
+        dmgs_host::note_launch(), radix_hist_kernel<<<dim3(rgrid, nv), RADIX_BLOCK, 0, s>>>(bv, pass);
         int r = launch_scan_views(hs, s);
         if (r != DMGS_OK) return r;
-        dmgs_host::note_launch(), radix_scatter_kernel<<<dim3(nb_radix, nv), RADIX_BLOCK, 0, s>>>(bv, pass);
+        dmgs_host::note_launch(), radix_scatter_kernel<<<dim3(rgrid, nv), RADIX_BLOCK, 0, s>>>(bv, pass);
       }
     });  // four passes: the sorted order ends in (k0, v0)
     DMGS_LAUNCH_CHECK("radix_sort");
     DMGS_TIMED(K_BIN_COUNT, s, {
-      dmgs_host::note_launch(), chunk_weight_kernel<<<dim3(nb_pre, nv), 256, 0, s>>>(bv);
+      dmgs_host::note_launch(), chunk_weight_kernel<<<dim3(pgrid, nv), 256, 0, s>>>(bv);
       int r = launch_scan_views(scan_views(bv, [](const BinView &B) {
         return ScanView{B.k1, B.counters + CI_V, (uint32_t)B.P, B.part, B.counters + CI_W, B.counters};
       }), s);
       if (r != DMGS_OK) return r;
-      dmgs_host::note_launch(), chunk_bounds_kernel<<<dim3(nb_pre, nv), 256, 0, s>>>(bv);
+      dmgs_host::note_launch(), chunk_bounds_kernel<<<dim3(pgrid, nv), 256, 0, s>>>(bv);
       dmgs_host::note_launch(), row_count_kernel<<<dim3(cmax, nv), 32, rows_smem, s>>>(bv);
       dmgs_host::note_launch(), seg_count_kernel<<<dim3(S * nb, nv), 256, seg_smem, s>>>(bv, S);
     });
