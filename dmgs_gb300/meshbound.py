@@ -107,6 +107,20 @@ def ssim(img1, img2, window=None):
     return m.mean()
 
 
+
+def view_tensors(view, device, cache):
+    """(camera centre, view matrix, projection matrix) of `view` on the
+    device, uploaded once per view and kept in `cache` — as the reference's
+    Camera holds them on the device (scene/cameras.py:54-57).  An upload per
+    step from host memory would wait for the work already queued on the GPU."""
+    hit = cache.get(id(view))
+    if hit is None or hit[0] is not view:
+        hit = (view, torch.tensor(view.campos, device=device),
+               torch.tensor(view.viewmatrix, device=device),
+               torch.tensor(view.projmatrix, device=device))
+        cache[id(view)] = hit
+    return hit[1:]
+
 class MeshBoundScene:
     """Gaussians bound to a mesh's faces (stage 2): learnable vertices and
     scale factor, G Gaussians per face at per-Gaussian Dirichlet(1,1,1)
@@ -136,6 +150,7 @@ class MeshBoundScene:
             device=self.device, requires_grad=True)
         self.sh_degree = sh_degree
         self.spatial_lr_scale = 1.0
+        self._views = {}
 
     def params(self):
         return [self.verts, self.scale_factor, self.features, self.opacity]
@@ -149,7 +164,7 @@ class MeshBoundScene:
         """render_dyn: precomputed covariance and sigmoid(SH) colours (the
         fused colour kernel, or the torch composition with fused_color=False)."""
         xyz, cov = self.gaussians()
-        campos = torch.tensor(view.campos, device=self.device)
+        campos, viewm, projm = view_tensors(view, self.device, self._views)
         if fused_color:
             colors = sh_colors(self.sh_degree, self.features, xyz, campos)
         else:
@@ -158,9 +173,7 @@ class MeshBoundScene:
             colors = torch.sigmoid(eval_sh(self.sh_degree, self.features, d))
         rs = GaussianRasterizationSettings(
             image_height=view.height, image_width=view.width, tanfovx=view.tanfovx,
-            tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0,
-            viewmatrix=torch.tensor(view.viewmatrix, device=self.device),
-            projmatrix=torch.tensor(view.projmatrix, device=self.device),
+            tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0, viewmatrix=viewm, projmatrix=projm,
             sh_degree=self.sh_degree, campos=campos, prefiltered=False, debug=False)
         means2D = torch.zeros_like(xyz, requires_grad=True)
         img, radii = GaussianRasterizer(rs)(means3D=xyz, means2D=means2D, opacities=self.opacity,
@@ -191,9 +204,13 @@ def sdf_reg_loss(sdf, edges):
     scene/gaussian_geo_model_mlp_flex.py:233-239): binary cross-entropy of
     each sign-changing edge's end values against the other end's sign."""
     s = sdf[edges.reshape(-1)].reshape(-1, 2)
-    s = s[torch.sign(s[:, 0]) != torch.sign(s[:, 1])]
-    return (F_.binary_cross_entropy_with_logits(s[:, 0], (s[:, 1] > 0).float()) +
-            F_.binary_cross_entropy_with_logits(s[:, 1], (s[:, 0] > 0).float()))
+    # the means over the sign-changing edges as masked sums: no host
+    # synchronisation for the selection's size
+    m = (torch.sign(s[:, 0]) != torch.sign(s[:, 1])).to(s.dtype)
+    n = m.sum()
+    bce = F_.binary_cross_entropy_with_logits
+    return ((bce(s[:, 0], (s[:, 1] > 0).to(s.dtype), reduction="none") * m).sum() / n +
+            (bce(s[:, 1], (s[:, 0] > 0).to(s.dtype), reduction="none") * m).sum() / n)
 
 
 class Stage2Model:
@@ -227,6 +244,7 @@ class Stage2Model:
                                        requires_grad=True)
         self.spatial_lr_scale = 1.0
         self.sh_degree = sh_degree
+        self._views = {}
         with torch.no_grad():
             v = self.mesh()[0]
             aabb = torch.stack([v.min(0).values, v.max(0).values]) * 1.1
@@ -248,13 +266,11 @@ class Stage2Model:
                                  self.spatial_lr_scale, self.max_scale)
         K = (self.sh_degree + 1) ** 2
         feats = self.texture.sample_noact(xyz).view(-1, 3, K)
-        campos = torch.tensor(view.campos, device=self.device)
+        campos, viewm, projm = view_tensors(view, self.device, self._views)
         colors = sh_colors(self.sh_degree, feats, xyz, campos)
         rs = GaussianRasterizationSettings(
             image_height=view.height, image_width=view.width, tanfovx=view.tanfovx,
-            tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0,
-            viewmatrix=torch.tensor(view.viewmatrix, device=self.device),
-            projmatrix=torch.tensor(view.projmatrix, device=self.device),
+            tanfovy=view.tanfovy, bg=bg, scale_modifier=1.0, viewmatrix=viewm, projmatrix=projm,
             sh_degree=self.sh_degree, campos=campos, prefiltered=False, debug=False)
         opac = torch.full((xyz.shape[0], 1), 0.9999, device=self.device)
         img, radii = GaussianRasterizer(rs)(
