@@ -153,3 +153,24 @@ def test_new_entry_points_reject_bad_arguments(lib):
     g = _lib.DmgsFcGrid(x=8, s=8, rx=4, ry=4, rz=4, beta_stride=5)
     counts = (C.c_uint32 * 8)()
     assert lib.dmgs_fc_count(C.byref(g), 8, 1 << 20, C.addressof(counts), None) == -1  # stride < 12
+
+
+def test_batch_rejects_unsupported_blend_tuning(lib):
+    """dmgs_raster_fwd_batched refuses a blend configuration it has no kernel
+    for (pixels per thread, Gaussians per batch, CTA shape) with DMGS_ERR_ARG
+    before any device work; the two-tile CTA shapes take 2 or 4 pixels per
+    thread and batches of 128 or 256."""
+    views = (_lib.DmgsView * 1)(_view())
+    out = (C.c_void_p * 1)(16)
+    cap = (C.c_int64 * 1)(1 << 20)
+
+    def run(ppt, gpb, shape):
+        b = _lib.DmgsBatch(1, views, out, None, cap, ppt, gpb, shape)
+        need = lib.dmgs_batch_state_bytes(C.byref(b), 10)
+        assert need > 0
+        return lib.dmgs_raster_fwd_batched(C.byref(b), C.byref(_gauss()), 256, need, None)
+
+    for ppt, gpb, shape in [(3, 128, 0), (4, 64, 0), (4, 128, 3), (4, 128, -1), (1, 128, 1),
+                            (4, 512, 2), (1, 256, 2)]:
+        assert run(ppt, gpb, shape) == -1, (ppt, gpb, shape)
+        assert b"unsupported blend tuning" in lib.dmgs_last_error()
