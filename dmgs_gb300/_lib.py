@@ -13,7 +13,7 @@ import torch  # noqa: F401  (loads libcudart before the extension)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdmgs_gb300.so")
-ABI_VERSION = 7  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
+ABI_VERSION = 8  # DMGS_ABI_VERSION of include/dmgs.h that SIGNATURES and the structs follow
 
 c_float_p = C.POINTER(C.c_float)
 vp = C.c_void_p
@@ -129,9 +129,12 @@ SIGNATURES = [
     ("dmgs_sh_colors_bwd", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, vp, vp, vp, vp, vp, vp]),
     ("dmgs_tex_table_entries", C.c_int64, [C.c_float]),
     ("dmgs_tex_fwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp]),
+    ("dmgs_tex_fwd_enc", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp]),
     ("dmgs_tex_bwd_scratch_bytes", C.c_size_t, [C.c_int64]),
     ("dmgs_tex_bwd", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp, vp, vp, vp, vp,
                                C.c_size_t, vp]),
+    ("dmgs_tex_bwd_enc", C.c_int, [C.POINTER(DmgsTexture), C.c_int64, vp, vp, vp, vp, vp, vp, vp,
+                                   vp, vp, C.c_size_t, vp]),
     ("dmgs_l1_ssim_scratch_bytes", C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     ("dmgs_l1_ssim", C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, vp, vp, vp,
                                C.c_size_t, vp]),

@@ -204,7 +204,8 @@ __device__ __forceinline__ void load_weights(const TexArgs &A, float *sW1, float
 
 template <int C>
 __global__ void __launch_bounds__(TEX_THREADS)
-tex_fwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz, float *__restrict__ out) {
+tex_fwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz, float *__restrict__ out,
+               float *__restrict__ enc_out) {
   __shared__ __align__(16) float sW1[32 * 32], sW2[32 * 32], sW3[C * 32];
   constexpr int SC = C | 1;  // odd row stride: conflict-free per-lane row writes
   __shared__ float stage[TEX_THREADS / 32][32 * SC];
@@ -220,6 +221,11 @@ tex_fwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
       tex_coord(A, xyz, p, t, pass);
       float enc[TEX_FEAT], h[32], g[32];
       encode(A, L, t, enc);
+      if (enc_out) {  // kept for the adjoint: [n][32] rows, 16-byte aligned
+        float4 *row = reinterpret_cast<float4 *>(enc_out + 32 * p);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) row[k] = make_float4(enc[4 * k], enc[4 * k + 1], enc[4 * k + 2], enc[4 * k + 3]);
+      }
       matvec<32>(sW1, enc, h);
 #pragma unroll
       for (int k = 0; k < 32; ++k) h[k] = fmaxf(h[k], 0.f);
@@ -268,7 +274,7 @@ __device__ __forceinline__ void outer_gemm(const float *__restrict__ a, int row0
 template <int C>
 __global__ void __launch_bounds__(TEX_THREADS)
 tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz,
-               const float *__restrict__ dout, float *__restrict__ denc,
+               const float *__restrict__ enc_in, const float *__restrict__ dout, float *__restrict__ denc,
                float *__restrict__ dW1, float *__restrict__ dW2, float *__restrict__ dW3) {
   extern __shared__ __align__(16) float smem[];
   float *sW1 = smem, *sW2 = sW1 + 32 * 32, *sW3 = sW2 + 32 * 32;
@@ -305,8 +311,17 @@ tex_bwd_kernel(const TexArgs A, const TexLevels L, const float *__restrict__ xyz
 #pragma unroll
       for (int k = 0; k < 32; ++k) enc[k] = h1[k] = h2[k] = 0.f;
       if (valid) {
-        tex_coord(A, xyz, p, t, pass);
-        encode(A, L, t, enc);
+        if (enc_in) {  // the forward's encoding (the same arithmetic, so the same values)
+          const float4 *row = reinterpret_cast<const float4 *>(enc_in + 32 * p);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const float4 v = __ldg(row + k);
+            enc[4 * k] = v.x; enc[4 * k + 1] = v.y; enc[4 * k + 2] = v.z; enc[4 * k + 3] = v.w;
+          }
+        } else {
+          tex_coord(A, xyz, p, t, pass);
+          encode(A, L, t, enc);
+        }
         matvec<32>(sW1, enc, h1);
 #pragma unroll
         for (int k = 0; k < 32; ++k) h1[k] = fmaxf(h1[k], 0.f);
@@ -477,26 +492,91 @@ int persistent_grid(K kernel, size_t smem, int64_t n, int &grid) {
 }
 
 template <int C>
-int run_fwd(const TexArgs &A, const TexLevels &L, const float *xyz, float *out, cudaStream_t s) {
+int run_fwd(const TexArgs &A, const TexLevels &L, const float *xyz, float *out, float *enc,
+            cudaStream_t s) {
   int grid;
   if (int r = persistent_grid(tex_fwd_kernel<C>, 0, A.n, grid)) return r;
-  dmgs_host::note_launch(), tex_fwd_kernel<C><<<grid, TEX_THREADS, 0, s>>>(A, L, xyz, out);
+  dmgs_host::note_launch(), tex_fwd_kernel<C><<<grid, TEX_THREADS, 0, s>>>(A, L, xyz, out, enc);
   return DMGS_OK;
 }
 
 template <int C>
-int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float *dout, float *dxyz,
-            float *dtable, float *dW1, float *dW2, float *dW3, float *denc, cudaStream_t s) {
+int run_bwd(const TexArgs &A, const TexLevels &L, const float *xyz, const float *enc,
+            const float *dout, float *dxyz, float *dtable, float *dW1, float *dW2, float *dW3,
+            float *denc, cudaStream_t s) {
   if (int r = dmgs_host::raise_smem_limit((const void *)tex_bwd_kernel<C>, tex_bwd_smem())) return r;
   int grid;
   if (int r = persistent_grid(tex_bwd_kernel<C>, tex_bwd_smem(), A.n, grid)) return r;
   // timed apart: the MLP adjoint (weight-gradient GEMMs) and the scatter of
   // the encoding gradients into the table and the positions
   DMGS_TIMED(K_TEX_BWD, s, dmgs_host::note_launch(), tex_bwd_kernel<C><<<grid, TEX_THREADS, tex_bwd_smem(), s>>>(
-      A, L, xyz, dout, denc, dW1, dW2, dW3));
+      A, L, xyz, enc, dout, denc, dW1, dW2, dW3));
   if (dxyz || dtable)
     DMGS_TIMED(K_TEX_SCATTER, s, dmgs_host::note_launch(), tex_scatter_kernel<<<(unsigned)((A.n + 255) / 256), 256, 0, s>>>(
         A, L, xyz, denc, dxyz, reinterpret_cast<float2 *>(dtable)));
+  return DMGS_OK;
+}
+
+}  // namespace
+
+namespace {
+
+int tex_fwd_impl(const DmgsTexture *tx, int64_t n, const float *xyz, float *out, float *enc,
+                 dmgs_stream_t stream) {
+  if (!tex_ok(tx) || n < 0 || (n > 0 && (!xyz || !out)) ||
+      (enc && (reinterpret_cast<uintptr_t>(enc) & 15))) {
+    dmgs_host::set_error("tex_fwd: invalid arguments");
+    return DMGS_ERR_ARG;
+  }
+  if (n == 0) return DMGS_OK;
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const TexArgs A = make_args(tx, n);
+  const TexLevels L = make_levels(tx->per_level_scale);
+  int r = DMGS_OK;
+  DMGS_TIMED(K_TEX_FWD, s, {
+    switch (tx->channels) {
+      case 3: r = run_fwd<3>(A, L, xyz, out, enc, s); break;
+      case 12: r = run_fwd<12>(A, L, xyz, out, enc, s); break;
+      case 27: r = run_fwd<27>(A, L, xyz, out, enc, s); break;
+      default: r = run_fwd<48>(A, L, xyz, out, enc, s); break;
+    }
+  });
+  if (r != DMGS_OK) return r;
+  DMGS_LAUNCH_CHECK("tex_fwd");
+  return DMGS_OK;
+}
+
+int tex_bwd_impl(const DmgsTexture *tx, int64_t n, const float *xyz, const float *enc,
+                 const float *dout, float *dxyz, float *dtable, float *dW1, float *dW2, float *dW3,
+                 void *scratch, size_t scratch_bytes, dmgs_stream_t stream) {
+  if (!tex_ok(tx) || n < 0 || !dW1 || !dW2 || !dW3 || (n > 0 && (!xyz || !dout)) ||
+      (enc && (reinterpret_cast<uintptr_t>(enc) & 15))) {
+    dmgs_host::set_error("tex_bwd: invalid arguments");
+    return DMGS_ERR_ARG;
+  }
+  if (n > 0 && (!scratch || scratch_bytes < dmgs_tex_bwd_scratch_bytes(n) ||
+                (reinterpret_cast<uintptr_t>(scratch) & 15))) {
+    dmgs_host::set_error("tex_bwd: scratch must hold dmgs_tex_bwd_scratch_bytes(n) bytes, 16-byte aligned");
+    return DMGS_ERR_STATE;
+  }
+  float *denc = static_cast<float *>(scratch);
+  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const TexLevels L = make_levels(tx->per_level_scale);
+  DMGS_CUDA(cudaMemsetAsync(dW1, 0, 32 * 32 * 4, s));
+  DMGS_CUDA(cudaMemsetAsync(dW2, 0, 32 * 32 * 4, s));
+  DMGS_CUDA(cudaMemsetAsync(dW3, 0, (size_t)tx->channels * 32 * 4, s));
+  if (dtable) DMGS_CUDA(cudaMemsetAsync(dtable, 0, (size_t)L.entries * 8, s));
+  if (n == 0) return DMGS_OK;
+  const TexArgs A = make_args(tx, n);
+  int r = DMGS_OK;
+  switch (tx->channels) {
+    case 3: r = run_bwd<3>(A, L, xyz, enc, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+    case 12: r = run_bwd<12>(A, L, xyz, enc, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+    case 27: r = run_bwd<27>(A, L, xyz, enc, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+    default: r = run_bwd<48>(A, L, xyz, enc, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
+  }
+  if (r != DMGS_OK) return r;
+  DMGS_LAUNCH_CHECK("tex_bwd");
   return DMGS_OK;
 }
 
@@ -514,27 +594,18 @@ int64_t dmgs_tex_table_entries(float per_level_scale) {
   return (int64_t)make_levels(per_level_scale).entries;
 }
 
+
 int dmgs_tex_fwd(const DmgsTexture *tx, int64_t n, const float *xyz, float *out, dmgs_stream_t stream) {
-  if (!tex_ok(tx) || n < 0 || (n > 0 && (!xyz || !out))) {
-    set_error("tex_fwd: invalid arguments");
+  return tex_fwd_impl(tx, n, xyz, out, nullptr, stream);
+}
+
+int dmgs_tex_fwd_enc(const DmgsTexture *tx, int64_t n, const float *xyz, float *out, float *enc,
+                     dmgs_stream_t stream) {
+  if (n > 0 && !enc) {
+    set_error("tex_fwd_enc: the encoding buffer is required");
     return DMGS_ERR_ARG;
   }
-  if (n == 0) return DMGS_OK;
-  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const TexArgs A = make_args(tx, n);
-  const TexLevels L = make_levels(tx->per_level_scale);
-  int r = DMGS_OK;
-  DMGS_TIMED(K_TEX_FWD, s, {
-    switch (tx->channels) {
-      case 3: r = run_fwd<3>(A, L, xyz, out, s); break;
-      case 12: r = run_fwd<12>(A, L, xyz, out, s); break;
-      case 27: r = run_fwd<27>(A, L, xyz, out, s); break;
-      default: r = run_fwd<48>(A, L, xyz, out, s); break;
-    }
-  });
-  if (r != DMGS_OK) return r;
-  DMGS_LAUNCH_CHECK("tex_fwd");
-  return DMGS_OK;
+  return tex_fwd_impl(tx, n, xyz, out, enc, stream);
 }
 
 size_t dmgs_tex_bwd_scratch_bytes(int64_t n) { return n > 0 ? (size_t)n * 32 * sizeof(float) : 0; }
@@ -542,34 +613,19 @@ size_t dmgs_tex_bwd_scratch_bytes(int64_t n) { return n > 0 ? (size_t)n * 32 * s
 int dmgs_tex_bwd(const DmgsTexture *tx, int64_t n, const float *xyz, const float *dout, float *dxyz,
                  float *dtable, float *dW1, float *dW2, float *dW3, void *scratch,
                  size_t scratch_bytes, dmgs_stream_t stream) {
-  if (!tex_ok(tx) || n < 0 || !dW1 || !dW2 || !dW3 || (n > 0 && (!xyz || !dout))) {
-    set_error("tex_bwd: invalid arguments");
+  return tex_bwd_impl(tx, n, xyz, nullptr, dout, dxyz, dtable, dW1, dW2, dW3, scratch,
+                      scratch_bytes, stream);
+}
+
+int dmgs_tex_bwd_enc(const DmgsTexture *tx, int64_t n, const float *xyz, const float *enc,
+                     const float *dout, float *dxyz, float *dtable, float *dW1, float *dW2,
+                     float *dW3, void *scratch, size_t scratch_bytes, dmgs_stream_t stream) {
+  if (n > 0 && !enc) {
+    set_error("tex_bwd_enc: the encoding buffer is required");
     return DMGS_ERR_ARG;
   }
-  if (n > 0 && (!scratch || scratch_bytes < dmgs_tex_bwd_scratch_bytes(n) ||
-                (reinterpret_cast<uintptr_t>(scratch) & 15))) {
-    set_error("tex_bwd: scratch must hold dmgs_tex_bwd_scratch_bytes(n) bytes, 16-byte aligned");
-    return DMGS_ERR_STATE;
-  }
-  float *denc = static_cast<float *>(scratch);
-  const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-  const TexLevels L = make_levels(tx->per_level_scale);
-  DMGS_CUDA(cudaMemsetAsync(dW1, 0, 32 * 32 * 4, s));
-  DMGS_CUDA(cudaMemsetAsync(dW2, 0, 32 * 32 * 4, s));
-  DMGS_CUDA(cudaMemsetAsync(dW3, 0, (size_t)tx->channels * 32 * 4, s));
-  if (dtable) DMGS_CUDA(cudaMemsetAsync(dtable, 0, (size_t)L.entries * 8, s));
-  if (n == 0) return DMGS_OK;
-  const TexArgs A = make_args(tx, n);
-  int r = DMGS_OK;
-  switch (tx->channels) {
-    case 3: r = run_bwd<3>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-    case 12: r = run_bwd<12>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-    case 27: r = run_bwd<27>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-    default: r = run_bwd<48>(A, L, xyz, dout, dxyz, dtable, dW1, dW2, dW3, denc, s); break;
-  }
-  if (r != DMGS_OK) return r;
-  DMGS_LAUNCH_CHECK("tex_bwd");
-  return DMGS_OK;
+  return tex_bwd_impl(tx, n, xyz, enc, dout, dxyz, dtable, dW1, dW2, dW3, scratch, scratch_bytes,
+                      stream);
 }
 
 }  // extern "C"

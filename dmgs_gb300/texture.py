@@ -41,23 +41,31 @@ def _desc(aabb, table, W1, W2, W3, channels, per_level_scale):
 
 class _TextureFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, xyz, table, W1, W2, W3, aabb_host, per_level_scale):
+    def forward(ctx, xyz, table, W1, W2, W3, aabb_host, per_level_scale, keep_enc):
         lib = _lib.load()
         x = xyz.detach().float().contiguous()
         t, w1, w2, w3 = (a.detach().float().contiguous() for a in (table, W1, W2, W3))
         channels = w3.shape[0]
         d = _desc(aabb_host, t, w1, w2, w3, channels, per_level_scale)
         out = torch.empty((x.shape[0], channels), dtype=torch.float32, device=x.device)
-        check(lib.dmgs_tex_fwd(C.byref(d), x.shape[0], ptr(x), ptr(out), stream_of(x.device)),
-              "tex_fwd")
-        ctx.save_for_backward(x, t, w1, w2, w3)
+        if keep_enc:
+            # keep the encoding for the adjoint (128 B per point) instead of
+            # recomputing its table gathers there
+            enc = torch.empty((x.shape[0], 32), dtype=torch.float32, device=x.device)
+            check(lib.dmgs_tex_fwd_enc(C.byref(d), x.shape[0], ptr(x), ptr(out), ptr(enc),
+                                       stream_of(x.device)), "tex_fwd")
+        else:
+            enc = None
+            check(lib.dmgs_tex_fwd(C.byref(d), x.shape[0], ptr(x), ptr(out), stream_of(x.device)),
+                  "tex_fwd")
+        ctx.save_for_backward(x, t, w1, w2, w3, enc)
         ctx.aabb, ctx.pls = aabb_host, per_level_scale
         return out
 
     @staticmethod
     def backward(ctx, dout):
         lib = _lib.load()
-        x, t, w1, w2, w3 = ctx.saved_tensors
+        x, t, w1, w2, w3, enc = ctx.saved_tensors
         d = _desc(ctx.aabb, t, w1, w2, w3, w3.shape[0], ctx.pls)
         g = dout.float().contiguous()
         dx = torch.empty_like(x) if ctx.needs_input_grad[0] else None
@@ -65,10 +73,16 @@ class _TextureFn(torch.autograd.Function):
         dw1, dw2, dw3 = torch.empty_like(w1), torch.empty_like(w2), torch.empty_like(w3)
         scratch = torch.empty(max(1, lib.dmgs_tex_bwd_scratch_bytes(x.shape[0]) // 4),
                               dtype=torch.float32, device=x.device)
-        check(lib.dmgs_tex_bwd(C.byref(d), x.shape[0], ptr(x), ptr(g), ptr(dx), ptr(dt),
-                               dw1.data_ptr(), dw2.data_ptr(), dw3.data_ptr(), scratch.data_ptr(),
-                               scratch.numel() * 4, stream_of(x.device)), "tex_bwd")
-        return dx, dt, dw1, dw2, dw3, None, None
+        if enc is not None:
+            check(lib.dmgs_tex_bwd_enc(C.byref(d), x.shape[0], ptr(x), ptr(enc), ptr(g), ptr(dx),
+                                       ptr(dt), dw1.data_ptr(), dw2.data_ptr(), dw3.data_ptr(),
+                                       scratch.data_ptr(), scratch.numel() * 4,
+                                       stream_of(x.device)), "tex_bwd")
+        else:
+            check(lib.dmgs_tex_bwd(C.byref(d), x.shape[0], ptr(x), ptr(g), ptr(dx), ptr(dt),
+                                   dw1.data_ptr(), dw2.data_ptr(), dw3.data_ptr(), scratch.data_ptr(),
+                                   scratch.numel() * 4, stream_of(x.device)), "tex_bwd")
+        return dx, dt, dw1, dw2, dw3, None, None, None
 
 
 class _HashGridParams(torch.nn.Module):
@@ -135,8 +149,10 @@ class MLPTexture3D(torch.nn.Module):
         if texc.numel() == 0:
             return torch.zeros(*texc.shape[:-1], self.channels, device=texc.device)
         W1, W2, W3 = self.net.weights()
+        keep = torch.is_grad_enabled() and any(
+            t.requires_grad for t in (texc, self.encoder.params, W1, W2, W3))
         out = _TextureFn.apply(texc.reshape(-1, 3), self.encoder.params, W1, W2, W3,
-                               self._aabb_host(), self.per_level_scale)
+                               self._aabb_host(), self.per_level_scale, keep)
         return out.view(*texc.shape[:-1], self.channels)
 
     def sample(self, texc):

@@ -27,7 +27,7 @@
 /* Version of the structs and entry points below; dmgs_abi_version() returns
  * the value the library was built with.  Raised whenever a struct layout or
  * a signature changes. */
-#define DMGS_ABI_VERSION 7
+#define DMGS_ABI_VERSION 8
 
 #ifdef __cplusplus
 extern "C" {
@@ -392,6 +392,17 @@ size_t dmgs_tex_bwd_scratch_bytes(int64_t n);  /* 128 B per point, 16-byte align
 int dmgs_tex_bwd(const DmgsTexture *t, int64_t n, const float *xyz, const float *dout,
                  float *dxyz, float *dtable, float *dW1, float *dW2, float *dW3,
                  void *scratch, size_t scratch_bytes, dmgs_stream_t stream);
+/* The same pair keeping the encoding: dmgs_tex_fwd_enc also writes each
+ * point's 32 encoding values to enc ([n, 32] f32, 128 B per point, 16-byte
+ * aligned), and dmgs_tex_bwd_enc reads them instead of recomputing the 128
+ * table gathers per point (the reference's autograd likewise keeps the
+ * MLP's input for its backward).  The values are those the forward used,
+ * so the gradients equal dmgs_tex_bwd's. */
+int dmgs_tex_fwd_enc(const DmgsTexture *t, int64_t n, const float *xyz, float *out, float *enc,
+                     dmgs_stream_t stream);
+int dmgs_tex_bwd_enc(const DmgsTexture *t, int64_t n, const float *xyz, const float *enc,
+                     const float *dout, float *dxyz, float *dtable, float *dW1, float *dW2,
+                     float *dW3, void *scratch, size_t scratch_bytes, dmgs_stream_t stream);
 
 /* ---------------------------------------------------------------------- *
  * The renderer's Python colour path (gaussian_renderer/__init__.py:165-170:

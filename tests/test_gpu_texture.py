@@ -82,3 +82,53 @@ def test_state_dict_and_empty_input():
     assert tex.encoder.params.numel() == 2 * otex.table_entries()
     out = tex.sample_noact(torch.zeros((0, 3), device="cuda"))
     assert out.shape == (0, 48)
+
+
+def test_kept_encoding_gives_the_recomputed_gradients():
+    """dmgs_tex_fwd_enc + dmgs_tex_bwd_enc (the encoding kept from the
+    forward) against dmgs_tex_fwd + dmgs_tex_bwd (recomputed in the adjoint)
+    through the C ABI: the same outputs, the same per-point encoding
+    gradients and position gradients bit for bit, the weight and table
+    gradients equal up to the order of their float atomics."""
+    import ctypes as C
+    from dmgs_gb300 import _lib
+    from dmgs_gb300._lib import check, ptr, stream_of
+    from dmgs_gb300.texture import _desc
+    lib = _lib.load()
+    rng = np.random.default_rng(7)
+    n, channels = 20000, 48
+    aabb = torch.tensor([[-1.0, -1.0, -1.0], [1.0, 1.0, 1.0]])
+    table = torch.tensor(rng.normal(0, 0.05, (otex.table_entries(), 2)).astype(np.float32), device="cuda")
+    W = [torch.tensor(rng.normal(0, 0.3, s).astype(np.float32), device="cuda")
+         for s in ((32, 32), (32, 32), (channels, 32))]
+    xyz = torch.tensor(rng.uniform(-1.1, 1.1, (n, 3)).astype(np.float32), device="cuda")
+    up = torch.tensor(rng.standard_normal((n, channels)).astype(np.float32), device="cuda")
+    pls = float(np.exp(np.log(4096 / 16) / 15))
+    d = _desc(aabb, table, *W, channels, pls)
+    s = stream_of(xyz.device)
+    res = []
+    for keep in (False, True):
+        out = torch.empty((n, channels), device="cuda")
+        enc = torch.empty((n, 32), device="cuda") if keep else None
+        if keep:
+            check(lib.dmgs_tex_fwd_enc(C.byref(d), n, ptr(xyz), ptr(out), ptr(enc), s), "fwd")
+        else:
+            check(lib.dmgs_tex_fwd(C.byref(d), n, ptr(xyz), ptr(out), s), "fwd")
+        dx, dt = torch.empty_like(xyz), torch.empty_like(table)
+        dw = [torch.empty_like(w) for w in W]
+        scratch = torch.empty(lib.dmgs_tex_bwd_scratch_bytes(n) // 4, device="cuda")
+        args = (ptr(up), ptr(dx), ptr(dt), *(w.data_ptr() for w in dw), scratch.data_ptr(),
+                scratch.numel() * 4, s)
+        if keep:
+            check(lib.dmgs_tex_bwd_enc(C.byref(d), n, ptr(xyz), ptr(enc), *args), "bwd")
+        else:
+            check(lib.dmgs_tex_bwd(C.byref(d), n, ptr(xyz), *args), "bwd")
+        torch.cuda.synchronize()
+        res.append((out, scratch, dx, dt, dw))
+    (o0, e0, x0, t0, w0), (o1, e1, x1, t1, w1) = res
+    assert torch.equal(o0, o1)
+    assert torch.equal(e0, e1)  # dL/denc per point
+    assert torch.equal(x0, x1)
+    assert rel_l2(t1.cpu(), t0.cpu()) < 1e-6
+    for a, b in zip(w1, w0):
+        assert rel_l2(a.cpu(), b.cpu()) < 1e-6
