@@ -38,3 +38,22 @@ def test_identical_images_have_zero_loss_and_l1_free_gradient():
     loss.backward()
     assert abs(float(loss.detach())) < 1e-5
     assert xr.grad.abs().max() < 1e-6  # SSIM is stationary there, sign(0) = 0
+
+
+def test_matches_the_reference_loss_golden_vectors():
+    """The fused kernels against golden vectors from the reference's own
+    utils/loss_utils.py (l1_loss and ssim as train_geo_stage2.py:114-116
+    combines them, float64 on the CPU): value to 1e-5 relative, gradient
+    to 1e-4 relative L2 (float32 kernels)."""
+    import os
+    import numpy as np
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "loss_golden.npz"))
+    for i in range(int(z["n"])):
+        x = torch.tensor(z[f"x{i}"], device="cuda", requires_grad=True)
+        y = torch.tensor(z[f"y{i}"], device="cuda")
+        loss = l1_ssim_loss(x, y, float(z[f"lam{i}"]))
+        loss.backward()
+        ref = float(z[f"loss{i}"])
+        assert abs(loss.item() - ref) <= 1e-5 * max(1.0, abs(ref))
+        g = z[f"grad{i}"].astype(np.float64)
+        assert np.linalg.norm(x.grad.double().cpu().numpy() - g) <= 1e-4 * np.linalg.norm(g)
