@@ -77,3 +77,20 @@ def test_binding_without_scale_factor_matches_reference(G, adaptive):
     ((xyz * torch.tensor(z[f"{tag}/gxyz"], dtype=torch.float64)).sum()
      + (cov * torch.tensor(z[f"{tag}/gcov"], dtype=torch.float64)).sum()).backward()
     assert rel_l2(v.grad, z[f"{tag}/dverts"]) <= 1e-5
+
+
+def test_face_culling_rule_matches_reference_in_frustum():
+    """The stage-3 face culling rule (in_frustum on face centroids,
+    scene/gaussian_geo_model_finetune.py:33-48 as renew_gaussian applies it,
+    :405-409) — the oracle's frustum test with no half-cube shift on the
+    centroids — against golden masks from the reference's own function
+    (tests/golden/make_facecull_golden.py), outside a 1e-4 band around the
+    bounds where float32 and float64 may decide differently."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "facecull_golden.npz"))
+    c = z["verts"].astype(np.float64)[z["faces"]].mean(axis=1)
+    for i in range(int(z["n"])):
+        m, margin = ob.vertex_frustum_mask(c, z[f"proj{i}"], 0.0)
+        ok = margin.numpy() > 1e-4
+        assert ok.mean() > 0.99
+        assert np.array_equal(m.numpy()[ok], z[f"mask{i}"][ok])
+        assert 0 < z[f"mask{i}"].sum() < len(z["faces"])
