@@ -128,3 +128,27 @@ def test_frustum_face_culling_matches_the_reference_rule():
     bad[0, 0] = len(v) + 5  # out-of-range vertex: never kept
     m2, _, _ = frustum_faces(verts, bad, M)
     assert not bool(m2[0])
+
+
+def test_frustum_face_culling_matches_reference_golden():
+    """frustum_faces (dmgs_face_cull) against the masks of the reference's
+    own in_frustum on face centroids (tests/golden/facecull_golden.npz),
+    outside a 1e-4 band around the bounds (the oracle's margin), with the
+    kept faces compacted in face order."""
+    import os
+    import numpy as np
+    from dmgs_gb300.binding import frustum_faces
+    from oracle import binding as ob
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "facecull_golden.npz"))
+    verts = torch.tensor(z["verts"], device="cuda")
+    faces = torch.tensor(z["faces"], device="cuda")
+    c = z["verts"].astype(np.float64)[z["faces"]].mean(axis=1)
+    for i in range(int(z["n"])):
+        M = torch.tensor(z[f"proj{i}"], device="cuda")
+        mask, kept, idx = frustum_faces(verts, faces, M)
+        _, margin = ob.vertex_frustum_mask(c, z[f"proj{i}"], 0.0)
+        ok = torch.tensor(margin.numpy() > 1e-4, device="cuda")
+        ref = torch.tensor(z[f"mask{i}"], device="cuda")
+        assert torch.equal(mask[ok], ref[ok])
+        assert torch.equal(idx, torch.nonzero(mask).squeeze(1))
+        assert torch.equal(kept, faces[mask])
