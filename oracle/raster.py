@@ -30,8 +30,11 @@ Two halves:
         densification consumes (``scene/gaussian_model.py:405-406``);
       * the quaternion is used as given (not normalised).
     Pixels whose result hinges on a threshold test that FP32 cannot decide
-    (alpha within 1e-5 relative of 1/255, or transmittance within 1e-5
-    relative of 1e-4) are reported in ``ambiguous``.
+    are reported in ``ambiguous``: alpha within a relative band of 1/255 (the
+    larger of 1e-5 and the exponent's FP32 reach: 4 ulp of the projected
+    mean's pixel coordinates times the exponent's derivative w.r.t. the
+    mean, plus 4 ulp of its terms), or transmittance within a relative band
+    of 1e-4 (1e-5 plus the bands of the alphas blended before it).
 """
 from __future__ import annotations
 
@@ -406,10 +409,25 @@ def _blend_tile(pix_xy, xy, conic, op, rgb, bg):
         a_v = torch.where(valid, alpha, torch.zeros_like(alpha))
         T_after = torch.cumprod(1 - a_v, dim=1)
         keep = T_after >= 1e-4
-        # ambiguity: a decision within FP32 reach of its threshold, before termination
+        # ambiguity: a decision within FP32 reach of its threshold, before
+        # termination.  An FP32 kernel holds the projected mean to about an
+        # ulp of its pixel coordinates (a few roundings: 4 ulp), which moves
+        # the exponent by |d power / d mean| times that, and evaluates the
+        # exponent's terms to a few ulp: the alpha test's relative band is
+        # the larger of 1e-5 and that reach; the transmittance test's band
+        # adds up the bands of the alphas blended before it.
         processed = torch.cat([torch.ones_like(keep[:, :1]), keep[:, :-1]], 1)
-        amb_a = ((alpha - 1.0 / 255.0).abs() <= 1e-5 / 255.0) & (power <= 0)
-        amb_t = valid & ((T_after - 1e-4).abs() <= 1e-5 * 1e-4)
+        ulp = lambda v: torch.ldexp(torch.ones_like(v), torch.frexp(v.abs().clamp_min(1.0))[1] - 24)  # noqa: E731
+        gx = (co[..., 0] * d[..., 0] + co[..., 1] * d[..., 1]).abs()
+        gy = (co[..., 2] * d[..., 1] + co[..., 1] * d[..., 0]).abs()
+        terms = (0.5 * co[..., 0] * d[..., 0] ** 2).abs() + (0.5 * co[..., 2] * d[..., 1] ** 2).abs() + \
+            (co[..., 1] * d[..., 0] * d[..., 1]).abs()
+        reach = 4.0 * (gx * ulp(xy[:, 0]).unsqueeze(0) + gy * ulp(xy[:, 1]).unsqueeze(0)) + \
+            4.0 * 2.0 ** -23 * terms
+        band_a = torch.clamp_min(reach, 1e-5)
+        amb_a = ((alpha - 1.0 / 255.0).abs() <= band_a / 255.0) & (power <= 0)
+        band_t = 1e-5 + torch.cumsum(a_v * band_a / (1 - a_v), dim=1)
+        amb_t = valid & ((T_after - 1e-4).abs() <= band_t * 1e-4)
         ambiguous = ((amb_a | amb_t) & processed).any(1)
         use = valid & keep
         idx = torch.arange(1, use.shape[1] + 1).unsqueeze(0).expand_as(use)

@@ -152,6 +152,24 @@ def test_ragged_image_and_long_tile_lists():
         assert rel_l2(gk[GRAD_NAMES[name]], gref) <= GRAD_TOL, name
 
 
+def test_wide_image_lists_bit_exact():
+    """An image 2,200 pixels wide (138 tiles per row: the emission's masks
+    span five 32-tile chunks, and one row of tiles holds more instances than
+    a staging sub-pass): sorted keys, values and tile ranges equal the
+    oracle's, and the image matches."""
+    sc = small_scene(P=20000, width=2200, height=400, fov_deg=60.0, seed=12)
+    view = sc.views[0]
+    inp = mode_inputs(sc, ("shs", "sr"))
+    cam = oracle_camera(view)
+    ref = R.render(cam, inp["means3D"], inp["opacities"], shs=inp["shs"], scales=inp["scales"],
+                   rotations=inp["rotations"])
+    assert (2200 + 15) // 16 > 128 and ref.num_rendered > 100_000
+    run = AbiRun(view, inp).forward()
+    _check_integer_outputs(run, ref, cam)
+    ok = ~ref.ambiguous
+    assert np.abs(run.color.cpu().numpy() - ref.image)[:, ok].max() <= IMG_TOL
+
+
 def test_large_footprints_and_clamped_jacobian():
     """Gaussians close to the camera (hundreds of tiles each) and beyond the
     1.3x field-of-view clamp."""
