@@ -32,8 +32,9 @@
 //   log2(1/(255 o)) is precomputed: a pair below it cannot reach alpha 1/255
 //   and is rejected before the exponential (the alpha test itself is still
 //   applied afterwards);
-// * each staged Gaussian carries a mask of the tile rows its alpha >= 1/255
-//   ellipse can reach (a superset): a warp whose band it misses never
+// * each staged Gaussian carries a mask of the warps' row bands its
+//   alpha >= 1/255 ellipse can reach (a superset, from the exponent's
+//   maximum over each band's rectangle): a warp whose band it misses never
 //   visits it (per-warp visit lists, one ballot per 32 staged Gaussians) —
 //   only pairs the exact test would reject are skipped;
 // * the forward and the adjoint evaluate the exponent with the same
@@ -64,9 +65,11 @@ __device__ __forceinline__ float ex2_approx(float x) {
 // s2 = (g, b, footprint rows, 0) with exponent2 = A dx^2 + B dx dy + C dy^2
 // (A = -a log2e / 2, B = -b log2e, C = -c log2e / 2) and thr = log2(1 / (255 o)).
 // The footprint rows (bits 0-15) cover the tile rows where alpha can reach
-// 1/255: the ellipse (a dx^2 + 2 b dx dy + c dy^2) <= 2 ln(255 o), whose
-// vertical half-extent is sqrt(R^2 a / det), inflated by 0.1% + 0.01 px so
-// that the mask is a superset of the rows the exact test accepts.
+// 1/255 (a superset of the rows the exact test accepts): with warp bands
+// of 4 or more rows, whole bands (band_rows); with bands of 2 rows, the
+// ellipse (a dx^2 + 2 b dx dy + c dy^2) <= 2 ln(255 o)'s vertical extent,
+// sqrt(R^2 a / det) inflated by 0.1% + 0.01 px (footprint), refined per row
+// (exact_rows).
 struct Staged {
   float4 s0, s1, s2;
 };
