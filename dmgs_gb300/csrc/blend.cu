@@ -286,7 +286,6 @@ __device__ __forceinline__ int visit_list(const uint32_t *masks, int cnt, uint32
 // Gaussian whose footprint misses a band is never visited by its warp.
 template <int PPT>
 struct PixelLayout {
-  static constexpr int THREADS = 256 / PPT;
   int col, r0;
   uint32_t warp_rows;
   __device__ __forceinline__ explicit PixelLayout(int tid) {  // tid: thread index in the tile's half

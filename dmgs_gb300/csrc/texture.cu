@@ -41,7 +41,6 @@ namespace {
 
 constexpr int TEX_LEVELS = 16;
 constexpr int TEX_FEAT = TEX_LEVELS * 2;  // encoding width
-constexpr int TEX_HID = 32;               // hidden width
 constexpr int TEX_MAXC = 48;              // channels (SH degree 3: 3 x 16)
 constexpr int TEX_THREADS = 128;
 constexpr uint32_t TEX_LOG2_HASHMAP = 19;
