@@ -53,6 +53,26 @@ __device__ __forceinline__ void cov3d_scale_rot(float sx, float sy, float sz, fl
 
 __device__ __forceinline__ int trunc_sat(float v) { return __float2int_rz(v); }
 
+// View-space z of a mean (column-major view matrix), in the op order the
+// CPU oracle uses.
+__device__ __forceinline__ float view_z(const float *V, float x, float y, float z) {
+  return add(add(add(mul(V[2], x), mul(V[6], y)), mul(V[10], z)), V[14]);
+}
+
+// Pixel-space position of a mean: homogeneous projection, perspective
+// divide, NDC -> pixel.
+__device__ __forceinline__ float2 pixel_of(const ViewParams &vp, const float *Pm, float x,
+                                           float y, float z) {
+  const float hx = add(add(add(mul(Pm[0], x), mul(Pm[4], y)), mul(Pm[8], z)), Pm[12]);
+  const float hy = add(add(add(mul(Pm[1], x), mul(Pm[5], y)), mul(Pm[9], z)), Pm[13]);
+  const float hw = add(add(add(mul(Pm[3], x), mul(Pm[7], y)), mul(Pm[11], z)), Pm[15]);
+  const float pw = dvd(1.f, add(hw, 1e-7f));
+  const float ndcx = mul(hx, pw), ndcy = mul(hy, pw);
+  const float Wf = (float)vp.W, Hf = (float)vp.H;
+  return make_float2(mul(sub(mul(add(ndcx, 1.f), Wf), 1.f), 0.5f),
+                     mul(sub(mul(add(ndcy, 1.f), Hf), 1.f), 0.5f));
+}
+
 // Geometry of one Gaussian in one view (position, 3D covariance S and
 // opacity o given): projection, EWA 2D covariance, conic, radius and tile
 // rectangle.  Writes radii[idx] and, when visible, every field of the record
@@ -66,7 +86,7 @@ geometry_one(int idx, const ViewParams &vp, const float *V, const float *Pm, flo
              uint32_t *__restrict__ counters) {
   const float vx = add(add(add(mul(V[0], x), mul(V[4], y)), mul(V[8], z)), V[12]);
   const float vy = add(add(add(mul(V[1], x), mul(V[5], y)), mul(V[9], z)), V[13]);
-  const float vz = add(add(add(mul(V[2], x), mul(V[6], y)), mul(V[10], z)), V[14]);
+  const float vz = view_z(V, x, y, z);
 
   auto cull = [&]() {
     radii[idx] = 0;
@@ -77,14 +97,8 @@ geometry_one(int idx, const ViewParams &vp, const float *V, const float *Pm, flo
     cull();
     return false;
   }
-  const float hx = add(add(add(mul(Pm[0], x), mul(Pm[4], y)), mul(Pm[8], z)), Pm[12]);
-  const float hy = add(add(add(mul(Pm[1], x), mul(Pm[5], y)), mul(Pm[9], z)), Pm[13]);
-  const float hw = add(add(add(mul(Pm[3], x), mul(Pm[7], y)), mul(Pm[11], z)), Pm[15]);
-  const float pw = dvd(1.f, add(hw, 1e-7f));
-  const float ndcx = mul(hx, pw), ndcy = mul(hy, pw);
-  const float Wf = (float)vp.W, Hf = (float)vp.H;
-  const float px = mul(sub(mul(add(ndcx, 1.f), Wf), 1.f), 0.5f);
-  const float py = mul(sub(mul(add(ndcy, 1.f), Hf), 1.f), 0.5f);
+  const float2 pix = pixel_of(vp, Pm, x, y, z);
+  const float px = pix.x, py = pix.y;
 
   // EWA: cov2D = (J W) Sigma (J W)^T with the Jacobian evaluated at the
   // position clamped to 1.3x the field of view.
@@ -255,14 +269,51 @@ preprocess_kernel(ViewParams vp, const float *__restrict__ viewm_g,
   if (threadIdx.x == 0) blkcnt[blockIdx.x] = (uint32_t)nvis;
 }
 
-// Multi-view preprocess.  Phase 1, one thread per Gaussian: the
-// view-independent inputs are loaded and the 3D covariance formed once, then
-// the geometry of every view is computed (each view's matrices are L1-
-// resident broadcasts).  A Gaussian is visible in few of the views, so the
-// colour (SH evaluation, 48 coefficient loads) is left to phase 2, which
-// takes the block's visible (Gaussian, view) pairs — listed by a block-wide
-// scan of the per-thread visibility masks — with every lane busy.  Each
-// view's per-block visible count feeds its compaction.
+// Lists the block's (Gaussian, view) pairs whose bits are set in the
+// per-thread view masks m into pairs[] as (thread << 4) | view, thread-major;
+// returns how many there are.  Every thread of the block calls it.
+template <int NW>
+__device__ __forceinline__ uint32_t list_pairs(uint32_t m, uint16_t *pairs, uint32_t *wsum) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const uint32_t cnt = __popc(m);
+  uint32_t inc = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, off);
+    if (lane >= off) inc += u;
+  }
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  uint32_t off = inc - cnt, total = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    off += w < wid ? wsum[w] : 0u;
+    total += wsum[w];
+  }
+  for (uint32_t mm = m; mm; mm &= mm - 1) pairs[off++] = (uint16_t)((t << 4) | (__ffs(mm) - 1));
+  __syncthreads();
+  return total;
+}
+
+// Multi-view preprocess, one block of PRE_BLOCK Gaussians and every view.
+//
+// Phase 1, a thread per Gaussian: the view-independent inputs are loaded and
+// the 3D covariance formed once; then, per view, an exact test of the view
+// depth and of the projected centre (the same IEEE ops as the full chain)
+// against a conservative radius bound decides whether the pair can be
+// visible at all.  The bound: the EWA chain's larger eigenvalue is at most
+// tr(J W Sigma W^T J^T) + 0.62 <= |J|_F^2 |W|_F^2 |Sigma|_F + 0.62, with
+// |J|_F^2 <= (fx^2 (1 + limx^2) + fy^2 (1 + limy^2)) / z^2 for the Jacobian
+// at the clamped position; widened by 0.1% and 2 pixels for rounding, and
+// the centre compared with a margin of 2 + 1e-4 |x| pixels, it never culls a
+// pair the full chain keeps.  About 40% of the pairs of an inward-looking
+// batch lie in front of the camera but only ~7% pass the test.
+// Phase 2 runs the full geometry on the block's candidate pairs, listed
+// compactly so that every lane does useful work (a per-lane early exit
+// would leave the warps running the chain for their slowest lane).
+// Phase 3 takes the visible pairs, listed the same way, through the colour
+// (SH evaluation, 48 coefficient loads).  Each view's per-block visible
+// count feeds its compaction.
 __global__ void __launch_bounds__(PRE_BLOCK)
 preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__restrict__ means,
                           const float *__restrict__ opac, const float *__restrict__ shs,
@@ -272,75 +323,128 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
   __shared__ uint32_t wcnt[NW][MAX_BATCH_VIEWS];
   __shared__ uint32_t wsum[NW];
   __shared__ uint16_t pairs[PRE_BLOCK * MAX_BATCH_VIEWS];
-  // per-view constants of the colour pass (a different view per lane: from
-  // the kernel parameters those would be serialised constant-bank loads)
+  __shared__ uint32_t s_vm[PRE_BLOCK];
+  // the block's Gaussians (position, covariance, opacity) for the per-pair
+  // passes, one array per field
+  __shared__ float s_g[10][PRE_BLOCK];
+  // per-view constants of the per-pair passes (a different view per lane:
+  // from the kernel parameters those would be serialised constant-bank
+  // loads); the matrices padded to 17 words so different views fall in
+  // different banks
   __shared__ ViewParams s_vp[MAX_BATCH_VIEWS];
+  __shared__ float s_V[MAX_BATCH_VIEWS][17], s_P[MAX_BATCH_VIEWS][17];
+  __shared__ float s_kv[MAX_BATCH_VIEWS];
   __shared__ float s_cam[MAX_BATCH_VIEWS][3];
   __shared__ float4 *s_feat[MAX_BATCH_VIEWS];
   __shared__ uint8_t *s_flags[MAX_BATCH_VIEWS];
+  __shared__ int32_t *s_radii[MAX_BATCH_VIEWS];
+  __shared__ uint32_t *s_counters[MAX_BATCH_VIEWS];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  if (t < bv.nviews) {
-    s_vp[t] = bv.v[t].vp;
-    s_cam[t][0] = __ldg(bv.v[t].campos);
-    s_cam[t][1] = __ldg(bv.v[t].campos + 1);
-    s_cam[t][2] = __ldg(bv.v[t].campos + 2);
-    s_feat[t] = bv.v[t].feat;
-    s_flags[t] = bv.v[t].flags;
+  const int nv = bv.nviews;
+  if (t < nv) {
+    const BatchView &V = bv.v[t];
+    s_vp[t] = V.vp;
+    s_cam[t][0] = __ldg(V.campos);
+    s_cam[t][1] = __ldg(V.campos + 1);
+    s_cam[t][2] = __ldg(V.campos + 2);
+    s_feat[t] = V.feat;
+    s_flags[t] = V.flags;
+    s_radii[t] = V.radii;
+    s_counters[t] = V.counters;
+    // |J|_F^2 z^2 |W|_F^2 bound factor of the pre-test
+    float w2 = 0.f;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float w = __ldg(V.viewm + 4 * j + i);
+        w2 += w * w;
+      }
+    const float limx = mul(1.3f, V.vp.tanfovx), limy = mul(1.3f, V.vp.tanfovy);
+    s_kv[t] = (V.vp.fx * V.vp.fx * (1.f + limx * limx) + V.vp.fy * V.vp.fy * (1.f + limy * limy)) * w2;
   }
-  const int idx = blockIdx.x * PRE_BLOCK + t;
-  uint32_t vm = 0u;
+  for (int i = t; i < nv * 32; i += PRE_BLOCK) {
+    const int v = i >> 5, k = i & 31;
+    if (k < 16) s_V[v][k] = __ldg(bv.v[v].viewm + k);
+    else s_P[v][k - 16] = __ldg(bv.v[v].projm + k - 16);
+  }
+  s_vm[t] = 0u;
+  __syncthreads();
+
+  const int base = blockIdx.x * PRE_BLOCK;
+  const int idx = base + t;
+  const float mod0 = s_vp[0].scale_modifier;
+  uint32_t cm = 0u;  // candidate views of this thread's Gaussian
   if (idx < P) {
     float S[6], x, y, z, o;
-    const float mod0 = bv.v[0].vp.scale_modifier;
     load_gaussian(idx, mod0, means, opac, scales, rots, cov3D, x, y, z, S, o);
-    for (int v = 0; v < bv.nviews; ++v) {
-      const BatchView &V = bv.v[v];
-      if (V.vp.scale_modifier != mod0)  // views with another scale modifier (uncommon)
-        load_gaussian(idx, V.vp.scale_modifier, means, opac, scales, rots, cov3D, x, y, z, S, o);
-      float Vm[16], Pm[16];
-      load_mat(V.viewm, Vm);
-      load_mat(V.projm, Pm);
-      if (geometry_one(idx, V.vp, Vm, Pm, x, y, z, S, o, V.radii, V.feat, V.flags, V.counters))
-        vm |= 1u << v;
-      if (V.vp.scale_modifier != mod0)
-        load_gaussian(idx, mod0, means, opac, scales, rots, cov3D, x, y, z, S, o);
+    s_g[0][t] = x; s_g[1][t] = y; s_g[2][t] = z;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s_g[3 + i][t] = S[i];
+    s_g[9][t] = o;
+    const float sfro =
+        sqrtf(S[0] * S[0] + S[3] * S[3] + S[5] * S[5] + 2.f * (S[1] * S[1] + S[2] * S[2] + S[4] * S[4]));
+    for (int v = 0; v < nv; ++v) {
+      const float vz = view_z(s_V[v], x, y, z);
+      bool cand;
+      if (!(vz > 0.2f)) {  // the full chain's first test, on the same value
+        if (s_vp[v].prefiltered) atomicOr(s_counters[v], ST_PREFILTER);
+        cand = false;
+      } else if (cov3D == nullptr && s_vp[v].scale_modifier != mod0) {
+        cand = true;  // another scale modifier (uncommon): no bound, full chain
+      } else {
+        const float2 pix = pixel_of(s_vp[v], s_P[v], x, y, z);
+        const float rb = 3.01f * sqrtf(1.001f * (s_kv[v] * sfro / (vz * vz) + 0.62f)) + 2.f;
+        const float mx = 2.f + 1e-4f * fabsf(pix.x), my = 2.f + 1e-4f * fabsf(pix.y);
+        const float xmax = (float)(TILE * s_vp[v].gx), ymax = (float)(TILE * s_vp[v].gy);
+        // NaN anywhere leaves every comparison false: the pair stays a candidate
+        cand = !(pix.x + rb < 1.f - mx || pix.x - rb > xmax + mx || pix.y + rb < 1.f - my ||
+                 pix.y - rb > ymax + my);
+      }
+      if (cand) {
+        cm |= 1u << v;
+      } else {
+        s_radii[v][idx] = 0;
+        s_flags[v][idx] = 0;
+      }
     }
   }
-  for (int v = 0; v < bv.nviews; ++v) {
+
+  // Phase 2: full geometry of the candidate pairs.
+  const uint32_t ncand = list_pairs<NW>(cm, pairs, wsum);
+  for (uint32_t i = t; i < ncand; i += PRE_BLOCK) {
+    const uint32_t pr = pairs[i];
+    const int gl = (int)(pr >> 4), v = (int)(pr & 15u);
+    float S[6], x = s_g[0][gl], y = s_g[1][gl], z = s_g[2][gl], o = s_g[9][gl];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) S[k] = s_g[3 + k][gl];
+    if (cov3D == nullptr && s_vp[v].scale_modifier != mod0)
+      load_gaussian(base + gl, s_vp[v].scale_modifier, means, opac, scales, rots, cov3D, x, y, z, S, o);
+    if (geometry_one(base + gl, s_vp[v], s_V[v], s_P[v], x, y, z, S, o, s_radii[v], s_feat[v],
+                     s_flags[v], s_counters[v]))
+      atomicOr(&s_vm[gl], 1u << v);
+  }
+  __syncthreads();
+
+  // Phase 3: colour of the visible pairs, and the per-view block counts.
+  const uint32_t vm = s_vm[t];
+  for (int v = 0; v < nv; ++v) {
     const uint32_t b = __ballot_sync(0xffffffffu, (vm >> v) & 1u);
     if (lane == 0) wcnt[wid][v] = __popc(b);
   }
-  const uint32_t cnt = __popc(vm);
-  uint32_t inc = cnt;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, off);
-    if (lane >= off) inc += u;
-  }
-  if (lane == 31) wsum[wid] = inc;
-  __syncthreads();
-  if (t < bv.nviews) {
+  const uint32_t total = list_pairs<NW>(vm, pairs, wsum);
+  if (t < nv) {
     uint32_t n = 0;
 #pragma unroll
     for (int w = 0; w < NW; ++w) n += wcnt[w][t];
     bv.v[t].blkcnt[blockIdx.x] = n;
   }
-  uint32_t off = inc - cnt, total = 0;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    off += w < wid ? wsum[w] : 0u;
-    total += wsum[w];
-  }
-  for (uint32_t m = vm; m; m &= m - 1) pairs[off++] = (uint16_t)((t << 4) | (__ffs(m) - 1));
-  __syncthreads();
-  const int base = blockIdx.x * PRE_BLOCK;
   for (uint32_t i = t; i < total; i += PRE_BLOCK) {
     const uint32_t pr = pairs[i];
-    const int g = base + (int)(pr >> 4);
-    const int v = (int)(pr & 15u);
+    const int gl = (int)(pr >> 4), v = (int)(pr & 15u);
     const ViewParams vp = s_vp[v];
-    color_one(g, vp, s_cam[v], M, __ldg(means + 3 * g), __ldg(means + 3 * g + 1),
-              __ldg(means + 3 * g + 2), shs, colors, s_feat[v], s_flags[v]);
+    color_one(base + gl, vp, s_cam[v], M, s_g[0][gl], s_g[1][gl], s_g[2][gl], shs, colors,
+              s_feat[v], s_flags[v]);
   }
 }
 

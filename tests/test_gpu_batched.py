@@ -262,6 +262,35 @@ def test_view_with_nothing_visible_in_a_batch():
         assert rel_l2(br.grads[k].cpu().numpy(), plain[1][k].cpu().numpy()) <= 1e-5, k
 
 
+def test_inside_views_with_mixed_modifiers_and_given_covariances_match_per_view_path():
+    """Cameras inside a large-scene cloud, where most (Gaussian, view) pairs
+    lie behind the camera or off screen and the batched preprocess culls them
+    by its conservative pre-test: radii and images bit-identical to the
+    per-view path, with views of other scale modifiers in the batch (no
+    pre-test bound for them when the covariance comes from scale and
+    rotation) and with given 3D covariances."""
+    from dmgs_gb300.scenes import large_scene
+    sc = large_scene(P=200_000, seed=7, n_views=1)
+    rng = np.random.default_rng(77)
+    views = [random_inside_view(rng, 320, 240) for _ in range(6)]
+    mods = [1.0, 1.0, 0.6, 1.0, 1.7, 1.0]
+    base = _gauss(sc)
+    cov = R.cov3d_from_scale_rot_f32(sc.scales, sc.rotations, np.float32(1.0))
+    given = {"means3D": base["means3D"], "opacities": base["opacities"], "shs": base["shs"],
+             "cov3D_precomp": torch.tensor(np.ascontiguousarray(cov, np.float32), device=D)}
+    for g in (base, given):
+        settings = [_settings(v)._replace(scale_modifier=m) for v, m in zip(views, mods)]
+        br = BatchedRasterizer(settings, g, means2D_grads=False)
+        br.forward()
+        torch.cuda.synchronize()
+        br.status()
+        for v, rs in enumerate(settings):
+            img, radii = dmgs_gb300.GaussianRasterizer(rs)(means2D=torch.zeros_like(g["means3D"]), **g)
+            assert torch.count_nonzero(radii) > 1000, v
+            assert torch.equal(br.radii[v], radii), (sorted(g), v)
+            assert torch.equal(br.images[v], img), (sorted(g), v)
+
+
 def test_configuration4_full_size_graph_matches_plain_and_oracle():
     """Configuration 4 at its full size: the 3M-Gaussian large scene, 16
     views at 400x400, 800x800, 1237x822 and 1600x900 round-robin, forward +
