@@ -333,7 +333,10 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
   // different banks
   __shared__ ViewParams s_vp[MAX_BATCH_VIEWS];
   __shared__ float s_V[MAX_BATCH_VIEWS][17], s_P[MAX_BATCH_VIEWS][17];
-  __shared__ float s_kv[MAX_BATCH_VIEWS];
+  // pre-test constants per view, read as 16-byte broadcasts: the view
+  // matrix's z row; the projection's x, y and w rows; (W, H, TILE gx + 2,
+  // TILE gy + 2); (bound factor, prefiltered, no bound, -)
+  __shared__ float4 s_pre[MAX_BATCH_VIEWS][6];
   __shared__ float s_cam[MAX_BATCH_VIEWS][3];
   __shared__ float4 *s_feat[MAX_BATCH_VIEWS];
   __shared__ uint8_t *s_flags[MAX_BATCH_VIEWS];
@@ -361,7 +364,17 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
         w2 += w * w;
       }
     const float limx = mul(1.3f, V.vp.tanfovx), limy = mul(1.3f, V.vp.tanfovy);
-    s_kv[t] = (V.vp.fx * V.vp.fx * (1.f + limx * limx) + V.vp.fy * V.vp.fy * (1.f + limy * limy)) * w2;
+    const float kv = (V.vp.fx * V.vp.fx * (1.f + limx * limx) + V.vp.fy * V.vp.fy * (1.f + limy * limy)) * w2;
+    const float *vm = V.viewm, *pm = V.projm;
+    s_pre[t][0] = make_float4(__ldg(vm + 2), __ldg(vm + 6), __ldg(vm + 10), __ldg(vm + 14));
+    s_pre[t][1] = make_float4(__ldg(pm + 0), __ldg(pm + 4), __ldg(pm + 8), __ldg(pm + 12));
+    s_pre[t][2] = make_float4(__ldg(pm + 1), __ldg(pm + 5), __ldg(pm + 9), __ldg(pm + 13));
+    s_pre[t][3] = make_float4(__ldg(pm + 3), __ldg(pm + 7), __ldg(pm + 11), __ldg(pm + 15));
+    s_pre[t][4] = make_float4((float)V.vp.W, (float)V.vp.H, (float)(TILE * V.vp.gx) + 2.f,
+                              (float)(TILE * V.vp.gy) + 2.f);
+    // another scale modifier than the first view's (uncommon): no bound
+    const bool nobound = cov3D == nullptr && V.vp.scale_modifier != bv.v[0].vp.scale_modifier;
+    s_pre[t][5] = make_float4(kv, V.vp.prefiltered ? 1.f : 0.f, nobound ? 1.f : 0.f, 0.f);
   }
   for (int i = t; i < nv * 32; i += PRE_BLOCK) {
     const int v = i >> 5, k = i & 31;
@@ -385,21 +398,32 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
     const float sfro =
         sqrtf(S[0] * S[0] + S[3] * S[3] + S[5] * S[5] + 2.f * (S[1] * S[1] + S[2] * S[2] + S[4] * S[4]));
     for (int v = 0; v < nv; ++v) {
-      const float vz = view_z(s_V[v], x, y, z);
+      // the full chain's view depth, same ops and operands
+      const float4 zr = s_pre[v][0];
+      const float vz = add(add(add(mul(zr.x, x), mul(zr.y, y)), mul(zr.z, z)), zr.w);
+      const float4 fl = s_pre[v][5];
       bool cand;
       if (!(vz > 0.2f)) {  // the full chain's first test, on the same value
-        if (s_vp[v].prefiltered) atomicOr(s_counters[v], ST_PREFILTER);
+        if (fl.y != 0.f) atomicOr(s_counters[v], ST_PREFILTER);
         cand = false;
-      } else if (cov3D == nullptr && s_vp[v].scale_modifier != mod0) {
-        cand = true;  // another scale modifier (uncommon): no bound, full chain
+      } else if (fl.z != 0.f || !(vz < 1e18f)) {
+        cand = true;
       } else {
-        const float2 pix = pixel_of(s_vp[v], s_P[v], x, y, z);
-        const float rb = 3.01f * sqrtf(1.001f * (s_kv[v] * sfro / (vz * vz) + 0.62f)) + 2.f;
-        const float mx = 2.f + 1e-4f * fabsf(pix.x), my = 2.f + 1e-4f * fabsf(pix.y);
-        const float xmax = (float)(TILE * s_vp[v].gx), ymax = (float)(TILE * s_vp[v].gy);
+        // The approximate reciprocals (2 ulp) move the centre by ~1e-6 of
+        // its value and the bound by less than its 0.1% widening.
+        const float4 a = s_pre[v][1], b = s_pre[v][2], c = s_pre[v][3], im = s_pre[v][4];
+        const float hx = add(add(add(mul(a.x, x), mul(a.y, y)), mul(a.z, z)), a.w);
+        const float hy = add(add(add(mul(b.x, x), mul(b.y, y)), mul(b.z, z)), b.w);
+        const float hw = add(add(add(mul(c.x, x), mul(c.y, y)), mul(c.z, z)), c.w);
+        const float pw = __fdividef(1.f, add(hw, 1e-7f));
+        const float px = mul(sub(mul(add(mul(hx, pw), 1.f), im.x), 1.f), 0.5f);
+        const float py = mul(sub(mul(add(mul(hy, pw), 1.f), im.y), 1.f), 0.5f);
+        const float q = __fdividef(fl.x * sfro, vz * vz) + 0.62f;
+        const float rb = 3.0116f * (q * rsqrtf(q)) + 2.f;  // 3.01 sqrt(1.001 q) + 2
+        const float ax = 1e-4f * fabsf(px), ay = 1e-4f * fabsf(py);
         // NaN anywhere leaves every comparison false: the pair stays a candidate
-        cand = !(pix.x + rb < 1.f - mx || pix.x - rb > xmax + mx || pix.y + rb < 1.f - my ||
-                 pix.y - rb > ymax + my);
+        cand = !(px + rb + ax < -1.f || px - rb - ax > im.z || py + rb + ay < -1.f ||
+                 py - rb - ay > im.w);
       }
       if (cand) {
         cm |= 1u << v;

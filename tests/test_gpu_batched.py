@@ -289,6 +289,13 @@ def test_inside_views_with_mixed_modifiers_and_given_covariances_match_per_view_
             assert torch.count_nonzero(radii) > 1000, v
             assert torch.equal(br.radii[v], radii), (sorted(g), v)
             assert torch.equal(br.images[v], img), (sorted(g), v)
+            # the per-view path runs the same pre-test: pin both on the FP32 oracle
+            cam = oracle_camera(views[v], scale_modifier=mods[v])
+            if "cov3D_precomp" in g:
+                geom = R.geometry_f32(sc.means3D, cam, sc.opacities, cov3D=cov)
+            else:
+                geom = R.geometry_f32(sc.means3D, cam, sc.opacities, sc.scales, sc.rotations)
+            np.testing.assert_array_equal(br.radii[v].cpu().numpy(), geom["radii"])
 
 
 def test_configuration4_full_size_graph_matches_plain_and_oracle():
