@@ -298,16 +298,16 @@ __device__ __forceinline__ uint32_t list_pairs(uint32_t m, uint16_t *pairs, uint
 // Multi-view preprocess, one block of PRE_BLOCK Gaussians and every view.
 //
 // Phase 1, a thread per Gaussian: the view-independent inputs are loaded and
-// the 3D covariance formed once; then, per view, an exact test of the view
-// depth and of the projected centre (the same IEEE ops as the full chain)
-// against a conservative radius bound decides whether the pair can be
-// visible at all.  The bound: the EWA chain's larger eigenvalue is at most
+// the 3D covariance formed once; then, per view, a test of the view depth
+// (the full chain's own value and test) and of the projected centre against
+// a conservative radius bound decides whether the pair can be visible at
+// all.  The bound: the EWA chain's larger eigenvalue is at most
 // tr(J W Sigma W^T J^T) + 0.62 <= |J|_F^2 |W|_F^2 |Sigma|_F + 0.62, with
 // |J|_F^2 <= (fx^2 (1 + limx^2) + fy^2 (1 + limy^2)) / z^2 for the Jacobian
 // at the clamped position; widened by 0.1% and 2 pixels for rounding, and
 // the centre compared with a margin of 2 + 1e-4 |x| pixels, it never culls a
-// pair the full chain keeps.  About 40% of the pairs of an inward-looking
-// batch lie in front of the camera but only ~7% pass the test.
+// pair the full chain keeps.  With cameras inside the scene about 40% of
+// the pairs lie in front of the camera but only ~7% pass the test.
 // Phase 2 runs the full geometry on the block's candidate pairs, listed
 // compactly so that every lane does useful work (a per-lane early exit
 // would leave the warps running the chain for their slowest lane).
