@@ -911,6 +911,9 @@ def main():
 
     if rank == 0:
         Kp = statistics.mean(counts)
+        in_mb = sum(v.numel() * v.element_size() for v in g.values()) / 1e6
+        l2_note = (f"inputs ({in_mb:.0f} MB) larger than L2" if in_mb > 129 else
+                   f"inputs ({in_mb:.0f} MB) smaller than L2: not a bench configuration")
         if plain is not None:
             plain["ratio_batched_over_plain"] = value / max(plain["views_per_s"], 1e-9)
             plain["kernels"] = kernel_table(kt_plain, (P, Vs / nv, Kp, npix / nv, 1, K1_sum / nv))
@@ -922,7 +925,7 @@ def main():
                        "views_per_step": nv, "parallelism": "replicas" if world > 1 else "1 gpu",
                        "outputs": "images, parameter gradients summed over views, densification "
                                   "statistics (fused add_densification_stats)",
-                       "l2": "inputs (708 MB) larger than L2", "mean_instances_K": int(Kp),
+                       "l2": l2_note, "mean_instances_K": int(Kp),
                        "mean_row_entries_K1": int(K1_sum / nv),
                        "blend_config": blend_config(br_cfg),
                        "graph": not args.no_graph},
