@@ -402,29 +402,24 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
       const float4 zr = s_pre[v][0];
       const float vz = add(add(add(mul(zr.x, x), mul(zr.y, y)), mul(zr.z, z)), zr.w);
       const float4 fl = s_pre[v][5];
-      bool cand;
-      if (!(vz > 0.2f)) {  // the full chain's first test, on the same value
-        if (fl.y != 0.f) atomicOr(s_counters[v], ST_PREFILTER);
-        cand = false;
-      } else if (fl.z != 0.f || !(vz < 1e18f)) {
-        cand = true;
-      } else {
-        // The approximate reciprocals (2 ulp) move the centre by ~1e-6 of
-        // its value and the bound by less than its 0.1% widening.
-        const float4 a = s_pre[v][1], b = s_pre[v][2], c = s_pre[v][3], im = s_pre[v][4];
-        const float hx = add(add(add(mul(a.x, x), mul(a.y, y)), mul(a.z, z)), a.w);
-        const float hy = add(add(add(mul(b.x, x), mul(b.y, y)), mul(b.z, z)), b.w);
-        const float hw = add(add(add(mul(c.x, x), mul(c.y, y)), mul(c.z, z)), c.w);
-        const float pw = __fdividef(1.f, add(hw, 1e-7f));
-        const float px = mul(sub(mul(add(mul(hx, pw), 1.f), im.x), 1.f), 0.5f);
-        const float py = mul(sub(mul(add(mul(hy, pw), 1.f), im.y), 1.f), 0.5f);
-        const float q = __fdividef(fl.x * sfro, vz * vz) + 0.62f;
-        const float rb = 3.0116f * (q * rsqrtf(q)) + 2.f;  // 3.01 sqrt(1.001 q) + 2
-        const float ax = 1e-4f * fabsf(px), ay = 1e-4f * fabsf(py);
-        // NaN anywhere leaves every comparison false: the pair stays a candidate
-        cand = !(px + rb + ax < -1.f || px - rb - ax > im.z || py + rb + ay < -1.f ||
-                 py - rb - ay > im.w);
-      }
+      // Branch-free: every lane evaluates the bound (a warp holds Gaussians
+      // on both sides of the camera in nearly every view), then selects.
+      const float4 a = s_pre[v][1], b = s_pre[v][2], c = s_pre[v][3], im = s_pre[v][4];
+      const float hx = add(add(add(mul(a.x, x), mul(a.y, y)), mul(a.z, z)), a.w);
+      const float hy = add(add(add(mul(b.x, x), mul(b.y, y)), mul(b.z, z)), b.w);
+      const float hw = add(add(add(mul(c.x, x), mul(c.y, y)), mul(c.z, z)), c.w);
+      const float pw = __fdividef(1.f, add(hw, 1e-7f));
+      const float px = mul(sub(mul(add(mul(hx, pw), 1.f), im.x), 1.f), 0.5f);
+      const float py = mul(sub(mul(add(mul(hy, pw), 1.f), im.y), 1.f), 0.5f);
+      const float q = __fdividef(fl.x * sfro, vz * vz) + 0.62f;
+      const float rb = 3.0116f * (q * rsqrtf(q)) + 2.f;  // 3.01 sqrt(1.001 q) + 2
+      const float ax = 1e-4f * fabsf(px), ay = 1e-4f * fabsf(py);
+      // NaN anywhere leaves every comparison false: the pair stays a candidate
+      const bool outside = px + rb + ax < -1.f || px - rb - ax > im.z || py + rb + ay < -1.f ||
+                           py - rb - ay > im.w;
+      const bool front = vz > 0.2f;  // the full chain's first test, on the same value
+      if (!front && fl.y != 0.f) atomicOr(s_counters[v], ST_PREFILTER);
+      const bool cand = front && (fl.z != 0.f || !(vz < 1e18f) || !outside);
       if (cand) {
         cm |= 1u << v;
       } else {
