@@ -404,6 +404,11 @@ preprocess_batched_kernel(const BatchViews bv, int P, int M, const float *__rest
       const float4 fl = s_pre[v][5];
       // Branch-free: every lane evaluates the bound (a warp holds Gaussians
       // on both sides of the camera in nearly every view), then selects.
+      // The approximate reciprocal and reciprocal square root (2 ulp) move
+      // the centre by ~1e-6 of its value and the bound by far less than its
+      // 0.1% widening; beyond z = 1e18 (z^2 near the end of the approximate
+      // division's range) and for views without a bound the pair is a
+      // candidate.
       const float4 a = s_pre[v][1], b = s_pre[v][2], c = s_pre[v][3], im = s_pre[v][4];
       const float hx = add(add(add(mul(a.x, x), mul(a.y, y)), mul(a.z, z)), a.w);
       const float hy = add(add(add(mul(b.x, x), mul(b.y, y)), mul(b.z, z)), b.w);
